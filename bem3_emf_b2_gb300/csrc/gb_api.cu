@@ -1,0 +1,722 @@
+// gb_api.cu -- the C ABI (gb_bem.h): device-resident BEM objects.
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <mutex>
+#include <vector>
+#include "gb_common.cuh"
+#include "gb_internal.h"
+#include "gb_bem.h"
+#include "gb_fieldobj.cuh"
+
+extern "C" {
+void gauleg(double x1, double x2, double x[], double w[], int n);
+int gbi_upload_tables_asm(const void* t);
+int gbi_upload_tables_field(const void* t);
+int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* G, cplx* H, cplx* dG, cplx* dH, double* dF,
+                        double* Fs, cudaStream_t st);
+int gbi_build_A_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
+                       const double* kn_dev, int did, int nrows, size_t base, size_t na, cplx* A, cudaStream_t st);
+int gbi_zgetrf(cplx* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
+int gbi_zgetrs(const cplx* LU, size_t lda, int n, const int64_t* ipiv, cplx* X, size_t ldx, int nrhs, cudaStream_t st);
+int gbi_zinverse(const cplx* LU, size_t lda, int n, const int64_t* ipiv, cplx* X, size_t ldx, cudaStream_t st);
+int gbi_zgemv(const cplx* M, size_t ldm, int n, int ncol, const cplx* x, cplx* y, cudaStream_t st);
+int gbi_build_B(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m, const double* kn_dev,
+                const cplx* Ui, const cplx* dUi, int did, int nrows, size_t base, cplx* B, cudaStream_t st);
+int gbi_store_bv(const cplx* X, const GbMeshDev* m, const double* kn_dev, const cplx* Ui, const cplx* dUi, int did,
+                 cplx* U, cplx* dU, cudaStream_t st);
+int gbi_eh_bv(const cplx* dG, const cplx* dH, const double* dF, const GbMeshDev* m, int did, double lambda0,
+              const cplx* U, const cplx* dU, cplx* E, cplx* H, cudaStream_t st);
+int gbi_deh_build(const cplx* G, const cplx* H, const int* rowk, int Ne, int nn, const cplx* E, const cplx* Hf, cplx* Ac,
+                  cplx* Bc, cudaStream_t st);
+int gbi_deh_scatter(const cplx* Bc, const int* rowk, int Ne, cplx* dE, cplx* dHf, cudaStream_t st);
+int gbi_add_incident(int n, const int* idx, const cplx* out, cplx* Ui, cplx* dUi, const int* did, int* bad,
+                     cudaStream_t st);
+int gbi_ccd(int Ne, const int* md, const cplx* Ui, const cplx* Uip, double* out, cudaStream_t st);
+int gbi_domain_id(const FieldObj* o, int n, const double* rt, int* did, cudaStream_t st);
+int gbi_field(const FieldObj* o, int mode, int type, int n, const double* rt, const double* v, const int* did, cplx* out,
+              int* flag, cudaStream_t st);
+int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, const int* t, const double* zt, cplx* out,
+                 cudaStream_t st);
+}
+
+// ------------------------------------------------------------------ errors
+static thread_local char g_err[1024];
+extern "C" void gbi_set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+extern "C" const char* gb_last_error(void) { return g_err; }
+
+// ------------------------------------------------------------------ tables
+static std::mutex g_init_mu;
+static int g_tables_dev = -1;
+
+static int ensure_tables() {
+  int dev;
+  GB_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  if (g_tables_dev == dev) return 0;
+  GbTables t;
+  memset(&t, 0, sizeof(t));
+  gauleg(-1.0, 1.0, t.xli, t.wli, GB_GLN);
+  gauleg(-1.0, 1.0, t.xhi, t.whi, GB_GHN);
+  const double a = GB_P44_N;
+  const double z44[4] = {-a, a, a, -a}, e44[4] = {-a, -a, a, a};
+  const double n9 = 0.7745966692414833770359;
+  const double w0 = 0.3086419753086419753086, w1 = 0.4938271604938271604938, w2 = 0.7901234567901234567901;
+  const double z49[9] = {-n9, n9, n9, -n9, 0.0, n9, 0.0, -n9, 0.0};
+  const double e49[9] = {-n9, -n9, n9, n9, -n9, 0.0, n9, 0.0, 0.0};
+  const double w49[9] = {w0, w0, w0, w0, w1, w1, w1, w1, w2};
+  const double p0 = 0.2, p1 = 0.3464101615137754587055;
+  const double z34[4] = {-p0, 2.0 * p0, -p0, 0.0}, e34[4] = {-p1, 0.0, p1, 0.0};
+  const double w34[4] = {0.5208333333333333333333, 0.5208333333333333333333, 0.5208333333333333333333, -0.5625};
+  const double q0 = 0.3480702390148154917985, q1 = 0.2052130961576726346557, q2 = 0.6028753385763033130539,
+               q3 = 0.3554395089236065568357;
+  const double v0 = 0.1259391805448271525957, v1 = 0.1323941527885061807376, v2 = 0.225;
+  const double z37[7] = {-q0, 2.0 * q0, -q0, q1, -2.0 * q1, q1, 0.0};
+  const double e37[7] = {-q2, 0.0, q2, q3, 0.0, -q3, 0.0};
+  const double w37[7] = {v0, v0, v0, v1, v1, v1, v2};
+  for (int i = 0; i < 4; i++) {
+    t.zt_44[i] = z44[i]; t.et_44[i] = e44[i]; t.wt_44[i] = 1.0;
+    t.zt_34[i] = z34[i]; t.et_34[i] = e34[i]; t.wt_34[i] = w34[i];
+  }
+  for (int i = 0; i < 9; i++) { t.zt_49[i] = z49[i]; t.et_49[i] = e49[i]; t.wt_49[i] = w49[i]; }
+  for (int i = 0; i < 7; i++) { t.zt_37[i] = z37[i]; t.et_37[i] = e37[i]; t.wt_37[i] = w37[i]; }
+  if (gbi_upload_tables_asm(&t)) return -1;
+  if (gbi_upload_tables_field(&t)) return -1;
+  g_tables_dev = dev;
+  return 0;
+}
+
+extern "C" int gb_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;
+  return n;
+}
+
+// ------------------------------------------------------------------ object
+struct gb_obj {
+  GbMeshDev m;
+  double lambda0;
+  cudaStream_t st;
+  double* kn_dev;
+  // per-domain coefficient matrices
+  cplx* G[GB_MAXDOM];
+  cplx* H[GB_MAXDOM];
+  cplx* dG[GB_MAXDOM];
+  cplx* dH[GB_MAXDOM];
+  double* dF[GB_MAXDOM];
+  int* rowk[GB_MAXDOM];   // device: row index inside the domain block of A (-1: unused node)
+  int nrows[GB_MAXDOM];
+  size_t na;
+  cplx* invA;             // na x na
+  int have_invA;
+  // boundary values per domain, [(Ne_d+1)][4][4] (U, dU) and [(Ne_d+1)][4][3] (E, dE, H, dH)
+  cplx* bU[GB_MAXDOM];
+  cplx* bdU[GB_MAXDOM];
+  cplx* bE[GB_MAXDOM];
+  cplx* bdE[GB_MAXDOM];
+  cplx* bH[GB_MAXDOM];
+  cplx* bdH[GB_MAXDOM];
+  // incident potential per element [(Ne+1)][4][4]
+  cplx *Ui, *dUi, *Ui0, *dUi0, *Uip;
+  // exterior nodes (md == 0) as field points: position, unit normal, flat index e*4+j
+  int next;
+  double* ext_r;
+  double* ext_v;
+  int* ext_idx;
+  std::vector<int> h_etype, h_sid;
+};
+
+static int dalloc(void** p, size_t bytes) {
+  GB_CUDA(cudaMalloc(p, bytes > 0 ? bytes : 16));
+  return 0;
+}
+template <class T>
+static int dup(T** dst, const T* src, size_t n) {
+  if (dalloc((void**)dst, n * sizeof(T))) return -1;
+  GB_CUDA(cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+extern "C" void gb_obj_destroy(gb_obj* o) {
+  if (!o) return;
+  cudaFree(o->m.cr); cudaFree(o->m.cw); cudaFree(o->m.ren); cudaFree(o->m.wen);
+  cudaFree(o->m.etype); cudaFree(o->m.eni); cudaFree(o->m.md); cudaFree(o->m.sd); cudaFree(o->m.sid);
+  cudaFree(o->kn_dev);
+  for (int d = 0; d < GB_MAXDOM; d++) {
+    cudaFree(o->G[d]); cudaFree(o->H[d]); cudaFree(o->dG[d]); cudaFree(o->dH[d]); cudaFree(o->dF[d]);
+    cudaFree(o->rowk[d]);
+  }
+  cudaFree(o->invA);
+  for (int d = 0; d < GB_MAXDOM; d++) {
+    cudaFree(o->bU[d]); cudaFree(o->bdU[d]); cudaFree(o->bE[d]); cudaFree(o->bdE[d]); cudaFree(o->bH[d]); cudaFree(o->bdH[d]);
+  }
+  cudaFree(o->Ui); cudaFree(o->dUi); cudaFree(o->Ui0); cudaFree(o->dUi0); cudaFree(o->Uip);
+  cudaFree(o->m.corner); cudaFree(o->ext_r); cudaFree(o->ext_v); cudaFree(o->ext_idx);
+  if (o->st) cudaStreamDestroy(o->st);
+  delete o;
+}
+
+extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
+  *out = nullptr;
+  if (md->MN + 1 > GB_MAXDOM) { gbi_set_error("gb_obj_create: %d media exceed the limit %d", md->MN, GB_MAXDOM - 1); return -1; }
+  if (md->Ne <= 0) { gbi_set_error("gb_obj_create: no elements"); return -1; }
+  if (ensure_tables()) return -1;
+  gb_obj* o = new gb_obj();
+  memset(&o->m, 0, sizeof(o->m));
+  for (int d = 0; d < GB_MAXDOM; d++) { o->G[d] = o->H[d] = o->dG[d] = o->dH[d] = nullptr; o->dF[d] = nullptr; o->rowk[d] = nullptr; }
+  o->invA = nullptr;
+  o->have_invA = 0;
+  for (int d = 0; d < GB_MAXDOM; d++) o->bU[d] = o->bdU[d] = o->bE[d] = o->bdE[d] = o->bH[d] = o->bdH[d] = nullptr;
+  o->Ui = o->dUi = o->Ui0 = o->dUi0 = o->Uip = nullptr;
+  o->next = 0;
+  o->ext_r = o->ext_v = nullptr;
+  o->ext_idx = nullptr;
+  o->kn_dev = nullptr;
+  o->st = nullptr;
+  GbMeshDev& m = o->m;
+  m.Ne = md->Ne; m.NN = md->NN; m.MN = md->MN;
+  size_t ne1 = (size_t)md->Ne + 1;
+  int tot = 0;
+  for (int d = 0; d <= md->MN; d++) { m.sb_Ne[d] = md->sb_Ne[d]; m.sb_off[d] = tot; tot += md->sb_Ne[d] + 1; }
+  m.sb_off[md->MN + 1] = tot;
+  for (int d = 0; d <= md->MN; d++) { m.kn[2 * d] = md->kn[2 * d]; m.kn[2 * d + 1] = md->kn[2 * d + 1]; }
+  o->lambda0 = md->lambda0;
+  if (cudaStreamCreateWithFlags(&o->st, cudaStreamNonBlocking) != cudaSuccess) { gbi_set_error("stream"); gb_obj_destroy(o); return -1; }
+  if (dup(&m.cr, md->cr, ne1 * 12) || dup(&m.cw, md->cw, ne1 * 9) || dup(&m.ren, md->ren, ne1 * 12) ||
+      dup(&m.wen, md->wen, ne1 * 12) || dup(&m.etype, md->etype, ne1) || dup(&m.eni, md->eni, ne1 * 4) ||
+      dup(&m.md, md->md, ne1) || dup(&m.sd, md->sd, ne1) || dup(&m.sid, md->sid, (size_t)tot) ||
+      dup(&o->kn_dev, md->kn, (size_t)2 * (md->MN + 1)) || dup(&m.corner, md->corner, ne1 * 12)) {
+    gb_obj_destroy(o);
+    return -1;
+  }
+  o->h_etype.assign(md->etype, md->etype + ne1);
+  o->h_sid.assign(md->sid, md->sid + tot);
+  // rows of A: per domain, collocation nodes (t,tn) in order, skipping the
+  // fourth node of triangles (reference solve_bieq2.c:228-239)
+  size_t na = 0;
+  for (int d = 0; d <= md->MN; d++) {
+    int Ne = md->sb_Ne[d];
+    std::vector<int> rk((size_t)Ne * 4, -1);
+    int k = 0;
+    for (int t = 1; t <= Ne; t++) {
+      int td = abs(o->h_sid[m.sb_off[d] + t]);
+      for (int tn = 0; tn < 4; tn++) {
+        if (tn == 3 && o->h_etype[td] == 0) continue;
+        rk[(size_t)(t - 1) * 4 + tn] = k++;
+      }
+    }
+    o->nrows[d] = k;
+    na += 4 * (size_t)k;
+    if (dup(&o->rowk[d], rk.data(), rk.size())) { gb_obj_destroy(o); return -1; }
+  }
+  o->na = na;
+  {  // exterior collocation points of the object (reference add_scattered_mEMP loop, mo_solve.c:306-346)
+    std::vector<double> er, ev;
+    std::vector<int> ei;
+    for (int e = 1; e <= md->Ne; e++) {
+      if (md->md[e] != 0) continue;
+      for (int j = 0; j < 4; j++) {
+        double w[3], a = 0.0;
+        for (int d = 0; d < 3; d++) { er.push_back(md->ren[(size_t)e * 12 + j * 3 + d]); w[d] = md->wen[(size_t)e * 12 + j * 3 + d]; a += w[d] * w[d]; }
+        a = sqrt(a);
+        for (int d = 0; d < 3; d++) ev.push_back(a != 0.0 ? w[d] / a : w[d]);
+        ei.push_back(e * 4 + j);
+      }
+    }
+    o->next = (int)ei.size();
+    if (dup(&o->ext_r, er.data(), er.size()) || dup(&o->ext_v, ev.data(), ev.size()) || dup(&o->ext_idx, ei.data(), ei.size())) {
+      gb_obj_destroy(o);
+      return -1;
+    }
+  }
+  if (na != 8 * (size_t)md->NN) {
+    gbi_set_error("gb_obj_create: inconsistent mesh (rows %zu != 8 NN = %zu)", na, 8 * (size_t)md->NN);
+    gb_obj_destroy(o);
+    return -1;
+  }
+  *out = o;
+  return 0;
+}
+
+static int ensure_cmatrix(gb_obj* o, int did) {
+  size_t N = (size_t)o->m.sb_Ne[did] * 4;
+  if (!o->G[did]) {
+    if (dalloc((void**)&o->G[did], N * N * sizeof(cplx)) || dalloc((void**)&o->H[did], N * N * sizeof(cplx)) ||
+        dalloc((void**)&o->dG[did], 2 * N * N * sizeof(cplx)) || dalloc((void**)&o->dH[did], 2 * N * N * sizeof(cplx)) ||
+        dalloc((void**)&o->dF[did], 3 * N * sizeof(double)))
+      return -1;
+  }
+  return 0;
+}
+
+static int check_did(gb_obj* o, int did) {
+  if (did < 0 || did > o->m.MN) { gbi_set_error("domain id %d out of range 0..%d", did, o->m.MN); return -1; }
+  return 0;
+}
+
+extern "C" int gb_assemble(gb_obj* o, int did, int type) {
+  if (check_did(o, did)) return -1;
+  if (type < 0 || type > 3) { gbi_set_error("gb_assemble: quadrature type %d not in 0..3", type); return -1; }
+  if (ensure_cmatrix(o, did)) return -1;
+  size_t Ne = (size_t)o->m.sb_Ne[did];
+  double* Fs = nullptr;
+  if (dalloc((void**)&Fs, 3 * 4 * Ne * Ne * sizeof(double))) return -1;
+  int rc = gbi_assemble_domain(&o->m, did, type, o->G[did], o->H[did], o->dG[did], o->dH[did], o->dF[did], Fs, o->st);
+  cudaError_t e = cudaStreamSynchronize(o->st);
+  cudaFree(Fs);
+  if (rc) return -1;
+  if (e != cudaSuccess) { gbi_set_error("gb_assemble: %s", cudaGetErrorString(e)); return -1; }
+  o->have_invA = 0;
+  return 0;
+}
+
+extern "C" int gb_cmatrix_download(gb_obj* o, int did, void* G, void* H, void* dG, void* dH, double* dF) {
+  if (check_did(o, did)) return -1;
+  if (!o->G[did]) { gbi_set_error("gb_cmatrix_download: domain %d not assembled", did); return -1; }
+  size_t N = (size_t)o->m.sb_Ne[did] * 4;
+  if (G) GB_CUDA(cudaMemcpy(G, o->G[did], N * N * sizeof(cplx), cudaMemcpyDeviceToHost));
+  if (H) GB_CUDA(cudaMemcpy(H, o->H[did], N * N * sizeof(cplx), cudaMemcpyDeviceToHost));
+  if (dG) GB_CUDA(cudaMemcpy(dG, o->dG[did], 2 * N * N * sizeof(cplx), cudaMemcpyDeviceToHost));
+  if (dH) GB_CUDA(cudaMemcpy(dH, o->dH[did], 2 * N * N * sizeof(cplx), cudaMemcpyDeviceToHost));
+  if (dF) GB_CUDA(cudaMemcpy(dF, o->dF[did], 3 * N * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int gb_cmatrix_upload(gb_obj* o, int did, const void* G, const void* H, const void* dG, const void* dH,
+                                 const double* dF) {
+  if (check_did(o, did)) return -1;
+  if (ensure_cmatrix(o, did)) return -1;
+  size_t N = (size_t)o->m.sb_Ne[did] * 4;
+  if (G) GB_CUDA(cudaMemcpy(o->G[did], G, N * N * sizeof(cplx), cudaMemcpyHostToDevice));
+  if (H) GB_CUDA(cudaMemcpy(o->H[did], H, N * N * sizeof(cplx), cudaMemcpyHostToDevice));
+  if (dG) GB_CUDA(cudaMemcpy(o->dG[did], dG, 2 * N * N * sizeof(cplx), cudaMemcpyHostToDevice));
+  if (dH) GB_CUDA(cudaMemcpy(o->dH[did], dH, 2 * N * N * sizeof(cplx), cudaMemcpyHostToDevice));
+  if (dF) GB_CUDA(cudaMemcpy(o->dF[did], dF, 3 * N * sizeof(double), cudaMemcpyHostToDevice));
+  o->have_invA = 0;
+  return 0;
+}
+
+static int build_A(gb_obj* o, cplx* A) {
+  size_t na = o->na;
+  GB_CUDA(cudaMemsetAsync(A, 0, na * na * sizeof(cplx), o->st));
+  size_t base = 0;
+  for (int d = 0; d <= o->m.MN; d++) {
+    if (!o->G[d]) { gbi_set_error("coupled matrix: domain %d has no coefficient matrices", d); return -1; }
+    if (gbi_build_A_domain(o->G[d], o->H[d], o->m.sid + o->m.sb_off[d], o->rowk[d], &o->m, o->kn_dev, d, o->nrows[d],
+                           base, na, A, o->st))
+      return -1;
+    base += 4 * (size_t)o->nrows[d];
+  }
+  return 0;
+}
+
+extern "C" int gb_A_download(gb_obj* o, void* Ah) {
+  size_t na = o->na;
+  cplx* A = nullptr;
+  if (dalloc((void**)&A, na * na * sizeof(cplx))) return -1;
+  int rc = build_A(o, A);
+  if (!rc) {
+    if (cudaMemcpyAsync(Ah, A, na * na * sizeof(cplx), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+        cudaStreamSynchronize(o->st) != cudaSuccess) {
+      gbi_set_error("gb_A_download: copy failed");
+      rc = -1;
+    }
+  }
+  cudaFree(A);
+  return rc;
+}
+
+extern "C" int gb_invA_compute(gb_obj* o) {
+  size_t na = o->na;
+  cplx* A = nullptr;
+  int64_t* ipiv = nullptr;
+  int* info = nullptr;
+  if (!o->invA && dalloc((void**)&o->invA, na * na * sizeof(cplx))) return -1;
+  if (dalloc((void**)&A, na * na * sizeof(cplx)) || dalloc((void**)&ipiv, na * sizeof(int64_t)) ||
+      dalloc((void**)&info, sizeof(int))) {
+    cudaFree(A); cudaFree(ipiv);
+    return -1;
+  }
+  int rc = build_A(o, A);
+  if (!rc) rc = gbi_zgetrf(A, na, (int)na, ipiv, info, o->st);
+  int hinfo = 0;
+  if (!rc) {
+    if (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+        cudaStreamSynchronize(o->st) != cudaSuccess) {
+      gbi_set_error("gb_invA_compute: LU failed: %s", cudaGetErrorString(cudaGetLastError()));
+      rc = -1;
+    } else if (hinfo != 0) {
+      gbi_set_error("gb_invA_compute: matrix is singular (zgetrf info=%d)", hinfo);
+      rc = -1;
+    }
+  }
+  if (!rc) rc = gbi_zinverse(A, na, (int)na, ipiv, o->invA, na, o->st);
+  if (!rc && cudaStreamSynchronize(o->st) != cudaSuccess) {
+    gbi_set_error("gb_invA_compute: inverse failed: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
+  }
+  cudaFree(A); cudaFree(ipiv); cudaFree(info);
+  if (!rc) o->have_invA = 1;
+  return rc;
+}
+
+extern "C" int gb_invA_download(gb_obj* o, void* invA) {
+  if (!o->have_invA) { gbi_set_error("gb_invA_download: no inverse"); return -1; }
+  GB_CUDA(cudaMemcpy(invA, o->invA, o->na * o->na * sizeof(cplx), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int gb_invA_upload(gb_obj* o, const void* invA) {
+  if (!o->invA && dalloc((void**)&o->invA, o->na * o->na * sizeof(cplx))) return -1;
+  GB_CUDA(cudaMemcpy(o->invA, invA, o->na * o->na * sizeof(cplx), cudaMemcpyHostToDevice));
+  o->have_invA = 1;
+  return 0;
+}
+
+extern "C" int gb_solve_AB(gb_obj* o, const void* b, void* x) {
+  if (!o->have_invA) { gbi_set_error("gb_solve_AB: no inverse"); return -1; }
+  size_t na = o->na;
+  cplx *db = nullptr, *dx = nullptr;
+  if (dalloc((void**)&db, na * sizeof(cplx)) || dalloc((void**)&dx, na * sizeof(cplx))) { cudaFree(db); return -1; }
+  int rc = 0;
+  if (cudaMemcpyAsync(db, b, na * sizeof(cplx), cudaMemcpyHostToDevice, o->st) != cudaSuccess) rc = -1;
+  if (!rc) rc = gbi_zgemv(o->invA, na, (int)na, (int)na, db, dx, o->st);
+  if (!rc && (cudaMemcpyAsync(x, dx, na * sizeof(cplx), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+              cudaStreamSynchronize(o->st) != cudaSuccess)) {
+    gbi_set_error("gb_solve_AB failed");
+    rc = -1;
+  }
+  cudaFree(db); cudaFree(dx);
+  return rc;
+}
+
+extern "C" int gb_zgesv(int n, int nrhs, void* Ah, void* Bh) {
+  if (n <= 0 || nrhs <= 0) { gbi_set_error("gb_zgesv: bad size n=%d nrhs=%d", n, nrhs); return -1; }
+  cplx *A = nullptr, *B = nullptr;
+  int64_t* ipiv = nullptr;
+  int* info = nullptr;
+  cudaStream_t st;
+  GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  int rc = 0;
+  if (dalloc((void**)&A, (size_t)n * n * sizeof(cplx)) || dalloc((void**)&B, (size_t)n * nrhs * sizeof(cplx)) ||
+      dalloc((void**)&ipiv, (size_t)n * sizeof(int64_t)) || dalloc((void**)&info, sizeof(int)))
+    rc = -1;
+  if (!rc && (cudaMemcpyAsync(A, Ah, (size_t)n * n * sizeof(cplx), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+              cudaMemcpyAsync(B, Bh, (size_t)n * nrhs * sizeof(cplx), cudaMemcpyHostToDevice, st) != cudaSuccess)) {
+    gbi_set_error("gb_zgesv: upload failed");
+    rc = -1;
+  }
+  if (!rc) rc = gbi_zgetrf(A, n, n, ipiv, info, st);
+  int hinfo = 0;
+  if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaStreamSynchronize(st) != cudaSuccess)) {
+    gbi_set_error("gb_zgesv: LU failed");
+    rc = -1;
+  }
+  if (!rc && hinfo) { gbi_set_error("gb_zgesv: singular matrix (info=%d)", hinfo); rc = -1; }
+  if (!rc) rc = gbi_zgetrs(A, n, n, ipiv, B, nrhs, nrhs, st);
+  if (!rc && (cudaMemcpyAsync(Bh, B, (size_t)n * nrhs * sizeof(cplx), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaStreamSynchronize(st) != cudaSuccess)) {
+    gbi_set_error("gb_zgesv: solve failed");
+    rc = -1;
+  }
+  cudaFree(A); cudaFree(B); cudaFree(ipiv); cudaFree(info);
+  cudaStreamDestroy(st);
+  return rc;
+}
+
+// ------------------------------------------------------------------ boundary values
+static int ensure_bv(gb_obj* o) {
+  for (int d = 0; d <= o->m.MN; d++) {
+    if (o->bU[d]) continue;
+    size_t n1 = (size_t)o->m.sb_Ne[d] + 1;
+    if (dalloc((void**)&o->bU[d], n1 * 16 * sizeof(cplx)) || dalloc((void**)&o->bdU[d], n1 * 16 * sizeof(cplx)) ||
+        dalloc((void**)&o->bE[d], n1 * 12 * sizeof(cplx)) || dalloc((void**)&o->bdE[d], n1 * 12 * sizeof(cplx)) ||
+        dalloc((void**)&o->bH[d], n1 * 12 * sizeof(cplx)) || dalloc((void**)&o->bdH[d], n1 * 12 * sizeof(cplx)))
+      return -1;
+    GB_CUDA(cudaMemset(o->bU[d], 0, n1 * 16 * sizeof(cplx)));
+    GB_CUDA(cudaMemset(o->bdU[d], 0, n1 * 16 * sizeof(cplx)));
+    GB_CUDA(cudaMemset(o->bE[d], 0, n1 * 12 * sizeof(cplx)));
+    GB_CUDA(cudaMemset(o->bdE[d], 0, n1 * 12 * sizeof(cplx)));
+    GB_CUDA(cudaMemset(o->bH[d], 0, n1 * 12 * sizeof(cplx)));
+    GB_CUDA(cudaMemset(o->bdH[d], 0, n1 * 12 * sizeof(cplx)));
+  }
+  if (!o->Ui) {
+    size_t n = ((size_t)o->m.Ne + 1) * 16 * sizeof(cplx);
+    if (dalloc((void**)&o->Ui, n) || dalloc((void**)&o->dUi, n) || dalloc((void**)&o->Ui0, n) ||
+        dalloc((void**)&o->dUi0, n) || dalloc((void**)&o->Uip, n))
+      return -1;
+    GB_CUDA(cudaMemset(o->Ui, 0, n)); GB_CUDA(cudaMemset(o->dUi, 0, n)); GB_CUDA(cudaMemset(o->Ui0, 0, n));
+    GB_CUDA(cudaMemset(o->dUi0, 0, n)); GB_CUDA(cudaMemset(o->Uip, 0, n));
+  }
+  return 0;
+}
+
+extern "C" int gb_bv_upload(gb_obj* o, int did, const void* U, const void* dU, const void* E, const void* dE,
+                            const void* H, const void* dH) {
+  if (check_did(o, did) || ensure_bv(o)) return -1;
+  size_t n1 = (size_t)o->m.sb_Ne[did] + 1;
+  if (U) GB_CUDA(cudaMemcpy(o->bU[did], U, n1 * 16 * sizeof(cplx), cudaMemcpyHostToDevice));
+  if (dU) GB_CUDA(cudaMemcpy(o->bdU[did], dU, n1 * 16 * sizeof(cplx), cudaMemcpyHostToDevice));
+  if (E) GB_CUDA(cudaMemcpy(o->bE[did], E, n1 * 12 * sizeof(cplx), cudaMemcpyHostToDevice));
+  if (dE) GB_CUDA(cudaMemcpy(o->bdE[did], dE, n1 * 12 * sizeof(cplx), cudaMemcpyHostToDevice));
+  if (H) GB_CUDA(cudaMemcpy(o->bH[did], H, n1 * 12 * sizeof(cplx), cudaMemcpyHostToDevice));
+  if (dH) GB_CUDA(cudaMemcpy(o->bdH[did], dH, n1 * 12 * sizeof(cplx), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+extern "C" int gb_bv_download(gb_obj* o, int did, void* U, void* dU, void* E, void* dE, void* H, void* dH) {
+  if (check_did(o, did) || ensure_bv(o)) return -1;
+  size_t n1 = (size_t)o->m.sb_Ne[did] + 1;
+  if (U) GB_CUDA(cudaMemcpy(U, o->bU[did], n1 * 16 * sizeof(cplx), cudaMemcpyDeviceToHost));
+  if (dU) GB_CUDA(cudaMemcpy(dU, o->bdU[did], n1 * 16 * sizeof(cplx), cudaMemcpyDeviceToHost));
+  if (E) GB_CUDA(cudaMemcpy(E, o->bE[did], n1 * 12 * sizeof(cplx), cudaMemcpyDeviceToHost));
+  if (dE) GB_CUDA(cudaMemcpy(dE, o->bdE[did], n1 * 12 * sizeof(cplx), cudaMemcpyDeviceToHost));
+  if (H) GB_CUDA(cudaMemcpy(H, o->bH[did], n1 * 12 * sizeof(cplx), cudaMemcpyDeviceToHost));
+  if (dH) GB_CUDA(cudaMemcpy(dH, o->bdH[did], n1 * 12 * sizeof(cplx), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int gb_incident_upload(gb_obj* o, const void* Ui0, const void* dUi0) {
+  if (ensure_bv(o)) return -1;
+  size_t n = ((size_t)o->m.Ne + 1) * 16 * sizeof(cplx);
+  GB_CUDA(cudaMemcpy(o->Ui0, Ui0, n, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(o->dUi0, dUi0, n, cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(o->Ui, o->Ui0, n, cudaMemcpyDeviceToDevice));
+  GB_CUDA(cudaMemcpy(o->Uip, o->Ui0, n, cudaMemcpyDeviceToDevice));
+  GB_CUDA(cudaMemcpy(o->dUi, o->dUi0, n, cudaMemcpyDeviceToDevice));
+  return 0;
+}
+
+extern "C" int gb_incident_download(gb_obj* o, void* Ui, void* dUi, void* Uip) {
+  if (ensure_bv(o)) return -1;
+  size_t n = ((size_t)o->m.Ne + 1) * 16 * sizeof(cplx);
+  if (Ui) GB_CUDA(cudaMemcpy(Ui, o->Ui, n, cudaMemcpyDeviceToHost));
+  if (dUi) GB_CUDA(cudaMemcpy(dUi, o->dUi, n, cudaMemcpyDeviceToHost));
+  if (Uip) GB_CUDA(cudaMemcpy(Uip, o->Uip, n, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+static int sync_obj(gb_obj* o, const char* what) {
+  cudaError_t e = cudaStreamSynchronize(o->st);
+  if (e != cudaSuccess) { gbi_set_error("%s: %s", what, cudaGetErrorString(e)); return -1; }
+  return 0;
+}
+
+extern "C" int gb_solve_mEMP(gb_obj* o) {
+  if (!o->have_invA) { gbi_set_error("gb_solve_mEMP: no inverse of A"); return -1; }
+  if (ensure_bv(o)) return -1;
+  size_t na = o->na;
+  cplx *B = nullptr, *X = nullptr;
+  if (dalloc((void**)&B, na * sizeof(cplx)) || dalloc((void**)&X, na * sizeof(cplx))) { cudaFree(B); return -1; }
+  int rc = 0;
+  size_t base = 0;
+  for (int d = 0; d <= o->m.MN && !rc; d++) {
+    if (!o->G[d]) { gbi_set_error("gb_solve_mEMP: domain %d has no coefficient matrices", d); rc = -1; break; }
+    rc = gbi_build_B(o->G[d], o->H[d], o->m.sid + o->m.sb_off[d], o->rowk[d], &o->m, o->kn_dev, o->Ui, o->dUi, d,
+                     o->nrows[d], base, B, o->st);
+    base += 4 * (size_t)o->nrows[d];
+  }
+  if (!rc) rc = gbi_zgemv(o->invA, na, (int)na, (int)na, B, X, o->st);
+  for (int d = 0; d <= o->m.MN && !rc; d++) rc = gbi_store_bv(X, &o->m, o->kn_dev, o->Ui, o->dUi, d, o->bU[d], o->bdU[d], o->st);
+  if (!rc) rc = sync_obj(o, "gb_solve_mEMP");
+  cudaFree(B);
+  cudaFree(X);
+  return rc;
+}
+
+
+extern "C" int gb_reset_incident(gb_obj* o) {
+  if (ensure_bv(o)) return -1;
+  size_t n = ((size_t)o->m.Ne + 1) * 16 * sizeof(cplx);
+  GB_CUDA(cudaMemcpyAsync(o->Uip, o->Ui, n, cudaMemcpyDeviceToDevice, o->st));
+  GB_CUDA(cudaMemcpyAsync(o->Ui, o->Ui0, n, cudaMemcpyDeviceToDevice, o->st));
+  GB_CUDA(cudaMemcpyAsync(o->dUi, o->dUi0, n, cudaMemcpyDeviceToDevice, o->st));
+  return sync_obj(o, "gb_reset_incident");
+}
+
+static FieldObj field_view(gb_obj* o) {
+  FieldObj f;
+  memset(&f, 0, sizeof(f));
+  f.cr = o->m.cr; f.cw = o->m.cw; f.corner = o->m.corner; f.etype = o->m.etype; f.sd = o->m.sd; f.sid = o->m.sid;
+  for (int d = 0; d <= o->m.MN; d++) {
+    f.sb_Ne[d] = o->m.sb_Ne[d];
+    f.sb_off[d] = o->m.sb_off[d];
+    f.kn[2 * d] = o->m.kn[2 * d];
+    f.kn[2 * d + 1] = o->m.kn[2 * d + 1];
+    f.U[d] = o->bU[d]; f.dU[d] = o->bdU[d]; f.E[d] = o->bE[d]; f.dE[d] = o->bdE[d]; f.H[d] = o->bH[d]; f.dH[d] = o->bdH[d];
+  }
+  f.sb_off[o->m.MN + 1] = o->m.sb_off[o->m.MN + 1];
+  f.MN = o->m.MN;
+  f.lambda0 = o->lambda0;
+  return f;
+}
+
+extern "C" int gb_add_scattered(gb_obj* dst, gb_obj* src, int type) {
+  if (ensure_bv(dst) || ensure_bv(src)) return -1;
+  int n = dst->next;
+  if (n == 0) return 0;
+  int *did = nullptr, *bad = nullptr;
+  cplx* out = nullptr;
+  if (dalloc((void**)&did, n * sizeof(int)) || dalloc((void**)&bad, sizeof(int)) ||
+      dalloc((void**)&out, (size_t)n * 8 * sizeof(cplx))) {
+    cudaFree(did); cudaFree(bad);
+    return -1;
+  }
+  FieldObj f = field_view(src);
+  int rc = 0;
+  if (cudaMemsetAsync(bad, 0, sizeof(int), dst->st) != cudaSuccess) rc = -1;
+  if (!rc) rc = gbi_domain_id(&f, n, dst->ext_r, did, dst->st);
+  if (!rc) rc = gbi_field(&f, 3, type, n, dst->ext_r, dst->ext_v, did, out, nullptr, dst->st);
+  if (!rc) rc = gbi_add_incident(n, dst->ext_idx, out, dst->Ui, dst->dUi, did, bad, dst->st);
+  int hbad = 0;
+  if (!rc && (cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, dst->st) != cudaSuccess ||
+              cudaStreamSynchronize(dst->st) != cudaSuccess)) {
+    gbi_set_error("gb_add_scattered: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
+  }
+  if (!rc && hbad) {
+    gbi_set_error("scattered field domain id error!(overlapped). domain id=%d", hbad - 1000);
+    rc = -1;
+  }
+  cudaFree(did); cudaFree(bad); cudaFree(out);
+  return rc;
+}
+
+extern "C" int gb_ccd_sums(gb_obj* o, double* hout) {
+  if (ensure_bv(o)) return -1;
+  double* out = nullptr;
+  if (dalloc((void**)&out, 3 * sizeof(double))) return -1;
+  int rc = gbi_ccd(o->m.Ne, o->m.md, o->Ui, o->Uip, out, o->st);
+  if (!rc && (cudaMemcpyAsync(hout, out, 3 * sizeof(double), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+              cudaStreamSynchronize(o->st) != cudaSuccess)) {
+    gbi_set_error("gb_ccd_sums failed");
+    rc = -1;
+  }
+  cudaFree(out);
+  return rc;
+}
+
+extern "C" int gb_solve_EH(gb_obj* o) {
+  if (ensure_bv(o)) return -1;
+  int rc = 0;
+  for (int d = 0; d <= o->m.MN && !rc; d++) {
+    int Ne = o->m.sb_Ne[d];
+    if (Ne == 0) continue;
+    if (!o->G[d]) { gbi_set_error("gb_solve_EH: domain %d has no coefficient matrices", d); return -1; }
+    rc = gbi_eh_bv(o->dG[d], o->dH[d], o->dF[d], &o->m, d, o->lambda0, o->bU[d], o->bdU[d], o->bE[d], o->bH[d], o->st);
+    if (rc) break;
+    int nn = o->nrows[d];
+    cplx *Ac = nullptr, *Bc = nullptr;
+    int64_t* ipiv = nullptr;
+    int* info = nullptr;
+    if (dalloc((void**)&Ac, (size_t)nn * nn * sizeof(cplx)) || dalloc((void**)&Bc, (size_t)nn * 6 * sizeof(cplx)) ||
+        dalloc((void**)&ipiv, (size_t)nn * sizeof(int64_t)) || dalloc((void**)&info, sizeof(int))) {
+      cudaFree(Ac); cudaFree(Bc); cudaFree(ipiv);
+      return -1;
+    }
+    rc = gbi_deh_build(o->G[d], o->H[d], o->rowk[d], Ne, nn, o->bE[d], o->bH[d], Ac, Bc, o->st);
+    if (!rc) rc = gbi_zgetrf(Ac, nn, nn, ipiv, info, o->st);
+    int hinfo = 0;
+    if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+                cudaStreamSynchronize(o->st) != cudaSuccess)) {
+      gbi_set_error("gb_solve_EH: LU failed");
+      rc = -1;
+    }
+    if (!rc && hinfo) { gbi_set_error("mo_solve.c, solve_deh_bv(), zgesv info=%d error", hinfo); rc = -1; }
+    if (!rc) rc = gbi_zgetrs(Ac, nn, nn, ipiv, Bc, 6, 6, o->st);
+    if (!rc) rc = gbi_deh_scatter(Bc, o->rowk[d], Ne, o->bdE[d], o->bdH[d], o->st);
+    if (!rc) rc = sync_obj(o, "gb_solve_EH");
+    cudaFree(Ac); cudaFree(Bc); cudaFree(ipiv); cudaFree(info);
+  }
+  return rc;
+}
+
+// ------------------------------------------------------------------ points
+extern "C" int gb_domain_id(gb_obj* o, int n, const double* rt, int* did) {
+  if (n <= 0) return 0;
+  double* drt = nullptr;
+  int* dd = nullptr;
+  if (dalloc((void**)&drt, (size_t)n * 3 * sizeof(double)) || dalloc((void**)&dd, (size_t)n * sizeof(int))) {
+    cudaFree(drt);
+    return -1;
+  }
+  FieldObj f = field_view(o);
+  int rc = 0;
+  if (cudaMemcpyAsync(drt, rt, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, o->st) != cudaSuccess) rc = -1;
+  if (!rc) rc = gbi_domain_id(&f, n, drt, dd, o->st);
+  if (!rc && (cudaMemcpyAsync(did, dd, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+              cudaStreamSynchronize(o->st) != cudaSuccess)) {
+    gbi_set_error("gb_domain_id failed");
+    rc = -1;
+  }
+  cudaFree(drt); cudaFree(dd);
+  return rc;
+}
+
+extern "C" int gb_field_points(gb_obj* o, int mode, int type, int n, const double* rt, const double* v, const int* did,
+                               void* out, int* flag) {
+  if (n <= 0) return 0;
+  if (mode < 0 || mode > 3 || type < 0 || type > 3) { gbi_set_error("gb_field_points: mode %d type %d", mode, type); return -1; }
+  if (ensure_bv(o)) return -1;
+  int nout = (mode == 0) ? 4 : (mode == 3 ? 8 : 6);
+  double *drt = nullptr, *dv = nullptr;
+  int *dd = nullptr, *df = nullptr;
+  cplx* dout = nullptr;
+  int rc = 0;
+  if (dalloc((void**)&drt, (size_t)n * 3 * sizeof(double)) || dalloc((void**)&dv, (size_t)n * 3 * sizeof(double)) ||
+      dalloc((void**)&dd, (size_t)n * sizeof(int)) || dalloc((void**)&df, (size_t)n * sizeof(int)) ||
+      dalloc((void**)&dout, (size_t)n * nout * sizeof(cplx)))
+    rc = -1;
+  FieldObj f = field_view(o);
+  if (!rc && (cudaMemcpyAsync(drt, rt, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, o->st) != cudaSuccess ||
+              (v && cudaMemcpyAsync(dv, v, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, o->st) != cudaSuccess) ||
+              cudaMemcpyAsync(dd, did, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, o->st) != cudaSuccess ||
+              cudaMemsetAsync(dout, 0, (size_t)n * nout * sizeof(cplx), o->st) != cudaSuccess)) {
+    gbi_set_error("gb_field_points: upload failed");
+    rc = -1;
+  }
+  if (!rc) rc = gbi_field(&f, mode, type, n, drt, dv, dd, dout, df, o->st);
+  if (!rc && cudaMemcpyAsync(out, dout, (size_t)n * nout * sizeof(cplx), cudaMemcpyDeviceToHost, o->st) != cudaSuccess) rc = -1;
+  if (!rc && flag && mode == 2 && cudaMemcpyAsync(flag, df, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess) rc = -1;
+  if (!rc && cudaStreamSynchronize(o->st) != cudaSuccess) rc = -1;
+  if (rc && !gb_last_error()[0]) gbi_set_error("gb_field_points failed");
+  cudaFree(drt); cudaFree(dv); cudaFree(dd); cudaFree(df); cudaFree(dout);
+  return rc;
+}
+
+extern "C" int gb_field_bd(gb_obj* o, int type, int n, const int* did, const int* t, const double* zt, void* out) {
+  if (n <= 0) return 0;
+  if (ensure_bv(o)) return -1;
+  int *dd = nullptr, *dt = nullptr;
+  double* dz = nullptr;
+  cplx* dout = nullptr;
+  int rc = 0;
+  if (dalloc((void**)&dd, (size_t)n * sizeof(int)) || dalloc((void**)&dt, (size_t)n * sizeof(int)) ||
+      dalloc((void**)&dz, (size_t)n * 2 * sizeof(double)) || dalloc((void**)&dout, (size_t)n * 6 * sizeof(cplx)))
+    rc = -1;
+  for (int i = 0; i < n && !rc; i++) {
+    if (did[i] < 0 || did[i] > o->m.MN || t[i] < 1 || t[i] > o->m.sb_Ne[did[i]]) {
+      gbi_set_error("gb_field_bd: point %d: domain %d element %d out of range", i, did[i], t[i]);
+      rc = -1;
+    }
+  }
+  FieldObj f = field_view(o);
+  if (!rc && (cudaMemcpyAsync(dd, did, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, o->st) != cudaSuccess ||
+              cudaMemcpyAsync(dt, t, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, o->st) != cudaSuccess ||
+              cudaMemcpyAsync(dz, zt, (size_t)n * 2 * sizeof(double), cudaMemcpyHostToDevice, o->st) != cudaSuccess))
+    rc = -1;
+  if (!rc) rc = gbi_field_bd(&f, type, n, dd, dt, dz, dout, o->st);
+  if (!rc && (cudaMemcpyAsync(out, dout, (size_t)n * 6 * sizeof(cplx), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+              cudaStreamSynchronize(o->st) != cudaSuccess))
+    rc = -1;
+  if (rc && !gb_last_error()[0]) gbi_set_error("gb_field_bd failed");
+  cudaFree(dd); cudaFree(dt); cudaFree(dz); cudaFree(dout);
+  return rc;
+}

@@ -1,0 +1,453 @@
+// gb_field.cu -- potentials and fields at arbitrary points (batched).
+//
+// Replaces, on the GPU:
+//   domain_id / fid_calc_solid_angle  reference setup2.c:871-978
+//   mEMP_s, EH_s, EH_mEMP_s           d3b1_field.c:12-209
+//   mEMP2_s (scattered potential and its directional derivative at the
+//            nodes of another object)  mo_solve.c:351-396
+//   EH_s_bd (fields on the boundary, own element integrated singularly)
+//                                     d3b1_field.c:238-279
+// One thread per point for the domain id (a sequential solid-angle sum in the
+// reference's element order, so that boundary and region decisions are the
+// reference's), one warp per point for the boundary-integral sums (lanes over
+// source elements).  A lane whose pair needs the GHN fallback
+// (|Re dF/dv| > CBD_SDF, d3b1_elem.c:296,314) gets it integrated by the whole
+// warp.
+#include "gb_quad.cuh"
+#include "gb_reduce.cuh"
+#include "gb_internal.h"
+#include "gb_fieldobj.cuh"
+
+extern "C" int gbi_upload_tables_field(const void* t) {
+  GB_CUDA(cudaMemcpyToSymbol(c_tab, t, sizeof(GbTables)));
+  return 0;
+}
+
+// ------------------------------------------------------------------ domain id
+__device__ __forceinline__ void cross3(const double a[3], const double b[3], double r[3]) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ int unit3(double a[3]) {
+  double n = norm3(a);
+  if (n == 0.0) return -1;
+  a[0] /= n; a[1] /= n; a[2] /= n;
+  return 0;
+}
+// solid angle of a triangle (r0,r1,r2) seen from the origin via its three
+// spherical angles; *onb = 1 if the origin lies on the triangle's plane
+__device__ __forceinline__ double tri_solid(const double r0[3], const double r1[3], const double r2[3], int* onb) {
+  double n01[3], n12[3], n20[3], nt[3];
+  cross3(r0, r1, n01);
+  cross3(r1, r2, n12);
+  cross3(r2, r0, n20);
+  cross3(n01, n20, nt);
+  double a0 = atan2(norm3(nt), -dot3(n01, n20));
+  cross3(n12, n01, nt);
+  double a1 = atan2(norm3(nt), -dot3(n12, n01));
+  cross3(n20, n12, nt);
+  double a2 = atan2(norm3(nt), -dot3(n20, n12));
+  double D = dot3(r0, n12);
+  if (D > 0.0) return a0 + a1 + a2 - GB_PI;
+  if (D < 0.0) return -(a0 + a1 + a2 - GB_PI);
+  *onb = 1;
+  return 0.0;
+}
+// element solid angle (reference fid_calc_solid_angle, setup2.c:871-942): the
+// quadrangle is split into (0,1,2) and (0,2,3) with unit corner vectors
+__device__ double elem_solid_angle(int quad, double r[4][3], int* onb) {
+  int nv = quad ? 4 : 3;
+  int st = 0;
+  for (int j = 0; j < nv; j++) st += unit3(r[j]);
+  if (st < 0) { *onb = 1; return 0.0; }
+  double om = tri_solid(r[0], r[1], r[2], onb);
+  if (*onb) return 0.0;
+  if (quad) {
+    om += tri_solid(r[0], r[2], r[3], onb);
+    if (*onb) return 0.0;
+  }
+  return om;
+}
+
+// sequential semantics of domain_id: per domain d in order, accumulate the
+// solid angles of its positively listed elements into Og[d] and subtract them
+// from Og[sd]; return at the first boundary hit or after domain d decides
+__device__ int domain_id_pt(const FieldObj& o, const double rt[3]) {
+  double Og[GB_MAXDOM];
+  for (int d = 0; d <= o.MN; d++) Og[d] = 0.0;
+  for (int d = 0; d <= o.MN; d++) {
+    const int* sid = o.sid + o.sb_off[d];
+    for (int i = 1; i <= o.sb_Ne[d]; i++) {
+      int s = sid[i];
+      if (s <= 0) continue;
+      double r[4][3];
+      for (int j = 0; j < 4; j++)
+        for (int k = 0; k < 3; k++) r[j][k] = o.corner[(size_t)s * 12 + j * 3 + k] - rt[k];
+      int onb = 0;
+      double om = elem_solid_angle(o.etype[s], r, &onb);
+      if (onb) return d;
+      Og[d] += om;
+      Og[o.sd[s]] -= om;
+    }
+    if (d == 0 && fabs(Og[0]) < 2.0 * GB_PI) return 0;
+    if (Og[d] > 2.0 * GB_PI) return d;
+  }
+  return -1;
+}
+
+__global__ void k_domain_id(FieldObj o, int n, const double* rt, int* did) {
+  int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  double r[3] = {rt[3 * p], rt[3 * p + 1], rt[3 * p + 2]};
+  did[p] = domain_id_pt(o, r);
+}
+
+// ------------------------------------------------------------------ field sums
+enum { FM_MEMP = 0, FM_EH = 1, FM_EH_MEMP = 2, FM_MEMP2 = 3 };
+
+// Per-lane GHN fallback of flagged pairs, integrated by the whole warp.
+template <int NDIR>
+__device__ void warp_fallback(bool fb, const Elem& S, const double rt[3], const double (*vt)[3], cplx k, bool neg,
+                              RegAcc<NDIR>& A) {
+  unsigned mask = __ballot_sync(0xffffffffu, fb);
+  const int lane = threadIdx.x & 31;
+  while (mask) {
+    int src = __ffs(mask) - 1;
+    mask &= mask - 1;
+    Elem Sb;
+    for (int i = 0; i < 12; i++) (&Sb.cr[0][0])[i] = __shfl_sync(0xffffffffu, (&S.cr[0][0])[i], src);
+    for (int i = 0; i < 9; i++) (&Sb.cw[0][0])[i] = __shfl_sync(0xffffffffu, (&S.cw[0][0])[i], src);
+    Sb.quad = __shfl_sync(0xffffffffu, S.quad, src);
+    bool negb = __shfl_sync(0xffffffffu, (int)neg, src) != 0;
+    RegAcc<NDIR> B;
+    reg_integrate_gh_part<NDIR>(Sb, lane, 32, rt, vt, k, B);
+    warp_allreduce<sizeof(RegAcc<NDIR>) / sizeof(double)>((double*)&B);
+    reg_finish<NDIR>(B, reg_scale_gh(Sb), negb);
+    if (lane == src) A = B;
+  }
+}
+
+struct FieldArgs {
+  FieldObj o;
+  int mode, type, n;
+  const double* rt;   // [n][3]
+  const double* v;    // [n][3] (FM_MEMP2)
+  const int* did;     // [n]
+  cplx* out;          // per point: FM_MEMP 4, FM_EH 6, FM_EH_MEMP 6, FM_MEMP2 8
+  int* flag;          // FM_EH_MEMP: -did where the near-boundary cutoff applies, else did
+};
+
+// one warp per point; the point's domain (and therefore its source list and
+// wave number) is uniform across the warp
+__global__ void __launch_bounds__(128) k_field(FieldArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= a.n) return;
+  const FieldObj& o = a.o;
+  int did = a.did[p];
+  if (did < 0 || did > o.MN) return;
+  double rt[3] = {a.rt[3 * p], a.rt[3 * p + 1], a.rt[3 * p + 2]};
+  cplx k = cmk(o.kn[2 * did], o.kn[2 * did + 1]);
+  const int* sid = o.sid + o.sb_off[did];
+  const int Ne = o.sb_Ne[did];
+  const cplx* U = o.U[did];
+  const cplx* dU = o.dU[did];
+  const cplx* Eb = o.E[did];
+  const cplx* dEb = o.dE[did];
+  const cplx* Hb = o.H[did];
+  const cplx* dHb = o.dH[did];
+  // accumulators (per lane), then reduced
+  double acc[34];
+  for (int i = 0; i < 34; i++) acc[i] = 0.0;
+  int niter = (Ne + 31) / 32;
+  for (int it = 0; it < niter; it++) {
+    int s = 1 + it * 32 + lane;
+    bool act = s <= Ne;
+    int sd = act ? sid[s] : sid[1];
+    Elem S;
+    load_elem(S, o.cr, o.cw, o.etype, abs(sd));
+    bool neg = sd < 0;
+    if (a.mode == FM_MEMP || a.mode == FM_EH) {
+      if (!act) continue;
+      RegAcc<0> A;
+      reg_integrate<0>(S, a.type, rt, nullptr, k, neg, A);
+      acc[0] += A.F;
+      if (a.mode == FM_MEMP) {
+        for (int n = 0; n < 4; n++)
+          for (int l = 0; l < 4; l++) {
+            cplx t = A.G[n] * dU[((size_t)s * 4 + n) * 4 + l] - A.H[n] * U[((size_t)s * 4 + n) * 4 + l];
+            acc[1 + 2 * l] += t.x;
+            acc[2 + 2 * l] += t.y;
+          }
+      } else {
+        for (int n = 0; n < 4; n++)
+          for (int l = 0; l < 3; l++) {
+            size_t q = ((size_t)s * 4 + n) * 3 + l;
+            cplx te = A.G[n] * dEb[q] - A.H[n] * Eb[q];
+            cplx th = A.G[n] * dHb[q] - A.H[n] * Hb[q];
+            acc[1 + 2 * l] += te.x;
+            acc[2 + 2 * l] += te.y;
+            acc[7 + 2 * l] += th.x;
+            acc[8 + 2 * l] += th.y;
+          }
+      }
+    } else if (a.mode == FM_MEMP2) {
+      double vt[1][3] = {{a.v[3 * p], a.v[3 * p + 1], a.v[3 * p + 2]}};
+      RegAcc<1> A;
+      bool fb = false;
+      if (act) {
+        reg_integrate<1>(S, a.type, rt, vt, k, neg, A);
+        fb = a.type < 3 && fabs(A.dF[0]) > GB_CBD_SDF;
+      }
+      warp_fallback<1>(fb, S, rt, vt, k, neg, A);
+      if (!act) continue;
+      acc[0] += A.F;
+      acc[1] += A.dF[0];
+      for (int n = 0; n < 4; n++)
+        for (int l = 0; l < 4; l++) {
+          size_t q = ((size_t)s * 4 + n) * 4 + l;
+          cplx u = A.G[n] * dU[q] - A.H[n] * U[q];
+          cplx du = A.dG[0][n] * dU[q] - A.dH[0][n] * U[q];
+          acc[2 + 2 * l] += u.x;
+          acc[3 + 2 * l] += u.y;
+          acc[10 + 2 * l] += du.x;
+          acc[11 + 2 * l] += du.y;
+        }
+    }
+  }
+  warp_allreduce<34>(acc);
+  if (lane != 0) return;
+  double F = acc[0];
+  double den = (did == 0) ? 1.0 + F : F;
+  cplx* out = a.out;
+  if (a.mode == FM_MEMP) {
+    for (int l = 0; l < 4; l++) out[(size_t)p * 4 + l] = cdivr(cmk(acc[1 + 2 * l], acc[2 + 2 * l]), den);
+  } else if (a.mode == FM_EH) {
+    for (int l = 0; l < 6; l++) out[(size_t)p * 6 + l] = cdivr(cmk(acc[1 + 2 * l], acc[2 + 2 * l]), den);
+  } else if (a.mode == FM_MEMP2) {
+    double dF = acc[1];
+    for (int l = 0; l < 4; l++) {
+      cplx u = cdivr(cmk(acc[2 + 2 * l], acc[3 + 2 * l]), den);
+      cplx du = cdivr(cmk(acc[10 + 2 * l], acc[11 + 2 * l]) - u * dF, den);
+      out[(size_t)p * 8 + l] = u;
+      out[(size_t)p * 8 + 4 + l] = du;
+    }
+  }
+}
+
+// FM_EH_MEMP (reference EH_mEMP_s): U and the x,y,z derivatives of all four
+// potential components; separate kernel because it needs 2 + 3 + 8 + 24
+// accumulators.
+__global__ void __launch_bounds__(128) k_field_eh_memp(FieldArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= a.n) return;
+  const FieldObj& o = a.o;
+  int did = a.did[p];
+  if (did < 0 || did > o.MN) return;
+  double rt[3] = {a.rt[3 * p], a.rt[3 * p + 1], a.rt[3 * p + 2]};
+  cplx k = cmk(o.kn[2 * did], o.kn[2 * did + 1]);
+  const int* sid = o.sid + o.sb_off[did];
+  const int Ne = o.sb_Ne[did];
+  const cplx* U = o.U[did];
+  const cplx* dU = o.dU[did];
+  double acc[36];  // F, dF[3], U[4] (8), dU[3][4] (24)
+  for (int i = 0; i < 36; i++) acc[i] = 0.0;
+  const double vt[3][3] = {{1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+  int niter = (Ne + 31) / 32;
+  for (int it = 0; it < niter; it++) {
+    int s = 1 + it * 32 + lane;
+    bool act = s <= Ne;
+    int sd = act ? sid[s] : sid[1];
+    Elem S;
+    load_elem(S, o.cr, o.cw, o.etype, abs(sd));
+    bool neg = sd < 0;
+    RegAcc<3> A;
+    bool fb[3] = {false, false, false};
+    if (act) {
+      reg_integrate<3>(S, a.type, rt, vt, k, neg, A);
+      if (a.type < 3)
+        for (int d = 0; d < 3; d++) fb[d] = fabs(A.dF[d]) > GB_CBD_SDF;
+    }
+    bool any = fb[0] || fb[1] || fb[2];
+    RegAcc<3> B = A;
+    warp_fallback<3>(any, S, rt, vt, k, neg, B);
+    if (!act) continue;
+    if (fb[2]) { for (int n = 0; n < 4; n++) { A.G[n] = B.G[n]; A.H[n] = B.H[n]; } A.F = B.F; }
+    for (int d = 0; d < 3; d++)
+      if (fb[d]) {
+        for (int n = 0; n < 4; n++) { A.dG[d][n] = B.dG[d][n]; A.dH[d][n] = B.dH[d][n]; }
+        A.dF[d] = B.dF[d];
+      }
+    acc[0] += A.F;
+    for (int d = 0; d < 3; d++) acc[1 + d] += A.dF[d];
+    for (int n = 0; n < 4; n++)
+      for (int l = 0; l < 4; l++) {
+        size_t q = ((size_t)s * 4 + n) * 4 + l;
+        cplx u = A.G[n] * dU[q] - A.H[n] * U[q];
+        acc[4 + 2 * l] += u.x;
+        acc[5 + 2 * l] += u.y;
+        for (int d = 0; d < 3; d++) {
+          cplx du = A.dG[d][n] * dU[q] - A.dH[d][n] * U[q];
+          acc[12 + d * 8 + 2 * l] += du.x;
+          acc[13 + d * 8 + 2 * l] += du.y;
+        }
+      }
+  }
+  warp_allreduce<36>(acc);
+  if (lane != 0) return;
+  double F = acc[0];
+  double den = (did == 0) ? 1.0 + F : F;
+  cplx Uv[4], dUv[3][4];
+  for (int l = 0; l < 4; l++) Uv[l] = cdivr(cmk(acc[4 + 2 * l], acc[5 + 2 * l]), den);
+  for (int d = 0; d < 3; d++)
+    for (int l = 0; l < 4; l++) dUv[d][l] = cdivr(cmk(acc[12 + d * 8 + 2 * l], acc[13 + d * 8 + 2 * l]) - Uv[l] * acc[1 + d], den);
+  cplx* out = a.out + (size_t)p * 6;
+  if (fabs(acc[1]) > GB_CBD_CDF || fabs(acc[2]) > GB_CBD_CDF || fabs(acc[3]) > GB_CBD_CDF) {
+    for (int i = 0; i < 6; i++) out[i] = cmk(0, 0);
+    a.flag[p] = -did;
+    return;
+  }
+  a.flag[p] = did;
+  for (int i = 0; i < 3; i++) out[i] = Uv[i] - dUv[i][3];
+  // ch = lambda0 / (2 pi i) = -i lambda0 / (2 pi)
+  cplx ch = cmk(0.0, -o.lambda0 / (2.0 * GB_PI));
+  out[3] = ch * (dUv[1][2] - dUv[2][1]);
+  out[4] = ch * (dUv[2][0] - dUv[0][2]);
+  out[5] = ch * (dUv[0][1] - dUv[1][0]);
+}
+
+// ------------------------------------------------------------------ on-boundary
+// Fields on the boundary of the own object (reference EH_s_bd): point on
+// element t (1-based index in domain did's list) at (zt, et); the pair s == t
+// is integrated singularly (coef_bd) by the whole warp.
+struct BdArgs {
+  FieldObj o;
+  int type, n;
+  const int* did;
+  const int* t;
+  const double* zt;  // [n][2]
+  cplx* out;         // [n][6]: E, H
+};
+
+__global__ void __launch_bounds__(128) k_field_bd(BdArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= a.n) return;
+  const FieldObj& o = a.o;
+  int did = a.did[p];
+  const int* sid = o.sid + o.sb_off[did];
+  const int Ne = o.sb_Ne[did];
+  int t = a.t[p];
+  int td = sid[t];
+  double zt = a.zt[2 * p], et = a.zt[2 * p + 1];
+  Elem T;
+  load_elem(T, o.cr, o.cw, o.etype, abs(td));
+  double rt[3];
+  for (int d = 0; d < 3; d++) {
+    rt[d] = T.cr[d][0] + T.cr[d][1] * zt + T.cr[d][2] * et;
+    if (T.quad) rt[d] += T.cr[d][3] * zt * et;
+  }
+  cplx k = cmk(o.kn[2 * did], o.kn[2 * did + 1]);
+  const cplx* Eb = o.E[did];
+  const cplx* dEb = o.dE[did];
+  const cplx* Hb = o.H[did];
+  const cplx* dHb = o.dH[did];
+  double acc[13];
+  for (int i = 0; i < 13; i++) acc[i] = 0.0;
+  for (int s = 1 + lane; s <= Ne; s += 32) {
+    int sd = sid[s];
+    if (sd == td) continue;
+    Elem S;
+    load_elem(S, o.cr, o.cw, o.etype, abs(sd));
+    RegAcc<0> A;
+    reg_integrate<0>(S, a.type, rt, nullptr, k, sd < 0, A);
+    acc[0] += A.F;
+    for (int n = 0; n < 4; n++)
+      for (int l = 0; l < 3; l++) {
+        size_t q = ((size_t)s * 4 + n) * 3 + l;
+        cplx te = A.G[n] * dEb[q] - A.H[n] * Eb[q];
+        cplx th = A.G[n] * dHb[q] - A.H[n] * Hb[q];
+        acc[1 + 2 * l] += te.x;
+        acc[2 + 2 * l] += te.y;
+        acc[7 + 2 * l] += th.x;
+        acc[8 + 2 * l] += th.y;
+      }
+  }
+  // singular self term
+  SingCtx c;
+  c.E = T;
+  c.zt = zt;
+  c.et = et;
+  c.k = k;
+  sing_setup(c);
+  SingAcc A;
+  singacc_zero(A);
+  int nit = sing_items(c, 0);
+  for (int q = lane; q < nit; q += 32) sing_item(c, q, A);
+  warp_allreduce<51>((double*)&A);
+  sing_finish(c, A, td < 0);
+  if (lane == 0) {
+    acc[0] += A.F;
+    for (int n = 0; n < 4; n++)
+      for (int l = 0; l < 3; l++) {
+        size_t q = ((size_t)t * 4 + n) * 3 + l;
+        cplx te = A.G[n] * dEb[q] - A.H[n] * Eb[q];
+        cplx th = A.G[n] * dHb[q] - A.H[n] * Hb[q];
+        acc[1 + 2 * l] += te.x;
+        acc[2 + 2 * l] += te.y;
+        acc[7 + 2 * l] += th.x;
+        acc[8 + 2 * l] += th.y;
+      }
+  }
+  warp_allreduce<13>(acc);
+  if (lane != 0) return;
+  double den = (did == 0) ? 1.0 + acc[0] : acc[0];
+  for (int l = 0; l < 6; l++) a.out[(size_t)p * 6 + l] = cdivr(cmk(acc[1 + 2 * l], acc[2 + 2 * l]), den);
+}
+
+// ------------------------------------------------------------------ launchers
+extern "C" int gbi_domain_id(const FieldObj* o, int n, const double* rt, int* did, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_domain_id<<<(n + 127) / 128, 128, 0, st>>>(*o, n, rt, did);
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+extern "C" int gbi_field(const FieldObj* o, int mode, int type, int n, const double* rt, const double* v, const int* did,
+                         cplx* out, int* flag, cudaStream_t st) {
+  if (n <= 0) return 0;
+  FieldArgs a;
+  a.o = *o;
+  a.mode = mode;
+  a.type = type;
+  a.n = n;
+  a.rt = rt;
+  a.v = v;
+  a.did = did;
+  a.out = out;
+  a.flag = flag;
+  unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
+  if (mode == FM_EH_MEMP) k_field_eh_memp<<<nb, 128, 0, st>>>(a);
+  else k_field<<<nb, 128, 0, st>>>(a);
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+extern "C" int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, const int* t, const double* zt, cplx* out,
+                            cudaStream_t st) {
+  if (n <= 0) return 0;
+  BdArgs a;
+  a.o = *o;
+  a.type = type;
+  a.n = n;
+  a.did = did;
+  a.t = t;
+  a.zt = zt;
+  a.out = out;
+  unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
+  k_field_bd<<<nb, 128, 0, st>>>(a);
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}

@@ -1,0 +1,43 @@
+// gb_internal.h -- declarations shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#define GB_MAXDOM 16
+
+// Device copy of one object's mesh (pointers are device addresses; the small
+// per-domain tables are host copies passed to kernels by value).
+typedef struct GbMeshDev {
+  int Ne, NN, MN;
+  double* cr;   // (Ne+1)*12
+  double* cw;   // (Ne+1)*9
+  double* ren;  // (Ne+1)*12
+  double* wen;  // (Ne+1)*12
+  int* etype;   // (Ne+1): 1 quadrangle, 0 triangle
+  int* eni;     // (Ne+1)*4
+  int* md;      // (Ne+1)
+  int* sd;      // (Ne+1)
+  int* sid;     // concatenated sid lists, domain d at sb_off[d] (1-based inside)
+  double* corner; // (Ne+1)*12 corner coordinates
+  int sb_Ne[GB_MAXDOM];
+  int sb_off[GB_MAXDOM + 1];
+  double kn[2 * GB_MAXDOM];
+} GbMeshDev;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+void gbi_set_error(const char* fmt, ...);
+#ifdef __cplusplus
+}
+#endif
+
+#define GB_CUDA(x)                                                                         \
+  do {                                                                                     \
+    cudaError_t e_ = (x);                                                                  \
+    if (e_ != cudaSuccess) {                                                               \
+      gbi_set_error("%s:%d %s: %s", __FILE__, __LINE__, #x, cudaGetErrorString(e_));       \
+      return -1;                                                                           \
+    }                                                                                      \
+  } while (0)

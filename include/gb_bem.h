@@ -1,0 +1,117 @@
+/*
+ * gb_bem.h -- C ABI of the GB300 BEM kernels (sm_103a).
+ *
+ * Plain pointers and sizes only.  Complex numbers are interleaved
+ * (real, imaginary) doubles, the memory layout of C99 `double complex`.
+ * Every entry point returns 0 on success and -1 on failure; gb_last_error()
+ * then describes the failure.  A gb_obj is one BEM object (one mesh with its
+ * media) resident in the GPU's memory: mesh, coefficient matrices, the
+ * inverse or LU factors of the coupled matrix A, and the boundary values.
+ *
+ * Each entry point replaces one stage of the reference (akohta/bem3_emf_b2);
+ * the file:line of the replaced code is given beside it.  The reference API
+ * (bem3_emf_b2.h) is implemented on top of these calls.
+ */
+#ifndef GB_BEM_H
+#define GB_BEM_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gb_obj gb_obj;
+
+/* Host description of one object, 1-based in the element index like the
+ * reference's BOUD (d3b1_elem.h:50-75): arrays have Ne+1 entries, slot 0
+ * unused. */
+typedef struct gb_mesh_desc {
+  int Ne;              /* elements */
+  int NN;              /* collocation nodes */
+  int MN;              /* media; domains are 0..MN */
+  const double *cr;    /* (Ne+1)*12: cr[e][xyz][a,b,c,d] */
+  const double *cw;    /* (Ne+1)*9:  cw[e][xyz][A,B,C] */
+  const double *ren;   /* (Ne+1)*12: collocation points ren[e][node][xyz] */
+  const double *wen;   /* (Ne+1)*12: normals at the collocation points */
+  const int *etype;    /* (Ne+1): 1 bilinear quadrangle, 0 linear triangle */
+  const int *eni;      /* (Ne+1)*4: collocation node ids (-1 unused) */
+  const int *md;       /* (Ne+1): main domain */
+  const int *sd;       /* (Ne+1): sub domain */
+  const double *kn;    /* 2*(MN+1): wave number of each domain (re, im) */
+  const int *sb_Ne;    /* MN+1: elements bounding each domain */
+  const int *sid;      /* sum_d (sb_Ne[d]+1): signed element ids, domain after domain, each list 1-based */
+  const double *corner;/* (Ne+1)*12: corner node coordinates rn[ed[e][j]] (solid angles) */
+  double lambda0;      /* vacuum wavelength */
+} gb_mesh_desc;
+
+const char *gb_last_error(void);
+int gb_device_count(void);
+
+int gb_obj_create(const gb_mesh_desc *m, gb_obj **out);
+void gb_obj_destroy(gb_obj *o);
+
+/* Coefficient matrices G, H (N x N), dG, dH (2N x N), dF (N x 3) of domain did,
+ * N = 4 sb_Ne[did], quadrature type 0..3 (4-point, 9/7-point, GLN, GHN; the
+ * reference uses 2).  Replaces create_cmatrix_domain, solve_bieq2.c:98-184. */
+int gb_assemble(gb_obj *o, int did, int type);
+/* copy the resident matrices of domain did to/from host buffers in the
+ * reference's .cmat layout (any pointer may be NULL to skip that matrix) */
+int gb_cmatrix_download(gb_obj *o, int did, void *G, void *H, void *dG, void *dH, double *dF);
+int gb_cmatrix_upload(gb_obj *o, int did, const void *G, const void *H, const void *dG, const void *dH, const double *dF);
+
+/* Coupled matrix A (na x na, na = 8 NN) from the resident G, H of all domains,
+ * LU-factorised with partial pivoting, and its explicit inverse.
+ * Replaces create_Amatrix_csr + lu_dec_A, solve_bieq2.c:186-408. */
+int gb_invA_compute(gb_obj *o);
+int gb_invA_download(gb_obj *o, void *invA);
+int gb_invA_upload(gb_obj *o, const void *invA);
+/* A alone (for tests): built from the resident G, H; not factorised */
+int gb_A_download(gb_obj *o, void *A);
+
+/* x <- invA b for host vectors of length na.  Replaces solve_ABmatrix,
+ * mo_solve.c:246-274. */
+int gb_solve_AB(gb_obj *o, const void *b, void *x);
+
+/* ---- boundary values and the multi-object iteration (reference mo_solve.c) ----
+ * Boundary values of domain did, reference layout: U, dU [(Ne_d+1)][4][4],
+ * E, dE, H, dH [(Ne_d+1)][4][3] (complex).  Incident potential per element:
+ * [(Ne+1)][4][4].  NULL pointers are skipped. */
+int gb_bv_upload(gb_obj *o, int did, const void *U, const void *dU, const void *E, const void *dE, const void *H, const void *dH);
+int gb_bv_download(gb_obj *o, int did, void *U, void *dU, void *E, void *dE, void *H, void *dH);
+int gb_incident_upload(gb_obj *o, const void *Ui0, const void *dUi0);      /* also sets Ui = Uip = Ui0, dUi = dUi0 */
+int gb_incident_download(gb_obj *o, void *Ui, void *dUi, void *Uip);
+/* B from the incident potential, X = invA B, U and dU of every domain
+ * (create_Bmatrix + solve_ABmatrix + tmatrix_bd_store, mo_solve.c:137-274,457) */
+int gb_solve_mEMP(gb_obj *o);
+/* Uip <- Ui, Ui <- Ui0, dUi <- dUi0 (reset_incident_bd, mo_solve.c:398-411) */
+int gb_reset_incident(gb_obj *o);
+/* dst.Ui, dst.dUi += potential scattered by src at dst's exterior nodes
+ * (add_scattered_mEMP, mo_solve.c:296-396); fails if a node lies inside src */
+int gb_add_scattered(gb_obj *dst, gb_obj *src, int type);
+/* sums of the convergence measure over the exterior nodes (ccd_f, mo_solve.c:413-455):
+ * out[0] sum of potential changes, out[1] sum of phi changes, out[2] node count */
+int gb_ccd_sums(gb_obj *o, double *out);
+/* E, H and dE/dn, dH/dn of every domain (solve_eh_bv, solve_deh_bv, mo_solve.c:547-789) */
+int gb_solve_EH(gb_obj *o);
+
+/* ---- points (reference setup2.c:944-978, d3b1_field.c, mo_field.c) ----
+ * rt: [n][3].  gb_domain_id: domain of each point (-1: none).
+ * gb_field_points, mode 0: potentials U[4] (mEMP_s); 1: E[3],H[3] (EH_s);
+ * 2: E[3],H[3] from potential derivatives (EH_mEMP_s; flag = -did where the
+ * near-boundary cutoff applied); 3: U[4], dU/dv[4] along v[n][3] (mEMP2_s).
+ * did: domain of each point (from gb_domain_id); type: quadrature 0..3.
+ * gb_field_bd: E[3],H[3] on the boundary (EH_s_bd) at element t (1-based in
+ * domain did's list), parameters zt[n][2]. */
+int gb_domain_id(gb_obj *o, int n, const double *rt, int *did);
+int gb_field_points(gb_obj *o, int mode, int type, int n, const double *rt, const double *v, const int *did, void *out, int *flag);
+int gb_field_bd(gb_obj *o, int type, int n, const int *did, const int *t, const double *zt, void *out);
+
+/* Dense complex FP64 LU solve of a host system: A (n x n, row-major) X = B
+ * (n x nrhs, row-major), B overwritten by X.  The kernel behind the dE/dn,
+ * dH/dn solve (LAPACKE_zgesv, mo_solve.c:751). */
+int gb_zgesv(int n, int nrhs, void *A, void *B);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
