@@ -48,6 +48,24 @@ __host__ __device__ __forceinline__ cplx cdivr(cplx a, double s) { return cmk(a.
 __host__ __device__ __forceinline__ cplx cmuli(cplx a) { return cmk(-a.y, a.x); }
 __host__ __device__ __forceinline__ double cabs2(cplx a) { return a.x * a.x + a.y * a.y; }
 
+// single-precision complex (the LU factors of the mixed-precision form)
+struct cplxf {
+  float x, y;
+};
+__host__ __device__ __forceinline__ cplxf cmkf(float a, float b) { cplxf r; r.x = a; r.y = b; return r; }
+__host__ __device__ __forceinline__ cplxf operator+(cplxf a, cplxf b) { return cmkf(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ cplxf operator-(cplxf a, cplxf b) { return cmkf(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ cplxf operator*(cplxf a, cplxf b) { return cmkf(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+__host__ __device__ __forceinline__ cplxf& operator+=(cplxf& a, cplxf b) { a.x += b.x; a.y += b.y; return a; }
+__host__ __device__ __forceinline__ cplxf& operator-=(cplxf& a, cplxf b) { a.x -= b.x; a.y -= b.y; return a; }
+__host__ __device__ __forceinline__ cplxf cdivc(cplxf a, cplxf b) {
+  float d = b.x * b.x + b.y * b.y;
+  return cmkf((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+template <class T> __host__ __device__ __forceinline__ T czero();
+template <> __host__ __device__ __forceinline__ cplx czero<cplx>() { return cmk(0.0, 0.0); }
+template <> __host__ __device__ __forceinline__ cplxf czero<cplxf>() { return cmkf(0.0f, 0.0f); }
+
 // e^{i k a} for complex k and real a >= 0
 __device__ __forceinline__ cplx cexpik(cplx k, double a) {
   double s, c;

@@ -113,10 +113,12 @@ extern "C" int gbi_build_A_domain(const cplx* G, const cplx* H, const int* sid, 
 
 // ------------------------------------------------------------------ LU
 __device__ __forceinline__ double cabs1(cplx a) { return fabs(a.x) + fabs(a.y); }
+__device__ __forceinline__ double cabs1(cplxf a) { return (double)(fabsf(a.x) + fabsf(a.y)); }
 
 // pivot search in column j over rows j..n-1, then the full-row interchange;
 // info[0] receives j+1 on an exactly zero pivot (LAPACK's info convention)
-__global__ void __launch_bounds__(1024) k_pivot_swap(cplx* A, size_t lda, int n, int j, int64_t* ipiv, int* info) {
+template <class T>
+__global__ void __launch_bounds__(1024) k_pivot_swap(T* A, size_t lda, int n, int j, int64_t* ipiv, int* info) {
   __shared__ double sv[32];
   __shared__ int si[32];
   double best = -1.0;
@@ -151,10 +153,10 @@ __global__ void __launch_bounds__(1024) k_pivot_swap(cplx* A, size_t lda, int n,
     if (!(sv[0] > 0.0) && info[0] == 0) info[0] = j + 1;
   }
   if (p != j) {
-    cplx* rj = A + (size_t)j * lda;
-    cplx* rp = A + (size_t)p * lda;
+    T* rj = A + (size_t)j * lda;
+    T* rp = A + (size_t)p * lda;
     for (int c = threadIdx.x; c < n; c += blockDim.x) {
-      cplx t = rj[c];
+      T t = rj[c];
       rj[c] = rp[c];
       rp[c] = t;
     }
@@ -162,15 +164,16 @@ __global__ void __launch_bounds__(1024) k_pivot_swap(cplx* A, size_t lda, int n,
 }
 
 // rows i > j: l = A[i][j] / A[j][j]; A[i][c] -= l A[j][c] for c in (j, kend)
-__global__ void k_panel_update(cplx* A, size_t lda, int n, int j, int kend) {
+template <class T>
+__global__ void k_panel_update(T* A, size_t lda, int n, int j, int kend) {
   int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int lane = threadIdx.x & 31;
   int i = j + 1 + warp;
   if (i >= n) return;
-  cplx piv = A[(size_t)j * lda + j];
-  cplx* ri = A + (size_t)i * lda;
-  const cplx* rj = A + (size_t)j * lda;
-  cplx l = (piv.x == 0.0 && piv.y == 0.0) ? ri[j] : cdivc(ri[j], piv);
+  T piv = A[(size_t)j * lda + j];
+  T* ri = A + (size_t)i * lda;
+  const T* rj = A + (size_t)j * lda;
+  T l = (piv.x == 0 && piv.y == 0) ? ri[j] : cdivc(ri[j], piv);
   for (int c = j + 1 + lane; c < kend; c += 32) ri[c] -= l * rj[c];
   if (lane == 0) ri[j] = l;
 }
@@ -179,15 +182,16 @@ __global__ void k_panel_update(cplx* A, size_t lda, int n, int j, int kend) {
 // triangle of A[k:k+nb][k:k+nb] (or, with upper = 1, X <- U11^-1 X with the
 // non-unit upper triangle), one thread per column.  Lsrc gives the triangle's
 // storage (row-major, leading dimension ldl).
-template <int UPPER>
-__global__ void __launch_bounds__(128) k_trsm_rows(const cplx* Lsrc, size_t ldl, cplx* X, size_t ldx, int nb, int c0,
+template <class T, int UPPER>
+__global__ void __launch_bounds__(128) k_trsm_rows(const T* Lsrc, size_t ldl, T* X, size_t ldx, int nb, int c0,
                                                    int c1) {
-  extern __shared__ cplx sL[];  // nb*nb
+  extern __shared__ __align__(16) unsigned char sLraw[];
+  T* sL = (T*)sLraw;  // nb*nb
   for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) sL[t] = Lsrc[(size_t)(t / nb) * ldl + (t % nb)];
   __syncthreads();
   int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= c1) return;
-  cplx x[LU_NB];
+  T x[LU_NB];
 #pragma unroll
   for (int i = 0; i < LU_NB; i++)
     if (i < nb) x[i] = X[(size_t)i * ldx + c];
@@ -195,7 +199,7 @@ __global__ void __launch_bounds__(128) k_trsm_rows(const cplx* Lsrc, size_t ldl,
 #pragma unroll
     for (int i = 0; i < LU_NB; i++) {
       if (i >= nb) break;
-      cplx s = x[i];
+      T s = x[i];
 #pragma unroll
       for (int jj = 0; jj < LU_NB; jj++) {
         if (jj >= i) break;
@@ -207,7 +211,7 @@ __global__ void __launch_bounds__(128) k_trsm_rows(const cplx* Lsrc, size_t ldl,
 #pragma unroll
     for (int i = LU_NB - 1; i >= 0; i--) {
       if (i >= nb) continue;
-      cplx s = x[i];
+      T s = x[i];
 #pragma unroll
       for (int jj = LU_NB - 1; jj >= 0; jj--) {
         if (jj <= i) break;
@@ -293,16 +297,17 @@ static int gemm_sub(int M, int N, int K, const cplx* A, size_t lda, const cplx* 
   return 0;
 }
 
-static int trsm_rows(int upper, const cplx* L, size_t ldl, cplx* X, size_t ldx, int nb, int c0, int c1, cudaStream_t st) {
+template <class T>
+static int trsm_rows(int upper, const T* L, size_t ldl, T* X, size_t ldx, int nb, int c0, int c1, cudaStream_t st) {
   if (c1 <= c0) return 0;
-  size_t sm = (size_t)nb * nb * sizeof(cplx);
+  size_t sm = (size_t)nb * nb * sizeof(T);
   unsigned nblk = (unsigned)((c1 - c0 + 127) / 128);
   if (upper) {
-    GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_trsm_rows<1><<<nblk, 128, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
+    GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_trsm_rows<T, 1><<<nblk, 128, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
   } else {
-    GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_trsm_rows<0><<<nblk, 128, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
+    GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    k_trsm_rows<T, 0><<<nblk, 128, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
   }
   GB_CUDA(cudaGetLastError());
   return 0;
@@ -311,39 +316,45 @@ static int trsm_rows(int upper, const cplx* L, size_t ldl, cplx* X, size_t ldx, 
 // In-place LU of the n x n row-major matrix A (lda); ipiv[j] = 0-based row
 // interchanged with row j (rows are swapped across the full width).
 // info (device int) receives LAPACK's info (0: success).
-extern "C" int gbi_zgetrf(cplx* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st) {
+template <class T, class GEMM>
+static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st, GEMM gemm) {
   GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), st));
   for (int k = 0; k < n; k += LU_NB) {
     int nb = (n - k < LU_NB) ? n - k : LU_NB;
     int kend = k + nb;
     for (int j = k; j < kend; j++) {
-      k_pivot_swap<<<1, 1024, 0, st>>>(A, lda, n, j, ipiv, info);
+      k_pivot_swap<T><<<1, 1024, 0, st>>>(A, lda, n, j, ipiv, info);
       GB_CUDA(cudaGetLastError());
       int rows = n - j - 1;
       if (rows > 0) {
         unsigned nbk = (unsigned)((rows * 32 + 255) / 256);
-        k_panel_update<<<nbk, 256, 0, st>>>(A, lda, n, j, kend);
+        k_panel_update<T><<<nbk, 256, 0, st>>>(A, lda, n, j, kend);
         GB_CUDA(cudaGetLastError());
       }
     }
     if (kend < n) {
-      if (trsm_rows(0, A + (size_t)k * lda + k, lda, A + (size_t)k * lda, lda, nb, kend, n, st)) return -1;
-      if (gemm_sub(n - kend, n - kend, nb, A + (size_t)kend * lda + k, lda, A + (size_t)k * lda + kend, lda,
-                   A + (size_t)kend * lda + kend, lda, st))
+      if (trsm_rows<T>(0, A + (size_t)k * lda + k, lda, A + (size_t)k * lda, lda, nb, kend, n, st)) return -1;
+      if (gemm(n - kend, n - kend, nb, A + (size_t)kend * lda + k, lda, A + (size_t)k * lda + kend, lda,
+               A + (size_t)kend * lda + kend, lda, st))
         return -1;
     }
   }
   return 0;
 }
 
+extern "C" int gbi_zgetrf(cplx* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st) {
+  return lu_factor<cplx>(A, lda, n, ipiv, info, st, gemm_sub);
+}
+
 // apply the row interchanges of zgetrf to X (n rows, ncol columns)
-__global__ void k_laswp(cplx* X, size_t ldx, int n, int ncol, const int64_t* ipiv) {
+template <class T>
+__global__ void k_laswp(T* X, size_t ldx, int n, int ncol, const int64_t* ipiv) {
   int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= ncol) return;
   for (int j = 0; j < n; j++) {
     int p = (int)ipiv[j];
     if (p != j) {
-      cplx t = X[(size_t)j * ldx + c];
+      T t = X[(size_t)j * ldx + c];
       X[(size_t)j * ldx + c] = X[(size_t)p * ldx + c];
       X[(size_t)p * ldx + c] = t;
     }
@@ -355,11 +366,11 @@ __global__ void k_laswp(cplx* X, size_t ldx, int n, int ncol, const int64_t* ipi
 // GEMM update of the remaining rows.
 extern "C" int gbi_zgetrs(const cplx* LU, size_t lda, int n, const int64_t* ipiv, cplx* X, size_t ldx, int nrhs,
                           cudaStream_t st) {
-  k_laswp<<<(nrhs + 127) / 128, 128, 0, st>>>(X, ldx, n, nrhs, ipiv);
+  k_laswp<cplx><<<(nrhs + 127) / 128, 128, 0, st>>>(X, ldx, n, nrhs, ipiv);
   GB_CUDA(cudaGetLastError());
   for (int k = 0; k < n; k += LU_NB) {  // forward: L Y = P B
     int nb = (n - k < LU_NB) ? n - k : LU_NB;
-    if (trsm_rows(0, LU + (size_t)k * lda + k, lda, X + (size_t)k * ldx, ldx, nb, 0, nrhs, st)) return -1;
+    if (trsm_rows<cplx>(0, LU + (size_t)k * lda + k, lda, X + (size_t)k * ldx, ldx, nb, 0, nrhs, st)) return -1;
     if (gemm_sub(n - k - nb, nrhs, nb, LU + (size_t)(k + nb) * lda + k, lda, X + (size_t)k * ldx, ldx,
                  X + (size_t)(k + nb) * ldx, ldx, st))
       return -1;
@@ -367,7 +378,7 @@ extern "C" int gbi_zgetrs(const cplx* LU, size_t lda, int n, const int64_t* ipiv
   int last = ((n - 1) / LU_NB) * LU_NB;
   for (int k = last; k >= 0; k -= LU_NB) {  // backward: U X = Y
     int nb = (n - k < LU_NB) ? n - k : LU_NB;
-    if (trsm_rows(1, LU + (size_t)k * lda + k, lda, X + (size_t)k * ldx, ldx, nb, 0, nrhs, st)) return -1;
+    if (trsm_rows<cplx>(1, LU + (size_t)k * lda + k, lda, X + (size_t)k * ldx, ldx, nb, 0, nrhs, st)) return -1;
     if (gemm_sub(k, nrhs, nb, LU + k, lda, X + (size_t)k * ldx, ldx, X, ldx, st)) return -1;
   }
   return 0;
