@@ -1,0 +1,108 @@
+"""GB300-native BEM hot path of bem3_emf_b2 (boundary-integral assembly, dense
+complex LU/inverse, multi-object iteration, field and force sums) behind the
+reference's C API.
+
+The product is the in-tree shared library ``_build/libbem3gb.so`` (C host
+library + sm_103a CUDA kernels, C ABI in include/gb_bem.h, include/gb_scene.h,
+include/bem3_emf_b2.h) and the drop-in tools next to it.  This module only
+loads that library for Python callers (tests, bench): there is no Python or
+CPU implementation of the kernels, and a missing library is an error.
+"""
+import ctypes
+import os
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(PKG, "_build")
+LIBPATH = os.path.join(BUILD, "libbem3gb.so")
+
+_lib = None
+
+
+def lib():
+    """The loaded libbem3gb.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIBPATH):
+        raise RuntimeError("libbem3gb.so is not built (run bem3_emf_b2_gb300.build.build()); "
+                           "the BEM kernels have no fallback")
+    L = ctypes.CDLL(LIBPATH)
+    c_int, c_dbl, vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+    L.gb_last_error.restype = ctypes.c_char_p
+    L.gb_device_count.restype = c_int
+    L.gb_zgesv.argtypes = [c_int, c_int, vp, vp]
+    L.gb_zgesv.restype = c_int
+    L.gbh_scene_open.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
+    L.gbh_scene_open.restype = vp
+    L.gbh_scene_step.argtypes = [vp, c_int, c_int, vp, vp, vp]
+    L.gbh_scene_step.restype = c_int
+    L.gbh_scene_drop_device.argtypes = [vp]
+    L.gbh_scene_h2d_bytes.argtypes = [vp]
+    L.gbh_scene_h2d_bytes.restype = ctypes.c_size_t
+    L.gbh_scene_d2h_bytes.argtypes = [vp]
+    L.gbh_scene_d2h_bytes.restype = ctypes.c_size_t
+    L.gbh_scene_close.argtypes = [vp]
+    L.gbh_scene_stream.argtypes = [vp]
+    L.gbh_scene_stream.restype = vp
+    L.gb_launch_count.restype = ctypes.c_ulonglong
+    L.gbh_scene_obj.argtypes = [vp]
+    L.gbh_scene_obj.restype = vp
+    for name in ("gb_assemble",):
+        getattr(L, name).argtypes = [vp, c_int, c_int]
+    for name in ("gb_invA_compute", "gb_factor_mixed", "gb_solve_mEMP", "gb_solve_EH"):
+        getattr(L, name).argtypes = [vp]
+        getattr(L, name).restype = c_int
+    L.gb_ir_info.argtypes = [vp, vp, vp]
+    _lib = L
+    return L
+
+
+def last_error():
+    return lib().gb_last_error().decode()
+
+
+class Scene:
+    """A single-object scene set up from the reference's input files and
+    solved on the GPU (gb_scene.h)."""
+
+    def __init__(self, medium, mesh, ipw):
+        L = lib()
+        self.h = L.gbh_scene_open(medium.encode(), mesh.encode(), ipw.encode())
+        if not self.h:
+            raise RuntimeError("gbh_scene_open failed")
+
+    def step(self, form=1, type_=2, rc=(0.0, 0.0, 0.0)):
+        import numpy as np
+        rcv = np.ascontiguousarray(rc, float)
+        F = np.zeros(3)
+        N = np.zeros(3)
+        rc_ = lib().gbh_scene_step(self.h, form, type_, rcv.ctypes.data, F.ctypes.data, N.ctypes.data)
+        if rc_ != 0:
+            raise RuntimeError("gbh_scene_step failed: %s" % last_error())
+        return F, N
+
+    def drop_device(self):
+        lib().gbh_scene_drop_device(self.h)
+
+    def h2d_bytes(self):
+        return int(lib().gbh_scene_h2d_bytes(self.h))
+
+    def d2h_bytes(self):
+        return int(lib().gbh_scene_d2h_bytes(self.h))
+
+    def stream(self):
+        return lib().gbh_scene_stream(self.h)
+
+    def obj(self):
+        return lib().gbh_scene_obj(self.h)
+
+    def ir_info(self):
+        it = ctypes.c_int(0)
+        rr = ctypes.c_double(0.0)
+        lib().gb_ir_info(self.obj(), ctypes.byref(it), ctypes.byref(rr))
+        return it.value, rr.value
+
+    def close(self):
+        if self.h:
+            lib().gbh_scene_close(self.h)
+            self.h = None

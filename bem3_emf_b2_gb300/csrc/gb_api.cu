@@ -39,6 +39,11 @@ int gbi_field(const FieldObj* o, int mode, int type, int n, const double* rt, co
               int* flag, cudaStream_t st);
 int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, const int* t, const double* zt, cplx* out,
                  cudaStream_t st);
+int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
+int gbi_to_c64(const cplx* a, cplxf* b, size_t n, cudaStream_t st);
+int gbi_residual(const cplx* A, size_t lda, int n, const cplx* x, const cplx* b, cplx* r, double* nrm, cudaStream_t st);
+int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, const cplxf* LU32, size_t lda, int n, const int64_t* ipiv,
+                cudaStream_t st);
 }
 
 // ------------------------------------------------------------------ errors
@@ -50,6 +55,13 @@ extern "C" void gbi_set_error(const char* fmt, ...) {
   va_end(ap);
 }
 extern "C" const char* gb_last_error(void) { return g_err; }
+
+// number of kernel launches made by this library (all threads)
+#include <atomic>
+static std::atomic<unsigned long long> g_launches{0};
+extern "C" void gbi_count_launch(void) { g_launches.fetch_add(1, std::memory_order_relaxed); }
+extern "C" unsigned long long gb_launch_count(void) { return g_launches.load(); }
+extern "C" void* gb_obj_stream(gb_obj* o);
 
 // ------------------------------------------------------------------ tables
 static std::mutex g_init_mu;
@@ -115,6 +127,13 @@ struct gb_obj {
   size_t na;
   cplx* invA;             // na x na
   int have_invA;
+  // mixed-precision form: FP64 A kept for the residuals, complex FP32 LU factors
+  cplx* A64;
+  cplxf* LU32;
+  int64_t* ipiv32;
+  int have_lu32;
+  int ir_iters;
+  double ir_relres;
   // boundary values per domain, [(Ne_d+1)][4][4] (U, dU) and [(Ne_d+1)][4][3] (E, dE, H, dH)
   cplx* bU[GB_MAXDOM];
   cplx* bdU[GB_MAXDOM];
@@ -153,6 +172,7 @@ extern "C" void gb_obj_destroy(gb_obj* o) {
     cudaFree(o->rowk[d]);
   }
   cudaFree(o->invA);
+  cudaFree(o->A64); cudaFree(o->LU32); cudaFree(o->ipiv32);
   for (int d = 0; d < GB_MAXDOM; d++) {
     cudaFree(o->bU[d]); cudaFree(o->bdU[d]); cudaFree(o->bE[d]); cudaFree(o->bdE[d]); cudaFree(o->bH[d]); cudaFree(o->bdH[d]);
   }
@@ -172,6 +192,7 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   for (int d = 0; d < GB_MAXDOM; d++) { o->G[d] = o->H[d] = o->dG[d] = o->dH[d] = nullptr; o->dF[d] = nullptr; o->rowk[d] = nullptr; }
   o->invA = nullptr;
   o->have_invA = 0;
+  o->A64 = nullptr; o->LU32 = nullptr; o->ipiv32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
   for (int d = 0; d < GB_MAXDOM; d++) o->bU[d] = o->bdU[d] = o->bE[d] = o->bdE[d] = o->bH[d] = o->bdH[d] = nullptr;
   o->Ui = o->dUi = o->Ui0 = o->dUi0 = o->Uip = nullptr;
   o->next = 0;
@@ -273,6 +294,7 @@ extern "C" int gb_assemble(gb_obj* o, int did, int type) {
   if (rc) return -1;
   if (e != cudaSuccess) { gbi_set_error("gb_assemble: %s", cudaGetErrorString(e)); return -1; }
   o->have_invA = 0;
+  o->have_lu32 = 0;
   return 0;
 }
 
@@ -509,8 +531,10 @@ static int sync_obj(gb_obj* o, const char* what) {
   return 0;
 }
 
+static int ir_solve(gb_obj* o, const cplx* B, cplx* X);
+
 extern "C" int gb_solve_mEMP(gb_obj* o) {
-  if (!o->have_invA) { gbi_set_error("gb_solve_mEMP: no inverse of A"); return -1; }
+  if (!o->have_invA && !o->have_lu32) { gbi_set_error("gb_solve_mEMP: A is neither inverted nor factorised"); return -1; }
   if (ensure_bv(o)) return -1;
   size_t na = o->na;
   cplx *B = nullptr, *X = nullptr;
@@ -523,7 +547,7 @@ extern "C" int gb_solve_mEMP(gb_obj* o) {
                      o->nrows[d], base, B, o->st);
     base += 4 * (size_t)o->nrows[d];
   }
-  if (!rc) rc = gbi_zgemv(o->invA, na, (int)na, (int)na, B, X, o->st);
+  if (!rc) rc = o->have_invA ? gbi_zgemv(o->invA, na, (int)na, (int)na, B, X, o->st) : ir_solve(o, B, X);
   for (int d = 0; d <= o->m.MN && !rc; d++) rc = gbi_store_bv(X, &o->m, o->kn_dev, o->Ui, o->dUi, d, o->bU[d], o->bdU[d], o->st);
   if (!rc) rc = sync_obj(o, "gb_solve_mEMP");
   cudaFree(B);
@@ -720,3 +744,84 @@ extern "C" int gb_field_bd(gb_obj* o, int type, int n, const int* did, const int
   cudaFree(dd); cudaFree(dt); cudaFree(dz); cudaFree(dout);
   return rc;
 }
+
+// ------------------------------------------------------------------ mixed precision
+// Complex FP32 LU of A (partial pivoting), FP64 A kept for the residuals.
+extern "C" int gb_factor_mixed(gb_obj* o) {
+  size_t na = o->na;
+  int* info = nullptr;
+  if (!o->A64 && dalloc((void**)&o->A64, na * na * sizeof(cplx))) return -1;
+  if (!o->LU32 && dalloc((void**)&o->LU32, na * na * sizeof(cplxf))) return -1;
+  if (!o->ipiv32 && dalloc((void**)&o->ipiv32, na * sizeof(int64_t))) return -1;
+  if (dalloc((void**)&info, sizeof(int))) return -1;
+  int rc = build_A(o, o->A64);
+  if (!rc) rc = gbi_to_c64(o->A64, o->LU32, na * na, o->st);
+  if (!rc) rc = gbi_cgetrf(o->LU32, na, (int)na, o->ipiv32, info, o->st);
+  int hinfo = 0;
+  if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+              cudaStreamSynchronize(o->st) != cudaSuccess)) {
+    gbi_set_error("gb_factor_mixed: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
+  }
+  if (!rc && hinfo) { gbi_set_error("gb_factor_mixed: FP32 factor singular (info=%d)", hinfo); rc = -1; }
+  cudaFree(info);
+  if (!rc) { o->have_lu32 = 1; o->have_invA = 0; }
+  return rc;
+}
+
+// FP64 iterative refinement with the FP32 factors: x <- x + LU32^-1 (b - A x)
+// until ||b - A x|| <= 1e-13 ||b|| (at most 30 corrections)
+static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
+  size_t na = o->na;
+  cplx* r = nullptr;
+  cplxf* d = nullptr;
+  double* nrm = nullptr;
+  if (dalloc((void**)&r, na * sizeof(cplx)) || dalloc((void**)&d, na * sizeof(cplxf)) ||
+      dalloc((void**)&nrm, 2 * sizeof(double))) {
+    cudaFree(r); cudaFree(d);
+    return -1;
+  }
+  int rc = 0;
+  if (cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess ||
+      cudaMemcpyAsync(r, B, na * sizeof(cplx), cudaMemcpyDeviceToDevice, o->st) != cudaSuccess)
+    rc = -1;
+  double h[2] = {0.0, 1.0}, rel = 1.0;
+  int it = 0;
+  for (; !rc && it < 31; it++) {
+    if (it > 0) {
+      rc = gbi_residual(o->A64, na, (int)na, X, B, r, nrm, o->st);
+      if (rc) break;
+      if (cudaMemcpyAsync(h, nrm, 2 * sizeof(double), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+          cudaStreamSynchronize(o->st) != cudaSuccess) { rc = -1; break; }
+      rel = (h[1] > 0.0) ? sqrt(h[0] / h[1]) : 0.0;
+      if (rel <= 1e-13) break;
+    }
+    rc = gbi_ir_step(X, r, d, o->LU32, na, (int)na, o->ipiv32, o->st);
+  }
+  o->ir_iters = it;
+  o->ir_relres = rel;
+  if (!rc && rel > 1e-10) { gbi_set_error("iterative refinement stalled at relative residual %g", rel); rc = -1; }
+  cudaFree(r); cudaFree(d); cudaFree(nrm);
+  return rc;
+}
+
+extern "C" int gb_ir_info(gb_obj* o, int* iters, double* relres) {
+  *iters = o->ir_iters;
+  *relres = o->ir_relres;
+  return 0;
+}
+
+// One scene step on the device for a single object: assembly of every
+// domain (quadrature type), factorisation of A (form 0: FP64 LU and explicit
+// inverse; form 1: complex FP32 LU + FP64 refinement), boundary values U,dU,
+// then E, H and their normal derivatives.
+extern "C" int gb_scene_step(gb_obj* o, int form, int type) {
+  for (int d = 0; d <= o->m.MN; d++)
+    if (gb_assemble(o, d, type)) return -1;
+  if (form == 0) { if (gb_invA_compute(o)) return -1; }
+  else if (gb_factor_mixed(o)) return -1;
+  if (gb_solve_mEMP(o)) return -1;
+  return gb_solve_EH(o);
+}
+
+extern "C" void* gb_obj_stream(gb_obj* o) { return (void*)o->st; }

@@ -231,10 +231,13 @@ extern "C" int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* 
   size_t npair = N * (size_t)Ne;
   unsigned nb = (unsigned)((npair + 127) / 128);
   k_asm_regular<<<nb, 128, 0, st>>>(a);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   k_asm_singular<<<(unsigned)N, 256, 0, st>>>(a);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   k_asm_rows<<<(unsigned)((N + 127) / 128), 128, 0, st>>>(a);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }

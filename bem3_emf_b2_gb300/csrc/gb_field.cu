@@ -411,6 +411,7 @@ __global__ void __launch_bounds__(128) k_field_bd(BdArgs a) {
 extern "C" int gbi_domain_id(const FieldObj* o, int n, const double* rt, int* did, cudaStream_t st) {
   if (n <= 0) return 0;
   k_domain_id<<<(n + 127) / 128, 128, 0, st>>>(*o, n, rt, did);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -431,6 +432,7 @@ extern "C" int gbi_field(const FieldObj* o, int mode, int type, int n, const dou
   unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
   if (mode == FM_EH_MEMP) k_field_eh_memp<<<nb, 128, 0, st>>>(a);
   else k_field<<<nb, 128, 0, st>>>(a);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -448,6 +450,7 @@ extern "C" int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, 
   a.out = out;
   unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
   k_field_bd<<<nb, 128, 0, st>>>(a);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }

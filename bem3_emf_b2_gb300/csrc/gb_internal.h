@@ -29,6 +29,7 @@ typedef struct GbMeshDev {
 extern "C" {
 #endif
 void gbi_set_error(const char* fmt, ...);
+void gbi_count_launch(void);
 #ifdef __cplusplus
 }
 #endif

@@ -107,6 +107,7 @@ extern "C" int gbi_build_A_domain(const cplx* G, const cplx* H, const int* sid, 
   size_t tot = 16 * (size_t)a.Ne * a.Ne;
   if (tot == 0) return 0;
   k_build_A<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(a);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -293,6 +294,7 @@ static int gemm_sub(int M, int N, int K, const cplx* A, size_t lda, const cplx* 
   if (M <= 0 || N <= 0 || K <= 0) return 0;
   dim3 grid((N + GT_BN - 1) / GT_BN, (M + GT_BM - 1) / GT_BM);
   k_zgemm_nn<<<grid, 256, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -305,9 +307,11 @@ static int trsm_rows(int upper, const T* L, size_t ldl, T* X, size_t ldx, int nb
   if (upper) {
     GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_trsm_rows<T, 1><<<nblk, 128, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
+    gbi_count_launch();
   } else {
     GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
     k_trsm_rows<T, 0><<<nblk, 128, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
+    gbi_count_launch();
   }
   GB_CUDA(cudaGetLastError());
   return 0;
@@ -324,11 +328,13 @@ static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStre
     int kend = k + nb;
     for (int j = k; j < kend; j++) {
       k_pivot_swap<T><<<1, 1024, 0, st>>>(A, lda, n, j, ipiv, info);
+      gbi_count_launch();
       GB_CUDA(cudaGetLastError());
       int rows = n - j - 1;
       if (rows > 0) {
         unsigned nbk = (unsigned)((rows * 32 + 255) / 256);
         k_panel_update<T><<<nbk, 256, 0, st>>>(A, lda, n, j, kend);
+        gbi_count_launch();
         GB_CUDA(cudaGetLastError());
       }
     }
@@ -367,6 +373,7 @@ __global__ void k_laswp(T* X, size_t ldx, int n, int ncol, const int64_t* ipiv) 
 extern "C" int gbi_zgetrs(const cplx* LU, size_t lda, int n, const int64_t* ipiv, cplx* X, size_t ldx, int nrhs,
                           cudaStream_t st) {
   k_laswp<cplx><<<(nrhs + 127) / 128, 128, 0, st>>>(X, ldx, n, nrhs, ipiv);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   for (int k = 0; k < n; k += LU_NB) {  // forward: L Y = P B
     int nb = (n - k < LU_NB) ? n - k : LU_NB;
@@ -396,6 +403,7 @@ extern "C" int gbi_zinverse(const cplx* LU, size_t lda, int n, const int64_t* ip
                             cudaStream_t st) {
   size_t nn = (size_t)n * n;
   k_set_identity<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(X, ldx, n);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return gbi_zgetrs(LU, lda, n, ipiv, X, ldx, n, st);
 }
@@ -424,6 +432,7 @@ __global__ void k_zgemv(const cplx* __restrict__ M, size_t ldm, int n, int ncol,
 extern "C" int gbi_zgemv(const cplx* M, size_t ldm, int n, int ncol, const cplx* x, cplx* y, cudaStream_t st) {
   unsigned nb = (unsigned)(((size_t)n * 32 + 255) / 256);
   k_zgemv<<<nb, 256, 0, st>>>(M, ldm, n, ncol, x, y);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -432,4 +441,250 @@ extern "C" int gbi_zgemv(const cplx* M, size_t ldm, int n, int ncol, const cplx*
 extern "C" int gbi_zgemm_sub(int M, int N, int K, const cplx* A, size_t lda, const cplx* B, size_t ldb, cplx* C,
                              size_t ldc, cudaStream_t st) {
   return gemm_sub(M, N, K, A, lda, B, ldb, C, ldc, st);
+}
+
+// ==================================================================== FP32
+// Mixed-precision form: complex FP32 factors of A, refined in FP64 against
+// the FP64 matrix (the residual b - A x is always formed in FP64).
+
+// C[M][N] -= A[M][K] B[K][N], complex FP32, row-major.  64 x 128 output tile
+// per 256-thread block, each thread a 4 x 8 complex sub-tile.
+#define CG_BM 64
+#define CG_BN 128
+#define CG_BK 16
+__global__ void __launch_bounds__(256) k_cgemm_nn(int M, int N, int K, const cplxf* __restrict__ A, size_t lda,
+                                                  const cplxf* __restrict__ B, size_t ldb, cplxf* C, size_t ldc) {
+  __shared__ cplxf As[CG_BK][CG_BM];
+  __shared__ cplxf Bs[CG_BK][CG_BN];
+  int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  int m0 = blockIdx.y * CG_BM, n0 = blockIdx.x * CG_BN;
+  float accr[4][8], acci[4][8];
+#pragma unroll
+  for (int i = 0; i < 4; i++)
+#pragma unroll
+    for (int j = 0; j < 8; j++) { accr[i][j] = 0.f; acci[i][j] = 0.f; }
+  for (int k0 = 0; k0 < K; k0 += CG_BK) {
+    for (int t = threadIdx.x; t < CG_BK * CG_BM; t += 256) {
+      int kk = t % CG_BK, mm = t / CG_BK;
+      int gm = m0 + mm, gk = k0 + kk;
+      As[kk][mm] = (gm < M && gk < K) ? A[(size_t)gm * lda + gk] : cmkf(0.f, 0.f);
+    }
+    for (int t = threadIdx.x; t < CG_BK * CG_BN; t += 256) {
+      int nn = t % CG_BN, kk = t / CG_BN;
+      int gn = n0 + nn, gk = k0 + kk;
+      Bs[kk][nn] = (gn < N && gk < K) ? B[(size_t)gk * ldb + gn] : cmkf(0.f, 0.f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < CG_BK; kk++) {
+      cplxf a[4], b[8];
+#pragma unroll
+      for (int i = 0; i < 4; i++) a[i] = As[kk][ty + 16 * i];
+#pragma unroll
+      for (int j = 0; j < 8; j++) b[j] = Bs[kk][tx + 16 * j];
+#pragma unroll
+      for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int j = 0; j < 8; j++) {
+          accr[i][j] = fmaf(a[i].x, b[j].x, accr[i][j]);
+          accr[i][j] = fmaf(-a[i].y, b[j].y, accr[i][j]);
+          acci[i][j] = fmaf(a[i].x, b[j].y, acci[i][j]);
+          acci[i][j] = fmaf(a[i].y, b[j].x, acci[i][j]);
+        }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    int gm = m0 + ty + 16 * i;
+    if (gm >= M) continue;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      int gn = n0 + tx + 16 * j;
+      if (gn >= N) continue;
+      cplxf* c = C + (size_t)gm * ldc + gn;
+      c->x -= accr[i][j];
+      c->y -= acci[i][j];
+    }
+  }
+}
+
+static int cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, const cplxf* B, size_t ldb, cplxf* C, size_t ldc,
+                     cudaStream_t st) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  dim3 grid((N + CG_BN - 1) / CG_BN, (M + CG_BM - 1) / CG_BM);
+  k_cgemm_nn<<<grid, 256, 0, st>>>(M, N, K, A, lda, B, ldb, C, ldc);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+extern "C" int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st) {
+  return lu_factor<cplxf>(A, lda, n, ipiv, info, st, cgemm_sub);
+}
+
+extern "C" int gbi_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, const cplxf* B, size_t ldb, cplxf* C,
+                             size_t ldc, cudaStream_t st) {
+  return cgemm_sub(M, N, K, A, lda, B, ldb, C, ldc, st);
+}
+
+__global__ void k_to_c64(const cplx* __restrict__ a, cplxf* __restrict__ b, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) b[i] = cmkf((float)a[i].x, (float)a[i].y);
+}
+extern "C" int gbi_to_c64(const cplx* a, cplxf* b, size_t n, cudaStream_t st) {
+  k_to_c64<<<152 * 8, 256, 0, st>>>(a, b, n);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// ---- single right-hand side solve with LU factors (row-major, in place on x)
+// x <- P x (interchanges in order)
+template <class T>
+__global__ void k_perm1(T* x, int n, const int64_t* ipiv) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int j = 0; j < n; j++) {
+    int p = (int)ipiv[j];
+    if (p != j) { T t = x[j]; x[j] = x[p]; x[p] = t; }
+  }
+}
+// diagonal block k0..k0+nb-1: unit lower (UPPER = 0) or non-unit upper solve,
+// column-oriented sweep, one thread per row of the block
+template <class T, int UPPER>
+__global__ void k_trsv_diag(const T* LU, size_t lda, int k0, int nb, T* x) {
+  __shared__ T xs[LU_NB];
+  int i = threadIdx.x;
+  if (i < nb) xs[i] = x[k0 + i];
+  __syncthreads();
+  if (!UPPER) {
+    for (int j = 0; j < nb; j++) {
+      T xj = xs[j];
+      __syncthreads();
+      if (i > j && i < nb) xs[i] -= LU[(size_t)(k0 + i) * lda + k0 + j] * xj;
+      __syncthreads();
+    }
+  } else {
+    for (int j = nb - 1; j >= 0; j--) {
+      if (i == j) xs[j] = cdivc(xs[j], LU[(size_t)(k0 + j) * lda + k0 + j]);
+      __syncthreads();
+      T xj = xs[j];
+      if (i < j) xs[i] -= LU[(size_t)(k0 + i) * lda + k0 + j] * xj;
+      __syncthreads();
+    }
+  }
+  if (i < nb) x[k0 + i] = xs[i];
+}
+// rows r in [r0, r1): x[r] -= sum_j LU[r][k0+j] x[k0+j], j < nb (warp per row)
+template <class T>
+__global__ void k_trsv_update(const T* LU, size_t lda, int r0, int r1, int k0, int nb, T* x) {
+  int w = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  int lane = threadIdx.x & 31;
+  int r = r0 + w;
+  if (r >= r1) return;
+  const T* row = LU + (size_t)r * lda + k0;
+  double sr = 0.0, si = 0.0;
+  for (int j = lane; j < nb; j += 32) {
+    T a = row[j], b = x[k0 + j];
+    sr += (double)a.x * (double)b.x - (double)a.y * (double)b.y;
+    si += (double)a.x * (double)b.y + (double)a.y * (double)b.x;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_down_sync(0xffffffffu, sr, o);
+    si += __shfl_down_sync(0xffffffffu, si, o);
+  }
+  if (lane == 0) { x[r].x -= sr; x[r].y -= si; }
+}
+
+template <class T>
+static int lu_solve1(const T* LU, size_t lda, int n, const int64_t* ipiv, T* x, cudaStream_t st) {
+  k_perm1<T><<<1, 32, 0, st>>>(x, n, ipiv);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  for (int k = 0; k < n; k += LU_NB) {
+    int nb = (n - k < LU_NB) ? n - k : LU_NB;
+    k_trsv_diag<T, 0><<<1, LU_NB, 0, st>>>(LU, lda, k, nb, x);
+    gbi_count_launch();
+    int rows = n - k - nb;
+    if (rows > 0) {
+      k_trsv_update<T><<<(unsigned)(((size_t)rows * 32 + 255) / 256), 256, 0, st>>>(LU, lda, k + nb, n, k, nb, x);
+      gbi_count_launch();
+    }
+  }
+  int last = ((n - 1) / LU_NB) * LU_NB;
+  for (int k = last; k >= 0; k -= LU_NB) {
+    int nb = (n - k < LU_NB) ? n - k : LU_NB;
+    k_trsv_diag<T, 1><<<1, LU_NB, 0, st>>>(LU, lda, k, nb, x);
+    gbi_count_launch();
+    if (k > 0) {
+      k_trsv_update<T><<<(unsigned)(((size_t)k * 32 + 255) / 256), 256, 0, st>>>(LU, lda, 0, k, k, nb, x);
+      gbi_count_launch();
+    }
+  }
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+extern "C" int gbi_csolve1(const cplxf* LU, size_t lda, int n, const int64_t* ipiv, cplxf* x, cudaStream_t st) {
+  return lu_solve1<cplxf>(LU, lda, n, ipiv, x, st);
+}
+extern "C" int gbi_zsolve1(const cplx* LU, size_t lda, int n, const int64_t* ipiv, cplx* x, cudaStream_t st) {
+  return lu_solve1<cplx>(LU, lda, n, ipiv, x, st);
+}
+
+// r = b - A x (FP64), and the squared norms of r and b accumulated into nrm[0], nrm[1]
+__global__ void k_residual(const cplx* __restrict__ A, size_t lda, int n, const cplx* __restrict__ x,
+                           const cplx* __restrict__ b, cplx* r, double* nrm) {
+  int w = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  int lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const cplx* row = A + (size_t)w * lda;
+  double sr = 0.0, si = 0.0;
+  for (int j = lane; j < n; j += 32) {
+    cplx a = row[j], v = x[j];
+    sr = fma(a.x, v.x, sr);
+    sr = fma(-a.y, v.y, sr);
+    si = fma(a.x, v.y, si);
+    si = fma(a.y, v.x, si);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    sr += __shfl_down_sync(0xffffffffu, sr, o);
+    si += __shfl_down_sync(0xffffffffu, si, o);
+  }
+  if (lane == 0) {
+    cplx rr = cmk(b[w].x - sr, b[w].y - si);
+    r[w] = rr;
+    atomicAdd(nrm, rr.x * rr.x + rr.y * rr.y);
+    atomicAdd(nrm + 1, b[w].x * b[w].x + b[w].y * b[w].y);
+  }
+}
+extern "C" int gbi_residual(const cplx* A, size_t lda, int n, const cplx* x, const cplx* b, cplx* r, double* nrm,
+                            cudaStream_t st) {
+  GB_CUDA(cudaMemsetAsync(nrm, 0, 2 * sizeof(double), st));
+  k_residual<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(A, lda, n, x, b, r, nrm);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// x += (cplx) d ; also converts: d64 -> d32 helper
+__global__ void k_axpy_c64(cplx* x, const cplxf* d, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) { x[i].x += (double)d[i].x; x[i].y += (double)d[i].y; }
+}
+__global__ void k_c128_to_c64_scaled(const cplx* r, cplxf* d, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) d[i] = cmkf((float)r[i].x, (float)r[i].y);
+}
+extern "C" int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, const cplxf* LU32, size_t lda, int n, const int64_t* ipiv,
+                           cudaStream_t st) {
+  k_c128_to_c64_scaled<<<(n + 255) / 256, 256, 0, st>>>(r, d, n);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  if (lu_solve1<cplxf>(LU32, lda, n, ipiv, d, st)) return -1;
+  k_axpy_c64<<<(n + 255) / 256, 256, 0, st>>>(x, d, n);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
 }

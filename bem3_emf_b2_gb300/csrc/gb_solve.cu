@@ -87,6 +87,7 @@ extern "C" int gbi_build_B(const cplx* G, const cplx* H, const int* sid, const i
   size_t warps = 4 * 4 * (size_t)a.Ne;
   if (warps == 0) return 0;
   k_build_B<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(a);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -159,6 +160,7 @@ extern "C" int gbi_store_bv(const cplx* X, const GbMeshDev* m, const double* kn_
   int n = a.Ne * 4;
   if (n == 0) return 0;
   k_store_bv<<<(n + 127) / 128, 128, 0, st>>>(a);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -264,6 +266,7 @@ extern "C" int gbi_eh_bv(const cplx* dG, const cplx* dH, const double* dF, const
   size_t warps = 4 * (size_t)a.Ne;
   if (!warps) return 0;
   k_eh_bv<<<(unsigned)((warps * 32 + 127) / 128), 128, 0, st>>>(a);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -321,6 +324,7 @@ extern "C" int gbi_deh_build(const cplx* G, const cplx* H, const int* rowk, int 
   if (!warps) return 0;
   GB_CUDA(cudaMemsetAsync(Ac, 0, (size_t)nn * nn * sizeof(cplx), st));
   k_deh_build<<<(unsigned)((warps * 32 + 127) / 128), 128, 0, st>>>(G, H, rowk, Ne, nn, E, Hf, Ac, Bc);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -328,6 +332,7 @@ extern "C" int gbi_deh_build(const cplx* G, const cplx* H, const int* rowk, int 
 extern "C" int gbi_deh_scatter(const cplx* Bc, const int* rowk, int Ne, cplx* dE, cplx* dHf, cudaStream_t st) {
   if (!Ne) return 0;
   k_deh_scatter<<<(Ne * 4 + 127) / 128, 128, 0, st>>>(Bc, rowk, Ne, dE, dHf);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -349,6 +354,7 @@ extern "C" int gbi_add_incident(int n, const int* idx, const cplx* out, cplx* Ui
                                 cudaStream_t st) {
   if (n <= 0) return 0;
   k_add_incident<<<(n + 127) / 128, 128, 0, st>>>(n, idx, out, Ui, dUi, did, bad);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }
@@ -388,6 +394,7 @@ __global__ void k_ccd(int Ne, const int* md, const cplx* Ui, const cplx* Uip, do
 
 extern "C" int gbi_ccd(int Ne, const int* md, const cplx* Ui, const cplx* Uip, double* out, cudaStream_t st) {
   k_ccd<<<1, 256, 0, st>>>(Ne, md, Ui, Uip, out);
+  gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
 }

@@ -1,0 +1,90 @@
+/*
+ * scene.c -- single-object scene without intermediate files (gb_scene.h).
+ */
+#include "gb_host.h"
+#include "gb_scene.h"
+
+DOMD *gbh_scene_open(const char *medium_file,const char *mesh_file,const char *ipw_file)
+{
+  DOMD *md=(DOMD *)m_alloc2(1,sizeof(DOMD),"scene.c md");
+  init_mfb(&md->mw);
+  if(read_data_mfb_ipw((char *)ipw_file,&md->mw)==0){ printf("scene.c: no plane wave in %s\n",ipw_file); free(md); return NULL; }
+  gb_read_medium_data((char *)medium_file,md);
+  gb_read_mesh_data((char *)mesh_file,md);
+  md->rv[0]=1.0;
+  initialize_domd2(md);
+  md->cm.MN=md->MN;
+  md->cm.nn=(size_t)md->bd.NN;
+  md->cm.na=8*md->cm.nn;
+  gb_initalize_cmd2(&md->cm);
+  gb_init_boundary_data_u2(md);
+  return md;
+}
+
+static void gb_upload_incident_now(DOMD *md)
+{
+  BOUD *bd=&md->bd;
+  size_t n=((size_t)bd->Ne+1)*16;
+  double complex *u=(double complex *)m_alloc2(n,sizeof(double complex),"scene.c u");
+  double complex *du=(double complex *)m_alloc2(n,sizeof(double complex),"scene.c du");
+  for(int i=0;i<=bd->Ne;i++) for(int j=0;j<4;j++) for(int l=0;l<4;l++){
+    u[(i*4+j)*4+l]=bd->Ui0[i][j][l];
+    du[(i*4+j)*4+l]=bd->dUi0[i][j][l];
+  }
+  if(gb_incident_upload(gb_dev(md),u,du)) gb_die("scene.c, gb_incident_upload()");
+  free(u); free(du);
+}
+
+int gbh_scene_step(DOMD *md,int form,int type,const double *rc,double *F,double *N)
+{
+  gb_obj *o=gb_dev(md);
+  if(!(gb_dev_flags(md)&GB_F_INC)){
+    gb_upload_incident_now(md);
+    gb_dev_set_flags(md,GB_F_INC,0);
+  }
+  if(gb_scene_step(o,form,type)){ printf("gbh_scene_step: %s\n",gb_last_error()); return -1; }
+  gb_bv_to_host(md);
+  gb_dev_set_flags(md,GB_F_BV,0);
+  MOBJ mo;
+  memset(&mo,0,sizeof(mo));
+  mo.N=1;
+  mo.md=md;
+  double c[3]={rc[0],rc[1],rc[2]};
+  return mo_force_FN(F,N,c,0,0,&mo);
+}
+
+void gbh_scene_drop_device(DOMD *md){ gb_dev_release(md); }
+
+size_t gbh_scene_h2d_bytes(DOMD *md)
+{
+  size_t n1=(size_t)md->bd.Ne+1,tot=0;
+  for(int d=0;d<=md->MN;d++) tot+=(size_t)md->bd.sb[d].Ne+1;
+  /* cr, cw, ren, wen, corner (doubles), etype, eni, md, sd (ints), sid, kn, incident Ui0/dUi0 */
+  return n1*(12+9+12+12+12)*8+n1*(1+4+1+1)*4+tot*4+(size_t)(md->MN+1)*16+2*n1*16*16;
+}
+
+size_t gbh_scene_d2h_bytes(DOMD *md)
+{
+  size_t tot=0;
+  for(int d=0;d<=md->MN;d++) tot+=((size_t)md->bd.sb[d].Ne+1)*(16+16+12*4)*16;
+  return tot+3*((size_t)md->bd.Ne+1)*16*16;
+}
+
+void gbh_scene_close(DOMD *md)
+{
+  gb_finalize_cmd2(&md->cm);
+  finalize_domd2(md);
+  free(md);
+}
+
+void *gbh_scene_stream(DOMD *md){ return gb_obj_stream(gb_dev(md)); }
+
+void *gbh_scene_obj(DOMD *md)
+{
+  gb_obj *o=gb_dev(md);
+  if(!(gb_dev_flags(md)&GB_F_INC)){
+    gb_upload_incident_now(md);
+    gb_dev_set_flags(md,GB_F_INC,0);
+  }
+  return o;
+}

@@ -46,6 +46,10 @@ typedef struct gb_mesh_desc {
 
 const char *gb_last_error(void);
 int gb_device_count(void);
+/* kernel launches made by this library so far (all threads) */
+unsigned long long gb_launch_count(void);
+/* the CUDA stream (cudaStream_t) the object's work runs on */
+void *gb_obj_stream(gb_obj *o);
 
 int gb_obj_create(const gb_mesh_desc *m, gb_obj **out);
 void gb_obj_destroy(gb_obj *o);
@@ -105,6 +109,18 @@ int gb_solve_EH(gb_obj *o);
 int gb_domain_id(gb_obj *o, int n, const double *rt, int *did);
 int gb_field_points(gb_obj *o, int mode, int type, int n, const double *rt, const double *v, const int *did, void *out, int *flag);
 int gb_field_bd(gb_obj *o, int type, int n, const int *did, const int *t, const double *zt, void *out);
+
+/* ---- mixed-precision form ----
+ * gb_factor_mixed: A from the resident G, H, kept in FP64, and its complex
+ * FP32 LU factors; later gb_solve_mEMP calls solve A x = b by FP64 iterative
+ * refinement with those factors (residual b - A x in FP64, relative residual
+ * <= 1e-13) instead of applying an explicit inverse.
+ * gb_ir_info: corrections and final relative residual of the last solve.
+ * gb_scene_step: assembly of every domain + factorisation (form 0: FP64 LU and
+ * explicit inverse as in the reference; form 1: mixed) + U, dU + E, H, dE, dH. */
+int gb_factor_mixed(gb_obj *o);
+int gb_ir_info(gb_obj *o, int *iters, double *relres);
+int gb_scene_step(gb_obj *o, int form, int type);
 
 /* Dense complex FP64 LU solve of a host system: A (n x n, row-major) X = B
  * (n x nrhs, row-major), B overwritten by X.  The kernel behind the dE/dn,

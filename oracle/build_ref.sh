@@ -32,5 +32,6 @@ done
 # that both libraries print the same quantities with full precision
 APPS="$HERE/../bem3_emf_b2_gb300/apps"
 gcc $CFLAGS -o "$OUT/bem3_analysis" "$APPS/bem3_analysis.c" -L"$OUT" -lbem3ref -Wl,-rpath,"$OUT" "$BLAS" -Wl,-rpath,"$BLASDIR" -lm
+gcc $CFLAGS -o "$OUT/ref_point" "$HERE/ref_point.c" -L"$OUT" -lbem3ref -Wl,-rpath,"$OUT" "$BLAS" -Wl,-rpath,"$BLASDIR" -lm
 rm -f "$OUT"/*.o
 echo "built $OUT"
