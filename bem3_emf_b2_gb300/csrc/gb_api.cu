@@ -104,6 +104,8 @@ static int ensure_tables() {
   return 0;
 }
 
+extern "C" int gbi_ensure_tables(void) { return ensure_tables(); }
+
 extern "C" int gb_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) return 0;

@@ -22,6 +22,7 @@
 #include "gb_quad.cuh"
 #include "gb_reduce.cuh"
 #include "gb_internal.h"
+#include <mutex>
 
 
 
@@ -245,4 +246,84 @@ extern "C" int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* 
 extern "C" int gbi_upload_tables_asm(const void* t) {
   GB_CUDA(cudaMemcpyToSymbol(c_tab, t, sizeof(GbTables)));
   return 0;
+}
+
+// ==================================================================== no allocation
+// Allocation-free variant of the domain assembly (gb_assemble_domain_noalloc
+// in gb_bem.h).  Some callers cannot allocate device memory: an application
+// whose device memory is entirely owned by another allocator (a framework's
+// caching pool holds the free memory, so a library cudaMalloc fails or
+// fragments it), a latency-critical loop that cannot afford cudaFree's
+// implicit device-wide synchronisation, or a code certified to allocate
+// nothing after start-up.  This entry point takes every input and output from
+// the caller and keeps its only scratch -- the per-pair solid-angle terms
+// Fs[4 Ne][Ne][3] -- in the fixed array below, so it never calls cudaMalloc,
+// cudaFree or an allocating library routine.
+//
+// The array is GB_NOALLOC_SCRATCH_DOUBLES doubles (16 MiB) of static device
+// memory: every GPU that loads this library holds it until the process exits.
+// It limits a domain to GB_NOALLOC_MAX_NE elements (12 Ne^2 <= 2^21).
+// All calls share the one array; it keeps the last call's contents and is
+// cleared at the start of every call.  Calls that overlap on the GPU (two
+// streams, or two host threads on one device) race on it and must be
+// serialised by the caller.
+#define GB_NOALLOC_SCRATCH_DOUBLES (2u * 1024u * 1024u)
+#define GB_NOALLOC_MAX_NE 418
+static __device__ __align__(256) double g_noalloc_scratch[GB_NOALLOC_SCRATCH_DOUBLES];
+
+// Host code may not use g_noalloc_scratch's name as a device address: the
+// device address is looked up once per device (with that device current) by
+// cudaGetSymbolAddress and cached here.
+static double* g_noalloc_dev_ptr[64];
+static std::mutex g_noalloc_mu;
+
+static int noalloc_scratch_ptr(double** out) {
+  int dev = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { gbi_set_error("gb_assemble_domain_noalloc: device ordinal %d not supported", dev); return -1; }
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_dev_ptr[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      gbi_set_error("gb_assemble_domain_noalloc: cudaGetSymbolAddress of the scratch failed: %s", cudaGetErrorString(e));
+      return -1;
+    }
+    g_noalloc_dev_ptr[dev] = (double*)p;
+  }
+  *out = g_noalloc_dev_ptr[dev];
+  return 0;
+}
+
+extern "C" int gbi_ensure_tables(void);
+
+extern "C" int gb_assemble_domain_noalloc(const double* cr, const double* cw, const int* etype, const double* ren,
+                                          const int* sid, int Ne, double k_re, double k_im, int did, int type, void* G,
+                                          void* H, void* dG, void* dH, double* dF, void* stream) {
+  if (Ne < 1 || Ne > GB_NOALLOC_MAX_NE) {
+    gbi_set_error("gb_assemble_domain_noalloc: %d elements in the domain; this entry point supports 1..%d "
+                  "(fixed 16 MiB scratch); use gb_assemble for larger domains", Ne, GB_NOALLOC_MAX_NE);
+    return -1;
+  }
+  if (type < 0 || type > 3) { gbi_set_error("gb_assemble_domain_noalloc: quadrature type %d not in 0..3", type); return -1; }
+  if (did < 0 || did >= GB_MAXDOM) { gbi_set_error("gb_assemble_domain_noalloc: domain id %d not in 0..%d", did, GB_MAXDOM - 1); return -1; }
+  if (!cr || !cw || !etype || !ren || !sid || !G || !H || !dG || !dH || !dF) {
+    gbi_set_error("gb_assemble_domain_noalloc: null input or output pointer");
+    return -1;
+  }
+  double* scratch = nullptr;
+  if (noalloc_scratch_ptr(&scratch)) return -1;
+  if (gbi_ensure_tables()) return -1;
+  GbMeshDev m;
+  memset(&m, 0, sizeof(m));
+  m.cr = (double*)cr;
+  m.cw = (double*)cw;
+  m.ren = (double*)ren;
+  m.etype = (int*)etype;
+  m.sid = (int*)sid;
+  m.sb_Ne[did] = Ne;
+  m.sb_off[did] = 0;
+  m.kn[2 * did] = k_re;
+  m.kn[2 * did + 1] = k_im;
+  return gbi_assemble_domain(&m, did, type, (cplx*)G, (cplx*)H, (cplx*)dG, (cplx*)dH, dF, scratch, (cudaStream_t)stream);
 }

@@ -110,6 +110,28 @@ int gb_domain_id(gb_obj *o, int n, const double *rt, int *did);
 int gb_field_points(gb_obj *o, int mode, int type, int n, const double *rt, const double *v, const int *did, void *out, int *flag);
 int gb_field_bd(gb_obj *o, int type, int n, const int *did, const int *t, const double *zt, void *out);
 
+/* Allocation-free domain assembly.  No counterpart in the reference.
+ * For callers that cannot allocate device memory -- their device memory is
+ * owned by another allocator (e.g. a framework's caching pool), they cannot
+ * accept cudaFree's implicit device synchronisation, or they must allocate
+ * nothing after start-up -- this computes the same G, H, dG, dH, dF of one
+ * domain as gb_assemble with every buffer supplied by the caller (all device
+ * pointers): mesh arrays as in gb_mesh_desc (cr, cw, ren, etype, 1-based),
+ * sid = the domain's signed element list (Ne+1 ints, slot 0 unused), wave
+ * number k, domain id did (0: the open region, which takes the free term
+ * 1 + F), quadrature type; outputs in the .cmat layout (N = 4 Ne); stream is a
+ * cudaStream_t (NULL: the default stream); the call is asynchronous.
+ * It calls no cudaMalloc, cudaFree or allocating routine: its scratch is a
+ * fixed 16 MiB static device array that every GPU loading the library holds
+ * until exit, so a domain may have at most 418 elements (larger: error).  The
+ * array's device address is looked up on the first call on each device, so
+ * make that first call before any stream capture.  All calls share the array
+ * (cleared at the start of each call): calls that overlap on the GPU race and
+ * must be serialised by the caller. */
+int gb_assemble_domain_noalloc(const double *cr, const double *cw, const int *etype, const double *ren, const int *sid,
+                               int Ne, double k_re, double k_im, int did, int type,
+                               void *G, void *H, void *dG, void *dH, double *dF, void *stream);
+
 /* ---- mixed-precision form ----
  * gb_factor_mixed: A from the resident G, H, kept in FP64, and its complex
  * FP32 LU factors; later gb_solve_mEMP calls solve A x = b by FP64 iterative
