@@ -42,8 +42,11 @@ int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, const int* 
 int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
 int gbi_to_c64(const cplx* a, cplxf* b, size_t n, cudaStream_t st);
 int gbi_residual(const cplx* A, size_t lda, int n, const cplx* x, const cplx* b, cplx* r, double* nrm, cudaStream_t st);
-int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, const cplxf* LU32, size_t lda, int n, const int64_t* ipiv,
+int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU32, size_t lda, int n, const int* perm,
                 cudaStream_t st);
+int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st);
+int gbi_zsolve_multi(const cplx* LU, size_t lda, int n, const int* perm, const cplx* X, size_t ldx, int nrhs, cplx* Y,
+                     cudaStream_t st);
 }
 
 // ------------------------------------------------------------------ errors
@@ -133,6 +136,7 @@ struct gb_obj {
   cplx* A64;
   cplxf* LU32;
   int64_t* ipiv32;
+  int* perm32;
   int have_lu32;
   int ir_iters;
   double ir_relres;
@@ -174,7 +178,7 @@ extern "C" void gb_obj_destroy(gb_obj* o) {
     cudaFree(o->rowk[d]);
   }
   cudaFree(o->invA);
-  cudaFree(o->A64); cudaFree(o->LU32); cudaFree(o->ipiv32);
+  cudaFree(o->A64); cudaFree(o->LU32); cudaFree(o->ipiv32); cudaFree(o->perm32);
   for (int d = 0; d < GB_MAXDOM; d++) {
     cudaFree(o->bU[d]); cudaFree(o->bdU[d]); cudaFree(o->bE[d]); cudaFree(o->bdE[d]); cudaFree(o->bH[d]); cudaFree(o->bdH[d]);
   }
@@ -194,7 +198,7 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   for (int d = 0; d < GB_MAXDOM; d++) { o->G[d] = o->H[d] = o->dG[d] = o->dH[d] = nullptr; o->dF[d] = nullptr; o->rowk[d] = nullptr; }
   o->invA = nullptr;
   o->have_invA = 0;
-  o->A64 = nullptr; o->LU32 = nullptr; o->ipiv32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
+  o->A64 = nullptr; o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
   for (int d = 0; d < GB_MAXDOM; d++) o->bU[d] = o->bdU[d] = o->bE[d] = o->bdE[d] = o->bH[d] = o->bdH[d] = nullptr;
   o->Ui = o->dUi = o->Ui0 = o->dUi0 = o->Uip = nullptr;
   o->next = 0;
@@ -639,12 +643,13 @@ extern "C" int gb_solve_EH(gb_obj* o) {
     rc = gbi_eh_bv(o->dG[d], o->dH[d], o->dF[d], &o->m, d, o->lambda0, o->bU[d], o->bdU[d], o->bE[d], o->bH[d], o->st);
     if (rc) break;
     int nn = o->nrows[d];
-    cplx *Ac = nullptr, *Bc = nullptr;
+    cplx *Ac = nullptr, *Bc = nullptr, *Yc = nullptr;
     int64_t* ipiv = nullptr;
-    int* info = nullptr;
+    int *info = nullptr, *perm = nullptr;
     if (dalloc((void**)&Ac, (size_t)nn * nn * sizeof(cplx)) || dalloc((void**)&Bc, (size_t)nn * 6 * sizeof(cplx)) ||
+        dalloc((void**)&Yc, (size_t)nn * 6 * sizeof(cplx)) || dalloc((void**)&perm, (size_t)nn * sizeof(int)) ||
         dalloc((void**)&ipiv, (size_t)nn * sizeof(int64_t)) || dalloc((void**)&info, sizeof(int))) {
-      cudaFree(Ac); cudaFree(Bc); cudaFree(ipiv);
+      cudaFree(Ac); cudaFree(Bc); cudaFree(Yc); cudaFree(perm); cudaFree(ipiv);
       return -1;
     }
     rc = gbi_deh_build(o->G[d], o->H[d], o->rowk[d], Ne, nn, o->bE[d], o->bH[d], Ac, Bc, o->st);
@@ -656,10 +661,11 @@ extern "C" int gb_solve_EH(gb_obj* o) {
       rc = -1;
     }
     if (!rc && hinfo) { gbi_set_error("mo_solve.c, solve_deh_bv(), zgesv info=%d error", hinfo); rc = -1; }
-    if (!rc) rc = gbi_zgetrs(Ac, nn, nn, ipiv, Bc, 6, 6, o->st);
-    if (!rc) rc = gbi_deh_scatter(Bc, o->rowk[d], Ne, o->bdE[d], o->bdH[d], o->st);
+    if (!rc) rc = gbi_make_perm(ipiv, nn, perm, o->st);
+    if (!rc) rc = gbi_zsolve_multi(Ac, nn, nn, perm, Bc, 6, 6, Yc, o->st);
+    if (!rc) rc = gbi_deh_scatter(Yc, o->rowk[d], Ne, o->bdE[d], o->bdH[d], o->st);
     if (!rc) rc = sync_obj(o, "gb_solve_EH");
-    cudaFree(Ac); cudaFree(Bc); cudaFree(ipiv); cudaFree(info);
+    cudaFree(Ac); cudaFree(Bc); cudaFree(Yc); cudaFree(perm); cudaFree(ipiv); cudaFree(info);
   }
   return rc;
 }
@@ -755,10 +761,12 @@ extern "C" int gb_factor_mixed(gb_obj* o) {
   if (!o->A64 && dalloc((void**)&o->A64, na * na * sizeof(cplx))) return -1;
   if (!o->LU32 && dalloc((void**)&o->LU32, na * na * sizeof(cplxf))) return -1;
   if (!o->ipiv32 && dalloc((void**)&o->ipiv32, na * sizeof(int64_t))) return -1;
+  if (!o->perm32 && dalloc((void**)&o->perm32, na * sizeof(int))) return -1;
   if (dalloc((void**)&info, sizeof(int))) return -1;
   int rc = build_A(o, o->A64);
   if (!rc) rc = gbi_to_c64(o->A64, o->LU32, na * na, o->st);
   if (!rc) rc = gbi_cgetrf(o->LU32, na, (int)na, o->ipiv32, info, o->st);
+  if (!rc) rc = gbi_make_perm(o->ipiv32, (int)na, o->perm32, o->st);
   int hinfo = 0;
   if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
               cudaStreamSynchronize(o->st) != cudaSuccess)) {
@@ -776,11 +784,11 @@ extern "C" int gb_factor_mixed(gb_obj* o) {
 static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
   size_t na = o->na;
   cplx* r = nullptr;
-  cplxf* d = nullptr;
+  cplxf *d = nullptr, *d2 = nullptr;
   double* nrm = nullptr;
   if (dalloc((void**)&r, na * sizeof(cplx)) || dalloc((void**)&d, na * sizeof(cplxf)) ||
-      dalloc((void**)&nrm, 2 * sizeof(double))) {
-    cudaFree(r); cudaFree(d);
+      dalloc((void**)&d2, na * sizeof(cplxf)) || dalloc((void**)&nrm, 2 * sizeof(double))) {
+    cudaFree(r); cudaFree(d); cudaFree(d2);
     return -1;
   }
   int rc = 0;
@@ -798,12 +806,12 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
       rel = (h[1] > 0.0) ? sqrt(h[0] / h[1]) : 0.0;
       if (rel <= 1e-13) break;
     }
-    rc = gbi_ir_step(X, r, d, o->LU32, na, (int)na, o->ipiv32, o->st);
+    rc = gbi_ir_step(X, r, d, d2, o->LU32, na, (int)na, o->perm32, o->st);
   }
   o->ir_iters = it;
   o->ir_relres = rel;
   if (!rc && rel > 1e-10) { gbi_set_error("iterative refinement stalled at relative residual %g", rel); rc = -1; }
-  cudaFree(r); cudaFree(d); cudaFree(nrm);
+  cudaFree(r); cudaFree(d); cudaFree(d2); cudaFree(nrm);
   return rc;
 }
 

@@ -8,12 +8,27 @@
 //   LAPACKE_zgesv             mo_solve.c:751 (dE/dn, dH/dn with 6 right-hand sides)
 // All matrices are row-major, as in the reference's files.
 //
-// LU: right-looking blocked factorisation with partial pivoting (LAPACK's
-// pivot rule: first index of max |Re|+|Im|).  Per panel of NB columns:
-//   k_pivot_swap   one block: pivot search in column j, full-row interchange
-//   k_panel_update warp per row: scale column j, rank-1 update of the panel
+// LU: right-looking blocked factorisation with tournament pivoting
+// (communication-avoiding LU, "CALU": Grigori, Demmel and Xiang, SIAM J.
+// Matrix Anal. Appl. 32 (2011) 1317-1350).  Per panel of nb <= LU_NB columns
+// starting at row and column k:
+//   k_tslu_leaf    one block per set of TS_ROWS panel rows: partial-pivoting
+//                  elimination in shared memory picks nb candidate rows
+//   k_tslu_merge   4-ary tree: four candidate sets (their original rows read
+//                  back from A) -> nb winners, until one set is left; the last
+//                  block writes the winners, in their pivot order, as
+//                  LAPACK-style sequential interchanges ipiv[k..k+nb)
+//   k_laswp_rows   the interchanges applied across the full row width
+//   k_diag_lu      L11 U11 of the (now leading) winner rows
+//   k_trsm_right   L21 = A21 U11^-1
 //   k_trsm_rows    U12 = L11^-1 A12 (L11 unit lower, staged in shared memory)
-//   k_zgemm_nn     A22 -= L21 U12 (complex FP64 GEMM, 64x64 tiles, DFMA)
+//   GEMM           A22 -= L21 U12 (FP64: k_zgemm_nn, DFMA; FP32: tensor
+//                  cores, gb_tc.cu)
+// Every elimination uses LAPACK's pivot rule (first maximum of |Re|+|Im|);
+// the tournament keeps the backward stability of partial pivoting in practice
+// while a panel needs about log4(n / TS_ROWS) + 1 dependent launches instead
+// of two per column.  The pivot sequence may differ from zgetrf's; the factors
+// solve the same system to rounding.
 // The inverse solves A X = I through the factors: X = U^-1 (L^-1 (P I)),
 // two blocked triangular solves whose updates use the same GEMM kernel.
 #include "gb_common.cuh"
@@ -114,70 +129,12 @@ extern "C" int gbi_build_A_domain(const cplx* G, const cplx* H, const int* sid, 
 
 // ------------------------------------------------------------------ LU
 __device__ __forceinline__ double cabs1(cplx a) { return fabs(a.x) + fabs(a.y); }
-__device__ __forceinline__ double cabs1(cplxf a) { return (double)(fabsf(a.x) + fabsf(a.y)); }
+__device__ __forceinline__ float cabs1(cplxf a) { return fabsf(a.x) + fabsf(a.y); }
 
-// pivot search in column j over rows j..n-1, then the full-row interchange;
-// info[0] receives j+1 on an exactly zero pivot (LAPACK's info convention)
-template <class T>
-__global__ void __launch_bounds__(1024) k_pivot_swap(T* A, size_t lda, int n, int j, int64_t* ipiv, int* info) {
-  __shared__ double sv[32];
-  __shared__ int si[32];
-  double best = -1.0;
-  int bi = n;
-  for (int i = j + threadIdx.x; i < n; i += blockDim.x) {
-    double v = cabs1(A[(size_t)i * lda + j]);
-    if (v > best) { best = v; bi = i; }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    double ov = __shfl_down_sync(0xffffffffu, best, o);
-    int oi = __shfl_down_sync(0xffffffffu, bi, o);
-    if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-  }
-  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) { sv[w] = best; si[w] = bi; }
-  __syncthreads();
-  if (w == 0) {
-    int nw = blockDim.x >> 5;
-    best = lane < nw ? sv[lane] : -1.0;
-    bi = lane < nw ? si[lane] : n;
-    for (int o = 16; o > 0; o >>= 1) {
-      double ov = __shfl_down_sync(0xffffffffu, best, o);
-      int oi = __shfl_down_sync(0xffffffffu, bi, o);
-      if (ov > best || (ov == best && oi < bi)) { best = ov; bi = oi; }
-    }
-    if (lane == 0) { si[0] = bi; sv[0] = best; }
-  }
-  __syncthreads();
-  int p = si[0];
-  if (threadIdx.x == 0) {
-    ipiv[j] = p;
-    if (!(sv[0] > 0.0) && info[0] == 0) info[0] = j + 1;
-  }
-  if (p != j) {
-    T* rj = A + (size_t)j * lda;
-    T* rp = A + (size_t)p * lda;
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-      T t = rj[c];
-      rj[c] = rp[c];
-      rp[c] = t;
-    }
-  }
-}
-
-// rows i > j: l = A[i][j] / A[j][j]; A[i][c] -= l A[j][c] for c in (j, kend)
-template <class T>
-__global__ void k_panel_update(T* A, size_t lda, int n, int j, int kend) {
-  int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  int i = j + 1 + warp;
-  if (i >= n) return;
-  T piv = A[(size_t)j * lda + j];
-  T* ri = A + (size_t)i * lda;
-  const T* rj = A + (size_t)j * lda;
-  T l = (piv.x == 0 && piv.y == 0) ? ri[j] : cdivc(ri[j], piv);
-  for (int c = j + 1 + lane; c < kend; c += 32) ri[c] -= l * rj[c];
-  if (lane == 0) ri[j] = l;
-}
+// real type of a complex element type (sums of FP32 solves stay in FP32: a
+// GB300 SM has a narrow FP64 pipe, and the FP64 refinement corrects them)
+template <class T> struct RealOf { typedef double type; };
+template <> struct RealOf<cplxf> { typedef float type; };
 
 // Rows k..k+nb-1, columns [c0, c1): X <- L11^-1 X with L11 the unit lower
 // triangle of A[k:k+nb][k:k+nb] (or, with upper = 1, X <- U11^-1 X with the
@@ -317,35 +274,347 @@ static int trsm_rows(int upper, const T* L, size_t ldl, T* X, size_t ldx, int nb
   return 0;
 }
 
-// In-place LU of the n x n row-major matrix A (lda); ipiv[j] = 0-based row
-// interchanged with row j (rows are swapped across the full width).
-// info (device int) receives LAPACK's info (0: success).
-template <class T, class GEMM>
-static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st, GEMM gemm) {
-  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), st));
-  for (int k = 0; k < n; k += LU_NB) {
-    int nb = (n - k < LU_NB) ? n - k : LU_NB;
-    int kend = k + nb;
-    for (int j = k; j < kend; j++) {
-      k_pivot_swap<T><<<1, 1024, 0, st>>>(A, lda, n, j, ipiv, info);
-      gbi_count_launch();
-      GB_CUDA(cudaGetLastError());
-      int rows = n - j - 1;
-      if (rows > 0) {
-        unsigned nbk = (unsigned)((rows * 32 + 255) / 256);
-        k_panel_update<T><<<nbk, 256, 0, st>>>(A, lda, n, j, kend);
-        gbi_count_launch();
-        GB_CUDA(cudaGetLastError());
-      }
-    }
-    if (kend < n) {
-      if (trsm_rows<T>(0, A + (size_t)k * lda + k, lda, A + (size_t)k * lda, lda, nb, kend, n, st)) return -1;
-      if (gemm(n - kend, n - kend, nb, A + (size_t)kend * lda + k, lda, A + (size_t)k * lda + kend, lda,
-               A + (size_t)kend * lda + kend, lda, st))
-        return -1;
+// ---- tournament-pivoting panel (CALU)
+#define TS_ARITY 4                   // candidate sets merged per tree node
+#define TS_ROWS (TS_ARITY * LU_NB)   // rows of a leaf set and of a merge
+#define TS_THREADS 1024              // elimination blocks: 32 warps, 8 rows each
+#define PANEL_THREADS 256
+
+__device__ __forceinline__ cplxf to_c64(cplx a) { return cmkf((float)a.x, (float)a.y); }
+__device__ __forceinline__ cplxf to_c64(cplxf a) { return a; }
+
+// Partial-pivoting elimination of the R <= TS_ROWS panel rows idx[0..R) of A
+// (columns k..k+nb-1, nb <= LU_NB): only the choice of rows is kept -- on
+// return idx[0..min(R, nb)) holds the selected rows in pivot order.  The
+// selection runs in complex FP32 for both LU types: it only ranks candidate
+// rows, and a block's FP64 pipe is too narrow for it (the FP64 factors
+// themselves are computed in FP64 by k_diag_lu / k_trsm_right).
+// The rows live in registers: warp w holds rows w + 32 i (i < TS_ROWS / 32),
+// lane l columns l and l + 32.  Per column: a block reduction for the pivot,
+// the interchange through two shared-memory row buffers, and a register-only
+// rank-1 update that also ranks the next column; two block barriers.
+template <class T>
+__device__ void ts_select(const T* A, size_t lda, int k, int nb, int* idx, int R) {
+  constexpr int NW = TS_THREADS / 32;
+  constexpr int RPW = TS_ROWS / NW;  // rows per warp
+  __shared__ uint32_t skey[NW];
+  __shared__ cplxf sP[LU_NB], sJ[LU_NB];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int c0 = lane, c1 = lane + 32;
+  const cplxf z = cmkf(0.f, 0.f);
+  cplxf v0[RPW], v1[RPW];
+#pragma unroll
+  for (int i = 0; i < RPW; i++) {
+    const int r = w + NW * i;
+    v0[i] = z;
+    v1[i] = z;
+    if (r < R) {
+      const T* src = A + (size_t)idx[r] * lda + k;
+      if (c0 < nb) v0[i] = to_c64(src[c0]);
+      if (c1 < nb) v1[i] = to_c64(src[c1]);
     }
   }
-  return 0;
+  const int steps = R < nb ? R : nb;
+  // pivot keys: |Re|+|Im| with its 8 low mantissa bits replaced by 255 - row
+  // (rows < 256), so one unsigned maximum picks the largest magnitude and, among
+  // magnitudes equal to 2^-15 relative, the first row -- any of them is an
+  // equally good pivot
+  static_assert(TS_ROWS <= 256, "pivot keys hold 8-bit row numbers");
+  uint32_t key = 0u;
+  if (lane == 0) {  // column 0
+#pragma unroll
+    for (int i = 0; i < RPW; i++) {
+      const int r = w + NW * i;
+      if (r < R) key = max(key, (__float_as_uint(cabs1(v0[i])) & ~0xFFu) | (uint32_t)(255 - r));
+    }
+  }
+  for (int j = 0; j < steps; j++) {
+    key = __reduce_max_sync(0xffffffffu, key);
+    if (lane == 0) skey[w] = key;
+    __syncthreads();
+    key = __reduce_max_sync(0xffffffffu, lane < NW ? skey[lane] : 0u);
+    const int p = (key >> 8) != 0u ? 255 - (int)(key & 0xFFu) : j;
+    // the pivot row to sP; with an interchange, the old row j to sJ
+    // (register slots are picked with bit masks: an indexed access, or a
+    // select chain the compiler turns into one, would move the row arrays to
+    // local memory)
+    if (w == (p % NW)) {
+      uint32_t t[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+      for (int i = 0; i < RPW; i++) {
+        const uint32_t msk = 0u - (uint32_t)(i == p / NW);
+        t[0] |= __float_as_uint(v0[i].x) & msk; t[1] |= __float_as_uint(v0[i].y) & msk;
+        t[2] |= __float_as_uint(v1[i].x) & msk; t[3] |= __float_as_uint(v1[i].y) & msk;
+      }
+      sP[c0] = cmkf(__uint_as_float(t[0]), __uint_as_float(t[1]));
+      sP[c1] = cmkf(__uint_as_float(t[2]), __uint_as_float(t[3]));
+    }
+    if (p != j && w == (j % NW)) {
+      uint32_t t[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+      for (int i = 0; i < RPW; i++) {
+        const uint32_t msk = 0u - (uint32_t)(i == j / NW);
+        t[0] |= __float_as_uint(v0[i].x) & msk; t[1] |= __float_as_uint(v0[i].y) & msk;
+        t[2] |= __float_as_uint(v1[i].x) & msk; t[3] |= __float_as_uint(v1[i].y) & msk;
+      }
+      sJ[c0] = cmkf(__uint_as_float(t[0]), __uint_as_float(t[1]));
+      sJ[c1] = cmkf(__uint_as_float(t[2]), __uint_as_float(t[3]));
+    }
+    if (p != j && threadIdx.x == 0) { int t = idx[j]; idx[j] = idx[p]; idx[p] = t; }
+    __syncthreads();
+    if (p != j && w == (p % NW)) {  // position p now holds the old row j
+      const cplxf t0 = sJ[c0], t1 = sJ[c1];
+#pragma unroll
+      for (int i = 0; i < RPW; i++) {
+        const uint32_t msk = 0u - (uint32_t)(i == p / NW);
+        v0[i].x = __uint_as_float((__float_as_uint(v0[i].x) & ~msk) | (__float_as_uint(t0.x) & msk));
+        v0[i].y = __uint_as_float((__float_as_uint(v0[i].y) & ~msk) | (__float_as_uint(t0.y) & msk));
+        v1[i].x = __uint_as_float((__float_as_uint(v1[i].x) & ~msk) | (__float_as_uint(t1.x) & msk));
+        v1[i].y = __uint_as_float((__float_as_uint(v1[i].y) & ~msk) | (__float_as_uint(t1.y) & msk));
+      }
+    }
+    const cplxf piv = sP[j];
+    const bool nz = !(piv.x == 0.f && piv.y == 0.f);
+    const cplxf pinv = nz ? cdivc(cmkf(1.f, 0.f), piv) : z;
+    const cplxf p0 = sP[c0], p1 = sP[c1];
+    const bool u0 = c0 > j && c0 < nb, u1 = c1 > j && c1 < nb;
+    const int cn = j + 1;
+    const bool own_next = lane == (cn & 31) && cn < nb;
+    key = 0u;
+#pragma unroll
+    for (int i = 0; i < RPW; i++) {
+      const int r = w + NW * i;
+      if (r > j && r < R) {  // warp-uniform
+        const cplxf xj = (j < 32) ? v0[i] : v1[i];
+        cplxf l;
+        l.x = __shfl_sync(0xffffffffu, xj.x, j & 31);
+        l.y = __shfl_sync(0xffffffffu, xj.y, j & 31);
+        l = l * pinv;
+        if (u0) v0[i] -= l * p0;
+        if (u1) v1[i] -= l * p1;
+        if (own_next) key = max(key, (__float_as_uint(cabs1(cn < 32 ? v0[i] : v1[i])) & ~0xFFu) | (uint32_t)(255 - r));
+      }
+    }
+  }
+  __syncthreads();
+}
+
+// the winners idx[0..nb) (global rows, pivot order) as LAPACK-style
+// interchanges: ipiv[k + j] = the row swapped with row k + j when the swaps
+// are applied in sequence.  Only rows of the block [k, k + nb) can move
+// before their turn, so two small tables suffice: where[] (current position
+// of each row of the block) and cont[] (current row at each block position).
+// One thread; where/cont: nb ints of shared memory each.
+__device__ void calu_ipiv(const int* win, int k, int nb, int64_t* ipiv, int* where, int* cont) {
+  for (int i = 0; i < nb; i++) { where[i] = k + i; cont[i] = k + i; }
+  for (int j = 0; j < nb; j++) {
+    const int wr = win[j];
+    const bool win_in = wr >= k && wr < k + nb;
+    const int pos = win_in ? where[wr - k] : wr;
+    ipiv[k + j] = pos;
+    const int c = cont[j];  // a row of the block
+    cont[j] = wr;
+    if (win_in) where[wr - k] = k + j;
+    if (pos >= k && pos < k + nb) cont[pos - k] = c;
+    where[c - k] = pos;
+  }
+}
+
+// one block per set of TS_ROWS rows of the panel: nb candidate rows (and the
+// interchanges, when the panel has a single set)
+template <class T>
+__global__ void __launch_bounds__(TS_THREADS) k_tslu_leaf(const T* A, size_t lda, int n, int k, int nb, int* cand,
+                                                         int64_t* ipiv) {
+  __shared__ int idx[TS_ROWS + 2 * LU_NB];
+  const int r0 = k + blockIdx.x * TS_ROWS;
+  const int R = (n - r0 < TS_ROWS) ? n - r0 : TS_ROWS;
+  for (int r = threadIdx.x; r < R; r += TS_THREADS) idx[r] = r0 + r;
+  __syncthreads();
+  ts_select<T>(A, lda, k, nb, idx, R);
+  const int steps = R < nb ? R : nb;
+  for (int j = threadIdx.x; j < nb; j += TS_THREADS) cand[(size_t)blockIdx.x * nb + j] = j < steps ? idx[j] : -1;
+  if (gridDim.x == 1 && threadIdx.x == 0) calu_ipiv(idx, k, nb, ipiv, idx + TS_ROWS, idx + TS_ROWS + LU_NB);
+}
+
+// sets TS_ARITY b .. TS_ARITY b + TS_ARITY - 1 of cin (nin sets of nb entries;
+// the valid entries of a set are a prefix) -> set b of cout; the last level
+// (one block) also writes the interchanges
+template <class T>
+__global__ void __launch_bounds__(TS_THREADS) k_tslu_merge(const T* A, size_t lda, int k, int nb, const int* cin, int nin,
+                                                          int* cout, int64_t* ipiv) {
+  __shared__ int idx[TS_ROWS + 2 * LU_NB];
+  __shared__ int cnt[TS_ARITY];
+  const int b = blockIdx.x;
+  if (threadIdx.x < TS_ARITY) cnt[threadIdx.x] = 0;
+  __syncthreads();
+  const int q = threadIdx.x / LU_NB, e = threadIdx.x % LU_NB;  // set q, entry e
+  const int set = TS_ARITY * b + q;
+  int v = -1;
+  if (q < TS_ARITY && set < nin && e < nb) v = cin[(size_t)set * nb + e];
+  if (v >= 0) atomicAdd(&cnt[q], 1);
+  __syncthreads();
+  if (v >= 0) {
+    int off = 0;
+    for (int u = 0; u < q; u++) off += cnt[u];
+    idx[off + e] = v;
+  }
+  int R = 0;
+  for (int u = 0; u < TS_ARITY; u++) R += cnt[u];
+  __syncthreads();
+  ts_select<T>(A, lda, k, nb, idx, R);
+  const int steps = R < nb ? R : nb;
+  for (int j = threadIdx.x; j < nb; j += TS_THREADS) cout[(size_t)b * nb + j] = j < steps ? idx[j] : -1;
+  if (gridDim.x == 1 && threadIdx.x == 0) calu_ipiv(idx, k, nb, ipiv, idx + TS_ROWS, idx + TS_ROWS + LU_NB);
+}
+
+// interchanges ipiv[k..k+nb) applied in sequence to columns [0, ncol)
+template <class T>
+__global__ void k_laswp_rows(T* A, size_t lda, int ncol, int k, int nb, const int64_t* ipiv) {
+  int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= ncol) return;
+  for (int j = k; j < k + nb; j++) {
+    int p = (int)ipiv[j];
+    if (p != j) {
+      T t = A[(size_t)j * lda + c];
+      A[(size_t)j * lda + c] = A[(size_t)p * lda + c];
+      A[(size_t)p * lda + c] = t;
+    }
+  }
+}
+
+// L11 U11 = A[k:k+nb][k:k+nb] in place, without interchanges; info[0] = k + j + 1
+// at the first exactly zero pivot (LAPACK's convention)
+template <class T>
+__global__ void __launch_bounds__(PANEL_THREADS) k_diag_lu(T* A, size_t lda, int k, int nb, int* info) {
+  extern __shared__ __align__(16) unsigned char tsraw[];
+  T* M = (T*)tsraw;
+  const int ld = nb + 1;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) M[(t / nb) * ld + t % nb] = A[(size_t)(k + t / nb) * lda + k + t % nb];
+  __syncthreads();
+  T one, zero;
+  one.x = 1; one.y = 0; zero.x = 0; zero.y = 0;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = PANEL_THREADS / 32;
+  const int c0 = lane, c1 = lane + 32;
+  for (int j = 0; j < nb; j++) {
+    const T piv = M[j * ld + j];
+    const bool nz = !(piv.x == 0 && piv.y == 0);
+    if (!nz && threadIdx.x == 0 && info[0] == 0) info[0] = k + j + 1;
+    const T pinv = nz ? cdivc(one, piv) : zero;
+    // warp w: rows j + 1 + ((w - j - 1) mod nw) + nw i; lanes: columns c0, c1 > j
+    const bool u0 = c0 > j && c0 < nb, u1 = c1 > j && c1 < nb;
+    const T p0 = u0 ? M[j * ld + c0] : zero;
+    const T p1 = u1 ? M[j * ld + c1] : zero;
+    for (int r = j + 1 + ((w - (j + 1)) % nw + nw) % nw; r < nb; r += nw) {
+      T* row = M + r * ld;
+      const T l = row[j] * pinv;
+      __syncwarp();
+      if (lane == (j & 31)) row[j] = l;
+      if (u0) row[c0] -= l * p0;
+      if (u1) row[c1] -= l * p1;
+    }
+    __syncthreads();
+  }
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) A[(size_t)(k + t / nb) * lda + k + t % nb] = M[(t / nb) * ld + t % nb];
+}
+
+// rows [r0, r1), columns k..k+nb-1: X <- X U11^-1 (U11 non-unit upper of
+// A[k:k+nb][k:k+nb]); one warp per row, lane l holds columns l and l + 32
+template <class T>
+__global__ void __launch_bounds__(PANEL_THREADS) k_trsm_right(T* A, size_t lda, int k, int nb, int r0, int r1) {
+  extern __shared__ __align__(16) unsigned char tsraw[];
+  T* U = (T*)tsraw;  // nb x nb
+  T* dinv = U + nb * nb;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) U[t] = A[(size_t)(k + t / nb) * lda + k + t % nb];
+  __syncthreads();
+  for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+    T d = U[j * nb + j];
+    T one;
+    one.x = 1;
+    one.y = 0;
+    dinv[j] = (d.x == 0 && d.y == 0) ? d : cdivc(one, d);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  for (int r = r0 + blockIdx.x * wpb + (threadIdx.x >> 5); r < r1; r += gridDim.x * wpb) {
+    T* row = A + (size_t)r * lda + k;
+    T a0, a1;
+    a0.x = 0; a0.y = 0; a1 = a0;
+    if (lane < nb) a0 = row[lane];
+    if (lane + 32 < nb) a1 = row[lane + 32];
+    for (int j = 0; j < nb; j++) {
+      const int owner = j & 31;
+      T v = (j < 32) ? a0 : a1;
+      T x;
+      x.x = __shfl_sync(0xffffffffu, v.x, owner);
+      x.y = __shfl_sync(0xffffffffu, v.y, owner);
+      x = x * dinv[j];
+      if (lane == owner) { if (j < 32) a0 = x; else a1 = x; }
+      if (lane > j && lane < nb) a0 -= x * U[j * nb + lane];
+      if (lane + 32 > j && lane + 32 < nb) a1 -= x * U[j * nb + lane + 32];
+    }
+    if (lane < nb) row[lane] = a0;
+    if (lane + 32 < nb) row[lane + 32] = a1;
+  }
+}
+
+// In-place LU of the n x n row-major matrix A (lda) with tournament pivoting;
+// ipiv[j] = 0-based row interchanged with row j (interchanges applied in
+// sequence across the full row width, as LAPACK's); info (device int)
+// receives LAPACK's info (0: success).  gemm(M, N, K, A, lda, B, ldb, C, ldc,
+// st) performs C -= A B.
+template <class T, class GEMM>
+static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st, GEMM gemm) {
+  if (n <= 0) return 0;
+  const int nsets0 = (n + TS_ROWS - 1) / TS_ROWS;
+  int* cand = nullptr;
+  GB_CUDA(cudaMallocAsync((void**)&cand, sizeof(int) * (size_t)2 * nsets0 * LU_NB, st));
+  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), st));
+  const size_t sm_diag = (size_t)LU_NB * (LU_NB + 1) * sizeof(T);
+  const size_t sm_right = (size_t)LU_NB * LU_NB * sizeof(T) + LU_NB * sizeof(T);
+  int rc = 0;
+  int dev = 0, nsm = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  GB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  GB_CUDA(cudaFuncSetAttribute(k_diag_lu<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_diag));
+  GB_CUDA(cudaFuncSetAttribute(k_trsm_right<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_right));
+  for (int k = 0; k < n && !rc; k += LU_NB) {
+    const int nb = (n - k < LU_NB) ? n - k : LU_NB;
+    const int kend = k + nb;
+    int nsets = (n - k + TS_ROWS - 1) / TS_ROWS;
+    int* cin = cand;
+    int* cout = cand + (size_t)nsets0 * LU_NB;
+    k_tslu_leaf<T><<<nsets, TS_THREADS, 0, st>>>(A, lda, n, k, nb, cin, ipiv);
+    gbi_count_launch();
+    while (nsets > 1) {
+      int nout = (nsets + TS_ARITY - 1) / TS_ARITY;
+      k_tslu_merge<T><<<nout, TS_THREADS, 0, st>>>(A, lda, k, nb, cin, nsets, cout, ipiv);
+      gbi_count_launch();
+      int* t = cin;
+      cin = cout;
+      cout = t;
+      nsets = nout;
+    }
+    k_laswp_rows<T><<<(n + 255) / 256, 256, 0, st>>>(A, lda, n, k, nb, ipiv);
+    gbi_count_launch();
+    k_diag_lu<T><<<1, PANEL_THREADS, sm_diag, st>>>(A, lda, k, nb, info);
+    gbi_count_launch();
+    if (kend < n) {
+      int rows = n - kend;
+      int wpb = PANEL_THREADS / 32;
+      int nblk = (rows + wpb - 1) / wpb;
+      if (nblk > 2 * nsm) nblk = 2 * nsm;
+      k_trsm_right<T><<<nblk, PANEL_THREADS, sm_right, st>>>(A, lda, k, nb, kend, n);
+      gbi_count_launch();
+      if (cudaGetLastError() != cudaSuccess) { gbi_set_error("LU panel launch failed"); rc = -1; break; }
+      if (trsm_rows<T>(0, A + (size_t)k * lda + k, lda, A + (size_t)k * lda, lda, nb, kend, n, st)) { rc = -1; break; }
+      if (gemm(n - kend, n - kend, nb, A + (size_t)kend * lda + k, lda, A + (size_t)k * lda + kend, lda,
+               A + (size_t)kend * lda + kend, lda, st)) { rc = -1; break; }
+    }
+  }
+  cudaFreeAsync(cand, st);
+  if (!rc) GB_CUDA(cudaGetLastError());
+  return rc;
 }
 
 extern "C" int gbi_zgetrf(cplx* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st) {
@@ -519,7 +788,41 @@ static int cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, const cplx
   return 0;
 }
 
+extern "C" size_t gbi_tc_scratch_floats(int M, int N, int K);
+extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, const cplxf* B, size_t ldb, cplxf* C,
+                                size_t ldc, int passes, float* scratch, int* err, cudaStream_t st);
+
+// Complex-FP32 LU: the trailing updates on the tensor cores (split TF32, three
+// passes: FP32-level products), scratch and the time-out flag shared by all
+// panels; the flag is read back once at the end.
 extern "C" int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st) {
+  if (n <= 0) return 0;
+  float* scratch = nullptr;
+  int* err = nullptr;
+  size_t need = gbi_tc_scratch_floats(n, n, LU_NB);
+  GB_CUDA(cudaMallocAsync((void**)&scratch, need * sizeof(float), st));
+  GB_CUDA(cudaMallocAsync((void**)&err, 16, st));
+  GB_CUDA(cudaMemsetAsync(err, 0, 4, st));
+  auto tc = [scratch, err](int M, int N, int K, const cplxf* a, size_t la, const cplxf* b, size_t lb, cplxf* c, size_t lc,
+                           cudaStream_t s) { return gbi_tc_cgemm_sub(M, N, K, a, la, b, lb, c, lc, 3, scratch, err, s); };
+  int rc = lu_factor<cplxf>(A, lda, n, ipiv, info, st, tc);
+  int h = 0;
+  if (!rc && (cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaStreamSynchronize(st) != cudaSuccess)) {
+    gbi_set_error("FP32 LU: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
+  }
+  cudaFreeAsync(scratch, st);
+  cudaFreeAsync(err, st);
+  if (!rc && h) {
+    gbi_set_error("FP32 LU: a tensor-core pipeline wait timed out");
+    rc = -1;
+  }
+  return rc;
+}
+
+// the previous FP32 path (SIMT GEMM), kept for comparison in tests and benches
+extern "C" int gbi_cgetrf_simt(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st) {
   return lu_factor<cplxf>(A, lda, n, ipiv, info, st, cgemm_sub);
 }
 
@@ -584,11 +887,12 @@ __global__ void k_trsv_update(const T* LU, size_t lda, int r0, int r1, int k0, i
   int r = r0 + w;
   if (r >= r1) return;
   const T* row = LU + (size_t)r * lda + k0;
-  double sr = 0.0, si = 0.0;
+  typedef typename RealOf<T>::type R;
+  R sr = 0, si = 0;
   for (int j = lane; j < nb; j += 32) {
     T a = row[j], b = x[k0 + j];
-    sr += (double)a.x * (double)b.x - (double)a.y * (double)b.y;
-    si += (double)a.x * (double)b.y + (double)a.y * (double)b.x;
+    sr += a.x * b.x - a.y * b.y;
+    si += a.x * b.y + a.y * b.x;
   }
   for (int o = 16; o > 0; o >>= 1) {
     sr += __shfl_down_sync(0xffffffffu, sr, o);
@@ -677,14 +981,147 @@ __global__ void k_c128_to_c64_scaled(const cplx* r, cplxf* d, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) d[i] = cmkf((float)r[i].x, (float)r[i].y);
 }
-extern "C" int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, const cplxf* LU32, size_t lda, int n, const int64_t* ipiv,
-                           cudaStream_t st) {
+template <class T>
+static int lu_solve_multi(const T* LU, size_t lda, int n, const int* perm, const T* X, size_t ldx, int nrhs, T* Y,
+                          cudaStream_t st);
+// x += LU32^-1 P r (r converted to FP32; d, d2: n-element FP32 work vectors)
+extern "C" int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU32, size_t lda, int n,
+                           const int* perm, cudaStream_t st) {
   k_c128_to_c64_scaled<<<(n + 255) / 256, 256, 0, st>>>(r, d, n);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
-  if (lu_solve1<cplxf>(LU32, lda, n, ipiv, d, st)) return -1;
-  k_axpy_c64<<<(n + 255) / 256, 256, 0, st>>>(x, d, n);
+  if (lu_solve_multi<cplxf>(LU32, lda, n, perm, d, 1, 1, d2, st)) return -1;
+  k_axpy_c64<<<(n + 255) / 256, 256, 0, st>>>(x, d2, n);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
+}
+
+// ---- permutation and multi-RHS triangular solves (nrhs <= 8)
+// perm[i] = original row at position i after the interchanges ipiv[0..n)
+// (sequential by nature: one block, the vector in shared memory when it fits)
+#define PERM_SMEM_MAX 49152
+__global__ void k_make_perm(const int64_t* ipiv, int n, int* perm) {
+  extern __shared__ int sperm[];
+  int* v = (n <= PERM_SMEM_MAX) ? sperm : perm;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) v[i] = i;
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int j = 0; j < n; j++) {
+      int p = (int)ipiv[j];
+      if (p != j) { int t = v[j]; v[j] = v[p]; v[p] = t; }
+    }
+  __syncthreads();
+  if (v != perm)
+    for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = v[i];
+}
+extern "C" int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st) {
+  size_t sm = (n <= PERM_SMEM_MAX) ? (size_t)n * sizeof(int) : 0;
+  GB_CUDA(cudaFuncSetAttribute(k_make_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM_MAX * (int)sizeof(int)));
+  k_make_perm<<<1, 1024, sm, st>>>(ipiv, n, perm);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+template <class T>
+__global__ void k_gather_rows(const T* X, size_t ldx, int n, int nrhs, const int* perm, T* Y) {
+  size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (size_t)n * nrhs) return;
+  int i = (int)(q / nrhs), c = (int)(q % nrhs);
+  Y[(size_t)i * nrhs + c] = X[(size_t)perm[i] * ldx + c];
+}
+template <class T, int UPPER>
+__global__ void k_trsm_diag_multi(const T* LU, size_t lda, int k0, int nb, T* X, int nrhs) {
+  __shared__ T xs[LU_NB];
+  const int c = blockIdx.x;  // right-hand side
+  int i = threadIdx.x;
+  if (i < nb) xs[i] = X[(size_t)(k0 + i) * nrhs + c];
+  __syncthreads();
+  if (!UPPER) {
+    for (int j = 0; j < nb; j++) {
+      T xj = xs[j];
+      __syncthreads();
+      if (i > j && i < nb) xs[i] -= LU[(size_t)(k0 + i) * lda + k0 + j] * xj;
+      __syncthreads();
+    }
+  } else {
+    for (int j = nb - 1; j >= 0; j--) {
+      if (i == j) xs[j] = cdivc(xs[j], LU[(size_t)(k0 + j) * lda + k0 + j]);
+      __syncthreads();
+      T xj = xs[j];
+      if (i < j) xs[i] -= LU[(size_t)(k0 + i) * lda + k0 + j] * xj;
+      __syncthreads();
+    }
+  }
+  if (i < nb) X[(size_t)(k0 + i) * nrhs + c] = xs[i];
+}
+template <class T>
+__global__ void k_trsm_update_multi(const T* LU, size_t lda, int r0, int r1, int k0, int nb, T* X, int nrhs) {
+  int w = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  int lane = threadIdx.x & 31;
+  int r = r0 + w;
+  if (r >= r1) return;
+  const T* row = LU + (size_t)r * lda + k0;
+  typedef typename RealOf<T>::type R;
+  R sr[8], si[8];
+  for (int c = 0; c < 8; c++) { sr[c] = 0; si[c] = 0; }
+  for (int j = lane; j < nb; j += 32) {
+    T a = row[j];
+    for (int c = 0; c < nrhs; c++) {
+      T b = X[(size_t)(k0 + j) * nrhs + c];
+      sr[c] += a.x * b.x - a.y * b.y;
+      si[c] += a.x * b.y + a.y * b.x;
+    }
+  }
+  for (int c = 0; c < nrhs; c++) {
+    for (int o = 16; o > 0; o >>= 1) {
+      sr[c] += __shfl_down_sync(0xffffffffu, sr[c], o);
+      si[c] += __shfl_down_sync(0xffffffffu, si[c], o);
+    }
+  }
+  if (lane == 0)
+    for (int c = 0; c < nrhs; c++) {
+      X[(size_t)r * nrhs + c].x -= sr[c];
+      X[(size_t)r * nrhs + c].y -= si[c];
+    }
+}
+
+// Y <- (LU)^-1 P X for nrhs <= 8 columns; X (ldx) is read, Y (n x nrhs, packed) written
+template <class T>
+static int lu_solve_multi(const T* LU, size_t lda, int n, const int* perm, const T* X, size_t ldx, int nrhs, T* Y,
+                          cudaStream_t st) {
+  if (nrhs < 1 || nrhs > 8) { gbi_set_error("lu_solve_multi: nrhs %d not in 1..8", nrhs); return -1; }
+  size_t tot = (size_t)n * nrhs;
+  k_gather_rows<T><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(X, ldx, n, nrhs, perm, Y);
+  gbi_count_launch();
+  for (int k = 0; k < n; k += LU_NB) {
+    int nb = (n - k < LU_NB) ? n - k : LU_NB;
+    k_trsm_diag_multi<T, 0><<<nrhs, LU_NB, 0, st>>>(LU, lda, k, nb, Y, nrhs);
+    gbi_count_launch();
+    int rows = n - k - nb;
+    if (rows > 0) {
+      k_trsm_update_multi<T><<<(unsigned)(((size_t)rows * 32 + 255) / 256), 256, 0, st>>>(LU, lda, k + nb, n, k, nb, Y, nrhs);
+      gbi_count_launch();
+    }
+  }
+  int last = ((n - 1) / LU_NB) * LU_NB;
+  for (int k = last; k >= 0; k -= LU_NB) {
+    int nb = (n - k < LU_NB) ? n - k : LU_NB;
+    k_trsm_diag_multi<T, 1><<<nrhs, LU_NB, 0, st>>>(LU, lda, k, nb, Y, nrhs);
+    gbi_count_launch();
+    if (k > 0) {
+      k_trsm_update_multi<T><<<(unsigned)(((size_t)k * 32 + 255) / 256), 256, 0, st>>>(LU, lda, 0, k, k, nb, Y, nrhs);
+      gbi_count_launch();
+    }
+  }
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+extern "C" int gbi_zsolve_multi(const cplx* LU, size_t lda, int n, const int* perm, const cplx* X, size_t ldx, int nrhs,
+                                cplx* Y, cudaStream_t st) {
+  return lu_solve_multi<cplx>(LU, lda, n, perm, X, ldx, nrhs, Y, st);
+}
+extern "C" int gbi_csolve_multi(const cplxf* LU, size_t lda, int n, const int* perm, const cplxf* X, size_t ldx, int nrhs,
+                                cplxf* Y, cudaStream_t st) {
+  return lu_solve_multi<cplxf>(LU, lda, n, perm, X, ldx, nrhs, Y, st);
 }

@@ -1,0 +1,472 @@
+// gb_tc.cu -- complex-FP32 GEMM update C -= A B on the 5th-generation tensor
+// cores (tcgen05.mma kind::tf32, TMA, TMEM): the trailing update of the
+// complex-FP32 LU of the chosen form.
+//
+// A complex product is a real GEMM on interleaved (re, im) storage.  With C, A,
+// B row-major complex64,
+//     Cr[m][2n] -= Ar[m][2k] * Bt[2n][2k]^T,
+//     Bt[2j+e][2l+f] = f == 0 ? (e == 0 ? Re b :  Im b)
+//                             : (e == 0 ? -Im b : Re b),      b = B[l][j],
+// and Ar is A itself read as floats (row i: re a_i0, im a_i0, re a_i1, ...).
+// TF32 keeps 10 mantissa bits.  With PASSES = 3 every operand x is split as
+// x = hi + lo (hi = x rounded to TF32, lo = x - hi exact in FP32) and the
+// tile accumulates hi*hi + hi*lo + lo*hi in FP32: products then carry about
+// 2^-21 relative error, close to FP32 arithmetic (the standard 3xTF32
+// emulation).  PASSES = 1 is plain TF32.
+//
+// Kernel: persistent, one CTA per SM, 128 x 256 tiles of Cr, 192 threads.
+//   warp 0     streams K-slices of 32 floats (one 128-byte swizzle atom) of
+//              the operands into a ring of shared-memory stages with TMA
+//              (SWIZZLE_128B), running ahead across tiles;
+//   warp 1     allocates 512 TMEM columns (two FP32 accumulators) and issues
+//              tcgen05.mma.cta_group::1.kind::tf32 (M = 128, N = 256, K = 8),
+//              committing each stage back to the producer and each finished
+//              accumulator to the epilogue;
+//   warps 2-5  read an accumulator (tcgen05.ld 32x32b: TMEM lane = tile row)
+//              and subtract it from C while the next tile accumulates in the
+//              other buffer.
+// Every mbarrier wait is bounded in time (TC_WAIT_NS); on time-out the CTA
+// raises *err, stops issuing work, frees its TMEM and returns.
+#include <cuda.h>
+
+#include "gb_common.cuh"
+#include "gb_internal.h"
+
+#define TC_BM 128
+#define TC_BN 256
+#define TC_BK 32  // floats per K-slice: 128 bytes, one swizzle atom
+#define TC_THREADS 192
+#define TC_WAIT_NS 2000000000ull  // 2 s
+
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// wait for the phase of the given parity to complete; false after TC_WAIT_NS
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  if (mbar_test(bar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  while (!mbar_test(bar, parity)) {
+    if (globaltimer() - t0 > TC_WAIT_NS) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cta.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major operand, 128-byte swizzle, rows of
+// 128 bytes, 8-row atoms 1024 bytes apart (stride byte offset); the leading
+// byte offset is unused for this layout.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // bits 0-13: start address >> 4
+  d |= (uint64_t)(1024u >> 4) << 32;          // bits 32-45: stride byte offset >> 4
+  d |= (uint64_t)1 << 46;                     // bits 46-47: descriptor version
+  d |= (uint64_t)2 << 61;                     // bits 61-63: SWIZZLE_128B
+  return d;
+}
+
+// instruction descriptor, kind::tf32: D = F32, A = B = TF32, both K-major, M x N
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4)                            // bits 4-5: D format F32
+         | (2u << 7)                          // bits 7-9: A format TF32
+         | (2u << 10)                         // bits 10-12: B format TF32
+         | ((uint32_t)(N >> 3) << 17)         // bits 17-22: N >> 3
+         | ((uint32_t)(M >> 4) << 24);        // bits 24-28: M >> 4
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// 16 consecutive 32-bit TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, "
+      "[%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tf32_round(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+template <int PASSES>
+struct TcLayout {
+  static constexpr int A_BYTES = TC_BM * TC_BK * 4;  // 16 KB
+  static constexpr int B_BYTES = TC_BN * TC_BK * 4;  // 32 KB
+  static constexpr int NOPS = PASSES == 3 ? 2 : 1;
+  static constexpr int STAGE = NOPS * (A_BYTES + B_BYTES);
+  static constexpr int STAGES = PASSES == 3 ? 2 : 4;  // 192 KB either way: one CTA per SM owns all of TMEM
+  static constexpr int SMEM = STAGES * STAGE + 1024 /* alignment */ + 256 /* barriers */;
+};
+
+// Persistent: CTA b takes tiles b, b + gridDim.x, ...; tile t covers rows
+// 128 (t / ntn) and real columns 256 (t % ntn) of Cr.  Warp roles:
+//   warp 0     (one lane) TMA producer, ring of STAGES K-slices across tiles
+//   warp 1     allocates TMEM (two 256-column accumulators); one lane issues
+//              the MMAs of a tile into accumulator (local tile index & 1)
+//   warps 2-5  epilogue: warp w reads TMEM lanes 32 (w & 3) .. + 31, i.e. tile
+//              rows, and subtracts them from C while the MMAs of the next tile
+//              fill the other accumulator
+template <int PASSES>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+    k_tc_cgemm_sub(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
+                   const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo, int m, int n2,
+                   int nkb, float* C, size_t ldcf, int* err) {
+  using L = TcLayout<PASSES>;
+  constexpr int S = L::STAGES;
+  extern __shared__ uint8_t smraw[];
+  const uint32_t raw_u32 = smem_u32(smraw);
+  uint8_t* sm = smraw + ((1024u - (raw_u32 & 1023u)) & 1023u);  // 1024-byte aligned (swizzle atoms)
+  const uint32_t sbase = smem_u32(sm);
+  // barriers: full[s] bar0 + 8 s, empty[s] bar0 + 64 + 8 s, tfull[b] bar0 + 128 + 8 b, tempty[b] bar0 + 144 + 8 b
+  const uint32_t bar0 = sbase + S * L::STAGE;
+  uint32_t* tslot = (uint32_t*)(sm + S * L::STAGE + 192);
+  volatile int* s_fail = (volatile int*)(sm + S * L::STAGE + 200);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntn = (n2 + TC_BN - 1) / TC_BN;
+  const int ntiles = ((m + TC_BM - 1) / TC_BM) * ntn;
+
+  if (threadIdx.x == 0) {
+    *s_fail = 0;
+    for (int s = 0; s < S; s++) {
+      mbar_init(bar0 + 8 * s, 1);
+      mbar_init(bar0 + 64 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; b++) {
+      mbar_init(bar0 + 128 + 8 * b, 1);
+      mbar_init(bar0 + 144 + 8 * b, 4);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tslot)),
+                 "r"(2 * TC_BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer
+      uint32_t g = 0;
+      for (int t = blockIdx.x; t < ntiles && !*s_fail; t += gridDim.x) {
+        const int i0 = (t / ntn) * TC_BM, c0 = (t % ntn) * TC_BN;
+        for (int kb = 0; kb < nkb; kb++, g++) {
+          const uint32_t s = g % S, u = g / S;
+          if (u >= 1 && !mbar_wait(bar0 + 64 + 8 * s, (u - 1) & 1)) { *s_fail = 1; break; }
+          const uint32_t st = sbase + s * L::STAGE;
+          const uint32_t fb = bar0 + 8 * s;
+          mbar_expect_tx(fb, L::STAGE);
+          tma_load_2d(st, &mAhi, fb, kb * TC_BK, i0);
+          tma_load_2d(st + L::A_BYTES, &mBhi, fb, kb * TC_BK, c0);
+          if (PASSES == 3) {
+            tma_load_2d(st + L::A_BYTES + L::B_BYTES, &mAlo, fb, kb * TC_BK, i0);
+            tma_load_2d(st + 2 * L::A_BYTES + L::B_BYTES, &mBlo, fb, kb * TC_BK, c0);
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      constexpr uint32_t idesc = idesc_tf32(TC_BM, TC_BN);
+      uint32_t g = 0, lt = 0;
+      for (int t = blockIdx.x; t < ntiles && !*s_fail; t += gridDim.x, lt++) {
+        const uint32_t b = lt & 1, u = lt >> 1;
+        if (u >= 1 && !mbar_wait(bar0 + 144 + 8 * b, (u - 1) & 1)) { *s_fail = 1; break; }
+        tc_fence_after();
+        const uint32_t d = tmem + b * TC_BN;
+        bool ok = true;
+        for (int kb = 0; kb < nkb; kb++, g++) {
+          const uint32_t s = g % S;
+          if (!mbar_wait(bar0 + 8 * s, (g / S) & 1)) { *s_fail = 1; ok = false; break; }
+          tc_fence_after();
+          const uint32_t ahi = sbase + s * L::STAGE, bhi = ahi + L::A_BYTES;
+          const uint32_t alo = bhi + L::B_BYTES, blo = alo + L::A_BYTES;
+#pragma unroll
+          for (int kk = 0; kk < TC_BK / 8; kk++) {
+            const uint32_t off = kk * 32;  // 8 TF32 = 32 bytes along K inside the swizzle atom
+            mma_tf32(d, sdesc_sw128(ahi + off), sdesc_sw128(bhi + off), idesc, (kb | kk) != 0);
+            if (PASSES == 3) {
+              mma_tf32(d, sdesc_sw128(ahi + off), sdesc_sw128(blo + off), idesc, 1);
+              mma_tf32(d, sdesc_sw128(alo + off), sdesc_sw128(bhi + off), idesc, 1);
+            }
+          }
+          mma_commit(bar0 + 64 + 8 * s);  // the stage is free once these MMAs have read it
+        }
+        if (!ok) break;
+        mma_commit(bar0 + 128 + 8 * b);  // accumulator b complete
+      }
+    }
+  } else {  // epilogue warps 2..5
+    const int q = warp & 3;
+    uint32_t lt = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, lt++) {
+      const uint32_t b = lt & 1, u = lt >> 1;
+      int ok = 1;
+      if (lane == 0) ok = mbar_wait(bar0 + 128 + 8 * b, u & 1) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok || *s_fail) { *s_fail = 1; break; }
+      __syncwarp();
+      tc_fence_after();
+      const int i0 = (t / ntn) * TC_BM, c0 = (t % ntn) * TC_BN;
+      const int row = i0 + q * 32 + lane;
+      float* crow = C + (size_t)row * ldcf;
+      const uint32_t ta = tmem + b * TC_BN + ((uint32_t)(q * 32) << 16);
+#pragma unroll 1
+      for (int cc = 0; cc < TC_BN; cc += 64) {
+        const int c = c0 + cc;
+        const bool full = row < m && c + 64 <= n2 && ((((uintptr_t)(crow + c)) & 15) == 0);
+        float4 cv[16];
+        if (full) {
+          const float4* p4 = (const float4*)(crow + c);
+#pragma unroll
+          for (int x = 0; x < 16; x++) cv[x] = p4[x];
+        }
+        float v[64];
+        tmem_ld16(ta + cc, v);
+        tmem_ld16(ta + cc + 16, v + 16);
+        tmem_ld16(ta + cc + 32, v + 32);
+        tmem_ld16(ta + cc + 48, v + 48);
+        if (cc + 64 == TC_BN) {  // accumulator b fully read: hand it back to the MMA warp
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar0 + 144 + 8 * b) : "memory");
+        }
+        if (full) {
+          float4* p4 = (float4*)(crow + c);
+#pragma unroll
+          for (int x = 0; x < 16; x++) {
+            float4 t4 = cv[x];
+            t4.x -= v[4 * x + 0];
+            t4.y -= v[4 * x + 1];
+            t4.z -= v[4 * x + 2];
+            t4.w -= v[4 * x + 3];
+            p4[x] = t4;
+          }
+        } else if (row < m) {
+#pragma unroll
+          for (int x = 0; x < 64; x++)
+            if (c + x < n2) crow[c + x] -= v[x];
+        }
+      }
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_BN) : "memory");
+  }
+  if (threadIdx.x == 0 && *s_fail) atomicExch(err, 1);
+}
+
+// A (m x kc complex, lda) -> hi, lo [m][Kp] floats (columns >= 2 kc zero)
+__global__ void k_tc_split_a(const cplxf* __restrict__ A, size_t lda, int m, int kc, int Kp, float* hi, float* lo) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)m * Kp) return;
+  int i = (int)(t / Kp), q = (int)(t % Kp);
+  float v = 0.f;
+  if (q < 2 * kc) {
+    cplxf a = A[(size_t)i * lda + (q >> 1)];
+    v = (q & 1) ? a.y : a.x;
+  }
+  float h = tf32_round(v);
+  hi[t] = h;
+  if (lo) lo[t] = v - h;
+}
+
+// B (kc x n complex, ldb) -> Bt hi, lo [2n][Kp] floats
+__global__ void k_tc_build_bt(const cplxf* __restrict__ B, size_t ldb, int kc, int n, int Kp, float* hi, float* lo) {
+  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)2 * n * Kp) return;
+  int cp = (int)(t / Kp), q = (int)(t % Kp);
+  float v = 0.f;
+  if (q < 2 * kc) {
+    cplxf b = B[(size_t)(q >> 1) * ldb + (cp >> 1)];
+    int e = cp & 1, f = q & 1;
+    v = f == 0 ? (e == 0 ? b.x : b.y) : (e == 0 ? -b.y : b.x);
+  }
+  float h = tf32_round(v);
+  hi[t] = h;
+  if (lo) lo[t] = v - h;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+// 2-D FP32 tensor map over rows x Kp floats (row stride Kp), box 32 x box_rows
+int make_map(CUtensorMap* map, const float* base, int rows, int Kp, int box_rows) {
+  EncodeTiledFn enc = encode_fn();
+  if (!enc) {
+    gbi_set_error("tensor-core GEMM: cuTensorMapEncodeTiled unavailable");
+    return -1;
+  }
+  cuuint64_t dims[2] = {(cuuint64_t)Kp, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)Kp * 4};
+  cuuint32_t box[2] = {TC_BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    gbi_set_error("cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return -1;
+  }
+  return 0;
+}
+
+}  // namespace
+
+// floats of scratch that gbi_tc_cgemm_sub needs for an M x N x K update
+extern "C" size_t gbi_tc_scratch_floats(int M, int N, int K) {
+  size_t Kp = (size_t)((2 * K + TC_BK - 1) / TC_BK) * TC_BK;
+  return 2 * Kp * ((size_t)M + 2 * (size_t)N) + 64;
+}
+
+// C[M][N] -= A[M][K] B[K][N], complex FP32, row-major with leading dimensions
+// (in complex elements).  passes: 3 (split TF32, FP32-level accuracy) or 1
+// (plain TF32).  scratch: gbi_tc_scratch_floats(M, N, K) floats of device
+// memory (16-byte aligned), or NULL to allocate on the stream.  err: device
+// int raised to 1 if a CTA timed out (may be NULL when the caller does not
+// check).
+extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, const cplxf* B, size_t ldb, cplxf* C,
+                                size_t ldc, int passes, float* scratch, int* err, cudaStream_t st) {
+  if (M <= 0 || N <= 0 || K <= 0) return 0;
+  if (passes != 1 && passes != 3) {
+    gbi_set_error("gbi_tc_cgemm_sub: passes must be 1 or 3");
+    return -1;
+  }
+  const int Kp = ((2 * K + TC_BK - 1) / TC_BK) * TC_BK;
+  const size_t need = gbi_tc_scratch_floats(M, N, K);
+  float* buf = scratch;
+  if (!buf) GB_CUDA(cudaMallocAsync((void**)&buf, need * sizeof(float), st));
+  int* e = err;
+  if (!e) GB_CUDA(cudaMallocAsync((void**)&e, 16, st));
+  if (!err) GB_CUDA(cudaMemsetAsync(e, 0, 4, st));
+  float* ahi = buf;
+  float* alo = ahi + (size_t)M * Kp;
+  float* bhi = alo + (size_t)M * Kp;
+  float* blo = bhi + (size_t)2 * N * Kp;
+  const bool three = passes == 3;
+  size_t ta = (size_t)M * Kp, tb = (size_t)2 * N * Kp;
+  k_tc_split_a<<<(unsigned)((ta + 255) / 256), 256, 0, st>>>(A, lda, M, K, Kp, ahi, three ? alo : nullptr);
+  gbi_count_launch();
+  k_tc_build_bt<<<(unsigned)((tb + 255) / 256), 256, 0, st>>>(B, ldb, K, N, Kp, bhi, three ? blo : nullptr);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  CUtensorMap mAhi, mAlo, mBhi, mBlo;
+  int rc = make_map(&mAhi, ahi, M, Kp, TC_BM);
+  if (!rc) rc = make_map(&mAlo, alo, M, Kp, TC_BM);
+  if (!rc) rc = make_map(&mBhi, bhi, 2 * N, Kp, TC_BN);
+  if (!rc) rc = make_map(&mBlo, blo, 2 * N, Kp, TC_BN);
+  if (!rc) {
+    int dev = 0, nsm = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    GB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const long ntiles = (long)((2 * N + TC_BN - 1) / TC_BN) * ((M + TC_BM - 1) / TC_BM);
+    dim3 grid((unsigned)(ntiles < nsm ? ntiles : nsm));
+    const int nkb = Kp / TC_BK;
+    cudaError_t ce;
+    if (three) {
+      GB_CUDA(cudaFuncSetAttribute(k_tc_cgemm_sub<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcLayout<3>::SMEM));
+      k_tc_cgemm_sub<3><<<grid, TC_THREADS, TcLayout<3>::SMEM, st>>>(mAhi, mAlo, mBhi, mBlo, M, 2 * N, nkb, (float*)C,
+                                                                      2 * ldc, e);
+    } else {
+      GB_CUDA(cudaFuncSetAttribute(k_tc_cgemm_sub<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcLayout<1>::SMEM));
+      k_tc_cgemm_sub<1><<<grid, TC_THREADS, TcLayout<1>::SMEM, st>>>(mAhi, mAlo, mBhi, mBlo, M, 2 * N, nkb, (float*)C,
+                                                                      2 * ldc, e);
+    }
+    gbi_count_launch();
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) {
+      gbi_set_error("tensor-core GEMM launch: %s", cudaGetErrorString(ce));
+      rc = -1;
+    }
+  }
+  if (!scratch) cudaFreeAsync(buf, st);
+  if (!err) {
+    int h = 0;
+    if (!rc && (cudaMemcpyAsync(&h, e, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+                cudaStreamSynchronize(st) != cudaSuccess)) {
+      gbi_set_error("tensor-core GEMM: %s", cudaGetErrorString(cudaGetLastError()));
+      rc = -1;
+    }
+    cudaFreeAsync(e, st);
+    if (!rc && h) {
+      gbi_set_error("tensor-core GEMM: a pipeline wait timed out");
+      rc = -1;
+    }
+  }
+  return rc;
+}

@@ -1,0 +1,97 @@
+"""GPU: the dense complex kernels of the LU, called through the C ABI.
+
+- gbi_tc_cgemm_sub (tcgen05 tensor cores, complex FP32 as a real TF32 GEMM on
+  interleaved storage) against a plain PyTorch reference of the same op:
+  the three-pass split must carry FP32-level error (<= 2e-6 relative
+  Frobenius), the one-pass form TF32-level error (<= 2e-3); shapes include
+  ragged edges and sub-matrices with leading dimensions, as in the LU.
+- gbi_cgetrf / gbi_zgetrf (tournament-pivoting LU): P A = L U to FP32 / FP64
+  rounding, against the factors read back to the host.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+vp, ci, csz = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t
+
+
+def _lib():
+    from bem3_emf_b2_gb300 import lib
+    L = lib()
+    L.gbi_tc_cgemm_sub.argtypes = [ci, ci, ci, vp, csz, vp, csz, vp, csz, ci, vp, vp, vp]
+    L.gbi_tc_cgemm_sub.restype = ci
+    for f in (L.gbi_cgetrf, L.gbi_zgetrf, L.gbi_cgetrf_simt):
+        f.argtypes = [vp, csz, ci, vp, vp, vp]
+        f.restype = ci
+    return L
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("M,N,K,pad", [(128, 128, 64, 0), (300, 200, 64, 0), (1000, 517, 50, 3), (77, 900, 7, 5),
+                                       (1536, 1536, 64, 64)])
+def test_tc_cgemm_matches_torch(M, N, K, pad, gb_build):
+    import torch
+    L = _lib()
+    g = torch.Generator().manual_seed(M * 7 + N + K)
+    ld = max(K, N) + pad
+    big = torch.randn(M + K, ld, 2, generator=g, dtype=torch.float32)
+    big = torch.view_as_complex(big).contiguous()
+    A = big[K:, :K]            # M x K at row offset K (leading dimension ld)
+    B = big[:K, :N]            # K x N
+    C0 = torch.randn(M, N + pad, 2, generator=g, dtype=torch.float32)
+    C0 = torch.view_as_complex(C0).contiguous()
+    ref = C0[:, :N].to(torch.complex128) - A.to(torch.complex128) @ B.to(torch.complex128)
+    ref32 = C0[:, :N] - A @ B  # the plain FP32 reference of the same op
+    dev = "cuda"
+    bigd = big.to(dev)
+    for passes, tol in ((3, 2e-6), (1, 2e-3)):
+        Cd = C0.to(dev)
+        Ad = bigd[K:, :K]
+        Bd = bigd[:K, :N]
+        rc = L.gbi_tc_cgemm_sub(M, N, K, Ad.data_ptr(), ld, Bd.data_ptr(), ld, Cd.data_ptr(), N + pad, passes, None,
+                                None, None)
+        assert rc == 0, L.gb_last_error()
+        torch.cuda.synchronize()
+        out = Cd[:, :N].cpu().to(torch.complex128)
+        err = _rel(out.numpy(), ref.numpy())
+        err32 = _rel(ref32.to(torch.complex128).numpy(), ref.numpy())
+        assert err <= tol, "passes %d: %g (fp32 reference %g)" % (passes, err, err32)
+        # the padding columns are untouched
+        assert torch.equal(Cd[:, N:].cpu(), C0[:, N:])
+
+
+def _check_lu(LU, ipiv, A0):
+    n = A0.shape[0]
+    P = np.arange(n)
+    for j in range(n):
+        p = int(ipiv[j])
+        P[[j, p]] = P[[p, j]]
+    Lm = np.tril(LU, -1) + np.eye(n)
+    U = np.triu(LU)
+    return _rel(Lm @ U, A0[P])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [1, 63, 300, 1000, 2113])
+def test_getrf_factors(n, gb_build):
+    import torch
+    L = _lib()
+    rng = np.random.default_rng(n)
+    A0 = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    for dt, f, tol in ((torch.complex128, L.gbi_zgetrf, 1e-13), (torch.complex64, L.gbi_cgetrf, 1e-4),
+                       (torch.complex64, L.gbi_cgetrf_simt, 1e-4)):
+        Ad = torch.tensor(A0, dtype=dt, device="cuda")
+        ip = torch.zeros(n, dtype=torch.int64, device="cuda")
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        assert f(Ad.data_ptr(), n, n, ip.data_ptr(), info.data_ptr(), None) == 0, L.gb_last_error()
+        torch.cuda.synchronize()
+        assert int(info.item()) == 0
+        ipiv = ip.cpu().numpy()
+        assert ipiv.min() >= 0 and ipiv.max() < n and np.all(ipiv >= np.arange(n))
+        err = _check_lu(Ad.cpu().numpy().astype(np.complex128), ipiv, A0)
+        assert err <= tol, "%s n=%d: %g" % (f.__name__, n, err)
