@@ -53,12 +53,25 @@ def lib():
         getattr(L, name).argtypes = [vp]
         getattr(L, name).restype = c_int
     L.gb_ir_info.argtypes = [vp, vp, vp]
+    L.gb_ktime_enable.argtypes = [c_int]
+    L.gb_ktime_enable.restype = None
+    L.gb_ktime_read.argtypes = [vp, vp, vp, vp]
+    L.gb_ktime_read.restype = c_int
     _lib = L
     return L
 
 
 def last_error():
     return lib().gb_last_error().decode()
+
+
+def ktime_read():
+    """(device ms, launches, complex-equivalent flops, HBM bytes) of the
+    tensor-core trailing-update launches recorded since gb_ktime_enable(1)."""
+    ms, n, fl, by = ctypes.c_double(), ctypes.c_long(), ctypes.c_double(), ctypes.c_double()
+    if lib().gb_ktime_read(ctypes.byref(ms), ctypes.byref(n), ctypes.byref(fl), ctypes.byref(by)) != 0:
+        raise RuntimeError(last_error())
+    return ms.value, n.value, fl.value, by.value
 
 
 class Scene:

@@ -29,6 +29,9 @@
 // raises *err, stops issuing work, frees its TMEM and returns.
 #include <cuda.h>
 
+#include <mutex>
+#include <vector>
+
 #include "gb_common.cuh"
 #include "gb_internal.h"
 
@@ -388,6 +391,52 @@ int make_map(CUtensorMap* map, const float* base, int rows, int Kp, int box_rows
 
 }  // namespace
 
+// Optional live timing of the tensor-core kernel (for roofline figures): while
+// enabled, every launch is bracketed by two CUDA events on its own stream and
+// its algorithmic work is recorded; gb_ktime_read() sums after the caller
+// synchronised.  Algorithmic HBM bytes of one launch: C read and written
+// (16 M N), the split operands read once (2 passes x 4 bytes x (M + 2N) Kp).
+namespace {
+struct KtRec {
+  cudaEvent_t a, b;
+  double flops, bytes;
+};
+std::mutex g_kt_mu;
+bool g_kt_on = false;
+std::vector<KtRec> g_kt;
+}  // namespace
+
+extern "C" void gb_ktime_enable(int on) {
+  std::lock_guard<std::mutex> lk(g_kt_mu);
+  for (auto& r : g_kt) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  g_kt.clear();
+  g_kt_on = on != 0;
+}
+
+// total device milliseconds, launches, algorithmic complex-equivalent flops
+// (8 M N K) and HBM bytes of the recorded launches; clears the record
+extern "C" int gb_ktime_read(double* ms, long* launches, double* flops, double* bytes) {
+  std::lock_guard<std::mutex> lk(g_kt_mu);
+  double t = 0.0, f = 0.0, b = 0.0;
+  int rc = 0;
+  for (auto& r : g_kt) {
+    float x = 0.f;
+    if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&x, r.a, r.b) != cudaSuccess) rc = -1;
+    t += x;
+    f += r.flops;
+    b += r.bytes;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  *ms = t;
+  *launches = (long)g_kt.size();
+  *flops = f;
+  *bytes = b;
+  g_kt.clear();
+  if (rc) gbi_set_error("gb_ktime_read: event query failed");
+  return rc;
+}
+
 // floats of scratch that gbi_tc_cgemm_sub needs for an M x N x K update
 extern "C" size_t gbi_tc_scratch_floats(int M, int N, int K) {
   size_t Kp = (size_t)((2 * K + TC_BK - 1) / TC_BK) * TC_BK;
@@ -438,6 +487,19 @@ extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda,
     dim3 grid((unsigned)(ntiles < nsm ? ntiles : nsm));
     const int nkb = Kp / TC_BK;
     cudaError_t ce;
+    KtRec rec;
+    bool timing = false;
+    {
+      std::lock_guard<std::mutex> lk(g_kt_mu);
+      timing = g_kt_on;
+    }
+    if (timing) {
+      GB_CUDA(cudaEventCreate(&rec.a));
+      GB_CUDA(cudaEventCreate(&rec.b));
+      rec.flops = 8.0 * M * (double)N * K;
+      rec.bytes = 16.0 * M * (double)N + (three ? 2.0 : 1.0) * 4.0 * ((double)M + 2.0 * N) * Kp;
+      GB_CUDA(cudaEventRecord(rec.a, st));
+    }
     if (three) {
       GB_CUDA(cudaFuncSetAttribute(k_tc_cgemm_sub<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcLayout<3>::SMEM));
       k_tc_cgemm_sub<3><<<grid, TC_THREADS, TcLayout<3>::SMEM, st>>>(mAhi, mAlo, mBhi, mBlo, M, 2 * N, nkb, (float*)C,
@@ -448,6 +510,11 @@ extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda,
                                                                       2 * ldc, e);
     }
     gbi_count_launch();
+    if (timing) {
+      GB_CUDA(cudaEventRecord(rec.b, st));
+      std::lock_guard<std::mutex> lk(g_kt_mu);
+      g_kt.push_back(rec);
+    }
     ce = cudaGetLastError();
     if (ce != cudaSuccess) {
       gbi_set_error("tensor-core GEMM launch: %s", cudaGetErrorString(ce));

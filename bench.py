@@ -182,14 +182,14 @@ def run_gpu(args):
     dist, rank, ws = dist_init()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    from bem3_emf_b2_gb300 import Scene, build, lib
+    from bem3_emf_b2_gb300 import Scene, build, lib, ktime_read
     build.build()
     wd = tempfile.mkdtemp(prefix="bench_")
     write_scene(wd)
     sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
     L = lib()
 
-    def timed(form, steps, warmup):
+    def timed(form, steps, warmup, ktime=False):
         for _ in range(warmup):
             sc.step(form=form)
         st = torch.cuda.ExternalStream(sc.stream())
@@ -198,6 +198,8 @@ def run_gpu(args):
         torch.cuda.synchronize()
         dist_barrier(dist)
         l0 = L.gb_launch_count()
+        if ktime:
+            L.gb_ktime_enable(1)
         for _ in range(steps):
             flush_l2()
             torch.cuda.synchronize()
@@ -210,13 +212,17 @@ def run_gpu(args):
             times.append(e0.elapsed_time(e1) / 1000.0)
         torch.cuda.synchronize()
         launches = (L.gb_launch_count() - l0) / steps
+        kt = None
+        if ktime:
+            kt = ktime_read()
+            L.gb_ktime_enable(0)
         dist_barrier(dist)
-        return times, F, N, launches
+        return times, F, N, launches, kt
 
     # plain FP64 form (reference-equivalent), then the chosen form
-    t64, F64, N64, _ = timed(0, max(1, min(args.steps, 2)), 1)
+    t64, F64, N64, _, _ = timed(0, max(1, min(args.steps, 2)), 1)
     with ClockSampler(local) as clk:
-        t32, F32, N32, launches = timed(1, args.steps, args.warmup)
+        t32, F32, N32, launches, kt = timed(1, args.steps, args.warmup, ktime=True)
     tsum = sum(t32)
     tmax = dist_max(dist, tsum)
     value = tmax / (args.steps * ws)
@@ -236,7 +242,7 @@ def run_gpu(args):
     force_err = rel_vec(np.concatenate([F32, N32]), np.concatenate([F64, N64]))
     out = None
     if rank == 0:
-        roof = roofline_from_env()
+        roof = roofline_live(kt, tsum, args.steps)
         cpu = cpu_baseline(wd) if (ws == 1 and not args.no_cpu) else None
         out = {"metric": METRIC, "value": value, "unit": "s/scene", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": 1000.0 * tmax / args.steps, "higher_is_better": False,
@@ -259,52 +265,38 @@ def run_gpu(args):
     return out
 
 
-def roofline_from_env():
-    """Dominant-kernel roofline, measured separately by bench_kernel() below."""
-    try:
-        return bench_kernel()
-    except Exception as e:  # the roofline is reported, never guessed
-        return {"error": str(e)}
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "tc_cgemm_traffic.json")
 
 
-def bench_kernel():
-    """Times the dominant kernel of the chosen form in isolation with CUDA
-    events and returns the roofline entry (see the design doc for the unit work)."""
-    import ctypes
-    import torch
-    from bem3_emf_b2_gb300 import lib
-    L = lib()
-    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
-        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
-    # complex FP32 GEMM of the LU trailing update: M = N = 8192, K = 64 (panel width)
-    M = Nn = 8192
-    K = 64
-    A = torch.zeros((M, K), dtype=torch.complex64, device="cuda")
-    B = torch.zeros((K, Nn), dtype=torch.complex64, device="cuda")
-    C = torch.zeros((M, Nn), dtype=torch.complex64, device="cuda")
-    A.real.normal_(); B.real.normal_()
-    f = L.gbi_cgemm_sub
-    f.argtypes = [ctypes.c_int] * 3 + [ctypes.c_void_p, ctypes.c_size_t] * 3 + [ctypes.c_void_p]
-    stream = torch.cuda.current_stream().cuda_stream
-    for _ in range(3):
-        f(M, Nn, K, A.data_ptr(), K, B.data_ptr(), Nn, C.data_ptr(), Nn, stream)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    reps = 20
-    e0.record()
-    for _ in range(reps):
-        f(M, Nn, K, A.data_ptr(), K, B.data_ptr(), Nn, C.data_ptr(), Nn, stream)
-    e1.record()
-    e1.synchronize()
-    dt = e0.elapsed_time(e1) / 1000.0 / reps
-    flops = 8.0 * M * Nn * K
-    ach = flops / dt / 1e12
-    peak = 2.0 * 152 * 128 * 2.07e9 / 1e12  # FP32 FMA pipe: 128 lanes/SM, 152 SMs, 2070 MHz
-    return {"kernel": "k_cgemm_nn (complex FP32 trailing update of the LU, 8192x8192x64)", "bound": "fp32-pipe",
-            "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-            "peak_source": "nominal FP32 FMA rate (no tensor or HBM bound applies; measured FFMA probe 69.8 TF)",
-            "traffic": None}
+def roofline_live(kt, step_seconds, steps):
+    """Roofline of the dominant kernel of the chosen form -- the tensor-core
+    trailing update of the complex-FP32 LU (k_tc_cgemm_sub) -- from CUDA
+    events around each of its launches on the library's stream inside the
+    timed steps.  With the panel width K = 64 it moves 16 M N bytes of C
+    (read + write) per 8 M N K complex-equivalent flops (K/2 flop/B, under the
+    TF32 ridge), so the bound is HBM: achieved = algorithmic bytes / time."""
+    if not kt or kt[1] == 0:
+        return None
+    ms, n, flops, nbytes = kt
+    peaks = {}
+    pf = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pf):
+        peaks = json.load(open(pf))
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    src = "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
+    dt = ms / 1000.0
+    ach = nbytes / dt / 1e9
+    traffic = None
+    if os.path.exists(TRAFFIC_FILE):
+        t = json.load(open(TRAFFIC_FILE))
+        # dram bytes per algorithmic byte of the captured launch, applied per launch
+        traffic = t["dram_bytes_per_algorithmic_byte"] * nbytes / n
+    return {"kernel": "k_tc_cgemm_sub (tcgen05 TF32 x3, complex trailing update of the LU, K = 64)", "bound": "hbm",
+            "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_source": src,
+            "traffic": traffic, "launches_per_step": n / steps,
+            "kernel_ms_total": ms, "kernel_share_of_timed_steps": dt / step_seconds,
+            "tensor_tflops_complex_equiv": flops / dt / 1e12,
+            "algorithmic_bytes_per_launch": nbytes / n}
 
 
 # ---------------------------------------------------------------- reference arm

@@ -50,6 +50,12 @@ int gb_device_count(void);
 unsigned long long gb_launch_count(void);
 /* the CUDA stream (cudaStream_t) the object's work runs on */
 void *gb_obj_stream(gb_obj *o);
+/* live timing of the tensor-core trailing-update kernel (roofline figures):
+ * enable(1) starts recording (CUDA events around every launch on its stream),
+ * read() returns total device ms, launches, complex-equivalent flops (8 M N K)
+ * and algorithmic HBM bytes since then and clears the record */
+void gb_ktime_enable(int on);
+int gb_ktime_read(double *ms, long *launches, double *flops, double *bytes);
 
 int gb_obj_create(const gb_mesh_desc *m, gb_obj **out);
 void gb_obj_destroy(gb_obj *o);
