@@ -53,6 +53,20 @@ def lib():
         getattr(L, name).argtypes = [vp]
         getattr(L, name).restype = c_int
     L.gb_ir_info.argtypes = [vp, vp, vp]
+    L.gbh_mscene_open.argtypes = [c_int, vp, vp, ctypes.c_char_p, vp, vp, vp]
+    L.gbh_mscene_open.restype = vp
+    L.gbh_mscene_step.argtypes = [vp, c_int, c_int, vp, vp, vp]
+    L.gbh_mscene_step.restype = c_int
+    for name in ("gbh_mscene_drop_device", "gbh_mscene_close"):
+        getattr(L, name).argtypes = [vp]
+        getattr(L, name).restype = None
+    for name in ("gbh_mscene_h2d_bytes", "gbh_mscene_d2h_bytes"):
+        getattr(L, name).argtypes = [vp]
+        getattr(L, name).restype = ctypes.c_size_t
+    L.gbh_set_quiet.argtypes = [c_int]
+    L.gbh_set_quiet.restype = None
+    L.gbh_last_iteration.argtypes = [vp, vp]
+    L.gbh_last_iteration.restype = None
     L.gb_ktime_enable.argtypes = [c_int]
     L.gb_ktime_enable.restype = None
     L.gb_ktime_read.argtypes = [vp, vp, vp, vp]
@@ -118,4 +132,59 @@ class Scene:
     def close(self):
         if self.h:
             lib().gbh_scene_close(self.h)
+            self.h = None
+
+
+class MultiScene:
+    """A multi-object scene (gbh_mscene_*): objects placed by rotation (axis
+    rv, angle th) and translation tv, solved together by the multiple-
+    scattering iteration on the GPU."""
+
+    def __init__(self, media, meshes, ipw, rv=None, th=None, tv=None, quiet=True):
+        import numpy as np
+        L = lib()
+        n = len(meshes)
+        self.n = n
+        self._keep = [m.encode() for m in media] + [m.encode() for m in meshes]
+        med = (ctypes.c_char_p * n)(*self._keep[:n])
+        msh = (ctypes.c_char_p * n)(*self._keep[n:])
+        self._rv = np.ascontiguousarray(rv if rv is not None else np.tile([1.0, 0.0, 0.0], n), float).reshape(-1)
+        self._th = np.ascontiguousarray(th if th is not None else np.zeros(n), float).reshape(-1)
+        self._tv = np.ascontiguousarray(tv if tv is not None else np.zeros(3 * n), float).reshape(-1)
+        L.gbh_set_quiet(1 if quiet else 0)
+        self.h = L.gbh_mscene_open(n, ctypes.cast(med, ctypes.c_void_p), ctypes.cast(msh, ctypes.c_void_p), ipw.encode(),
+                                   self._rv.ctypes.data, self._th.ctypes.data, self._tv.ctypes.data)
+        if not self.h:
+            raise RuntimeError("gbh_mscene_open failed")
+
+    def step(self, form=1, type_=2, rc=None):
+        """rc: torque reference points (n x 3); default the translation points"""
+        import numpy as np
+        F = np.zeros(3 * self.n)
+        N = np.zeros(3 * self.n)
+        rcp = None
+        if rc is not None:
+            rca = np.ascontiguousarray(rc, float).reshape(-1)
+            rcp = rca.ctypes.data
+        if lib().gbh_mscene_step(self.h, form, type_, rcp, F.ctypes.data, N.ctypes.data) != 0:
+            raise RuntimeError("gbh_mscene_step failed: %s" % last_error())
+        return F.reshape(self.n, 3), N.reshape(self.n, 3)
+
+    def iteration(self):
+        it, cc = ctypes.c_int(0), ctypes.c_double(0.0)
+        lib().gbh_last_iteration(ctypes.byref(it), ctypes.byref(cc))
+        return it.value, cc.value
+
+    def drop_device(self):
+        lib().gbh_mscene_drop_device(self.h)
+
+    def h2d_bytes(self):
+        return int(lib().gbh_mscene_h2d_bytes(self.h))
+
+    def d2h_bytes(self):
+        return int(lib().gbh_mscene_d2h_bytes(self.h))
+
+    def close(self):
+        if self.h:
+            lib().gbh_mscene_close(self.h)
             self.h = None

@@ -3,6 +3,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <algorithm>
 #include <mutex>
 #include <vector>
 #include "gb_common.cuh"
@@ -40,8 +41,12 @@ int gbi_field(const FieldObj* o, int mode, int type, int n, const double* rt, co
 int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, const int* t, const double* zt, cplx* out,
                  cudaStream_t st);
 int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
-int gbi_to_c64(const cplx* a, cplxf* b, size_t n, cudaStream_t st);
-int gbi_residual(const cplx* A, size_t lda, int n, const cplx* x, const cplx* b, cplx* r, double* nrm, cudaStream_t st);
+int gbi_build_A32_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
+                         const double* kn_dev, int did, int nrows, size_t base, size_t na, cplxf* A32, cudaStream_t st);
+int gbi_apply_A_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
+                       const double* kn_dev, int did, int nrows, size_t base, const cplx* x, cplx* PQ, cplx* y,
+                       cudaStream_t st);
+int gbi_resid_finish(const cplx* b, const cplx* y, cplx* r, size_t n, double* nrm, cudaStream_t st);
 int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU32, size_t lda, int n, const int* perm,
                 cudaStream_t st);
 int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st);
@@ -132,8 +137,8 @@ struct gb_obj {
   size_t na;
   cplx* invA;             // na x na
   int have_invA;
-  // mixed-precision form: FP64 A kept for the residuals, complex FP32 LU factors
-  cplx* A64;
+  // mixed-precision form: complex FP32 LU factors of A; the FP64 residuals
+  // are formed from G and H (A itself is never stored in FP64)
   cplxf* LU32;
   int64_t* ipiv32;
   int* perm32;
@@ -178,7 +183,7 @@ extern "C" void gb_obj_destroy(gb_obj* o) {
     cudaFree(o->rowk[d]);
   }
   cudaFree(o->invA);
-  cudaFree(o->A64); cudaFree(o->LU32); cudaFree(o->ipiv32); cudaFree(o->perm32);
+  cudaFree(o->LU32); cudaFree(o->ipiv32); cudaFree(o->perm32);
   for (int d = 0; d < GB_MAXDOM; d++) {
     cudaFree(o->bU[d]); cudaFree(o->bdU[d]); cudaFree(o->bE[d]); cudaFree(o->bdE[d]); cudaFree(o->bH[d]); cudaFree(o->bdH[d]);
   }
@@ -198,7 +203,7 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   for (int d = 0; d < GB_MAXDOM; d++) { o->G[d] = o->H[d] = o->dG[d] = o->dH[d] = nullptr; o->dF[d] = nullptr; o->rowk[d] = nullptr; }
   o->invA = nullptr;
   o->have_invA = 0;
-  o->A64 = nullptr; o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
+  o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
   for (int d = 0; d < GB_MAXDOM; d++) o->bU[d] = o->bdU[d] = o->bE[d] = o->bdE[d] = o->bH[d] = o->bdH[d] = nullptr;
   o->Ui = o->dUi = o->Ui0 = o->dUi0 = o->Uip = nullptr;
   o->next = 0;
@@ -754,17 +759,24 @@ extern "C" int gb_field_bd(gb_obj* o, int type, int n, const int* did, const int
 }
 
 // ------------------------------------------------------------------ mixed precision
-// Complex FP32 LU of A (partial pivoting), FP64 A kept for the residuals.
+// Complex FP32 LU of A (tournament pivoting, tensor-core trailing updates);
+// A is built directly in FP32 into the factor's buffer.
 extern "C" int gb_factor_mixed(gb_obj* o) {
   size_t na = o->na;
   int* info = nullptr;
-  if (!o->A64 && dalloc((void**)&o->A64, na * na * sizeof(cplx))) return -1;
   if (!o->LU32 && dalloc((void**)&o->LU32, na * na * sizeof(cplxf))) return -1;
   if (!o->ipiv32 && dalloc((void**)&o->ipiv32, na * sizeof(int64_t))) return -1;
   if (!o->perm32 && dalloc((void**)&o->perm32, na * sizeof(int))) return -1;
   if (dalloc((void**)&info, sizeof(int))) return -1;
-  int rc = build_A(o, o->A64);
-  if (!rc) rc = gbi_to_c64(o->A64, o->LU32, na * na, o->st);
+  int rc = 0;
+  if (cudaMemsetAsync(o->LU32, 0, na * na * sizeof(cplxf), o->st) != cudaSuccess) { gbi_set_error("memset"); rc = -1; }
+  size_t base = 0;
+  for (int d = 0; d <= o->m.MN && !rc; d++) {
+    if (!o->G[d]) { gbi_set_error("coupled matrix: domain %d has no coefficient matrices", d); rc = -1; break; }
+    rc = gbi_build_A32_domain(o->G[d], o->H[d], o->m.sid + o->m.sb_off[d], o->rowk[d], &o->m, o->kn_dev, d,
+                              o->nrows[d], base, na, o->LU32, o->st);
+    base += 4 * (size_t)o->nrows[d];
+  }
   if (!rc) rc = gbi_cgetrf(o->LU32, na, (int)na, o->ipiv32, info, o->st);
   if (!rc) rc = gbi_make_perm(o->ipiv32, (int)na, o->perm32, o->st);
   int hinfo = 0;
@@ -779,16 +791,32 @@ extern "C" int gb_factor_mixed(gb_obj* o) {
   return rc;
 }
 
+// y = A x in FP64 from G and H (PQ: scratch of 8 N_max complex)
+static int apply_A(gb_obj* o, const cplx* x, cplx* PQ, cplx* y) {
+  size_t base = 0;
+  for (int d = 0; d <= o->m.MN; d++) {
+    if (gbi_apply_A_domain(o->G[d], o->H[d], o->m.sid + o->m.sb_off[d], o->rowk[d], &o->m, o->kn_dev, d, o->nrows[d],
+                           base, x, PQ, y, o->st))
+      return -1;
+    base += 4 * (size_t)o->nrows[d];
+  }
+  return 0;
+}
+
 // FP64 iterative refinement with the FP32 factors: x <- x + LU32^-1 (b - A x)
-// until ||b - A x|| <= 1e-13 ||b|| (at most 30 corrections)
+// until ||b - A x|| <= 1e-13 ||b|| (at most 30 corrections); b - A x is formed
+// in FP64 from G and H
 static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
   size_t na = o->na;
-  cplx* r = nullptr;
+  size_t nmax = 0;
+  for (int d = 0; d <= o->m.MN; d++) nmax = std::max(nmax, 4 * (size_t)o->m.sb_Ne[d]);
+  cplx *r = nullptr, *y = nullptr, *PQ = nullptr;
   cplxf *d = nullptr, *d2 = nullptr;
   double* nrm = nullptr;
-  if (dalloc((void**)&r, na * sizeof(cplx)) || dalloc((void**)&d, na * sizeof(cplxf)) ||
+  if (dalloc((void**)&r, na * sizeof(cplx)) || dalloc((void**)&y, na * sizeof(cplx)) ||
+      dalloc((void**)&PQ, 8 * nmax * sizeof(cplx)) || dalloc((void**)&d, na * sizeof(cplxf)) ||
       dalloc((void**)&d2, na * sizeof(cplxf)) || dalloc((void**)&nrm, 2 * sizeof(double))) {
-    cudaFree(r); cudaFree(d); cudaFree(d2);
+    cudaFree(r); cudaFree(y); cudaFree(PQ); cudaFree(d); cudaFree(d2);
     return -1;
   }
   int rc = 0;
@@ -799,7 +827,8 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
   int it = 0;
   for (; !rc && it < 31; it++) {
     if (it > 0) {
-      rc = gbi_residual(o->A64, na, (int)na, X, B, r, nrm, o->st);
+      rc = apply_A(o, X, PQ, y);
+      if (!rc) rc = gbi_resid_finish(B, y, r, na, nrm, o->st);
       if (rc) break;
       if (cudaMemcpyAsync(h, nrm, 2 * sizeof(double), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
           cudaStreamSynchronize(o->st) != cudaSuccess) { rc = -1; break; }
@@ -811,7 +840,7 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
   o->ir_iters = it;
   o->ir_relres = rel;
   if (!rc && rel > 1e-10) { gbi_set_error("iterative refinement stalled at relative residual %g", rel); rc = -1; }
-  cudaFree(r); cudaFree(d); cudaFree(d2); cudaFree(nrm);
+  cudaFree(r); cudaFree(y); cudaFree(PQ); cudaFree(d); cudaFree(d2); cudaFree(nrm);
   return rc;
 }
 

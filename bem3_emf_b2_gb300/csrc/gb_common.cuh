@@ -62,6 +62,7 @@ __host__ __device__ __forceinline__ cplxf cdivc(cplxf a, cplxf b) {
   float d = b.x * b.x + b.y * b.y;
   return cmkf((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
 }
+__host__ __device__ __forceinline__ cplxf to_c64f(cplx a) { return cmkf((float)a.x, (float)a.y); }
 template <class T> __host__ __device__ __forceinline__ T czero();
 template <> __host__ __device__ __forceinline__ cplx czero<cplx>() { return cmk(0.0, 0.0); }
 template <> __host__ __device__ __forceinline__ cplxf czero<cplxf>() { return cmkf(0.0f, 0.0f); }

@@ -127,6 +127,208 @@ extern "C" int gbi_build_A_domain(const cplx* G, const cplx* H, const int* sid, 
   return 0;
 }
 
+// A built directly in complex FP32 (chosen form: the FP32 factors start from
+// it; no FP64 copy of A is kept)
+__global__ void k_build_A32(ABuildArgs a, cplxf* A32) {
+  size_t N = (size_t)a.Ne * 4;
+  size_t tot = 4 * N * (size_t)a.Ne;
+  size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= tot) return;
+  int sidx = (int)(p % a.Ne);
+  size_t q = p / a.Ne;
+  int row = (int)(q % N);
+  int cid = (int)(q / N);
+  int k = a.rowk[row];
+  if (k < 0) return;
+  size_t j = a.base + (size_t)cid * a.nrows + k;
+  int sd = a.sid[sidx + 1];
+  int asd = abs(sd);
+  int mdid = a.md[asd], sdid = a.sd[asd];
+  int nl = a.etype[asd] ? 4 : 3;
+  const cplx* g = a.G + (size_t)row * N + (size_t)sidx * 4;
+  const cplx* h = a.H + (size_t)row * N + (size_t)sidx * 4;
+  cplxf* Aj = A32 + j * a.na;
+  const size_t nn = a.nn;
+  if (a.did == mdid) {
+    for (int l = 0; l < nl; l++) {
+      size_t c = (size_t)a.eni[asd * 4 + l];
+      Aj[nn * (cid + 0) + c] = to_c64f(h[l]);
+      Aj[nn * (cid + 4) + c] = to_c64f(-g[l]);
+    }
+    return;
+  }
+  cplx k1 = cmk(a.kn[2 * mdid], a.kn[2 * mdid + 1]);
+  cplx k2 = cmk(a.kn[2 * sdid], a.kn[2 * sdid + 1]);
+  cplx k12 = k1 * k1, k22 = k2 * k2;
+  cplx delt = k12 - k22;
+  cplx beps = cdivc(k12, k22);
+  cplx sigm = cmk(1.0, 0.0) - beps;
+  for (int l = 0; l < nl; l++) {
+    size_t c = (size_t)a.eni[asd * 4 + l];
+    double vn[3];
+    for (int d = 0; d < 3; d++) vn[d] = a.wen[(size_t)asd * 12 + l * 3 + d];
+    double an = sqrt(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
+    if (an != 0.0) { vn[0] /= an; vn[1] /= an; vn[2] /= an; }
+    if (cid < 3) {
+      Aj[nn * (cid + 0) + c] = to_c64f(h[l]);
+      Aj[nn * 3 + c] = to_c64f((delt * vn[cid]) * g[l]);
+      Aj[nn * (cid + 4) + c] = to_c64f(g[l]);
+    } else {
+      Aj[nn * 0 + c] = to_c64f((sigm * vn[0]) * g[l]);
+      Aj[nn * 1 + c] = to_c64f((sigm * vn[1]) * g[l]);
+      Aj[nn * 2 + c] = to_c64f((sigm * vn[2]) * g[l]);
+      Aj[nn * 3 + c] = to_c64f(h[l]);
+      Aj[nn * 7 + c] = to_c64f(beps * g[l]);
+    }
+  }
+}
+
+extern "C" int gbi_build_A32_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
+                                    const double* kn_dev, int did, int nrows, size_t base, size_t na, cplxf* A32,
+                                    cudaStream_t st) {
+  ABuildArgs a;
+  a.G = G; a.H = H; a.sid = sid; a.rowk = rowk;
+  a.eni = m->eni; a.md = m->md; a.sd = m->sd; a.etype = m->etype; a.wen = m->wen; a.kn = kn_dev;
+  a.Ne = m->sb_Ne[did]; a.did = did; a.nrows = nrows; a.base = base; a.nn = (size_t)m->NN; a.na = na; a.A = nullptr;
+  size_t tot = 16 * (size_t)a.Ne * a.Ne;
+  if (tot == 0) return 0;
+  k_build_A32<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(a, A32);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// ---- y = A x without forming A (FP64), for the refinement residual.
+// Row (domain d, collocation row, block cid) of A holds, for each column
+// (source element s, node l), h_l at x-component cid and g_l-terms at other
+// components (the coupling rules of k_build_A).  Per column they collapse to
+// two numbers per cid, P_cid (multiplies H) and Q_cid (multiplies G), so the
+// four rows of a collocation node are H P + G Q: one pass over G and H with
+// four right-hand sides.
+struct PQArgs {
+  const int* sid;
+  const int* eni;
+  const int* md;
+  const int* sd;
+  const int* etype;
+  const double* wen;
+  const double* kn;
+  int Ne, did;
+  size_t nn;
+  const cplx* x;
+  cplx* PQ;  // [8][N]: P_0..P_3, Q_0..Q_3
+};
+
+__global__ void k_pq_gather(PQArgs a) {
+  const size_t N = (size_t)a.Ne * 4;
+  size_t col = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= N) return;
+  int sidx = (int)(col / 4), l = (int)(col % 4);
+  int asd = abs(a.sid[sidx + 1]);
+  int nl = a.etype[asd] ? 4 : 3;
+  cplx P[4], Q[4];
+  for (int c = 0; c < 4; c++) { P[c] = cmk(0, 0); Q[c] = cmk(0, 0); }
+  if (l < nl) {
+    size_t c = (size_t)a.eni[asd * 4 + l];
+    cplx xv[8];
+    for (int q = 0; q < 8; q++) xv[q] = a.x[a.nn * q + c];
+    int mdid = a.md[asd], sdid = a.sd[asd];
+    if (a.did == mdid) {
+      for (int q = 0; q < 4; q++) { P[q] = xv[q]; Q[q] = -xv[q + 4]; }
+    } else {
+      cplx k1 = cmk(a.kn[2 * mdid], a.kn[2 * mdid + 1]);
+      cplx k2 = cmk(a.kn[2 * sdid], a.kn[2 * sdid + 1]);
+      cplx k12 = k1 * k1, k22 = k2 * k2;
+      cplx delt = k12 - k22;
+      cplx beps = cdivc(k12, k22);
+      cplx sigm = cmk(1.0, 0.0) - beps;
+      double vn[3];
+      for (int d = 0; d < 3; d++) vn[d] = a.wen[(size_t)asd * 12 + l * 3 + d];
+      double an = sqrt(vn[0] * vn[0] + vn[1] * vn[1] + vn[2] * vn[2]);
+      if (an != 0.0) { vn[0] /= an; vn[1] /= an; vn[2] /= an; }
+      for (int q = 0; q < 3; q++) { P[q] = xv[q]; Q[q] = (delt * vn[q]) * xv[3] + xv[q + 4]; }
+      P[3] = xv[3];
+      Q[3] = sigm * (xv[0] * vn[0] + xv[1] * vn[1] + xv[2] * vn[2]) + beps * xv[7];
+    }
+  }
+  for (int q = 0; q < 4; q++) { a.PQ[(size_t)q * N + col] = P[q]; a.PQ[(size_t)(4 + q) * N + col] = Q[q]; }
+}
+
+// one warp per collocation row: y[base + cid nrows + k] = (H P_cid + G Q_cid)[row]
+__global__ void k_apply_rows(const cplx* __restrict__ G, const cplx* __restrict__ H, const int* rowk, int Ne, int nrows,
+                             size_t base, const cplx* __restrict__ PQ, cplx* y) {
+  const int lane = threadIdx.x & 31;
+  const size_t N = (size_t)Ne * 4;
+  size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (row >= N) return;
+  int k = rowk[row];
+  if (k < 0) return;
+  const cplx* g = G + row * N;
+  const cplx* h = H + row * N;
+  double acc[8];
+  for (int i = 0; i < 8; i++) acc[i] = 0.0;
+  for (size_t c = lane; c < N; c += 32) {
+    cplx gv = g[c], hv = h[c];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      cplx p = PQ[(size_t)q * N + c], qq = PQ[(size_t)(4 + q) * N + c];
+      acc[2 * q] = fma(hv.x, p.x, acc[2 * q]);
+      acc[2 * q] = fma(-hv.y, p.y, acc[2 * q]);
+      acc[2 * q] = fma(gv.x, qq.x, acc[2 * q]);
+      acc[2 * q] = fma(-gv.y, qq.y, acc[2 * q]);
+      acc[2 * q + 1] = fma(hv.x, p.y, acc[2 * q + 1]);
+      acc[2 * q + 1] = fma(hv.y, p.x, acc[2 * q + 1]);
+      acc[2 * q + 1] = fma(gv.x, qq.y, acc[2 * q + 1]);
+      acc[2 * q + 1] = fma(gv.y, qq.x, acc[2 * q + 1]);
+    }
+  }
+  for (int i = 0; i < 8; i++)
+    for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], o);
+  if (lane == 0)
+    for (int q = 0; q < 4; q++) y[base + (size_t)q * nrows + k] = cmk(acc[2 * q], acc[2 * q + 1]);
+}
+
+extern "C" int gbi_apply_A_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
+                                  const double* kn_dev, int did, int nrows, size_t base, const cplx* x, cplx* PQ, cplx* y,
+                                  cudaStream_t st) {
+  const int Ne = m->sb_Ne[did];
+  const size_t N = (size_t)Ne * 4;
+  if (N == 0) return 0;
+  PQArgs a;
+  a.sid = sid; a.eni = m->eni; a.md = m->md; a.sd = m->sd; a.etype = m->etype; a.wen = m->wen; a.kn = kn_dev;
+  a.Ne = Ne; a.did = did; a.nn = (size_t)m->NN; a.x = x; a.PQ = PQ;
+  k_pq_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(a);
+  gbi_count_launch();
+  k_apply_rows<<<(unsigned)((N * 32 + 255) / 256), 256, 0, st>>>(G, H, rowk, Ne, nrows, base, PQ, y);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// r = b - y and the squared norms of r and b accumulated into nrm[0], nrm[1]
+__global__ void k_resid_finish(const cplx* b, const cplx* y, cplx* r, size_t n, double* nrm) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double rr = 0.0, bb = 0.0;
+  if (i < n) {
+    cplx t = cmk(b[i].x - y[i].x, b[i].y - y[i].y);
+    r[i] = t;
+    rr = t.x * t.x + t.y * t.y;
+    bb = b[i].x * b[i].x + b[i].y * b[i].y;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    rr += __shfl_down_sync(0xffffffffu, rr, o);
+    bb += __shfl_down_sync(0xffffffffu, bb, o);
+  }
+  if ((threadIdx.x & 31) == 0) { atomicAdd(nrm, rr); atomicAdd(nrm + 1, bb); }
+}
+extern "C" int gbi_resid_finish(const cplx* b, const cplx* y, cplx* r, size_t n, double* nrm, cudaStream_t st) {
+  GB_CUDA(cudaMemsetAsync(nrm, 0, 2 * sizeof(double), st));
+  k_resid_finish<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(b, y, r, n, nrm);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
 // ------------------------------------------------------------------ LU
 __device__ __forceinline__ double cabs1(cplx a) { return fabs(a.x) + fabs(a.y); }
 __device__ __forceinline__ float cabs1(cplxf a) { return fabsf(a.x) + fabsf(a.y); }
@@ -831,148 +1033,7 @@ extern "C" int gbi_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, co
   return cgemm_sub(M, N, K, A, lda, B, ldb, C, ldc, st);
 }
 
-__global__ void k_to_c64(const cplx* __restrict__ a, cplxf* __restrict__ b, size_t n) {
-  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (; i < n; i += stride) b[i] = cmkf((float)a[i].x, (float)a[i].y);
-}
-extern "C" int gbi_to_c64(const cplx* a, cplxf* b, size_t n, cudaStream_t st) {
-  k_to_c64<<<152 * 8, 256, 0, st>>>(a, b, n);
-  gbi_count_launch();
-  GB_CUDA(cudaGetLastError());
-  return 0;
-}
-
-// ---- single right-hand side solve with LU factors (row-major, in place on x)
-// x <- P x (interchanges in order)
-template <class T>
-__global__ void k_perm1(T* x, int n, const int64_t* ipiv) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  for (int j = 0; j < n; j++) {
-    int p = (int)ipiv[j];
-    if (p != j) { T t = x[j]; x[j] = x[p]; x[p] = t; }
-  }
-}
-// diagonal block k0..k0+nb-1: unit lower (UPPER = 0) or non-unit upper solve,
-// column-oriented sweep, one thread per row of the block
-template <class T, int UPPER>
-__global__ void k_trsv_diag(const T* LU, size_t lda, int k0, int nb, T* x) {
-  __shared__ T xs[LU_NB];
-  int i = threadIdx.x;
-  if (i < nb) xs[i] = x[k0 + i];
-  __syncthreads();
-  if (!UPPER) {
-    for (int j = 0; j < nb; j++) {
-      T xj = xs[j];
-      __syncthreads();
-      if (i > j && i < nb) xs[i] -= LU[(size_t)(k0 + i) * lda + k0 + j] * xj;
-      __syncthreads();
-    }
-  } else {
-    for (int j = nb - 1; j >= 0; j--) {
-      if (i == j) xs[j] = cdivc(xs[j], LU[(size_t)(k0 + j) * lda + k0 + j]);
-      __syncthreads();
-      T xj = xs[j];
-      if (i < j) xs[i] -= LU[(size_t)(k0 + i) * lda + k0 + j] * xj;
-      __syncthreads();
-    }
-  }
-  if (i < nb) x[k0 + i] = xs[i];
-}
-// rows r in [r0, r1): x[r] -= sum_j LU[r][k0+j] x[k0+j], j < nb (warp per row)
-template <class T>
-__global__ void k_trsv_update(const T* LU, size_t lda, int r0, int r1, int k0, int nb, T* x) {
-  int w = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  int lane = threadIdx.x & 31;
-  int r = r0 + w;
-  if (r >= r1) return;
-  const T* row = LU + (size_t)r * lda + k0;
-  typedef typename RealOf<T>::type R;
-  R sr = 0, si = 0;
-  for (int j = lane; j < nb; j += 32) {
-    T a = row[j], b = x[k0 + j];
-    sr += a.x * b.x - a.y * b.y;
-    si += a.x * b.y + a.y * b.x;
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    sr += __shfl_down_sync(0xffffffffu, sr, o);
-    si += __shfl_down_sync(0xffffffffu, si, o);
-  }
-  if (lane == 0) { x[r].x -= sr; x[r].y -= si; }
-}
-
-template <class T>
-static int lu_solve1(const T* LU, size_t lda, int n, const int64_t* ipiv, T* x, cudaStream_t st) {
-  k_perm1<T><<<1, 32, 0, st>>>(x, n, ipiv);
-  gbi_count_launch();
-  GB_CUDA(cudaGetLastError());
-  for (int k = 0; k < n; k += LU_NB) {
-    int nb = (n - k < LU_NB) ? n - k : LU_NB;
-    k_trsv_diag<T, 0><<<1, LU_NB, 0, st>>>(LU, lda, k, nb, x);
-    gbi_count_launch();
-    int rows = n - k - nb;
-    if (rows > 0) {
-      k_trsv_update<T><<<(unsigned)(((size_t)rows * 32 + 255) / 256), 256, 0, st>>>(LU, lda, k + nb, n, k, nb, x);
-      gbi_count_launch();
-    }
-  }
-  int last = ((n - 1) / LU_NB) * LU_NB;
-  for (int k = last; k >= 0; k -= LU_NB) {
-    int nb = (n - k < LU_NB) ? n - k : LU_NB;
-    k_trsv_diag<T, 1><<<1, LU_NB, 0, st>>>(LU, lda, k, nb, x);
-    gbi_count_launch();
-    if (k > 0) {
-      k_trsv_update<T><<<(unsigned)(((size_t)k * 32 + 255) / 256), 256, 0, st>>>(LU, lda, 0, k, k, nb, x);
-      gbi_count_launch();
-    }
-  }
-  GB_CUDA(cudaGetLastError());
-  return 0;
-}
-
-extern "C" int gbi_csolve1(const cplxf* LU, size_t lda, int n, const int64_t* ipiv, cplxf* x, cudaStream_t st) {
-  return lu_solve1<cplxf>(LU, lda, n, ipiv, x, st);
-}
-extern "C" int gbi_zsolve1(const cplx* LU, size_t lda, int n, const int64_t* ipiv, cplx* x, cudaStream_t st) {
-  return lu_solve1<cplx>(LU, lda, n, ipiv, x, st);
-}
-
-// r = b - A x (FP64), and the squared norms of r and b accumulated into nrm[0], nrm[1]
-__global__ void k_residual(const cplx* __restrict__ A, size_t lda, int n, const cplx* __restrict__ x,
-                           const cplx* __restrict__ b, cplx* r, double* nrm) {
-  int w = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  int lane = threadIdx.x & 31;
-  if (w >= n) return;
-  const cplx* row = A + (size_t)w * lda;
-  double sr = 0.0, si = 0.0;
-  for (int j = lane; j < n; j += 32) {
-    cplx a = row[j], v = x[j];
-    sr = fma(a.x, v.x, sr);
-    sr = fma(-a.y, v.y, sr);
-    si = fma(a.x, v.y, si);
-    si = fma(a.y, v.x, si);
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    sr += __shfl_down_sync(0xffffffffu, sr, o);
-    si += __shfl_down_sync(0xffffffffu, si, o);
-  }
-  if (lane == 0) {
-    cplx rr = cmk(b[w].x - sr, b[w].y - si);
-    r[w] = rr;
-    atomicAdd(nrm, rr.x * rr.x + rr.y * rr.y);
-    atomicAdd(nrm + 1, b[w].x * b[w].x + b[w].y * b[w].y);
-  }
-}
-extern "C" int gbi_residual(const cplx* A, size_t lda, int n, const cplx* x, const cplx* b, cplx* r, double* nrm,
-                            cudaStream_t st) {
-  GB_CUDA(cudaMemsetAsync(nrm, 0, 2 * sizeof(double), st));
-  k_residual<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(A, lda, n, x, b, r, nrm);
-  gbi_count_launch();
-  GB_CUDA(cudaGetLastError());
-  return 0;
-}
-
-// x += (cplx) d ; also converts: d64 -> d32 helper
+// x += d (FP32 correction) and r -> d (FP64 residual rounded to FP32)
 __global__ void k_axpy_c64(cplx* x, const cplxf* d, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) { x[i].x += (double)d[i].x; x[i].y += (double)d[i].y; }

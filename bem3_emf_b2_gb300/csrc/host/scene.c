@@ -1,23 +1,37 @@
 /*
- * scene.c -- single-object scene without intermediate files (gb_scene.h).
+ * scene.c -- single- and multi-object scenes without intermediate files
+ * (gb_scene.h).
  */
 #include "gb_host.h"
 #include "gb_scene.h"
 
-DOMD *gbh_scene_open(const char *medium_file,const char *mesh_file,const char *ipw_file)
+/* host setup of one object in md (rotation th about rv, then translation tv,
+ * as d3b2_create_matrix's optional arguments); 0 on success */
+static int gbh_setup_object(DOMD *md,const char *medium_file,const char *mesh_file,const char *ipw_file,
+                            const double *rv,double th,const double *tv)
 {
-  DOMD *md=(DOMD *)m_alloc2(1,sizeof(DOMD),"scene.c md");
+  memset(md,0,sizeof(DOMD));
   init_mfb(&md->mw);
-  if(read_data_mfb_ipw((char *)ipw_file,&md->mw)==0){ printf("scene.c: no plane wave in %s\n",ipw_file); free(md); return NULL; }
+  if(read_data_mfb_ipw((char *)ipw_file,&md->mw)==0){ printf("scene.c: no plane wave in %s\n",ipw_file); return -1; }
   gb_read_medium_data((char *)medium_file,md);
   gb_read_mesh_data((char *)mesh_file,md);
   md->rv[0]=1.0;
+  if(rv){ md->rv[0]=rv[0]; md->rv[1]=rv[1]; md->rv[2]=rv[2]; }
+  md->th=th;
+  if(tv){ md->tv[0]=tv[0]; md->tv[1]=tv[1]; md->tv[2]=tv[2]; }
   initialize_domd2(md);
   md->cm.MN=md->MN;
   md->cm.nn=(size_t)md->bd.NN;
   md->cm.na=8*md->cm.nn;
   gb_initalize_cmd2(&md->cm);
   gb_init_boundary_data_u2(md);
+  return 0;
+}
+
+DOMD *gbh_scene_open(const char *medium_file,const char *mesh_file,const char *ipw_file)
+{
+  DOMD *md=(DOMD *)m_alloc2(1,sizeof(DOMD),"scene.c md");
+  if(gbh_setup_object(md,medium_file,mesh_file,ipw_file,NULL,0.0,NULL)){ free(md); return NULL; }
   return md;
 }
 
@@ -87,4 +101,64 @@ void *gbh_scene_obj(DOMD *md)
     gb_dev_set_flags(md,GB_F_INC,0);
   }
   return o;
+}
+
+/* ------------------------------------------------------------ multi-object */
+MOBJ *gbh_mscene_open(int n,const char *const *medium_files,const char *const *mesh_files,const char *ipw_file,
+                      const double *rv,const double *th,const double *tv)
+{
+  if(n<1){ printf("gbh_mscene_open: no objects\n"); return NULL; }
+  MOBJ *mo=(MOBJ *)m_alloc2(1,sizeof(MOBJ),"scene.c mo");
+  mo->N=n;
+  gb_mo_malloc(mo);
+  for(int m=0;m<n;m++){
+    if(gbh_setup_object(&mo->md[m],medium_files[m],mesh_files[m],ipw_file,rv?rv+3*m:NULL,th?th[m]:0.0,tv?tv+3*m:NULL)){
+      printf("gbh_mscene_open: object %d failed\n",m);
+      return NULL;
+    }
+    snprintf(mo->mod_fn[m],FNLGTH,"object_%02d",m);
+  }
+  return mo;
+}
+
+int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double *N)
+{
+  for(int m=0;m<mo->N;m++){
+    DOMD *md=&mo->md[m];
+    gb_obj *o=gb_dev(md);
+    for(int d=0;d<=md->MN;d++)
+      if(gb_assemble(o,d,type)){ printf("gbh_mscene_step: %s\n",gb_last_error()); return -1; }
+    if(form==0 ? gb_invA_compute(o) : gb_factor_mixed(o)){ printf("gbh_mscene_step: %s\n",gb_last_error()); return -1; }
+    /* matrices and the factors are resident: the iteration reads no .cmat file */
+    gb_dev_set_flags(md,GB_F_CMAT|GB_F_INV,GB_F_BV);
+  }
+  mo_solve_bv(mo);
+  for(int m=0;m<mo->N;m++){
+    double c[3];
+    for(int i=0;i<3;i++) c[i]=rc?rc[3*m+i]:mo->md[m].tv[i];
+    if(mo_force_FN(F+3*m,N+3*m,c,m,0,mo)<0) return -1;
+  }
+  return 0;
+}
+
+void gbh_mscene_drop_device(MOBJ *mo){ for(int m=0;m<mo->N;m++) gb_dev_release(&mo->md[m]); }
+
+size_t gbh_mscene_h2d_bytes(MOBJ *mo)
+{
+  size_t t=0;
+  for(int m=0;m<mo->N;m++) t+=gbh_scene_h2d_bytes(&mo->md[m]);
+  return t;
+}
+
+size_t gbh_mscene_d2h_bytes(MOBJ *mo)
+{
+  size_t t=0;
+  for(int m=0;m<mo->N;m++) t+=gbh_scene_d2h_bytes(&mo->md[m]);
+  return t;
+}
+
+void gbh_mscene_close(MOBJ *mo)
+{
+  mo_finalize(mo);  /* releases the device copies too */
+  free(mo);
 }

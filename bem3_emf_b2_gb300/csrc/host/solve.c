@@ -11,6 +11,15 @@
  */
 #include "gb_host.h"
 
+/* progress messages of mo_solve_bv (the reference's); off with gbh_set_quiet(1) */
+static int g_quiet=0;
+void gbh_set_quiet(int q){ g_quiet=q; }
+/* iteration count and convergence measure of the last mo_solve_bv */
+static int g_last_iter=0;
+static double g_last_cc=0.0;
+void gbh_last_iteration(int *iter,double *cc){ *iter=g_last_iter; *cc=g_last_cc; }
+#define MSG(...) do{ if(!g_quiet){ printf(__VA_ARGS__); fflush(stdout); } }while(0)
+
 static double complex *gb_read_cmat_file(const char *fn,size_t n)
 {
   FILE *fp=fopen(fn,"rb");
@@ -139,21 +148,21 @@ void gb_bv_to_device(DOMD *md)
 static void gb_solve_coefficient_mEMP(int flg,DOMD *md)
 {
   time_t ms,me;
-  if(flg==1){ printf("  solve mEMP boundary value "); fflush(stdout); }
+  if(flg==1){ MSG("  solve mEMP boundary value ");  }
   time(&ms);
   if(gb_solve_mEMP(gb_dev(md))) gb_die("mo_solve.c, solve_coefficient_mEMP()");
   time(&me);
-  if(flg==1) printf("finished. Elapsed time : %5g (sec)\n",difftime(me,ms));
+  if(flg==1) MSG("finished. Elapsed time : %5g (sec)\n",difftime(me,ms));
 }
 
 static void gb_solve_coefficient_EH(int flg,DOMD *md)
 {
   time_t ms,me;
-  if(flg==1){ printf("  solve EH boundary value   "); fflush(stdout); }
+  if(flg==1){ MSG("  solve EH boundary value   ");  }
   time(&ms);
   if(gb_solve_EH(gb_dev(md))) gb_die("mo_solve.c, solve_coefficient_EH()");
   time(&me);
-  if(flg==1) printf("finished. Elapsed time : %5g (sec)\n",difftime(me,ms));
+  if(flg==1) MSG("finished. Elapsed time : %5g (sec)\n",difftime(me,ms));
 }
 
 static double gb_ccd_f(MOBJ *mo)
@@ -174,41 +183,43 @@ void mo_solve_bv(MOBJ *mo)
     gb_cmat_read(&mo->md[m],1);
     gb_upload_incident(&mo->md[m]);
   }
+  g_last_iter=1;
+  g_last_cc=0.0;
   if(mo->N==1){
-    printf("\nsingle object\n");
+    MSG("\nsingle object\n");
     gb_solve_coefficient_mEMP(1,&mo->md[0]);
     gb_solve_coefficient_EH(1,&mo->md[0]);
   }
   else {
-    printf("\ninitialize boundary value\n");
+    MSG("\ninitialize boundary value\n");
     for(int m=0;m<mo->N;m++){
-      printf("object % 2d\n",m);
+      MSG("object % 2d\n",m);
       gb_solve_coefficient_mEMP(1,&mo->md[m]);
     }
-    printf("\nthe first iterative operation\n");
+    MSG("\nthe first iterative operation\n");
     time(&start);
     for(int m=0;m<mo->N;m++) if(gb_reset_incident(gb_dev(&mo->md[m]))) gb_die("mo_solve.c, reset_incident_bd()");
     for(int m=0;m<mo->N;m++){
-      printf("object % 2d\n",m);
-      printf("  add scattered field       "); fflush(stdout);
+      MSG("object % 2d\n",m);
+      MSG("  add scattered field       "); 
       time(&ms);
       for(int d=0;d<mo->N;d++){
         if(d==m) continue;
         if(gb_add_scattered(gb_dev(&mo->md[d]),gb_dev(&mo->md[m]),PREC_DEF)) gb_die("mo_solve.c, add_scattered_mEMP()");
       }
       time(&me);
-      printf("finished. Elapsed time : %5g (sec)\n",difftime(me,ms));
+      MSG("finished. Elapsed time : %5g (sec)\n",difftime(me,ms));
     }
     for(int m=0;m<mo->N;m++){
-      printf("object % 2d\n",m);
+      MSG("object % 2d\n",m);
       gb_solve_coefficient_mEMP(1,&mo->md[m]);
     }
     time(&end);
-    printf("Estimated time per one iteration : %5g (sec)\n\n",difftime(end,start));
-    printf("iterative operation start. convergence criterion cc < %g and count > %d\n",CCD,ITER_MIN);
+    MSG("Estimated time per one iteration : %5g (sec)\n\n",difftime(end,start));
+    MSG("iterative operation start. convergence criterion cc < %g and count > %d\n",CCD,ITER_MIN);
     time(&start);
     for(iter=2;iter<itermax;iter++){
-      printf("count =% 3d",iter);
+      MSG("count =% 3d",iter);
       for(int m=0;m<mo->N;m++) if(gb_reset_incident(gb_dev(&mo->md[m]))) gb_die("mo_solve.c, reset_incident_bd()");
       for(int m=0;m<mo->N;m++)
         for(int d=0;d<mo->N;d++){
@@ -217,14 +228,16 @@ void mo_solve_bv(MOBJ *mo)
         }
       for(int m=0;m<mo->N;m++) gb_solve_coefficient_mEMP(0,&mo->md[m]);
       double cc=gb_ccd_f(mo);
-      printf(", cc = %g\n",cc);
-      fflush(stdout);
+      g_last_iter=iter;
+      g_last_cc=cc;
+      MSG(", cc = %g\n",cc);
+      
       if(cc<CCD && iter>ITER_MIN) break;
     }
-    if(iter==itermax) printf("The maximum number of iterations has been reached (The result has not converged).\n");
+    if(iter==itermax) MSG("The maximum number of iterations has been reached (The result has not converged).\n");
     for(int m=0;m<mo->N;m++) gb_solve_coefficient_EH(0,&mo->md[m]);
     time(&end);
-    printf("finished. Elapsed time : %5g (sec)\n",difftime(end,start));
+    MSG("finished. Elapsed time : %5g (sec)\n",difftime(end,start));
   }
   for(int m=0;m<mo->N;m++){
     gb_bv_to_host(&mo->md[m]);

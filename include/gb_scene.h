@@ -32,6 +32,27 @@ void *gbh_scene_stream(DOMD *md);
  * the incident potential is uploaded on first use */
 void *gbh_scene_obj(DOMD *md);
 
+/* Multi-object scene (reference d3b2_create_matrix per object + mo_solve_bv
+ * + mo_force_FN, mo_solve.c:10-88): object m is read from medium_files[m] and
+ * mesh_files[m], rotated by th[m] about the axis rv[3m..3m+2] and then
+ * translated by tv[3m..3m+2] (d3b2_create_matrix's optional arguments; rv, th,
+ * tv may be NULL), all lit by the plane waves of ipw_file.  NULL on failure. */
+MOBJ *gbh_mscene_open(int n, const char *const *medium_files, const char *const *mesh_files, const char *ipw_file,
+                      const double *rv, const double *th, const double *tv);
+/* device step of the whole scene: assembly and factorisation (form as in
+ * gbh_scene_step) of every object, the multiple-scattering iteration, then
+ * force and torque of each object (type-0 surface rule) about rc[3m..3m+2]
+ * (rc NULL: the object's translation point); F, N: 3 n */
+int gbh_mscene_step(MOBJ *mo, int form, int type, const double *rc, double *F, double *N);
+void gbh_mscene_drop_device(MOBJ *mo);
+size_t gbh_mscene_h2d_bytes(MOBJ *mo);
+size_t gbh_mscene_d2h_bytes(MOBJ *mo);
+void gbh_mscene_close(MOBJ *mo);
+/* suppress (1) or restore (0) the progress messages of mo_solve_bv */
+void gbh_set_quiet(int q);
+/* iteration count and convergence measure cc of the last mo_solve_bv */
+void gbh_last_iteration(int *iter, double *cc);
+
 #ifdef __cplusplus
 }
 #endif
