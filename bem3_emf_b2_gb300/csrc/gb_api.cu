@@ -47,6 +47,7 @@ int gbi_apply_A_domain(const cplx* G, const cplx* H, const int* sid, const int* 
                        const double* kn_dev, int did, int nrows, size_t base, const cplx* x, cplx* PQ, cplx* y,
                        cudaStream_t st);
 int gbi_resid_finish(const cplx* b, const cplx* y, cplx* r, size_t n, double* nrm, cudaStream_t st);
+int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cplx* X, int* iters, double* relres, cudaStream_t st);
 int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU32, size_t lda, int n, const int* perm,
                 cudaStream_t st);
 int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st);
@@ -658,6 +659,14 @@ extern "C" int gb_solve_EH(gb_obj* o) {
       return -1;
     }
     rc = gbi_deh_build(o->G[d], o->H[d], o->rowk[d], Ne, nn, o->bE[d], o->bH[d], Ac, Bc, o->st);
+    if (!rc && o->have_lu32) {
+      // chosen form: complex-FP32 factors + FP64 refinement (as for A)
+      rc = gbi_zgesv_mixed(Ac, nn, Bc, 6, Yc, nullptr, nullptr, o->st);
+      if (!rc) rc = gbi_deh_scatter(Yc, o->rowk[d], Ne, o->bdE[d], o->bdH[d], o->st);
+      if (!rc) rc = sync_obj(o, "gb_solve_EH");
+      cudaFree(Ac); cudaFree(Bc); cudaFree(Yc); cudaFree(perm); cudaFree(ipiv); cudaFree(info);
+      continue;
+    }
     if (!rc) rc = gbi_zgetrf(Ac, nn, nn, ipiv, info, o->st);
     int hinfo = 0;
     if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||

@@ -1033,6 +1033,34 @@ extern "C" int gbi_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, co
   return cgemm_sub(M, N, K, A, lda, B, ldb, C, ldc, st);
 }
 
+// complex FP64 -> complex FP32 (n elements)
+__global__ void k_to_c64(const cplx* __restrict__ a, cplxf* __restrict__ b, size_t n) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (; i < n; i += stride) b[i] = cmkf((float)a[i].x, (float)a[i].y);
+}
+extern "C" int gbi_to_c64(const cplx* a, cplxf* b, size_t n, cudaStream_t st) {
+  k_to_c64<<<152 * 8, 256, 0, st>>>(a, b, n);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+// out[0] += sum |a_i|^2
+__global__ void k_sqnorm(const cplx* a, size_t n, double* out) {
+  size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  double v = 0.0;
+  if (i < n) v = a[i].x * a[i].x + a[i].y * a[i].y;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) atomicAdd(out, v);
+}
+
+// Solve A X = B (A n x n FP64, B n x nrhs, nrhs <= 8, packed) with complex-FP32
+// factors of A (tensor-core LU) and FP64 iterative refinement on the FP64 A:
+// X += LU32^-1 (B - A X) until ||B - A X||_F <= 1e-13 ||B||_F (at most 30
+// corrections).  *iters, *relres report the refinement.
+extern "C" int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cplx* X, int* iters, double* relres,
+                               cudaStream_t st);
 // x += d (FP32 correction) and r -> d (FP64 residual rounded to FP32)
 __global__ void k_axpy_c64(cplx* x, const cplxf* d, int n) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1091,30 +1119,60 @@ __global__ void k_gather_rows(const T* X, size_t ldx, int n, int nrhs, const int
   int i = (int)(q / nrhs), c = (int)(q % nrhs);
   Y[(size_t)i * nrhs + c] = X[(size_t)perm[i] * ldx + c];
 }
+// X[k0..k0+nb) <- L11^-1 X (UPPER = 0, unit lower) or U11^-1 X (UPPER = 1)
+// for the packed right-hand sides X (n x nrhs): one warp per right-hand side,
+// lane l holds rows l and l + 32; the diagonal block is staged transposed in
+// shared memory by the whole block (256 threads), with the inverted diagonal
 template <class T, int UPPER>
 __global__ void k_trsm_diag_multi(const T* LU, size_t lda, int k0, int nb, T* X, int nrhs) {
-  __shared__ T xs[LU_NB];
-  const int c = blockIdx.x;  // right-hand side
-  int i = threadIdx.x;
-  if (i < nb) xs[i] = X[(size_t)(k0 + i) * nrhs + c];
+  extern __shared__ __align__(16) unsigned char tdraw[];
+  const int ld = nb + 1;  // padded: the transposing stores spread over the banks
+  T* sT = (T*)tdraw;      // sT[j * ld + i] = block[i][j]
+  T* dinv = sT + nb * ld;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    int i = t / nb, j = t % nb;
+    sT[j * ld + i] = LU[(size_t)(k0 + i) * lda + k0 + j];
+  }
   __syncthreads();
+  if (UPPER)
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+      T one;
+      one.x = 1; one.y = 0;
+      dinv[j] = cdivc(one, sT[j * ld + j]);
+    }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
+  if (c >= nrhs) return;
+  const int i0 = lane, i1 = lane + 32;
+  T x0, x1;
+  x0.x = 0; x0.y = 0; x1 = x0;
+  if (i0 < nb) x0 = X[(size_t)(k0 + i0) * nrhs + c];
+  if (i1 < nb) x1 = X[(size_t)(k0 + i1) * nrhs + c];
   if (!UPPER) {
     for (int j = 0; j < nb; j++) {
-      T xj = xs[j];
-      __syncthreads();
-      if (i > j && i < nb) xs[i] -= LU[(size_t)(k0 + i) * lda + k0 + j] * xj;
-      __syncthreads();
+      T v = (j < 32) ? x0 : x1;
+      T xj;
+      xj.x = __shfl_sync(0xffffffffu, v.x, j & 31);
+      xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
+      const T* col = sT + j * ld;
+      if (i0 > j && i0 < nb) x0 -= col[i0] * xj;
+      if (i1 > j && i1 < nb) x1 -= col[i1] * xj;
     }
   } else {
     for (int j = nb - 1; j >= 0; j--) {
-      if (i == j) xs[j] = cdivc(xs[j], LU[(size_t)(k0 + j) * lda + k0 + j]);
-      __syncthreads();
-      T xj = xs[j];
-      if (i < j) xs[i] -= LU[(size_t)(k0 + i) * lda + k0 + j] * xj;
-      __syncthreads();
+      T v = (j < 32) ? x0 : x1;
+      T xj;
+      xj.x = __shfl_sync(0xffffffffu, v.x, j & 31);
+      xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
+      xj = xj * dinv[j];
+      if (lane == (j & 31)) { if (j < 32) x0 = xj; else x1 = xj; }
+      const T* col = sT + j * ld;
+      if (i0 < j) x0 -= col[i0] * xj;
+      if (i1 < j) x1 -= col[i1] * xj;
     }
   }
-  if (i < nb) X[(size_t)(k0 + i) * nrhs + c] = xs[i];
+  if (i0 < nb) X[(size_t)(k0 + i0) * nrhs + c] = x0;
+  if (i1 < nb) X[(size_t)(k0 + i1) * nrhs + c] = x1;
 }
 template <class T>
 __global__ void k_trsm_update_multi(const T* LU, size_t lda, int r0, int r1, int k0, int nb, T* X, int nrhs) {
@@ -1153,11 +1211,14 @@ static int lu_solve_multi(const T* LU, size_t lda, int n, const int* perm, const
                           cudaStream_t st) {
   if (nrhs < 1 || nrhs > 8) { gbi_set_error("lu_solve_multi: nrhs %d not in 1..8", nrhs); return -1; }
   size_t tot = (size_t)n * nrhs;
+  const size_t sm_diag = (size_t)(LU_NB * (LU_NB + 1) + LU_NB) * sizeof(T);
+  GB_CUDA(cudaFuncSetAttribute(k_trsm_diag_multi<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_diag));
+  GB_CUDA(cudaFuncSetAttribute(k_trsm_diag_multi<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_diag));
   k_gather_rows<T><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(X, ldx, n, nrhs, perm, Y);
   gbi_count_launch();
   for (int k = 0; k < n; k += LU_NB) {
     int nb = (n - k < LU_NB) ? n - k : LU_NB;
-    k_trsm_diag_multi<T, 0><<<nrhs, LU_NB, 0, st>>>(LU, lda, k, nb, Y, nrhs);
+    k_trsm_diag_multi<T, 0><<<1, 256, sm_diag, st>>>(LU, lda, k, nb, Y, nrhs);
     gbi_count_launch();
     int rows = n - k - nb;
     if (rows > 0) {
@@ -1168,7 +1229,7 @@ static int lu_solve_multi(const T* LU, size_t lda, int n, const int* perm, const
   int last = ((n - 1) / LU_NB) * LU_NB;
   for (int k = last; k >= 0; k -= LU_NB) {
     int nb = (n - k < LU_NB) ? n - k : LU_NB;
-    k_trsm_diag_multi<T, 1><<<nrhs, LU_NB, 0, st>>>(LU, lda, k, nb, Y, nrhs);
+    k_trsm_diag_multi<T, 1><<<1, 256, sm_diag, st>>>(LU, lda, k, nb, Y, nrhs);
     gbi_count_launch();
     if (k > 0) {
       k_trsm_update_multi<T><<<(unsigned)(((size_t)k * 32 + 255) / 256), 256, 0, st>>>(LU, lda, 0, k, k, nb, Y, nrhs);
@@ -1185,4 +1246,71 @@ extern "C" int gbi_zsolve_multi(const cplx* LU, size_t lda, int n, const int* pe
 extern "C" int gbi_csolve_multi(const cplxf* LU, size_t lda, int n, const int* perm, const cplxf* X, size_t ldx, int nrhs,
                                 cplxf* Y, cudaStream_t st) {
   return lu_solve_multi<cplxf>(LU, lda, n, perm, X, ldx, nrhs, Y, st);
+}
+
+extern "C" int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
+extern "C" int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st);
+
+extern "C" int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cplx* X, int* iters, double* relres,
+                               cudaStream_t st) {
+  if (nrhs < 1 || nrhs > 8) { gbi_set_error("gbi_zgesv_mixed: nrhs %d not in 1..8", nrhs); return -1; }
+  const size_t nn = (size_t)n * n, nb = (size_t)n * nrhs;
+  cplxf *A32 = nullptr, *D = nullptr, *Y = nullptr;
+  cplx* R = nullptr;
+  int64_t* ipiv = nullptr;
+  int *perm = nullptr, *info = nullptr;
+  double* nrm = nullptr;
+  GB_CUDA(cudaMallocAsync((void**)&A32, nn * sizeof(cplxf), st));
+  GB_CUDA(cudaMallocAsync((void**)&D, nb * sizeof(cplxf), st));
+  GB_CUDA(cudaMallocAsync((void**)&Y, nb * sizeof(cplxf), st));
+  GB_CUDA(cudaMallocAsync((void**)&R, nb * sizeof(cplx), st));
+  GB_CUDA(cudaMallocAsync((void**)&ipiv, (size_t)n * sizeof(int64_t), st));
+  GB_CUDA(cudaMallocAsync((void**)&perm, (size_t)n * sizeof(int), st));
+  GB_CUDA(cudaMallocAsync((void**)&info, sizeof(int), st));
+  GB_CUDA(cudaMallocAsync((void**)&nrm, 2 * sizeof(double), st));
+  int rc = gbi_to_c64(A, A32, nn, st);
+  if (!rc) rc = gbi_cgetrf(A32, n, n, ipiv, info, st);
+  if (!rc) rc = gbi_make_perm(ipiv, n, perm, st);
+  int hinfo = 0;
+  if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaStreamSynchronize(st) != cudaSuccess)) {
+    gbi_set_error("gbi_zgesv_mixed: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
+  }
+  if (!rc && hinfo) { gbi_set_error("mixed solve: FP32 factor singular (info=%d)", hinfo); rc = -1; }
+  if (!rc && (cudaMemsetAsync(X, 0, nb * sizeof(cplx), st) != cudaSuccess ||
+              cudaMemcpyAsync(R, B, nb * sizeof(cplx), cudaMemcpyDeviceToDevice, st) != cudaSuccess))
+    rc = -1;
+  double rel = 1.0;
+  int it = 0;
+  const unsigned gb = (unsigned)((nb + 255) / 256);
+  for (; !rc && it < 31; it++) {
+    if (it > 0) {
+      // R = B - A X (FP64)
+      if (cudaMemcpyAsync(R, B, nb * sizeof(cplx), cudaMemcpyDeviceToDevice, st) != cudaSuccess) { rc = -1; break; }
+      if (gemm_sub(n, nrhs, n, A, n, X, nrhs, R, nrhs, st)) { rc = -1; break; }
+      if (cudaMemsetAsync(nrm, 0, 2 * sizeof(double), st) != cudaSuccess) { rc = -1; break; }
+      k_sqnorm<<<gb, 256, 0, st>>>(R, nb, nrm);
+      k_sqnorm<<<gb, 256, 0, st>>>(B, nb, nrm + 1);
+      gbi_count_launch();
+      gbi_count_launch();
+      double h[2];
+      if (cudaMemcpyAsync(h, nrm, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess) { rc = -1; break; }
+      rel = (h[1] > 0.0) ? sqrt(h[0] / h[1]) : 0.0;
+      if (rel <= 1e-13) break;
+    }
+    k_c128_to_c64_scaled<<<gb, 256, 0, st>>>(R, D, (int)nb);
+    gbi_count_launch();
+    if (lu_solve_multi<cplxf>(A32, n, n, perm, D, nrhs, nrhs, Y, st)) { rc = -1; break; }
+    k_axpy_c64<<<gb, 256, 0, st>>>(X, Y, (int)nb);
+    gbi_count_launch();
+  }
+  if (iters) *iters = it;
+  if (relres) *relres = rel;
+  if (!rc && rel > 1e-10) { gbi_set_error("mixed solve: refinement stalled at relative residual %g", rel); rc = -1; }
+  cudaFreeAsync(A32, st); cudaFreeAsync(D, st); cudaFreeAsync(Y, st); cudaFreeAsync(R, st);
+  cudaFreeAsync(ipiv, st); cudaFreeAsync(perm, st); cudaFreeAsync(info, st); cudaFreeAsync(nrm, st);
+  if (!rc) GB_CUDA(cudaGetLastError());
+  return rc;
 }
