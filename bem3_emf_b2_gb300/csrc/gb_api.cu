@@ -17,6 +17,8 @@ int gbi_upload_tables_asm(const void* t);
 int gbi_upload_tables_field(const void* t);
 int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* G, cplx* H, cplx* dG, cplx* dH, double* dF,
                         double* Fs, cudaStream_t st);
+int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG, cplx* dH,
+                         double* dF, double* Fs, cudaStream_t st);
 int gbi_build_A_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
                        const double* kn_dev, int did, int nrows, size_t base, size_t na, cplx* A, cudaStream_t st);
 int gbi_zgetrf(cplx* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
@@ -293,14 +295,18 @@ static int check_did(gb_obj* o, int did) {
   return 0;
 }
 
-extern "C" int gb_assemble(gb_obj* o, int did, int type) {
+extern "C" int gb_assemble(gb_obj* o, int did, int type) { return gb_assemble2(o, did, type, 0); }
+
+extern "C" int gb_assemble2(gb_obj* o, int did, int type, int precision) {
   if (check_did(o, did)) return -1;
   if (type < 0 || type > 3) { gbi_set_error("gb_assemble: quadrature type %d not in 0..3", type); return -1; }
+  if (precision != 0 && precision != 1) { gbi_set_error("gb_assemble: precision %d not 0 or 1", precision); return -1; }
   if (ensure_cmatrix(o, did)) return -1;
   size_t Ne = (size_t)o->m.sb_Ne[did];
   double* Fs = nullptr;
   if (dalloc((void**)&Fs, 3 * 4 * Ne * Ne * sizeof(double))) return -1;
-  int rc = gbi_assemble_domain(&o->m, did, type, o->G[did], o->H[did], o->dG[did], o->dH[did], o->dF[did], Fs, o->st);
+  int rc = gbi_assemble_domain2(&o->m, did, type, precision, o->G[did], o->H[did], o->dG[did], o->dH[did], o->dF[did],
+                                Fs, o->st);
   cudaError_t e = cudaStreamSynchronize(o->st);
   cudaFree(Fs);
   if (rc) return -1;

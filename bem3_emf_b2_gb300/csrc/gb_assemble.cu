@@ -19,6 +19,20 @@
 //                   1 + F (domain 0) or F on the diagonal of H.
 // Per-pair solid-angle terms go through a scratch array Fs[N][Ne][3] so the
 // row sums are deterministic.
+//
+// Opt-in FP32 regular pairs (precision 1; the scene steps use precision 0
+// because the per-pair FP32 constants -- wave number, scale, weights --
+// bias every far entry alike by ~1e-7, which moves the radiation force by up
+// to ~1e-6): k_asm_regular_f32 integrates the GLN x GLN rule
+// of every regular pair in FP32, relative to the source element's centre
+// (the phase e^{ikR} = e^{ik|R0|} e^{ik(|R|-|R0|)}, the first factor in FP64
+// once per pair, the second from the stably computed difference
+// (2 R0.d + |d|^2) / (|R| + |R0|), so the phase error does not grow with the
+// distance).  Pairs closer than GB_F32_NEAR element radii, and pairs whose
+// FP32 |Re dF/dt| exceeds 0.45 (the CBD_SDF = 0.5 decision and its
+// neighbourhood) or is not finite, are flagged and integrated by the FP64
+// kernel, which makes the GLN/GHN decision exactly as the reference.
+// Singular pairs stay FP64.
 #include "gb_quad.cuh"
 #include "gb_reduce.cuh"
 #include "gb_internal.h"
@@ -42,6 +56,7 @@ struct AsmArgs {
   cplx* dH;
   double* dF;
   double* Fs;      // scratch [N][Ne][3]
+  const uint8_t* only;  // non-null: k_asm_regular integrates only the pairs flagged here
 };
 
 // unit tangents at collocation node tn of element |td| (reference tz_te_bd_node d3b1_elem.c:122-143)
@@ -84,6 +99,179 @@ __device__ __forceinline__ void store_pair(const AsmArgs& a, size_t N, int row, 
   f[2] = A.dF[1];
 }
 
+// ------------------------------------------------------------------ FP32 regular pairs
+#define GB_F32_NEAR 3.0  // pairs closer than this many element radii are integrated in FP64
+
+struct GbTablesF {
+  float xli[GB_GLN], wli[GB_GLN];
+};
+static __constant__ GbTablesF c_tabf;
+
+// per-pair constants in FP32, relative to the source element's point (0, 0)
+struct PairF {
+  float R0[3];   // r_s(0,0) - r_t
+  float a0;      // |R0| (FP64, rounded)
+  float c1[3], c2[3], c3[3];  // r_s(z,e) - r_s(0,0) = c1 z + c2 e + c3 z e
+  float w0[3], w1[3], w2[3];  // W(z,e) = w0 + w1 z + w2 e
+  float vt[2][3];
+  cplxf E0;      // e^{i k |R0|} (FP64, rounded)
+  cplxf k;
+};
+
+struct RegAccF {
+  cplxf G[4], H[4];
+  float F;
+  cplxf dG[2][4], dH[2][4];
+  float dF[2];
+};
+
+__device__ __forceinline__ float dot3f(const float a[3], const float b[3]) {
+  return fmaf(a[0], b[0], fmaf(a[1], b[1], a[2] * b[2]));
+}
+
+__device__ __forceinline__ void reg_point_f32(const PairF& P, bool quad, float z, float e, float w, RegAccF& A) {
+  float d[3], R[3], W[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    d[i] = fmaf(P.c3[i] * z, e, fmaf(P.c2[i], e, P.c1[i] * z));
+    R[i] = P.R0[i] + d[i];
+    W[i] = fmaf(P.w2[i], e, fmaf(P.w1[i], z, P.w0[i]));
+  }
+  const float aR = sqrtf(dot3f(R, R));
+  const float iR = 1.0f / aR;
+  const float aW = sqrtf(dot3f(W, W));
+  const float dl = (2.0f * dot3f(P.R0, d) + dot3f(d, d)) / (aR + P.a0);  // |R| - |R0|
+  float sn, cs;
+  sincosf(P.k.x * dl, &sn, &cs);
+  const float ex = (P.k.y == 0.0f) ? 1.0f : expf(-P.k.y * dl);
+  const cplxf ce = P.E0 * cmkf(cs * ex, sn * ex);
+  const cplxf cb = cmkf(-P.k.y * aR - 1.0f, P.k.x * aR);  // i k R - 1
+  const float rdW = dot3f(R, W) * iR;
+  const float tD = rdW * iR * iR;
+  float N[4];
+  if (quad) {
+    const float ia = (float)(1.0 / GB_P44_N);
+    const float zm = 1.0f - z * ia, zp = 1.0f + z * ia, em = 1.0f - e * ia, ep = 1.0f + e * ia;
+    N[0] = 0.25f * zm * em; N[1] = 0.25f * zp * em; N[2] = 0.25f * zp * ep; N[3] = 0.25f * zm * ep;
+  } else {
+    const float ia = (float)(0.5 / GB_P34_N0), s3 = 1.7320508075688772f, t3 = 1.0f / 3.0f;
+    N[0] = t3 * (1.0f - ia * (z + s3 * e)); N[1] = t3 * (1.0f + 2.0f * ia * z); N[2] = t3 * (1.0f - ia * (z - s3 * e));
+    N[3] = 0.0f;
+  }
+  const cplxf g = ce * (iR * aW * w);
+  const cplxf cbe = cb * ce;
+  const cplxf h = cbe * (tD * w);
+#pragma unroll
+  for (int n = 0; n < 4; n++) { A.G[n] += g * N[n]; A.H[n] += h * N[n]; }
+  A.F += w * tD;
+  const cplxf kR = P.k * aR;
+  const cplxf t1 = kR * kR + cb * 3.0f;
+  const float iR3 = iR * iR * iR;
+#pragma unroll
+  for (int q = 0; q < 2; q++) {
+    const float rdv = dot3f(R, P.vt[q]) * iR;
+    const float Wdv = dot3f(W, P.vt[q]);
+    const cplxf dg = cbe * (iR * iR * rdv * aW * w);
+    const cplxf dh = (ce * (t1 * (rdv * rdW) - cb * Wdv)) * (iR3 * w);
+#pragma unroll
+    for (int n = 0; n < 4; n++) { A.dG[q][n] += dg * N[n]; A.dH[q][n] += dh * N[n]; }
+    A.dF[q] += w * iR3 * (3.0f * rdv * rdW - Wdv);
+  }
+}
+
+// one thread per (row, source) pair, FP32 GLN x GLN rule; flags the pairs the
+// FP64 kernel must redo
+__global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, uint8_t* redo) {
+  const size_t N = (size_t)a.Ne * 4;
+  const size_t npair = N * (size_t)a.Ne;
+  size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npair) return;
+  const int row = (int)(p / a.Ne), sidx = (int)(p % a.Ne);
+  const int t = row / 4 + 1, tn = row % 4;
+  const int td = __ldg(a.sid + t), sd = __ldg(a.sid + sidx + 1);
+  const int atd = abs(td);
+  Elem T;
+  load_elem(T, a.cr, a.cw, a.etype, atd);
+  redo[p] = 0;
+  if (!(T.quad || tn < 3) || sd == td) return;
+  Elem S;
+  load_elem(S, a.cr, a.cw, a.etype, abs(sd));
+  double rt[3], vt[2][3];
+  for (int d = 0; d < 3; d++) rt[d] = __ldg(a.ren + (size_t)atd * 12 + tn * 3 + d);
+  node_tangents(T, tn, vt);
+  PairF P;
+  double R0[3];
+  for (int d = 0; d < 3; d++) {
+    R0[d] = S.cr[d][0] - rt[d];
+    P.R0[d] = (float)R0[d];
+    P.c1[d] = (float)S.cr[d][1]; P.c2[d] = (float)S.cr[d][2]; P.c3[d] = (float)S.cr[d][3];
+    P.w0[d] = (float)S.cw[d][0]; P.w1[d] = (float)S.cw[d][1]; P.w2[d] = (float)S.cw[d][2];
+    P.vt[0][d] = (float)vt[0][d]; P.vt[1][d] = (float)vt[1][d];
+  }
+  const double a0 = norm3(R0);
+  // near pairs stay FP64: their entries are the row's largest, so their
+  // relative rounding would dominate the matrix error (hs bounds |r - r(0,0)|
+  // over the element)
+  double hs = 0.0;
+  for (int d = 0; d < 3; d++) hs += S.cr[d][1] * S.cr[d][1] + S.cr[d][2] * S.cr[d][2] + S.cr[d][3] * S.cr[d][3];
+  hs = (S.quad ? 1.8 : 3.0) * sqrt(hs);
+  if (a0 < GB_F32_NEAR * hs) {
+    redo[p] = 1;
+    return;
+  }
+  P.a0 = (float)a0;
+  const cplx E0 = cexpik(a.k, a0);
+  P.E0 = cmkf((float)E0.x, (float)E0.y);
+  P.k = cmkf((float)a.k.x, (float)a.k.y);
+  RegAccF A;
+#pragma unroll
+  for (int n = 0; n < 4; n++) {
+    A.G[n] = cmkf(0, 0); A.H[n] = cmkf(0, 0);
+    A.dG[0][n] = cmkf(0, 0); A.dG[1][n] = cmkf(0, 0); A.dH[0][n] = cmkf(0, 0); A.dH[1][n] = cmkf(0, 0);
+  }
+  A.F = 0.f; A.dF[0] = 0.f; A.dF[1] = 0.f;
+  float S0;
+  if (S.quad) {
+    S0 = (float)GB_I_FP;
+    for (int i = 0; i < GB_GLN; i++)
+      for (int j = 0; j < GB_GLN; j++)
+        reg_point_f32(P, true, c_tabf.xli[i], c_tabf.xli[j], c_tabf.wli[i] * c_tabf.wli[j], A);
+  } else {
+    S0 = (float)(0.0625 * GB_SQ3 * GB_I_SPSQ3);
+    const float s3 = 1.7320508075688772f;
+    for (int i = 0; i < GB_GLN; i++) {
+      const float x = c_tabf.xli[i];
+      for (int j = 0; j < GB_GLN; j++) {
+        const float y = c_tabf.xli[j];
+        const float w = c_tabf.wli[i] * c_tabf.wli[j] * (1.0f + 0.25f * x + 0.25f * y);
+        reg_point_f32(P, false, 0.125f * (3.0f + 2.0f * x + 2.0f * y + x * y), 0.125f * s3 * (-x + y), w, A);
+        reg_point_f32(P, false, 0.0625f * (-3.0f + x - 5.0f * y - x * y), 0.0625f * s3 * (3.0f + 3.0f * x + y + x * y), w, A);
+        reg_point_f32(P, false, 0.0625f * (-3.0f - 5.0f * x + y - x * y), 0.0625f * s3 * (-3.0f - x - 3.0f * y - x * y), w, A);
+      }
+    }
+  }
+  const float sh = sd < 0 ? -S0 : S0;
+  const float dF0 = A.dF[0] * sh, dF1 = A.dF[1] * sh;
+  if (!(fabsf(dF0) <= 0.45f && fabsf(dF1) <= 0.45f)) {  // near the GLN/GHN decision (or not finite): FP64
+    redo[p] = 1;
+    return;
+  }
+  RegAcc<2> D;
+#pragma unroll
+  for (int n = 0; n < 4; n++) {
+    D.G[n] = cmk(A.G[n].x * S0, A.G[n].y * S0);
+    D.H[n] = cmk(A.H[n].x * sh, A.H[n].y * sh);
+    for (int q = 0; q < 2; q++) {
+      D.dG[q][n] = cmk(-A.dG[q][n].x * S0, -A.dG[q][n].y * S0);
+      D.dH[q][n] = cmk(A.dH[q][n].x * sh, A.dH[q][n].y * sh);
+    }
+  }
+  D.F = A.F * sh;
+  D.dF[0] = dF0;
+  D.dF[1] = dF1;
+  store_pair(a, N, row, sidx, D);
+}
+
 __global__ void __launch_bounds__(128) k_asm_regular(AsmArgs a) {
   const size_t N = (size_t)a.Ne * 4;
   const size_t npair = N * (size_t)a.Ne;
@@ -106,7 +294,7 @@ __global__ void __launch_bounds__(128) k_asm_regular(AsmArgs a) {
     Elem T;
     load_elem(T, a.cr, a.cw, a.etype, atd);
     bool rowok = T.quad || tn < 3;
-    if (rowok && sd != td) {
+    if (rowok && sd != td && (a.only == nullptr || a.only[p] != 0)) {
       work = true;
       for (int d = 0; d < 3; d++) rt[d] = __ldg(a.ren + (size_t)atd * 12 + tn * 3 + d);
       node_tangents(T, tn, vt);
@@ -199,11 +387,21 @@ __global__ void k_asm_rows(AsmArgs a) {
   a.dF[(size_t)row * 3 + 2] = Fe;
 }
 
+extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG,
+                                    cplx* dH, double* dF, double* Fs, cudaStream_t st);
+
 // Assemble G,H,dG,dH,dF of one domain into device buffers.  Fs is scratch of
 // 3 N Ne doubles.  Buffers are cleared here (rows of the unused fourth node of
 // triangles and columns of the fourth shape function of triangles stay zero).
 extern "C" int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* G, cplx* H, cplx* dG, cplx* dH,
                                    double* dF, double* Fs, cudaStream_t st) {
+  return gbi_assemble_domain2(m, did, type, 0, G, H, dG, dH, dF, Fs, st);
+}
+
+// precision 0: FP64 throughout (the reference's arithmetic); 1: regular pairs
+// of the GLN x GLN rule in FP32 with FP64 near pairs (chosen form)
+extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG,
+                                    cplx* dH, double* dF, double* Fs, cudaStream_t st) {
   int Ne = m->sb_Ne[did];
   if (Ne <= 0) return 0;
   size_t N = (size_t)Ne * 4;
@@ -223,6 +421,7 @@ extern "C" int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* 
   a.dH = dH;
   a.dF = dF;
   a.Fs = Fs;
+  a.only = nullptr;
   GB_CUDA(cudaMemsetAsync(G, 0, N * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(H, 0, N * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(dG, 0, 2 * N * N * sizeof(cplx), st));
@@ -231,9 +430,18 @@ extern "C" int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* 
   GB_CUDA(cudaMemsetAsync(Fs, 0, 3 * N * (size_t)Ne * sizeof(double), st));
   size_t npair = N * (size_t)Ne;
   unsigned nb = (unsigned)((npair + 127) / 128);
+  uint8_t* redo = nullptr;
+  if (precision == 1 && type == 2) {
+    GB_CUDA(cudaMallocAsync((void**)&redo, npair, st));
+    k_asm_regular_f32<<<nb, 128, 0, st>>>(a, redo);
+    gbi_count_launch();
+    GB_CUDA(cudaGetLastError());
+    a.only = redo;
+  }
   k_asm_regular<<<nb, 128, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
+  if (redo) GB_CUDA(cudaFreeAsync(redo, st));
   k_asm_singular<<<(unsigned)N, 256, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
@@ -245,6 +453,10 @@ extern "C" int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* 
 
 extern "C" int gbi_upload_tables_asm(const void* t) {
   GB_CUDA(cudaMemcpyToSymbol(c_tab, t, sizeof(GbTables)));
+  const GbTables* d = (const GbTables*)t;
+  GbTablesF f;
+  for (int i = 0; i < GB_GLN; i++) { f.xli[i] = (float)d->xli[i]; f.wli[i] = (float)d->wli[i]; }
+  GB_CUDA(cudaMemcpyToSymbol(c_tabf, &f, sizeof(GbTablesF)));
   return 0;
 }
 

@@ -54,6 +54,7 @@ struct cplxf {
 };
 __host__ __device__ __forceinline__ cplxf cmkf(float a, float b) { cplxf r; r.x = a; r.y = b; return r; }
 __host__ __device__ __forceinline__ cplxf operator+(cplxf a, cplxf b) { return cmkf(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ cplxf operator*(cplxf a, float s) { return cmkf(a.x * s, a.y * s); }
 __host__ __device__ __forceinline__ cplxf operator-(cplxf a, cplxf b) { return cmkf(a.x - b.x, a.y - b.y); }
 __host__ __device__ __forceinline__ cplxf operator*(cplxf a, cplxf b) { return cmkf(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 __host__ __device__ __forceinline__ cplxf& operator+=(cplxf& a, cplxf b) { a.x += b.x; a.y += b.y; return a; }

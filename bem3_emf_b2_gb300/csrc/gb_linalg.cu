@@ -487,59 +487,64 @@ __device__ __forceinline__ cplxf to_c64(cplxf a) { return a; }
 
 // Partial-pivoting elimination of the R <= TS_ROWS panel rows idx[0..R) of A
 // (columns k..k+nb-1, nb <= LU_NB): only the choice of rows is kept -- on
-// return idx[0..min(R, nb)) holds the selected rows in pivot order.  The
-// selection runs in complex FP32 for both LU types: it only ranks candidate
-// rows, and a block's FP64 pipe is too narrow for it (the FP64 factors
-// themselves are computed in FP64 by k_diag_lu / k_trsm_right).
+// return win[0..min(R, nb)) holds the selected rows (global indices) in pivot
+// order.  The selection runs in complex FP32 for both LU types: it only ranks
+// candidate rows, and a block's FP64 pipe is too narrow for it (the FP64
+// factors themselves are computed in FP64 by k_diag_lu / k_trsm_right).
 // The rows live in registers: warp w holds rows w + 32 i (i < TS_ROWS / 32),
-// lane l columns l and l + 32.  Per column: a block reduction for the pivot,
-// the interchange through two shared-memory row buffers, and a register-only
-// rank-1 update that also ranks the next column; two block barriers.
+// lane l columns l and l + 32.  Rows are never moved: a chosen pivot row is
+// retired from its warp's active mask (the interchange of partial pivoting
+// only reorders, and the order is kept in win[]).  Per column: a block
+// reduction for the pivot (one REDUX per warp on a 32-bit key), the pivot row
+// and its reciprocal published through shared memory by its owner warp, and a
+// register-only rank-1 update of the active rows that also ranks the next
+// column; two block barriers.
 template <class T>
-__device__ void ts_select(const T* A, size_t lda, int k, int nb, int* idx, int R) {
+__device__ void ts_select(const T* A, size_t lda, int k, int nb, const int* idx, int R, int* win) {
   constexpr int NW = TS_THREADS / 32;
   constexpr int RPW = TS_ROWS / NW;  // rows per warp
+  static_assert(TS_ROWS <= 256, "pivot keys hold 9-bit row numbers");
   __shared__ uint32_t skey[NW];
-  __shared__ cplxf sP[LU_NB], sJ[LU_NB];
+  __shared__ cplxf sP[LU_NB];
+  __shared__ cplxf sPinv;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int c0 = lane, c1 = lane + 32;
   const cplxf z = cmkf(0.f, 0.f);
   cplxf v0[RPW], v1[RPW];
+  uint32_t active = 0u;  // warp-uniform: bit i = row w + NW i still a candidate
 #pragma unroll
   for (int i = 0; i < RPW; i++) {
     const int r = w + NW * i;
     v0[i] = z;
     v1[i] = z;
     if (r < R) {
+      active |= 1u << i;
       const T* src = A + (size_t)idx[r] * lda + k;
       if (c0 < nb) v0[i] = to_c64(src[c0]);
       if (c1 < nb) v1[i] = to_c64(src[c1]);
     }
   }
+  // pivot keys: |Re|+|Im| with its 9 low mantissa bits replaced by 511 - row,
+  // so one unsigned maximum picks the largest magnitude and, among magnitudes
+  // within 2^-14 relative, the first row (any of them is as good a pivot);
+  // every active row has a non-zero key, so a zero column still yields a row
   const int steps = R < nb ? R : nb;
-  // pivot keys: |Re|+|Im| with its 8 low mantissa bits replaced by 255 - row
-  // (rows < 256), so one unsigned maximum picks the largest magnitude and, among
-  // magnitudes equal to 2^-15 relative, the first row -- any of them is an
-  // equally good pivot
-  static_assert(TS_ROWS <= 256, "pivot keys hold 8-bit row numbers");
   uint32_t key = 0u;
   if (lane == 0) {  // column 0
 #pragma unroll
-    for (int i = 0; i < RPW; i++) {
-      const int r = w + NW * i;
-      if (r < R) key = max(key, (__float_as_uint(cabs1(v0[i])) & ~0xFFu) | (uint32_t)(255 - r));
-    }
+    for (int i = 0; i < RPW; i++)
+      if ((active >> i) & 1u) key = max(key, (__float_as_uint(cabs1(v0[i])) & ~0x1FFu) | (uint32_t)(511 - (w + NW * i)));
   }
   for (int j = 0; j < steps; j++) {
     key = __reduce_max_sync(0xffffffffu, key);
     if (lane == 0) skey[w] = key;
     __syncthreads();
     key = __reduce_max_sync(0xffffffffu, lane < NW ? skey[lane] : 0u);
-    const int p = (key >> 8) != 0u ? 255 - (int)(key & 0xFFu) : j;
-    // the pivot row to sP; with an interchange, the old row j to sJ
-    // (register slots are picked with bit masks: an indexed access, or a
-    // select chain the compiler turns into one, would move the row arrays to
-    // local memory)
+    const int p = 511 - (int)(key & 0x1FFu);
+    // the owner warp publishes the pivot row and its reciprocal and retires it
+    // (register slots are picked with bit masks: an indexed access, or a select
+    // chain the compiler turns into one, would move the row arrays to local
+    // memory)
     if (w == (p % NW)) {
       uint32_t t[4] = {0u, 0u, 0u, 0u};
 #pragma unroll
@@ -548,55 +553,54 @@ __device__ void ts_select(const T* A, size_t lda, int k, int nb, int* idx, int R
         t[0] |= __float_as_uint(v0[i].x) & msk; t[1] |= __float_as_uint(v0[i].y) & msk;
         t[2] |= __float_as_uint(v1[i].x) & msk; t[3] |= __float_as_uint(v1[i].y) & msk;
       }
-      sP[c0] = cmkf(__uint_as_float(t[0]), __uint_as_float(t[1]));
-      sP[c1] = cmkf(__uint_as_float(t[2]), __uint_as_float(t[3]));
-    }
-    if (p != j && w == (j % NW)) {
-      uint32_t t[4] = {0u, 0u, 0u, 0u};
-#pragma unroll
-      for (int i = 0; i < RPW; i++) {
-        const uint32_t msk = 0u - (uint32_t)(i == j / NW);
-        t[0] |= __float_as_uint(v0[i].x) & msk; t[1] |= __float_as_uint(v0[i].y) & msk;
-        t[2] |= __float_as_uint(v1[i].x) & msk; t[3] |= __float_as_uint(v1[i].y) & msk;
+      const cplxf q0 = cmkf(__uint_as_float(t[0]), __uint_as_float(t[1]));
+      const cplxf q1 = cmkf(__uint_as_float(t[2]), __uint_as_float(t[3]));
+      sP[c0] = q0;
+      sP[c1] = q1;
+      if (lane == (j & 31)) {
+        const cplxf piv = (j < 32) ? q0 : q1;
+        sPinv = (piv.x == 0.f && piv.y == 0.f) ? z : cdivc(cmkf(1.f, 0.f), piv);
       }
-      sJ[c0] = cmkf(__uint_as_float(t[0]), __uint_as_float(t[1]));
-      sJ[c1] = cmkf(__uint_as_float(t[2]), __uint_as_float(t[3]));
+      active &= ~(1u << (p / NW));
+      if (lane == 0) win[j] = idx[p];
     }
-    if (p != j && threadIdx.x == 0) { int t = idx[j]; idx[j] = idx[p]; idx[p] = t; }
     __syncthreads();
-    if (p != j && w == (p % NW)) {  // position p now holds the old row j
-      const cplxf t0 = sJ[c0], t1 = sJ[c1];
-#pragma unroll
-      for (int i = 0; i < RPW; i++) {
-        const uint32_t msk = 0u - (uint32_t)(i == p / NW);
-        v0[i].x = __uint_as_float((__float_as_uint(v0[i].x) & ~msk) | (__float_as_uint(t0.x) & msk));
-        v0[i].y = __uint_as_float((__float_as_uint(v0[i].y) & ~msk) | (__float_as_uint(t0.y) & msk));
-        v1[i].x = __uint_as_float((__float_as_uint(v1[i].x) & ~msk) | (__float_as_uint(t1.x) & msk));
-        v1[i].y = __uint_as_float((__float_as_uint(v1[i].y) & ~msk) | (__float_as_uint(t1.y) & msk));
-      }
-    }
-    const cplxf piv = sP[j];
-    const bool nz = !(piv.x == 0.f && piv.y == 0.f);
-    const cplxf pinv = nz ? cdivc(cmkf(1.f, 0.f), piv) : z;
-    const cplxf p0 = sP[c0], p1 = sP[c1];
-    const bool u0 = c0 > j && c0 < nb, u1 = c1 > j && c1 < nb;
+    const cplxf pinv = sPinv;
     const int cn = j + 1;
     const bool own_next = lane == (cn & 31) && cn < nb;
     key = 0u;
+    if (j < 31) {  // both column halves still have entries to the right of j
+      const cplxf p0 = (c0 > j && c0 < nb) ? sP[c0] : z;
+      const cplxf p1 = (c1 < nb) ? sP[c1] : z;
 #pragma unroll
-    for (int i = 0; i < RPW; i++) {
-      const int r = w + NW * i;
-      if (r > j && r < R) {  // warp-uniform
-        const cplxf xj = (j < 32) ? v0[i] : v1[i];
+      for (int i = 0; i < RPW; i++) {
+        if (!((active >> i) & 1u)) continue;  // warp-uniform
         cplxf l;
-        l.x = __shfl_sync(0xffffffffu, xj.x, j & 31);
-        l.y = __shfl_sync(0xffffffffu, xj.y, j & 31);
+        l.x = __shfl_sync(0xffffffffu, v0[i].x, j);
+        l.y = __shfl_sync(0xffffffffu, v0[i].y, j);
         l = l * pinv;
-        if (u0) v0[i] -= l * p0;
-        if (u1) v1[i] -= l * p1;
-        if (own_next) key = max(key, (__float_as_uint(cabs1(cn < 32 ? v0[i] : v1[i])) & ~0xFFu) | (uint32_t)(255 - r));
+        v0[i] -= l * p0;
+        v1[i] -= l * p1;
+        if (own_next)
+          key = max(key, (__float_as_uint(cabs1(cn < 32 ? v0[i] : v1[i])) & ~0x1FFu) | (uint32_t)(511 - (w + NW * i)));
+      }
+    } else {  // only the upper half (columns 32..63) is still to the right of j
+      const cplxf p1 = (c1 > j && c1 < nb) ? sP[c1] : z;
+      const int src = (j < 32) ? j : j - 32;
+#pragma unroll
+      for (int i = 0; i < RPW; i++) {
+        if (!((active >> i) & 1u)) continue;  // warp-uniform
+        const cplxf xv = (j < 32) ? v0[i] : v1[i];
+        cplxf l;
+        l.x = __shfl_sync(0xffffffffu, xv.x, src);
+        l.y = __shfl_sync(0xffffffffu, xv.y, src);
+        l = l * pinv;
+        v1[i] -= l * p1;
+        if (own_next) key = max(key, (__float_as_uint(cabs1(v1[i])) & ~0x1FFu) | (uint32_t)(511 - (w + NW * i)));
       }
     }
+    // the next step's reductions start only after every thread passed the
+    // barrier above, and its first barrier orders these updates before use
   }
   __syncthreads();
 }
@@ -630,12 +634,13 @@ __global__ void __launch_bounds__(TS_THREADS) k_tslu_leaf(const T* A, size_t lda
   __shared__ int idx[TS_ROWS + 2 * LU_NB];
   const int r0 = k + blockIdx.x * TS_ROWS;
   const int R = (n - r0 < TS_ROWS) ? n - r0 : TS_ROWS;
+  __shared__ int win[LU_NB];
   for (int r = threadIdx.x; r < R; r += TS_THREADS) idx[r] = r0 + r;
   __syncthreads();
-  ts_select<T>(A, lda, k, nb, idx, R);
+  ts_select<T>(A, lda, k, nb, idx, R, win);
   const int steps = R < nb ? R : nb;
-  for (int j = threadIdx.x; j < nb; j += TS_THREADS) cand[(size_t)blockIdx.x * nb + j] = j < steps ? idx[j] : -1;
-  if (gridDim.x == 1 && threadIdx.x == 0) calu_ipiv(idx, k, nb, ipiv, idx + TS_ROWS, idx + TS_ROWS + LU_NB);
+  for (int j = threadIdx.x; j < nb; j += TS_THREADS) cand[(size_t)blockIdx.x * nb + j] = j < steps ? win[j] : -1;
+  if (gridDim.x == 1 && threadIdx.x == 0) calu_ipiv(win, k, nb, ipiv, idx + TS_ROWS, idx + TS_ROWS + LU_NB);
 }
 
 // sets TS_ARITY b .. TS_ARITY b + TS_ARITY - 1 of cin (nin sets of nb entries;
@@ -662,11 +667,12 @@ __global__ void __launch_bounds__(TS_THREADS) k_tslu_merge(const T* A, size_t ld
   }
   int R = 0;
   for (int u = 0; u < TS_ARITY; u++) R += cnt[u];
+  __shared__ int win[LU_NB];
   __syncthreads();
-  ts_select<T>(A, lda, k, nb, idx, R);
+  ts_select<T>(A, lda, k, nb, idx, R, win);
   const int steps = R < nb ? R : nb;
-  for (int j = threadIdx.x; j < nb; j += TS_THREADS) cout[(size_t)b * nb + j] = j < steps ? idx[j] : -1;
-  if (gridDim.x == 1 && threadIdx.x == 0) calu_ipiv(idx, k, nb, ipiv, idx + TS_ROWS, idx + TS_ROWS + LU_NB);
+  for (int j = threadIdx.x; j < nb; j += TS_THREADS) cout[(size_t)b * nb + j] = j < steps ? win[j] : -1;
+  if (gridDim.x == 1 && threadIdx.x == 0) calu_ipiv(win, k, nb, ipiv, idx + TS_ROWS, idx + TS_ROWS + LU_NB);
 }
 
 // interchanges ipiv[k..k+nb) applied in sequence to columns [0, ncol)

@@ -14,7 +14,7 @@
 // 2^-21 relative error, close to FP32 arithmetic (the standard 3xTF32
 // emulation).  PASSES = 1 is plain TF32.
 //
-// Kernel: persistent, one CTA per SM, 128 x 256 tiles of Cr, 192 threads.
+// Kernel: persistent, one CTA per SM, 128 x 256 tiles of Cr, 320 threads.
 //   warp 0     streams K-slices of 32 floats (one 128-byte swizzle atom) of
 //              the operands into a ring of shared-memory stages with TMA
 //              (SWIZZLE_128B), running ahead across tiles;
@@ -22,8 +22,9 @@
 //              tcgen05.mma.cta_group::1.kind::tf32 (M = 128, N = 256, K = 8),
 //              committing each stage back to the producer and each finished
 //              accumulator to the epilogue;
-//   warps 2-5  read an accumulator (tcgen05.ld 32x32b: TMEM lane = tile row)
-//              and subtract it from C while the next tile accumulates in the
+//   warps 2-9  read an accumulator (tcgen05.ld 32x32b: TMEM lane = tile row,
+//              two warps per lane quarter, one per half of the columns) and
+//              subtract it from C while the next tile accumulates in the
 //              other buffer.
 // Every mbarrier wait is bounded in time (TC_WAIT_NS); on time-out the CTA
 // raises *err, stops issuing work, frees its TMEM and returns.
@@ -38,7 +39,7 @@
 #define TC_BM 128
 #define TC_BN 256
 #define TC_BK 32  // floats per K-slice: 128 bytes, one swizzle atom
-#define TC_THREADS 192
+#define TC_THREADS 320
 #define TC_WAIT_NS 2000000000ull  // 2 s
 
 namespace {
@@ -162,9 +163,11 @@ struct TcLayout {
 //   warp 0     (one lane) TMA producer, ring of STAGES K-slices across tiles
 //   warp 1     allocates TMEM (two 256-column accumulators); one lane issues
 //              the MMAs of a tile into accumulator (local tile index & 1)
-//   warps 2-5  epilogue: warp w reads TMEM lanes 32 (w & 3) .. + 31, i.e. tile
-//              rows, and subtracts them from C while the MMAs of the next tile
-//              fill the other accumulator
+//   warps 2-9  epilogue: warp w reads TMEM lanes 32 (w & 3) .. + 31 (tile
+//              rows) for one half of the tile's columns and subtracts them
+//              from C while the MMAs of the next tile fill the other
+//              accumulator; the first chunk of C is loaded before the tile's
+//              accumulator is ready
 template <int PASSES>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_cgemm_sub(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
@@ -192,7 +195,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     for (int b = 0; b < 2; b++) {
       mbar_init(bar0 + 128 + 8 * b, 1);
-      mbar_init(bar0 + 144 + 8 * b, 4);
+      mbar_init(bar0 + 144 + 8 * b, 8);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -258,37 +261,46 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         mma_commit(bar0 + 128 + 8 * b);  // accumulator b complete
       }
     }
-  } else {  // epilogue warps 2..5
-    const int q = warp & 3;
+  } else {  // epilogue warps 2..9: warp w reads TMEM lanes 32 (w & 3).. (tile rows), columns 128 h.. (h = (w-2) / 4)
+    const int q = warp & 3, h = (warp - 2) >> 2;
     uint32_t lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, lt++) {
       const uint32_t b = lt & 1, u = lt >> 1;
+      const int i0 = (t / ntn) * TC_BM, c0 = (t % ntn) * TC_BN + h * (TC_BN / 2);
+      const int row = i0 + q * 32 + lane;
+      float* crow = C + (size_t)row * ldcf;
+      // the first chunk of C is loaded while the tile's MMAs run
+      float4 cv[16];
+      bool full = row < m && c0 + 64 <= n2 && ((((uintptr_t)(crow + c0)) & 15) == 0);
+      if (full) {
+        const float4* p4 = (const float4*)(crow + c0);
+#pragma unroll
+        for (int x = 0; x < 16; x++) cv[x] = p4[x];
+      }
       int ok = 1;
       if (lane == 0) ok = mbar_wait(bar0 + 128 + 8 * b, u & 1) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok || *s_fail) { *s_fail = 1; break; }
       __syncwarp();
       tc_fence_after();
-      const int i0 = (t / ntn) * TC_BM, c0 = (t % ntn) * TC_BN;
-      const int row = i0 + q * 32 + lane;
-      float* crow = C + (size_t)row * ldcf;
-      const uint32_t ta = tmem + b * TC_BN + ((uint32_t)(q * 32) << 16);
+      const uint32_t ta = tmem + b * TC_BN + (uint32_t)(h * (TC_BN / 2)) + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-      for (int cc = 0; cc < TC_BN; cc += 64) {
+      for (int cc = 0; cc < TC_BN / 2; cc += 64) {
         const int c = c0 + cc;
-        const bool full = row < m && c + 64 <= n2 && ((((uintptr_t)(crow + c)) & 15) == 0);
-        float4 cv[16];
-        if (full) {
-          const float4* p4 = (const float4*)(crow + c);
+        if (cc > 0) {
+          full = row < m && c + 64 <= n2 && ((((uintptr_t)(crow + c)) & 15) == 0);
+          if (full) {
+            const float4* p4 = (const float4*)(crow + c);
 #pragma unroll
-          for (int x = 0; x < 16; x++) cv[x] = p4[x];
+            for (int x = 0; x < 16; x++) cv[x] = p4[x];
+          }
         }
         float v[64];
         tmem_ld16(ta + cc, v);
         tmem_ld16(ta + cc + 16, v + 16);
         tmem_ld16(ta + cc + 32, v + 32);
         tmem_ld16(ta + cc + 48, v + 48);
-        if (cc + 64 == TC_BN) {  // accumulator b fully read: hand it back to the MMA warp
+        if (cc + 64 == TC_BN / 2) {  // this warp's part of accumulator b is read: signal the MMA warp
           tc_fence_before();
           __syncwarp();
           if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar0 + 144 + 8 * b) : "memory");

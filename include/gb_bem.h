@@ -64,6 +64,14 @@ void gb_obj_destroy(gb_obj *o);
  * N = 4 sb_Ne[did], quadrature type 0..3 (4-point, 9/7-point, GLN, GHN; the
  * reference uses 2).  Replaces create_cmatrix_domain, solve_bieq2.c:98-184. */
 int gb_assemble(gb_obj *o, int did, int type);
+/* as gb_assemble; precision 1: regular pairs of the GLN x GLN rule farther
+ * than three element radii integrated in FP32 relative to the source
+ * element's centre (FP64 phase at the centre), all other pairs, the GHN
+ * fallback and the singular elements in FP64.  Matrix entries then carry
+ * ~1e-7 relative error (measured: G 9e-8, dH 2e-7, radiation force up to
+ * 8e-7 on the 384-element sphere), so the scene steps use precision 0;
+ * precision 1 is an opt-in for large scenes where assembly dominates. */
+int gb_assemble2(gb_obj *o, int did, int type, int precision);
 /* copy the resident matrices of domain did to/from host buffers in the
  * reference's .cmat layout (any pointer may be NULL to skip that matrix) */
 int gb_cmatrix_download(gb_obj *o, int did, void *G, void *H, void *dG, void *dH, double *dF);

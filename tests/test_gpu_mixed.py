@@ -31,3 +31,36 @@ def test_mixed_form_force_matches_fp64_and_reference(case, gb_build, tmp_path):
         assert err <= 1e-6, "force/torque relative error %g" % err
     d = np.linalg.norm(np.concatenate([F32 - F64, N32 - N64])) / np.linalg.norm(np.concatenate([F64, N64]))
     assert d <= 1e-9, "mixed vs FP64 force/torque %g" % d
+
+
+@pytest.mark.gpu
+def test_fp32_far_pair_assembly_error(gb_build, tmp_path):
+    """gb_assemble2(precision 1): FP32 regular far pairs.  The matrices must
+    stay within 3e-7 relative Frobenius of the FP64 assembly (measured about
+    1e-7 on G and 2e-7 on dH) and precision 0 must be the FP64 path itself."""
+    import ctypes
+    from bem3_emf_b2_gb300 import Scene, formats, lib
+    import bench
+    L = lib()
+    vp, ci = ctypes.c_void_p, ctypes.c_int
+    L.gb_assemble2.argtypes = [vp, ci, ci, ci]
+    L.gb_assemble2.restype = ci
+    L.gb_cmatrix_download.argtypes = [vp, ci] + [vp] * 5
+    wd = str(tmp_path)
+    bench.write_scene(wd, 6)
+    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+    o = sc.obj()
+    N = 4 * 6 * 36
+    for d in range(2):
+        out = {}
+        for prec in (0, 1):
+            assert L.gb_assemble2(o, d, 2, prec) == 0, L.gb_last_error()
+            m = [np.zeros((N, N), complex), np.zeros((N, N), complex), np.zeros((2 * N, N), complex),
+                 np.zeros((2 * N, N), complex)]
+            assert L.gb_cmatrix_download(o, d, m[0].ctypes.data, m[1].ctypes.data, m[2].ctypes.data, m[3].ctypes.data,
+                                         None) == 0
+            out[prec] = m
+        errs = [formats.rel_fro(a, b) for a, b in zip(out[1], out[0])]
+        assert max(errs) <= 3e-7, errs
+        assert max(errs) > 0.0  # the FP32 path did run
+    sc.close()
