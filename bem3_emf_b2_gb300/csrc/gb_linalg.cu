@@ -338,51 +338,80 @@ __device__ __forceinline__ float cabs1(cplxf a) { return fabsf(a.x) + fabsf(a.y)
 template <class T> struct RealOf { typedef double type; };
 template <> struct RealOf<cplxf> { typedef float type; };
 
-// Rows k..k+nb-1, columns [c0, c1): X <- L11^-1 X with L11 the unit lower
-// triangle of A[k:k+nb][k:k+nb] (or, with upper = 1, X <- U11^-1 X with the
-// non-unit upper triangle), one thread per column.  Lsrc gives the triangle's
-// storage (row-major, leading dimension ldl).
+// Rows k..k+nb-1 (nb <= LU_NB), columns [c0, c1): X <- L11^-1 X with L11 the
+// unit lower triangle of A[k:k+nb][k:k+nb] (or, with UPPER = 1, X <- U11^-1 X
+// with the non-unit upper triangle).  Lsrc gives the triangle's storage
+// (row-major, leading dimension ldl).  A block takes 32 columns: the triangle
+// is staged transposed in shared memory (with the inverted diagonal), the
+// nb x 32 tile of X is loaded and stored coalesced, and each warp solves four
+// columns with the column in registers (lane l: rows l and l + 32) by
+// substitution with warp shuffles.
+#define TRSM_COLS 32
 template <class T, int UPPER>
-__global__ void __launch_bounds__(128) k_trsm_rows(const T* Lsrc, size_t ldl, T* X, size_t ldx, int nb, int c0,
+__global__ void __launch_bounds__(256) k_trsm_rows(const T* Lsrc, size_t ldl, T* X, size_t ldx, int nb, int c0,
                                                    int c1) {
   extern __shared__ __align__(16) unsigned char sLraw[];
-  T* sL = (T*)sLraw;  // nb*nb
-  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) sL[t] = Lsrc[(size_t)(t / nb) * ldl + (t % nb)];
-  __syncthreads();
-  int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= c1) return;
-  T x[LU_NB];
-#pragma unroll
-  for (int i = 0; i < LU_NB; i++)
-    if (i < nb) x[i] = X[(size_t)i * ldx + c];
-  if (!UPPER) {
-#pragma unroll
-    for (int i = 0; i < LU_NB; i++) {
-      if (i >= nb) break;
-      T s = x[i];
-#pragma unroll
-      for (int jj = 0; jj < LU_NB; jj++) {
-        if (jj >= i) break;
-        s -= sL[i * nb + jj] * x[jj];
-      }
-      x[i] = s;
-    }
-  } else {
-#pragma unroll
-    for (int i = LU_NB - 1; i >= 0; i--) {
-      if (i >= nb) continue;
-      T s = x[i];
-#pragma unroll
-      for (int jj = LU_NB - 1; jj >= 0; jj--) {
-        if (jj <= i) break;
-        if (jj < nb) s -= sL[i * nb + jj] * x[jj];
-      }
-      x[i] = cdivc(s, sL[i * nb + i]);
-    }
+  const int ld = nb + 1;
+  T* sT = (T*)sLraw;           // sT[j * ld + i] = triangle[i][j]
+  T* dinv = sT + nb * ld;      // LU_NB
+  T* Xs = dinv + LU_NB;        // LU_NB x (TRSM_COLS + 1)
+  constexpr int XL = TRSM_COLS + 1;
+  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+    int i = t / nb, j = t % nb;
+    sT[j * ld + i] = Lsrc[(size_t)i * ldl + j];
   }
-#pragma unroll
-  for (int i = 0; i < LU_NB; i++)
-    if (i < nb) X[(size_t)i * ldx + c] = x[i];
+  const int cb = c0 + blockIdx.x * TRSM_COLS;
+  for (int t = threadIdx.x; t < nb * TRSM_COLS; t += blockDim.x) {
+    int i = t / TRSM_COLS, c = t % TRSM_COLS;
+    if (cb + c < c1) Xs[i * XL + c] = X[(size_t)i * ldx + cb + c];
+  }
+  __syncthreads();
+  if (UPPER)
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+      T one;
+      one.x = 1; one.y = 0;
+      dinv[j] = cdivc(one, sT[j * ld + j]);
+    }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int i0 = lane, i1 = lane + 32;
+  for (int c = w; c < TRSM_COLS; c += nw) {
+    if (cb + c >= c1) break;  // warp-uniform
+    T x0, x1;
+    x0.x = 0; x0.y = 0; x1 = x0;
+    if (i0 < nb) x0 = Xs[i0 * XL + c];
+    if (i1 < nb) x1 = Xs[i1 * XL + c];
+    if (!UPPER) {
+      for (int j = 0; j < nb; j++) {
+        T v = (j < 32) ? x0 : x1;
+        T xj;
+        xj.x = __shfl_sync(0xffffffffu, v.x, j & 31);
+        xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
+        const T* col = sT + j * ld;
+        if (i0 > j && i0 < nb) x0 -= col[i0] * xj;
+        if (i1 > j && i1 < nb) x1 -= col[i1] * xj;
+      }
+    } else {
+      for (int j = nb - 1; j >= 0; j--) {
+        T v = (j < 32) ? x0 : x1;
+        T xj;
+        xj.x = __shfl_sync(0xffffffffu, v.x, j & 31);
+        xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
+        xj = xj * dinv[j];
+        if (lane == (j & 31)) { if (j < 32) x0 = xj; else x1 = xj; }
+        const T* col = sT + j * ld;
+        if (i0 < j) x0 -= col[i0] * xj;
+        if (i1 < j) x1 -= col[i1] * xj;
+      }
+    }
+    if (i0 < nb) Xs[i0 * XL + c] = x0;
+    if (i1 < nb) Xs[i1 * XL + c] = x1;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nb * TRSM_COLS; t += blockDim.x) {
+    int i = t / TRSM_COLS, c = t % TRSM_COLS;
+    if (cb + c < c1) X[(size_t)i * ldx + cb + c] = Xs[i * XL + c];
+  }
 }
 
 // C[M][N] -= A[M][K] B[K][N], complex FP64, row-major with leading dims.
@@ -461,15 +490,15 @@ static int gemm_sub(int M, int N, int K, const cplx* A, size_t lda, const cplx* 
 template <class T>
 static int trsm_rows(int upper, const T* L, size_t ldl, T* X, size_t ldx, int nb, int c0, int c1, cudaStream_t st) {
   if (c1 <= c0) return 0;
-  size_t sm = (size_t)nb * nb * sizeof(T);
-  unsigned nblk = (unsigned)((c1 - c0 + 127) / 128);
+  size_t sm = ((size_t)nb * (nb + 1) + LU_NB + (size_t)LU_NB * (TRSM_COLS + 1)) * sizeof(T);
+  unsigned nblk = (unsigned)((c1 - c0 + TRSM_COLS - 1) / TRSM_COLS);
   if (upper) {
     GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_trsm_rows<T, 1><<<nblk, 128, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
+    k_trsm_rows<T, 1><<<nblk, 256, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
     gbi_count_launch();
   } else {
     GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
-    k_trsm_rows<T, 0><<<nblk, 128, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
+    k_trsm_rows<T, 0><<<nblk, 256, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
     gbi_count_launch();
   }
   GB_CUDA(cudaGetLastError());
@@ -1257,6 +1286,35 @@ extern "C" int gbi_csolve_multi(const cplxf* LU, size_t lda, int n, const int* p
 extern "C" int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
 extern "C" int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st);
 
+// R = B - A X for A n x n, X and B n x nrhs packed (nrhs <= 8); one warp per row
+__global__ void k_resid_multi(const cplx* __restrict__ A, int n, const cplx* __restrict__ X, const cplx* __restrict__ B,
+                              int nrhs, cplx* R) {
+  const int lane = threadIdx.x & 31;
+  const int row = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  if (row >= n) return;
+  const cplx* a = A + (size_t)row * n;
+  double sr[8], si[8];
+  for (int c = 0; c < 8; c++) { sr[c] = 0.0; si[c] = 0.0; }
+  for (int j = lane; j < n; j += 32) {
+    const cplx av = a[j];
+    for (int c = 0; c < nrhs; c++) {
+      const cplx xv = X[(size_t)j * nrhs + c];
+      sr[c] = fma(av.x, xv.x, fma(-av.y, xv.y, sr[c]));
+      si[c] = fma(av.x, xv.y, fma(av.y, xv.x, si[c]));
+    }
+  }
+  for (int c = 0; c < nrhs; c++)
+    for (int o = 16; o > 0; o >>= 1) {
+      sr[c] += __shfl_down_sync(0xffffffffu, sr[c], o);
+      si[c] += __shfl_down_sync(0xffffffffu, si[c], o);
+    }
+  if (lane == 0)
+    for (int c = 0; c < nrhs; c++) {
+      const cplx b = B[(size_t)row * nrhs + c];
+      R[(size_t)row * nrhs + c] = cmk(b.x - sr[c], b.y - si[c]);
+    }
+}
+
 extern "C" int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cplx* X, int* iters, double* relres,
                                cudaStream_t st) {
   if (nrhs < 1 || nrhs > 8) { gbi_set_error("gbi_zgesv_mixed: nrhs %d not in 1..8", nrhs); return -1; }
@@ -1293,8 +1351,8 @@ extern "C" int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cp
   for (; !rc && it < 31; it++) {
     if (it > 0) {
       // R = B - A X (FP64)
-      if (cudaMemcpyAsync(R, B, nb * sizeof(cplx), cudaMemcpyDeviceToDevice, st) != cudaSuccess) { rc = -1; break; }
-      if (gemm_sub(n, nrhs, n, A, n, X, nrhs, R, nrhs, st)) { rc = -1; break; }
+      k_resid_multi<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(A, n, X, B, nrhs, R);
+      gbi_count_launch();
       if (cudaMemsetAsync(nrm, 0, 2 * sizeof(double), st) != cudaSuccess) { rc = -1; break; }
       k_sqnorm<<<gb, 256, 0, st>>>(R, nb, nrm);
       k_sqnorm<<<gb, 256, 0, st>>>(B, nb, nrm + 1);
