@@ -23,9 +23,10 @@
 //              committing each stage back to the producer and each finished
 //              accumulator to the epilogue;
 //   warps 2-9  read an accumulator (tcgen05.ld 32x32b: TMEM lane = tile row,
-//              two warps per lane quarter, one per half of the columns) and
-//              subtract it from C while the next tile accumulates in the
-//              other buffer.
+//              two warps per lane quarter, one per half of the columns),
+//              transpose it through shared memory and subtract it from C
+//              (lanes on consecutive columns) while the next tile accumulates
+//              in the other buffer.
 // Every mbarrier wait is bounded in time (TC_WAIT_NS); on time-out the CTA
 // raises *err, stops issuing work, frees its TMEM and returns.
 #include <cuda.h>
@@ -155,7 +156,8 @@ struct TcLayout {
   static constexpr int NOPS = PASSES == 3 ? 2 : 1;
   static constexpr int STAGE = NOPS * (A_BYTES + B_BYTES);
   static constexpr int STAGES = PASSES == 3 ? 2 : 4;  // 192 KB either way: one CTA per SM owns all of TMEM
-  static constexpr int SMEM = STAGES * STAGE + 1024 /* alignment */ + 256 /* barriers */;
+  static constexpr int EPI = 8 * 32 * 33 * 4;  // per epilogue warp a 32 x 33 float transpose buffer
+  static constexpr int SMEM = STAGES * STAGE + 1024 /* alignment */ + 256 /* barriers */ + EPI;
 };
 
 // Persistent: CTA b takes tiles b, b + gridDim.x, ...; tile t covers rows
@@ -164,10 +166,10 @@ struct TcLayout {
 //   warp 1     allocates TMEM (two 256-column accumulators); one lane issues
 //              the MMAs of a tile into accumulator (local tile index & 1)
 //   warps 2-9  epilogue: warp w reads TMEM lanes 32 (w & 3) .. + 31 (tile
-//              rows) for one half of the tile's columns and subtracts them
-//              from C while the MMAs of the next tile fill the other
-//              accumulator; the first chunk of C is loaded before the tile's
-//              accumulator is ready
+//              rows) for one half of the tile's columns, transposes 32 x 32
+//              chunks through shared memory and subtracts them from C with
+//              coalesced accesses, while the MMAs of the next tile fill the
+//              other accumulator
 template <int PASSES>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_cgemm_sub(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
@@ -263,20 +265,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else {  // epilogue warps 2..9: warp w reads TMEM lanes 32 (w & 3).. (tile rows), columns 128 h.. (h = (w-2) / 4)
     const int q = warp & 3, h = (warp - 2) >> 2;
+    // accumulator rows arrive one per lane; a 32 x 32 transpose through shared
+    // memory turns them into row segments, so that C is read and written with
+    // lanes on consecutive columns (coalesced)
+    float* tb = (float*)(sm + S * L::STAGE + 256) + (warp - 2) * (32 * 33);
     uint32_t lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, lt++) {
       const uint32_t b = lt & 1, u = lt >> 1;
-      const int i0 = (t / ntn) * TC_BM, c0 = (t % ntn) * TC_BN + h * (TC_BN / 2);
-      const int row = i0 + q * 32 + lane;
-      float* crow = C + (size_t)row * ldcf;
-      // the first chunk of C is loaded while the tile's MMAs run
-      float4 cv[16];
-      bool full = row < m && c0 + 64 <= n2 && ((((uintptr_t)(crow + c0)) & 15) == 0);
-      if (full) {
-        const float4* p4 = (const float4*)(crow + c0);
-#pragma unroll
-        for (int x = 0; x < 16; x++) cv[x] = p4[x];
-      }
+      const int i0 = (t / ntn) * TC_BM + q * 32, c0 = (t % ntn) * TC_BN + h * (TC_BN / 2);
       int ok = 1;
       if (lane == 0) ok = mbar_wait(bar0 + 128 + 8 * b, u & 1) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -285,42 +281,27 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       tc_fence_after();
       const uint32_t ta = tmem + b * TC_BN + (uint32_t)(h * (TC_BN / 2)) + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
-      for (int cc = 0; cc < TC_BN / 2; cc += 64) {
-        const int c = c0 + cc;
-        if (cc > 0) {
-          full = row < m && c + 64 <= n2 && ((((uintptr_t)(crow + c)) & 15) == 0);
-          if (full) {
-            const float4* p4 = (const float4*)(crow + c);
+      for (int cc = 0; cc < TC_BN / 2; cc += 32) {
+        const int col = c0 + cc + lane;
+        const bool colok = col < n2;
+        float cv[32];
 #pragma unroll
-            for (int x = 0; x < 16; x++) cv[x] = p4[x];
-          }
-        }
-        float v[64];
+        for (int r = 0; r < 32; r++) cv[r] = (colok && i0 + r < m) ? C[(size_t)(i0 + r) * ldcf + col] : 0.f;
+        float v[32];
         tmem_ld16(ta + cc, v);
         tmem_ld16(ta + cc + 16, v + 16);
-        tmem_ld16(ta + cc + 32, v + 32);
-        tmem_ld16(ta + cc + 48, v + 48);
-        if (cc + 64 == TC_BN / 2) {  // this warp's part of accumulator b is read: signal the MMA warp
+        if (cc + 32 == TC_BN / 2) {  // this warp's part of accumulator b is read: signal the MMA warp
           tc_fence_before();
           __syncwarp();
           if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar0 + 144 + 8 * b) : "memory");
         }
-        if (full) {
-          float4* p4 = (float4*)(crow + c);
 #pragma unroll
-          for (int x = 0; x < 16; x++) {
-            float4 t4 = cv[x];
-            t4.x -= v[4 * x + 0];
-            t4.y -= v[4 * x + 1];
-            t4.z -= v[4 * x + 2];
-            t4.w -= v[4 * x + 3];
-            p4[x] = t4;
-          }
-        } else if (row < m) {
+        for (int c = 0; c < 32; c++) tb[lane * 33 + c] = v[c];
+        __syncwarp();
 #pragma unroll
-          for (int x = 0; x < 64; x++)
-            if (c + x < n2) crow[c + x] -= v[x];
-        }
+        for (int r = 0; r < 32; r++)
+          if (colok && i0 + r < m) C[(size_t)(i0 + r) * ldcf + col] = cv[r] - tb[r * 33 + lane];
+        __syncwarp();
       }
     }
   }
