@@ -1154,125 +1154,177 @@ __global__ void k_gather_rows(const T* X, size_t ldx, int n, int nrhs, const int
   int i = (int)(q / nrhs), c = (int)(q % nrhs);
   Y[(size_t)i * nrhs + c] = X[(size_t)perm[i] * ldx + c];
 }
-// X[k0..k0+nb) <- L11^-1 X (UPPER = 0, unit lower) or U11^-1 X (UPPER = 1)
-// for the packed right-hand sides X (n x nrhs): one warp per right-hand side,
-// lane l holds rows l and l + 32; the diagonal block is staged transposed in
-// shared memory by the whole block (256 threads), with the inverted diagonal
+// One cooperative launch per triangular solve.  Row blocks of LU_NB rows are
+// owned by the CTAs (block q by CTA q mod gridDim, in increasing q); a block
+// folds in the contribution of every block it depends on as soon as that
+// block's flag is set, solves its diagonal block (warp per right-hand side,
+// substitution with shuffles), publishes its rows of Y and sets its flag.
+// All CTAs are co-resident (cooperative launch) and every block waits only
+// on blocks of smaller q, so the waits end; each wait is also bounded
+// (TRSV_SPIN_LIMIT polls): on time-out *err is raised and every CTA returns.
+#define TRSV_SPIN_LIMIT (1 << 22)
+__device__ __forceinline__ cplx ldcg_c(const cplx* p) { return cmk(__ldcg(&p->x), __ldcg(&p->y)); }
+__device__ __forceinline__ cplxf ldcg_c(const cplxf* p) { return cmkf(__ldcg(&p->x), __ldcg(&p->y)); }
+
 template <class T, int UPPER>
-__global__ void k_trsm_diag_multi(const T* LU, size_t lda, int k0, int nb, T* X, int nrhs) {
-  extern __shared__ __align__(16) unsigned char tdraw[];
-  const int ld = nb + 1;  // padded: the transposing stores spread over the banks
-  T* sT = (T*)tdraw;      // sT[j * ld + i] = block[i][j]
-  T* dinv = sT + nb * ld;
-  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
-    int i = t / nb, j = t % nb;
-    sT[j * ld + i] = LU[(size_t)(k0 + i) * lda + k0 + j];
+__global__ void __launch_bounds__(256) k_trsv_flags(const T* __restrict__ LU, size_t lda, int n, T* Y, int nrhs,
+                                                    int* flags, int* err) {
+  typedef typename RealOf<T>::type Rt;
+  extern __shared__ __align__(16) unsigned char tfraw[];
+  constexpr int LD = LU_NB + 1;
+  T* sT = (T*)tfraw;             // diagonal block, transposed: sT[j * LD + i] = block[i][j]
+  T* sdinv = sT + LU_NB * LD;    // inverted diagonal (UPPER)
+  T* sx = sdinv + LU_NB;         // the block's right-hand sides, LU_NB x 8
+  __shared__ int s_abort;
+  const int nbk = (n + LU_NB - 1) / LU_NB;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int q = blockIdx.x; q < nbk; q += gridDim.x) {
+    const int b = UPPER ? nbk - 1 - q : q;
+    const int r0 = b * LU_NB, rows = min(LU_NB, n - r0);
+    for (int t = threadIdx.x; t < rows * nrhs; t += blockDim.x) sx[t] = Y[(size_t)r0 * nrhs + t];
+    for (int t = threadIdx.x; t < rows * rows; t += blockDim.x) {
+      const int i = t / rows, j = t % rows;
+      sT[j * LD + i] = LU[(size_t)(r0 + i) * lda + r0 + j];
+    }
+    if (threadIdx.x == 0) s_abort = 0;
+    __syncthreads();
+    if (UPPER) {
+      for (int j = threadIdx.x; j < rows; j += blockDim.x) {
+        T one;
+        one.x = 1; one.y = 0;
+        sdinv[j] = cdivc(one, sT[j * LD + j]);
+      }
+      __syncthreads();  // the diagonal solve may follow without a dependency round
+    }
+    for (int jq = 0; jq < q; jq++) {
+      const int jb = UPPER ? nbk - 1 - jq : jq;
+      const int c0 = jb * LU_NB, cols = min(LU_NB, n - c0);
+      if (threadIdx.x == 0) {
+        int it = 0;
+        while (*(volatile int*)(flags + jb) == 0) {
+          if (*(volatile int*)err != 0 || ++it > TRSV_SPIN_LIMIT) { atomicExch(err, 1); s_abort = 1; break; }
+          __nanosleep(32);
+        }
+        __threadfence();
+      }
+      __syncthreads();
+      if (s_abort) return;
+      for (int i = w; i < rows; i += nw) {  // sx[i] -= LU[r0+i][c0..] Y[c0..]
+        const T* a = LU + (size_t)(r0 + i) * lda + c0;
+        Rt sr[8], si[8];
+#pragma unroll
+        for (int c = 0; c < 8; c++) { sr[c] = 0; si[c] = 0; }
+        for (int k = lane; k < cols; k += 32) {
+          const T av = a[k];
+#pragma unroll
+          for (int c = 0; c < 8; c++) {
+            if (c < nrhs) {
+              const T yv = ldcg_c(Y + (size_t)(c0 + k) * nrhs + c);
+              sr[c] += av.x * yv.x - av.y * yv.y;
+              si[c] += av.x * yv.y + av.y * yv.x;
+            }
+          }
+        }
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+          if (c < nrhs) {
+            for (int o = 16; o > 0; o >>= 1) {
+              sr[c] += __shfl_down_sync(0xffffffffu, sr[c], o);
+              si[c] += __shfl_down_sync(0xffffffffu, si[c], o);
+            }
+          }
+        }
+        if (lane == 0) {
+#pragma unroll
+          for (int c = 0; c < 8; c++)
+            if (c < nrhs) { sx[i * nrhs + c].x -= sr[c]; sx[i * nrhs + c].y -= si[c]; }
+        }
+      }
+      __syncthreads();
+    }
+    if (w < nrhs) {  // diagonal block: warp w solves right-hand side w
+      const int i0 = lane, i1 = lane + 32;
+      T x0, x1;
+      x0.x = 0; x0.y = 0; x1 = x0;
+      if (i0 < rows) x0 = sx[i0 * nrhs + w];
+      if (i1 < rows) x1 = sx[i1 * nrhs + w];
+      if (!UPPER) {
+        for (int j = 0; j < rows; j++) {
+          T v = (j < 32) ? x0 : x1;
+          T xj;
+          xj.x = __shfl_sync(0xffffffffu, v.x, j & 31);
+          xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
+          const T* col = sT + j * LD;
+          if (i0 > j && i0 < rows) x0 -= col[i0] * xj;
+          if (i1 > j && i1 < rows) x1 -= col[i1] * xj;
+        }
+      } else {
+        for (int j = rows - 1; j >= 0; j--) {
+          T v = (j < 32) ? x0 : x1;
+          T xj;
+          xj.x = __shfl_sync(0xffffffffu, v.x, j & 31);
+          xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
+          xj = xj * sdinv[j];
+          if (lane == (j & 31)) { if (j < 32) x0 = xj; else x1 = xj; }
+          const T* col = sT + j * LD;
+          if (i0 < j) x0 -= col[i0] * xj;
+          if (i1 < j) x1 -= col[i1] * xj;
+        }
+      }
+      if (i0 < rows) Y[(size_t)(r0 + i0) * nrhs + w] = x0;
+      if (i1 < rows) Y[(size_t)(r0 + i1) * nrhs + w] = x1;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicExch(flags + b, 1);
   }
-  __syncthreads();
-  if (UPPER)
-    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
-      T one;
-      one.x = 1; one.y = 0;
-      dinv[j] = cdivc(one, sT[j * ld + j]);
-    }
-  __syncthreads();
-  const int lane = threadIdx.x & 31, c = threadIdx.x >> 5;
-  if (c >= nrhs) return;
-  const int i0 = lane, i1 = lane + 32;
-  T x0, x1;
-  x0.x = 0; x0.y = 0; x1 = x0;
-  if (i0 < nb) x0 = X[(size_t)(k0 + i0) * nrhs + c];
-  if (i1 < nb) x1 = X[(size_t)(k0 + i1) * nrhs + c];
-  if (!UPPER) {
-    for (int j = 0; j < nb; j++) {
-      T v = (j < 32) ? x0 : x1;
-      T xj;
-      xj.x = __shfl_sync(0xffffffffu, v.x, j & 31);
-      xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
-      const T* col = sT + j * ld;
-      if (i0 > j && i0 < nb) x0 -= col[i0] * xj;
-      if (i1 > j && i1 < nb) x1 -= col[i1] * xj;
-    }
-  } else {
-    for (int j = nb - 1; j >= 0; j--) {
-      T v = (j < 32) ? x0 : x1;
-      T xj;
-      xj.x = __shfl_sync(0xffffffffu, v.x, j & 31);
-      xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
-      xj = xj * dinv[j];
-      if (lane == (j & 31)) { if (j < 32) x0 = xj; else x1 = xj; }
-      const T* col = sT + j * ld;
-      if (i0 < j) x0 -= col[i0] * xj;
-      if (i1 < j) x1 -= col[i1] * xj;
-    }
-  }
-  if (i0 < nb) X[(size_t)(k0 + i0) * nrhs + c] = x0;
-  if (i1 < nb) X[(size_t)(k0 + i1) * nrhs + c] = x1;
-}
-template <class T>
-__global__ void k_trsm_update_multi(const T* LU, size_t lda, int r0, int r1, int k0, int nb, T* X, int nrhs) {
-  int w = (int)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-  int lane = threadIdx.x & 31;
-  int r = r0 + w;
-  if (r >= r1) return;
-  const T* row = LU + (size_t)r * lda + k0;
-  typedef typename RealOf<T>::type R;
-  R sr[8], si[8];
-  for (int c = 0; c < 8; c++) { sr[c] = 0; si[c] = 0; }
-  for (int j = lane; j < nb; j += 32) {
-    T a = row[j];
-    for (int c = 0; c < nrhs; c++) {
-      T b = X[(size_t)(k0 + j) * nrhs + c];
-      sr[c] += a.x * b.x - a.y * b.y;
-      si[c] += a.x * b.y + a.y * b.x;
-    }
-  }
-  for (int c = 0; c < nrhs; c++) {
-    for (int o = 16; o > 0; o >>= 1) {
-      sr[c] += __shfl_down_sync(0xffffffffu, sr[c], o);
-      si[c] += __shfl_down_sync(0xffffffffu, si[c], o);
-    }
-  }
-  if (lane == 0)
-    for (int c = 0; c < nrhs; c++) {
-      X[(size_t)r * nrhs + c].x -= sr[c];
-      X[(size_t)r * nrhs + c].y -= si[c];
-    }
 }
 
-// Y <- (LU)^-1 P X for nrhs <= 8 columns; X (ldx) is read, Y (n x nrhs, packed) written
+template <class T, int UPPER>
+static int trsv_flags(const T* LU, size_t lda, int n, T* Y, int nrhs, int* flags, int* err, cudaStream_t st) {
+  const size_t sm = ((size_t)LU_NB * (LU_NB + 1) + LU_NB + (size_t)LU_NB * 8) * sizeof(T);
+  GB_CUDA(cudaFuncSetAttribute(k_trsv_flags<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  int dev = 0, nsm = 0, occ = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  GB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_flags<T, UPPER>, 256, sm));
+  const int nbk = (n + LU_NB - 1) / LU_NB;
+  int grid = nsm * (occ > 0 ? occ : 1);
+  if (grid > nbk) grid = nbk;
+  GB_CUDA(cudaMemsetAsync(flags, 0, (size_t)nbk * sizeof(int), st));
+  void* args[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&Y, (void*)&nrhs, (void*)&flags, (void*)&err};
+  GB_CUDA(cudaLaunchCooperativeKernel((const void*)k_trsv_flags<T, UPPER>, dim3(grid), dim3(256), args, sm, st));
+  gbi_count_launch();
+  return 0;
+}
+
+// Y <- (LU)^-1 P X for nrhs <= 8 columns; X (ldx) is read, Y (n x nrhs, packed)
+// written; a forward and a backward cooperative launch (k_trsv_flags).  The
+// time-out flag is checked once at the end (one host synchronisation).
 template <class T>
 static int lu_solve_multi(const T* LU, size_t lda, int n, const int* perm, const T* X, size_t ldx, int nrhs, T* Y,
                           cudaStream_t st) {
   if (nrhs < 1 || nrhs > 8) { gbi_set_error("lu_solve_multi: nrhs %d not in 1..8", nrhs); return -1; }
   size_t tot = (size_t)n * nrhs;
-  const size_t sm_diag = (size_t)(LU_NB * (LU_NB + 1) + LU_NB) * sizeof(T);
-  GB_CUDA(cudaFuncSetAttribute(k_trsm_diag_multi<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_diag));
-  GB_CUDA(cudaFuncSetAttribute(k_trsm_diag_multi<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm_diag));
+  const int nbk = (n + LU_NB - 1) / LU_NB;
+  int* flags = nullptr;
+  GB_CUDA(cudaMallocAsync((void**)&flags, ((size_t)nbk + 1) * sizeof(int), st));
+  int* err = flags + nbk;
+  GB_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
   k_gather_rows<T><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(X, ldx, n, nrhs, perm, Y);
   gbi_count_launch();
-  for (int k = 0; k < n; k += LU_NB) {
-    int nb = (n - k < LU_NB) ? n - k : LU_NB;
-    k_trsm_diag_multi<T, 0><<<1, 256, sm_diag, st>>>(LU, lda, k, nb, Y, nrhs);
-    gbi_count_launch();
-    int rows = n - k - nb;
-    if (rows > 0) {
-      k_trsm_update_multi<T><<<(unsigned)(((size_t)rows * 32 + 255) / 256), 256, 0, st>>>(LU, lda, k + nb, n, k, nb, Y, nrhs);
-      gbi_count_launch();
-    }
+  int rc = trsv_flags<T, 0>(LU, lda, n, Y, nrhs, flags, err, st);
+  if (!rc) rc = trsv_flags<T, 1>(LU, lda, n, Y, nrhs, flags, err, st);
+  int herr = 0;
+  if (!rc && (cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaStreamSynchronize(st) != cudaSuccess)) {
+    gbi_set_error("lu_solve_multi: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
   }
-  int last = ((n - 1) / LU_NB) * LU_NB;
-  for (int k = last; k >= 0; k -= LU_NB) {
-    int nb = (n - k < LU_NB) ? n - k : LU_NB;
-    k_trsm_diag_multi<T, 1><<<1, 256, sm_diag, st>>>(LU, lda, k, nb, Y, nrhs);
-    gbi_count_launch();
-    if (k > 0) {
-      k_trsm_update_multi<T><<<(unsigned)(((size_t)k * 32 + 255) / 256), 256, 0, st>>>(LU, lda, 0, k, k, nb, Y, nrhs);
-      gbi_count_launch();
-    }
-  }
-  GB_CUDA(cudaGetLastError());
-  return 0;
+  cudaFreeAsync(flags, st);
+  if (!rc && herr) { gbi_set_error("lu_solve_multi: a block wait timed out"); rc = -1; }
+  if (!rc) GB_CUDA(cudaGetLastError());
+  return rc;
 }
 extern "C" int gbi_zsolve_multi(const cplx* LU, size_t lda, int n, const int* perm, const cplx* X, size_t ldx, int nrhs,
                                 cplx* Y, cudaStream_t st) {
