@@ -31,6 +31,7 @@
 // raises *err, stops issuing work, frees its TMEM and returns.
 #include <cuda.h>
 
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -156,8 +157,8 @@ struct TcLayout {
   static constexpr int NOPS = PASSES == 3 ? 2 : 1;
   static constexpr int STAGE = NOPS * (A_BYTES + B_BYTES);
   static constexpr int STAGES = PASSES == 3 ? 2 : 4;  // 192 KB either way: one CTA per SM owns all of TMEM
-  static constexpr int EPI = 8 * 32 * 33 * 4;  // per epilogue warp a 32 x 33 float transpose buffer
-  static constexpr int SMEM = STAGES * STAGE + 1024 /* alignment */ + 256 /* barriers */ + EPI;
+  static constexpr int EPI = 8 * 32 * 32 * 4;  // per epilogue warp a 32 x 32 float chunk (128-byte swizzle)
+  static constexpr int SMEM = STAGES * STAGE + 1024 /* alignment */ + 1024 /* barriers */ + EPI;
 };
 
 // Persistent: CTA b takes tiles b, b + gridDim.x, ...; tile t covers rows
@@ -173,8 +174,9 @@ struct TcLayout {
 template <int PASSES>
 __global__ void __launch_bounds__(TC_THREADS, 1)
     k_tc_cgemm_sub(const __grid_constant__ CUtensorMap mAhi, const __grid_constant__ CUtensorMap mAlo,
-                   const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo, int m, int n2,
-                   int nkb, float* C, size_t ldcf, int* err) {
+                   const __grid_constant__ CUtensorMap mBhi, const __grid_constant__ CUtensorMap mBlo,
+                   const __grid_constant__ CUtensorMap mC, int use_tma_c, int m, int n2, int nkb, float* C, size_t ldcf,
+                   int* err) {
   using L = TcLayout<PASSES>;
   constexpr int S = L::STAGES;
   extern __shared__ uint8_t smraw[];
@@ -265,10 +267,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
   } else {  // epilogue warps 2..9: warp w reads TMEM lanes 32 (w & 3).. (tile rows), columns 128 h.. (h = (w-2) / 4)
     const int q = warp & 3, h = (warp - 2) >> 2;
-    // accumulator rows arrive one per lane; a 32 x 32 transpose through shared
-    // memory turns them into row segments, so that C is read and written with
-    // lanes on consecutive columns (coalesced)
-    float* tb = (float*)(sm + S * L::STAGE + 256) + (warp - 2) * (32 * 33);
+    // Accumulator rows arrive one per lane.  With use_tma_c each 32 x 32 chunk
+    // is negated into a 128-byte-swizzled shared-memory tile and added to C by
+    // a TMA reduction (cp.reduce.async.bulk.tensor ... .add: the L2 does the
+    // read-modify-write, the SM never loads C); otherwise the chunk is
+    // transposed through the same buffer and C is read and written with lanes
+    // on consecutive columns.
+    uint8_t* tbb = sm + S * L::STAGE + 1024 + (warp - 2) * 4096;  // 1024-byte aligned, 4 KB
+    float* tb = (float*)tbb;
+    const uint32_t tb_s = smem_u32(tbb);
     uint32_t lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, lt++) {
       const uint32_t b = lt & 1, u = lt >> 1;
@@ -282,28 +289,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const uint32_t ta = tmem + b * TC_BN + (uint32_t)(h * (TC_BN / 2)) + ((uint32_t)(q * 32) << 16);
 #pragma unroll 1
       for (int cc = 0; cc < TC_BN / 2; cc += 32) {
-        const int col = c0 + cc + lane;
-        const bool colok = col < n2;
-        float cv[32];
-#pragma unroll
-        for (int r = 0; r < 32; r++) cv[r] = (colok && i0 + r < m) ? C[(size_t)(i0 + r) * ldcf + col] : 0.f;
-        float v[32];
-        tmem_ld16(ta + cc, v);
-        tmem_ld16(ta + cc + 16, v + 16);
-        if (cc + 32 == TC_BN / 2) {  // this warp's part of accumulator b is read: signal the MMA warp
-          tc_fence_before();
+        if (use_tma_c) {
+          float v[32];
+          tmem_ld16(ta + cc, v);
+          tmem_ld16(ta + cc + 16, v + 16);
+          if (cc + 32 == TC_BN / 2) {  // this warp's part of accumulator b is read: signal the MMA warp
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar0 + 144 + 8 * b) : "memory");
+          }
+          if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // the buffer is free
           __syncwarp();
-          if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar0 + 144 + 8 * b) : "memory");
+          // row lane: 16-byte chunk c4 sits at chunk position c4 ^ (lane & 7)
+#pragma unroll
+          for (int c4 = 0; c4 < 8; c4++) {
+            float4 t4 = make_float4(-v[4 * c4], -v[4 * c4 + 1], -v[4 * c4 + 2], -v[4 * c4 + 3]);
+            *(float4*)(tbb + lane * 128 + ((c4 ^ (lane & 7)) << 4)) = t4;
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) {
+            asm volatile(
+                "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+                    (uint64_t)&mC),
+                "r"(c0 + cc), "r"(i0), "r"(tb_s)
+                : "memory");
+            asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+          }
+        } else {
+          const int col = c0 + cc + lane;
+          const bool colok = col < n2;
+          float cv[32];
+#pragma unroll
+          for (int r = 0; r < 32; r++) cv[r] = (colok && i0 + r < m) ? C[(size_t)(i0 + r) * ldcf + col] : 0.f;
+          float v[32];
+          tmem_ld16(ta + cc, v);
+          tmem_ld16(ta + cc + 16, v + 16);
+          if (cc + 32 == TC_BN / 2) {
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar0 + 144 + 8 * b) : "memory");
+          }
+#pragma unroll
+          for (int c = 0; c < 32; c++) tb[lane * 32 + (c ^ lane)] = v[c];  // XOR layout: conflict-free both ways
+          __syncwarp();
+#pragma unroll
+          for (int r = 0; r < 32; r++)
+            if (colok && i0 + r < m) C[(size_t)(i0 + r) * ldcf + col] = cv[r] - tb[r * 32 + (lane ^ r)];
+          __syncwarp();
         }
-#pragma unroll
-        for (int c = 0; c < 32; c++) tb[lane * 33 + c] = v[c];
-        __syncwarp();
-#pragma unroll
-        for (int r = 0; r < 32; r++)
-          if (colok && i0 + r < m) C[(size_t)(i0 + r) * ldcf + col] = cv[r] - tb[r * 33 + lane];
-        __syncwarp();
       }
     }
+    if (use_tma_c && lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
   tc_fence_before();
   __syncthreads();
@@ -472,6 +509,23 @@ extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda,
   if (!rc) rc = make_map(&mAlo, alo, M, Kp, TC_BM);
   if (!rc) rc = make_map(&mBhi, bhi, 2 * N, Kp, TC_BN);
   if (!rc) rc = make_map(&mBlo, blo, 2 * N, Kp, TC_BN);
+  // C as a 2-D FP32 tensor (rows M, 2N floats each, row stride 2 ldc floats)
+  // for the TMA reduce-add epilogue: needs a 16-byte aligned base and stride
+  CUtensorMap mC;
+  memset(&mC, 0, sizeof(mC));
+  int use_tma_c = ((((uintptr_t)C) & 15) == 0) && ((ldc * 8) % 16 == 0);
+  if (!rc && use_tma_c) {
+    EncodeTiledFn enc = encode_fn();
+    cuuint64_t dims[2] = {(cuuint64_t)2 * N, (cuuint64_t)M};
+    cuuint64_t strides[1] = {(cuuint64_t)ldc * 8};
+    cuuint32_t box[2] = {32, 32};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = enc ? enc(&mC, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)C, dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE)
+                     : CUDA_ERROR_NOT_SUPPORTED;
+    if (r != CUDA_SUCCESS) use_tma_c = 0;  // the register epilogue handles it
+  }
   if (!rc) {
     int dev = 0, nsm = 0;
     GB_CUDA(cudaGetDevice(&dev));
@@ -495,11 +549,11 @@ extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda,
     }
     if (three) {
       GB_CUDA(cudaFuncSetAttribute(k_tc_cgemm_sub<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcLayout<3>::SMEM));
-      k_tc_cgemm_sub<3><<<grid, TC_THREADS, TcLayout<3>::SMEM, st>>>(mAhi, mAlo, mBhi, mBlo, M, 2 * N, nkb, (float*)C,
+      k_tc_cgemm_sub<3><<<grid, TC_THREADS, TcLayout<3>::SMEM, st>>>(mAhi, mAlo, mBhi, mBlo, mC, use_tma_c, M, 2 * N, nkb, (float*)C,
                                                                       2 * ldc, e);
     } else {
       GB_CUDA(cudaFuncSetAttribute(k_tc_cgemm_sub<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, TcLayout<1>::SMEM));
-      k_tc_cgemm_sub<1><<<grid, TC_THREADS, TcLayout<1>::SMEM, st>>>(mAhi, mAlo, mBhi, mBlo, M, 2 * N, nkb, (float*)C,
+      k_tc_cgemm_sub<1><<<grid, TC_THREADS, TcLayout<1>::SMEM, st>>>(mAhi, mAlo, mBhi, mBlo, mC, use_tma_c, M, 2 * N, nkb, (float*)C,
                                                                       2 * ldc, e);
     }
     gbi_count_launch();
