@@ -867,11 +867,12 @@ extern "C" int gb_ir_info(gb_obj* o, int* iters, double* relres) {
 
 // One scene step on the device for a single object: assembly of every
 // domain (quadrature type), factorisation of A (form 0: FP64 LU and explicit
-// inverse; form 1: complex FP32 LU + FP64 refinement), boundary values U,dU,
-// then E, H and their normal derivatives.
+// inverse; form 1: complex FP32 LU + FP64 refinement; form 2: form 1 with the
+// FP32 far-pair assembly of gb_assemble2), boundary values U,dU, then E, H
+// and their normal derivatives.
 extern "C" int gb_scene_step(gb_obj* o, int form, int type) {
   for (int d = 0; d <= o->m.MN; d++)
-    if (gb_assemble(o, d, type)) return -1;
+    if (gb_assemble2(o, d, type, form == 2 ? 1 : 0)) return -1;
   if (form == 0) { if (gb_invA_compute(o)) return -1; }
   else if (gb_factor_mixed(o)) return -1;
   if (gb_solve_mEMP(o)) return -1;

@@ -114,8 +114,7 @@ struct PairF {
   float c1[3], c2[3], c3[3];  // r_s(z,e) - r_s(0,0) = c1 z + c2 e + c3 z e
   float w0[3], w1[3], w2[3];  // W(z,e) = w0 + w1 z + w2 e
   float vt[2][3];
-  cplxf E0;      // e^{i k |R0|} (FP64, rounded)
-  cplxf k;
+  cplxf k, klo;  // k = k + klo exactly (the FP32 rounding of k would bias every far entry alike)
 };
 
 struct RegAccF {
@@ -129,6 +128,11 @@ __device__ __forceinline__ float dot3f(const float a[3], const float b[3]) {
   return fmaf(a[0], b[0], fmaf(a[1], b[1], a[2] * b[2]));
 }
 
+// FP32 point evaluation relative to the source element's point (0,0).  The
+// common factor e^{ik|R0|} of all phased sums is left out (applied in FP64 to
+// the sums), the triangle's shape functions are accumulated times 3 (the 1/3
+// applied in FP64), and k and sqrt(3) carry a low part: constants that would
+// otherwise round alike for every pair do not bias the matrix.
 __device__ __forceinline__ void reg_point_f32(const PairF& P, bool quad, float z, float e, float w, RegAccF& A) {
   float d[3], R[3], W[3];
 #pragma unroll
@@ -144,18 +148,21 @@ __device__ __forceinline__ void reg_point_f32(const PairF& P, bool quad, float z
   float sn, cs;
   sincosf(P.k.x * dl, &sn, &cs);
   const float ex = (P.k.y == 0.0f) ? 1.0f : expf(-P.k.y * dl);
-  const cplxf ce = P.E0 * cmkf(cs * ex, sn * ex);
-  const cplxf cb = cmkf(-P.k.y * aR - 1.0f, P.k.x * aR);  // i k R - 1
+  const cplxf ce = cmkf(cs * ex, sn * ex);  // e^{ik(|R| - |R0|)}
+  const cplxf kR = cmkf(fmaf(P.k.x, aR, P.klo.x * aR), fmaf(P.k.y, aR, P.klo.y * aR));
+  const cplxf cb = cmkf(-kR.y - 1.0f, kR.x);  // i k R - 1
   const float rdW = dot3f(R, W) * iR;
   const float tD = rdW * iR * iR;
   float N[4];
   if (quad) {
-    const float ia = (float)(1.0 / GB_P44_N);
-    const float zm = 1.0f - z * ia, zp = 1.0f + z * ia, em = 1.0f - e * ia, ep = 1.0f + e * ia;
+    const float ia = 1.7320508f, ial = 3.1087249e-08f;  // 1 / GB_P44_N = sqrt(3), high + low
+    const float za = fmaf(z, ia, z * ial), ea = fmaf(e, ia, e * ial);
+    const float zm = 1.0f - za, zp = 1.0f + za, em = 1.0f - ea, ep = 1.0f + ea;
     N[0] = 0.25f * zm * em; N[1] = 0.25f * zp * em; N[2] = 0.25f * zp * ep; N[3] = 0.25f * zm * ep;
-  } else {
-    const float ia = (float)(0.5 / GB_P34_N0), s3 = 1.7320508075688772f, t3 = 1.0f / 3.0f;
-    N[0] = t3 * (1.0f - ia * (z + s3 * e)); N[1] = t3 * (1.0f + 2.0f * ia * z); N[2] = t3 * (1.0f - ia * (z - s3 * e));
+  } else {  // 3 x the shape functions (ia = 0.5 / GB_P34_N0 = 2.5 exactly)
+    const float ia = 2.5f, s3 = 1.7320508f, s3l = 3.1087249e-08f;
+    const float se = fmaf(s3, e, s3l * e);
+    N[0] = 1.0f - ia * (z + se); N[1] = 1.0f + 2.0f * ia * z; N[2] = 1.0f - ia * (z - se);
     N[3] = 0.0f;
   }
   const cplxf g = ce * (iR * aW * w);
@@ -164,7 +171,6 @@ __device__ __forceinline__ void reg_point_f32(const PairF& P, bool quad, float z
 #pragma unroll
   for (int n = 0; n < 4; n++) { A.G[n] += g * N[n]; A.H[n] += h * N[n]; }
   A.F += w * tD;
-  const cplxf kR = P.k * aR;
   const cplxf t1 = kR * kR + cb * 3.0f;
   const float iR3 = iR * iR * iR;
 #pragma unroll
@@ -221,8 +227,8 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, uint8_t* red
   }
   P.a0 = (float)a0;
   const cplx E0 = cexpik(a.k, a0);
-  P.E0 = cmkf((float)E0.x, (float)E0.y);
   P.k = cmkf((float)a.k.x, (float)a.k.y);
+  P.klo = cmkf((float)(a.k.x - (double)P.k.x), (float)(a.k.y - (double)P.k.y));
   RegAccF A;
 #pragma unroll
   for (int n = 0; n < 4; n++) {
@@ -230,43 +236,46 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, uint8_t* red
     A.dG[0][n] = cmkf(0, 0); A.dG[1][n] = cmkf(0, 0); A.dH[0][n] = cmkf(0, 0); A.dH[1][n] = cmkf(0, 0);
   }
   A.F = 0.f; A.dF[0] = 0.f; A.dF[1] = 0.f;
-  float S0;
+  double S0;  // scale in FP64, with the 1/3 of the triangle's shape functions
   if (S.quad) {
-    S0 = (float)GB_I_FP;
+    S0 = GB_I_FP;
     for (int i = 0; i < GB_GLN; i++)
       for (int j = 0; j < GB_GLN; j++)
         reg_point_f32(P, true, c_tabf.xli[i], c_tabf.xli[j], c_tabf.wli[i] * c_tabf.wli[j], A);
   } else {
-    S0 = (float)(0.0625 * GB_SQ3 * GB_I_SPSQ3);
-    const float s3 = 1.7320508075688772f;
+    S0 = 0.0625 * GB_SQ3 * GB_I_SPSQ3;
+    const float s3 = 1.7320508f, s3l = 3.1087249e-08f;
     for (int i = 0; i < GB_GLN; i++) {
       const float x = c_tabf.xli[i];
       for (int j = 0; j < GB_GLN; j++) {
         const float y = c_tabf.xli[j];
         const float w = c_tabf.wli[i] * c_tabf.wli[j] * (1.0f + 0.25f * x + 0.25f * y);
-        reg_point_f32(P, false, 0.125f * (3.0f + 2.0f * x + 2.0f * y + x * y), 0.125f * s3 * (-x + y), w, A);
-        reg_point_f32(P, false, 0.0625f * (-3.0f + x - 5.0f * y - x * y), 0.0625f * s3 * (3.0f + 3.0f * x + y + x * y), w, A);
-        reg_point_f32(P, false, 0.0625f * (-3.0f - 5.0f * x + y - x * y), 0.0625f * s3 * (-3.0f - x - 3.0f * y - x * y), w, A);
+        const float q1 = -x + y, q2 = 3.0f + 3.0f * x + y + x * y, q3 = -3.0f - x - 3.0f * y - x * y;
+        reg_point_f32(P, false, 0.125f * (3.0f + 2.0f * x + 2.0f * y + x * y), 0.125f * fmaf(s3, q1, s3l * q1), w, A);
+        reg_point_f32(P, false, 0.0625f * (-3.0f + x - 5.0f * y - x * y), 0.0625f * fmaf(s3, q2, s3l * q2), w, A);
+        reg_point_f32(P, false, 0.0625f * (-3.0f - 5.0f * x + y - x * y), 0.0625f * fmaf(s3, q3, s3l * q3), w, A);
       }
     }
   }
-  const float sh = sd < 0 ? -S0 : S0;
-  const float dF0 = A.dF[0] * sh, dF1 = A.dF[1] * sh;
-  if (!(fabsf(dF0) <= 0.45f && fabsf(dF1) <= 0.45f)) {  // near the GLN/GHN decision (or not finite): FP64
+  const double sh = sd < 0 ? -S0 : S0;
+  const double s3n = S.quad ? 1.0 : 1.0 / 3.0;  // the triangle's shape functions were accumulated times 3
+  const double dF0 = (double)A.dF[0] * sh, dF1 = (double)A.dF[1] * sh;
+  if (!(fabs(dF0) <= 0.45 && fabs(dF1) <= 0.45)) {  // near the GLN/GHN decision (or not finite): FP64
     redo[p] = 1;
     return;
   }
   RegAcc<2> D;
+  const cplx eS = E0 * (S0 * s3n), eH = E0 * (sh * s3n), eDG = E0 * (-S0 * s3n);
 #pragma unroll
   for (int n = 0; n < 4; n++) {
-    D.G[n] = cmk(A.G[n].x * S0, A.G[n].y * S0);
-    D.H[n] = cmk(A.H[n].x * sh, A.H[n].y * sh);
+    D.G[n] = cmk(A.G[n].x, A.G[n].y) * eS;
+    D.H[n] = cmk(A.H[n].x, A.H[n].y) * eH;
     for (int q = 0; q < 2; q++) {
-      D.dG[q][n] = cmk(-A.dG[q][n].x * S0, -A.dG[q][n].y * S0);
-      D.dH[q][n] = cmk(A.dH[q][n].x * sh, A.dH[q][n].y * sh);
+      D.dG[q][n] = cmk(A.dG[q][n].x, A.dG[q][n].y) * eDG;
+      D.dH[q][n] = cmk(A.dH[q][n].x, A.dH[q][n].y) * eH;
     }
   }
-  D.F = A.F * sh;
+  D.F = (double)A.F * sh;
   D.dF[0] = dF0;
   D.dF[1] = dF1;
   store_pair(a, N, row, sidx, D);
