@@ -42,6 +42,10 @@ int gbi_field(const FieldObj* o, int mode, int type, int n, const double* rt, co
               int* flag, cudaStream_t st);
 int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, const int* t, const double* zt, cplx* out,
                  cudaStream_t st);
+int gbi_cross_build(const FieldObj* o, int type, int n, const double* rt, const double* v, int C, cplx* Gm, cplx* Hm,
+                    cplx* dGm, cplx* dHm, double* Fp, cudaStream_t st);
+int gbi_cross_apply(int n, int C, const cplx* Gm, const cplx* Hm, const cplx* dGm, const cplx* dHm, const double* Fp,
+                    const cplx* U, const cplx* dU, cplx* out, cudaStream_t st);
 int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
 int gbi_build_A32_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
                          const double* kn_dev, int did, int nrows, size_t base, size_t na, cplxf* A32, cudaStream_t st);
@@ -124,7 +128,25 @@ extern "C" int gb_device_count(void) {
 }
 
 // ------------------------------------------------------------------ object
+// Cached pieces of add_scattered for one (destination, source, quadrature
+// type): the domain of each destination node with respect to the source (a
+// sequential solid-angle sum per node, fixed by the geometry) and, when they
+// fit, the coefficients of the source's scattered potential at those nodes
+// (k_cross_build), so that every later iteration is a product with the
+// source's current boundary values.
+struct CrossCache {
+  unsigned long long src_uid;
+  int type;
+  int n, C;
+  int* did;
+  int bad;  // first invalid domain id (+1000), 0 if all nodes are outside the source
+  cplx *Gm, *Hm, *dGm, *dHm;
+  double* Fp;
+};
+
 struct gb_obj {
+  unsigned long long uid;
+  std::vector<CrossCache> xc;
   GbMeshDev m;
   double lambda0;
   cudaStream_t st;
@@ -178,6 +200,9 @@ static int dup(T** dst, const T* src, size_t n) {
 
 extern "C" void gb_obj_destroy(gb_obj* o) {
   if (!o) return;
+  for (auto& e : o->xc) {
+    cudaFree(e.did); cudaFree(e.Gm); cudaFree(e.Hm); cudaFree(e.dGm); cudaFree(e.dHm); cudaFree(e.Fp);
+  }
   cudaFree(o->m.cr); cudaFree(o->m.cw); cudaFree(o->m.ren); cudaFree(o->m.wen);
   cudaFree(o->m.etype); cudaFree(o->m.eni); cudaFree(o->m.md); cudaFree(o->m.sd); cudaFree(o->m.sid);
   cudaFree(o->kn_dev);
@@ -202,6 +227,8 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   if (md->Ne <= 0) { gbi_set_error("gb_obj_create: no elements"); return -1; }
   if (ensure_tables()) return -1;
   gb_obj* o = new gb_obj();
+  static std::atomic<unsigned long long> s_uid{1};
+  o->uid = s_uid.fetch_add(1);
   memset(&o->m, 0, sizeof(o->m));
   for (int d = 0; d < GB_MAXDOM; d++) { o->G[d] = o->H[d] = o->dG[d] = o->dH[d] = nullptr; o->dF[d] = nullptr; o->rowk[d] = nullptr; }
   o->invA = nullptr;
@@ -600,34 +627,87 @@ static FieldObj field_view(gb_obj* o) {
   return f;
 }
 
+// cross operators are kept while they need at most this share of the free device memory
+#define GB_CROSS_MEM_SHARE 0.25
+
+static CrossCache* cross_entry(gb_obj* dst, gb_obj* src, int type) {
+  for (auto& e : dst->xc)
+    if (e.src_uid == src->uid && e.type == type) return &e;
+  CrossCache e;
+  memset(&e, 0, sizeof(e));
+  e.src_uid = src->uid;
+  e.type = type;
+  e.n = dst->next;
+  e.C = 4 * src->m.sb_Ne[0];
+  if (dalloc((void**)&e.did, (size_t)e.n * sizeof(int))) return nullptr;
+  FieldObj f = field_view(src);
+  int* bad = nullptr;
+  if (dalloc((void**)&bad, sizeof(int))) { cudaFree(e.did); return nullptr; }
+  int rc = 0;
+  if (cudaMemsetAsync(bad, 0, sizeof(int), dst->st) != cudaSuccess) rc = -1;
+  if (!rc) rc = gbi_domain_id(&f, e.n, dst->ext_r, e.did, dst->st);
+  // the validity of every node is fixed by the geometry: checked once, here
+  std::vector<int> hd((size_t)e.n);
+  if (!rc && (cudaMemcpyAsync(hd.data(), e.did, (size_t)e.n * sizeof(int), cudaMemcpyDeviceToHost, dst->st) != cudaSuccess ||
+              cudaStreamSynchronize(dst->st) != cudaSuccess))
+    rc = -1;
+  cudaFree(bad);
+  if (rc) { cudaFree(e.did); if (!gb_last_error()[0]) gbi_set_error("add_scattered: domain id failed"); return nullptr; }
+  for (int i = 0; i < e.n && !e.bad; i++)
+    if (hd[i] != 0) e.bad = 1000 + hd[i];
+  size_t bytes = (size_t)e.n * e.C * 4 * sizeof(cplx);
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  if (!e.bad && e.n > 0 && e.C > 0 && bytes <= (size_t)(GB_CROSS_MEM_SHARE * (double)fr)) {
+    size_t nc = (size_t)e.n * e.C;
+    if (cudaMalloc((void**)&e.Gm, nc * sizeof(cplx)) == cudaSuccess &&
+        cudaMalloc((void**)&e.Hm, nc * sizeof(cplx)) == cudaSuccess &&
+        cudaMalloc((void**)&e.dGm, nc * sizeof(cplx)) == cudaSuccess &&
+        cudaMalloc((void**)&e.dHm, nc * sizeof(cplx)) == cudaSuccess &&
+        cudaMalloc((void**)&e.Fp, (size_t)e.n * 2 * sizeof(double)) == cudaSuccess &&
+        gbi_cross_build(&f, type, e.n, dst->ext_r, dst->ext_v, e.C, e.Gm, e.Hm, e.dGm, e.dHm, e.Fp, dst->st) == 0 &&
+        cudaStreamSynchronize(dst->st) == cudaSuccess) {
+      // kept
+    } else {
+      cudaGetLastError();  // an allocation failure is not an error here: the direct path serves
+      cudaFree(e.Gm); cudaFree(e.Hm); cudaFree(e.dGm); cudaFree(e.dHm); cudaFree(e.Fp);
+      e.Gm = e.Hm = e.dGm = e.dHm = nullptr;
+      e.Fp = nullptr;
+    }
+  }
+  dst->xc.push_back(e);
+  return &dst->xc.back();
+}
+
 extern "C" int gb_add_scattered(gb_obj* dst, gb_obj* src, int type) {
   if (ensure_bv(dst) || ensure_bv(src)) return -1;
   int n = dst->next;
   if (n == 0) return 0;
-  int *did = nullptr, *bad = nullptr;
-  cplx* out = nullptr;
-  if (dalloc((void**)&did, n * sizeof(int)) || dalloc((void**)&bad, sizeof(int)) ||
-      dalloc((void**)&out, (size_t)n * 8 * sizeof(cplx))) {
-    cudaFree(did); cudaFree(bad);
+  CrossCache* e = cross_entry(dst, src, type);
+  if (!e) return -1;
+  if (e->bad) {
+    gbi_set_error("scattered field domain id error!(overlapped). domain id=%d", e->bad - 1000);
     return -1;
   }
-  FieldObj f = field_view(src);
+  cplx* out = nullptr;
+  if (dalloc((void**)&out, (size_t)n * 8 * sizeof(cplx))) return -1;
   int rc = 0;
-  if (cudaMemsetAsync(bad, 0, sizeof(int), dst->st) != cudaSuccess) rc = -1;
-  if (!rc) rc = gbi_domain_id(&f, n, dst->ext_r, did, dst->st);
-  if (!rc) rc = gbi_field(&f, 3, type, n, dst->ext_r, dst->ext_v, did, out, nullptr, dst->st);
-  if (!rc) rc = gbi_add_incident(n, dst->ext_idx, out, dst->Ui, dst->dUi, did, bad, dst->st);
-  int hbad = 0;
-  if (!rc && (cudaMemcpyAsync(&hbad, bad, sizeof(int), cudaMemcpyDeviceToHost, dst->st) != cudaSuccess ||
-              cudaStreamSynchronize(dst->st) != cudaSuccess)) {
+  if (e->Gm) {
+    rc = gbi_cross_apply(n, e->C, e->Gm, e->Hm, e->dGm, e->dHm, e->Fp, src->bU[0], src->bdU[0], out, dst->st);
+  } else {
+    FieldObj f = field_view(src);
+    rc = gbi_field(&f, 3, type, n, dst->ext_r, dst->ext_v, e->did, out, nullptr, dst->st);
+  }
+  int* bad = nullptr;
+  if (!rc && dalloc((void**)&bad, sizeof(int))) rc = -1;
+  if (!rc && cudaMemsetAsync(bad, 0, sizeof(int), dst->st) != cudaSuccess) rc = -1;
+  if (!rc) rc = gbi_add_incident(n, dst->ext_idx, out, dst->Ui, dst->dUi, e->did, bad, dst->st);
+  if (!rc && cudaStreamSynchronize(dst->st) != cudaSuccess) {
     gbi_set_error("gb_add_scattered: %s", cudaGetErrorString(cudaGetLastError()));
     rc = -1;
   }
-  if (!rc && hbad) {
-    gbi_set_error("scattered field domain id error!(overlapped). domain id=%d", hbad - 1000);
-    rc = -1;
-  }
-  cudaFree(did); cudaFree(bad); cudaFree(out);
+  cudaFree(out);
+  cudaFree(bad);
   return rc;
 }
 

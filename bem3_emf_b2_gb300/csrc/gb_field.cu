@@ -407,6 +407,132 @@ __global__ void __launch_bounds__(128) k_field_bd(BdArgs a) {
   for (int l = 0; l < 6; l++) a.out[(size_t)p * 6 + l] = cdivr(cmk(acc[1 + 2 * l], acc[2 + 2 * l]), den);
 }
 
+// ------------------------------------------------------------------ cross operators
+// The potential scattered by object src at fixed points (the exterior nodes
+// of another object, mEMP2_s of add_scattered_mEMP, reference mo_solve.c:351-396)
+// is linear in src's boundary values of domain 0:
+//   u_l(p)  = (sum_c G[p][c] dU[c][l] - H[p][c] U[c][l]) / den_p
+//   du_l(p) = (sum_c dG[p][c] dU[c][l] - dH[p][c] U[c][l] - u_l(p) dF_p) / den_p
+// with c = (element s, shape function n) of src's domain-0 list and
+// den_p = 1 + F_p.  k_cross_build integrates these coefficients once, with
+// the quadrature and GHN fallback of k_field's mode 3, and stores them with
+// F_p and dF_p; k_cross_apply evaluates the sums at every iteration of the
+// multiple-scattering loop (a matrix-vector product instead of a quadrature).
+struct CrossArgs {
+  FieldObj o;
+  int type, n, C;
+  const double* rt;  // [n][3]
+  const double* v;   // [n][3]
+  cplx* Gm;          // [n][C]
+  cplx* Hm;
+  cplx* dGm;
+  cplx* dHm;
+  double* Fp;        // [n][2]: F, dF
+};
+
+__global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= a.n) return;
+  const FieldObj& o = a.o;
+  const double rt[3] = {a.rt[3 * p], a.rt[3 * p + 1], a.rt[3 * p + 2]};
+  const double vt[1][3] = {{a.v[3 * p], a.v[3 * p + 1], a.v[3 * p + 2]}};
+  const cplx k = cmk(o.kn[0], o.kn[1]);
+  const int* sid = o.sid + o.sb_off[0];
+  const int Ne = o.sb_Ne[0];
+  double F = 0.0, dF = 0.0;
+  const size_t row = (size_t)p * a.C;
+  const int niter = (Ne + 31) / 32;
+  for (int it = 0; it < niter; it++) {
+    const int s = 1 + it * 32 + lane;
+    const bool act = s <= Ne;
+    const int sd = act ? sid[s] : sid[1];
+    Elem S;
+    load_elem(S, o.cr, o.cw, o.etype, abs(sd));
+    const bool neg = sd < 0;
+    RegAcc<1> A;
+    bool fb = false;
+    if (act) {
+      reg_integrate<1>(S, a.type, rt, vt, k, neg, A);
+      fb = a.type < 3 && fabs(A.dF[0]) > GB_CBD_SDF;
+    }
+    warp_fallback<1>(fb, S, rt, vt, k, neg, A);
+    if (!act) continue;
+    F += A.F;
+    dF += A.dF[0];
+    const size_t c = row + (size_t)(s - 1) * 4;
+    for (int nn = 0; nn < 4; nn++) {
+      a.Gm[c + nn] = A.G[nn];
+      a.Hm[c + nn] = A.H[nn];
+      a.dGm[c + nn] = A.dG[0][nn];
+      a.dHm[c + nn] = A.dH[0][nn];
+    }
+  }
+  for (int o2 = 16; o2 > 0; o2 >>= 1) {
+    F += __shfl_down_sync(0xffffffffu, F, o2);
+    dF += __shfl_down_sync(0xffffffffu, dF, o2);
+  }
+  if (lane == 0) { a.Fp[2 * p] = F; a.Fp[2 * p + 1] = dF; }
+}
+
+// one warp per point: out[p][0..3] = u, out[p][4..7] = du (layout of k_field's mode 3)
+__global__ void __launch_bounds__(128) k_cross_apply(int n, int C, const cplx* __restrict__ Gm, const cplx* __restrict__ Hm,
+                                                     const cplx* __restrict__ dGm, const cplx* __restrict__ dHm,
+                                                     const double* __restrict__ Fp, const cplx* __restrict__ U,
+                                                     const cplx* __restrict__ dU, cplx* out) {
+  const int lane = threadIdx.x & 31;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= n) return;
+  double acc[16];
+#pragma unroll
+  for (int i = 0; i < 16; i++) acc[i] = 0.0;
+  const size_t row = (size_t)p * C;
+  for (int c = lane; c < C; c += 32) {
+    const cplx g = Gm[row + c], h = Hm[row + c], dg = dGm[row + c], dh = dHm[row + c];
+    const cplx* u = U + (size_t)(c + 4) * 4;    // element c / 4 + 1 (1-based), node c % 4
+    const cplx* du = dU + (size_t)(c + 4) * 4;
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+      const cplx t = g * du[l] - h * u[l];
+      const cplx td = dg * du[l] - dh * u[l];
+      acc[2 * l] += t.x;
+      acc[2 * l + 1] += t.y;
+      acc[8 + 2 * l] += td.x;
+      acc[9 + 2 * l] += td.y;
+    }
+  }
+  warp_allreduce<16>(acc);
+  if (lane != 0) return;
+  const double den = 1.0 + Fp[2 * p], dF = Fp[2 * p + 1];
+  for (int l = 0; l < 4; l++) {
+    const cplx uu = cdivr(cmk(acc[2 * l], acc[2 * l + 1]), den);
+    const cplx dd = cdivr(cmk(acc[8 + 2 * l], acc[9 + 2 * l]) - uu * dF, den);
+    out[(size_t)p * 8 + l] = uu;
+    out[(size_t)p * 8 + 4 + l] = dd;
+  }
+}
+
+extern "C" int gbi_cross_build(const FieldObj* o, int type, int n, const double* rt, const double* v, int C, cplx* Gm,
+                               cplx* Hm, cplx* dGm, cplx* dHm, double* Fp, cudaStream_t st) {
+  if (n <= 0) return 0;
+  CrossArgs a;
+  a.o = *o; a.type = type; a.n = n; a.C = C; a.rt = rt; a.v = v;
+  a.Gm = Gm; a.Hm = Hm; a.dGm = dGm; a.dHm = dHm; a.Fp = Fp;
+  k_cross_build<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(a);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+extern "C" int gbi_cross_apply(int n, int C, const cplx* Gm, const cplx* Hm, const cplx* dGm, const cplx* dHm,
+                               const double* Fp, const cplx* U, const cplx* dU, cplx* out, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_cross_apply<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(n, C, Gm, Hm, dGm, dHm, Fp, U, dU, out);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
 // ------------------------------------------------------------------ launchers
 extern "C" int gbi_domain_id(const FieldObj* o, int n, const double* rt, int* did, cudaStream_t st) {
   if (n <= 0) return 0;

@@ -322,6 +322,63 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "s/scene", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+CONES = dict(name="two cones (base radius 0.5, height 1, n = 1.59 in 1.33, lambda0 = 1), 12 m^2 linear triangles "
+                   "each (m = 16: 3,072 triangles, na = 73,728 per cone, node jitter 5 % of the ring spacing, "
+                   "seed 7); cone 2 rotated pi about x and shifted 1.5 along x; right-circularly polarised plane "
+                   "wave along +z; multiple-scattering iteration to the reference's convergence rule",
+             m=16, radius=0.5, height=1.0, n_obj=1.59, n_host=1.33, lambda0=1.0, seed=7)
+
+
+def write_cones(wd, m=None):
+    from bem3_emf_b2_gb300 import meshgen
+    m = m or CONES["m"]
+    nodes, elems = meshgen.cone_tri(m, CONES["radius"], CONES["height"], jitter=0.05, seed=CONES["seed"])
+    meshgen.write_mesh(os.path.join(wd, "cone.msh"), nodes, elems)
+    meshgen.write_medium(os.path.join(wd, "medium.txt"), [CONES["n_obj"]])
+    meshgen.write_ipw(os.path.join(wd, "ipw.txt"), [dict(lambda0=CONES["lambda0"], ni=CONES["n_host"], power=1.0,
+                                                          e0x=1.0, e0y=1j)])
+    return len(elems)
+
+
+def run_cones(args):
+    """The two-cone scene in the chosen form (one GPU): seconds per scene and
+    force/torque on each cone.  Its plain FP64 form (an FP64 LU and inverse of
+    na = 73,728 per cone, ~3e15 flop each) is not timed here."""
+    import torch
+    from bem3_emf_b2_gb300 import MultiScene, build, lib
+    build.build()
+    L = lib()
+    wd = tempfile.mkdtemp(prefix="cones_")
+    ne = write_cones(wd, args.cone_m)
+    med = [os.path.join(wd, "medium.txt")] * 2
+    msh = [os.path.join(wd, "cone.msh")] * 2
+    rv = np.array([[1.0, 0.0, 0.0], [1.0, 0.0, 0.0]])
+    th = np.array([0.0, np.pi])
+    tv = np.array([[0.0, 0.0, 0.0], [1.5, 0.0, 0.0]])
+    sc = MultiScene(med, msh, os.path.join(wd, "ipw.txt"), rv=rv, th=th, tv=tv)
+    times = []
+    F = N = None
+    l0 = L.gb_launch_count()
+    for i in range(args.warmup + args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        F, N = sc.step(form=1)
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t0)
+    it, cc = sc.iteration()
+    launches = (L.gb_launch_count() - l0) / (args.warmup + args.steps)
+    sc.close()
+    v = sum(times) / len(times)
+    return {"metric": METRIC, "value": v, "unit": "s/scene", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * v, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64 quadrature, c64 LU + c128 refinement", "data": "synthetic (meshgen cones, seed 7)",
+            "config": {"workload": CONES["name"], "elements_per_cone": ne, "form": "mixed",
+                       "timing": "host wall clock around each scene step (synchronised)"},
+            "iterations": it, "cc": cc, "force": F.tolist(), "torque": N.tolist(),
+            "gpu_launches": int(round(launches))}
+
+
 def profile_step(args):
     """Warm-up steps then exactly one chosen-form step (for ncu launch lists)."""
     import torch
@@ -349,11 +406,17 @@ def main():
     ap.add_argument("--profile-step", action="store_true",
                     help="profiling run: one chosen-form scene step after --warmup steps, nothing else, no JSON line")
     ap.add_argument("--faces", type=int, default=8, help="quadrangles per cube face of the profiling scene")
+    ap.add_argument("--workload", choices=["sphere", "cones"], default="sphere",
+                    help="sphere: the bench line (both forms); cones: the two-cone scene, chosen form only")
+    ap.add_argument("--cone-m", type=int, default=None, help="rings per cone surface (12 m^2 triangles per cone)")
     args = ap.parse_args()
     if args.profile_step:
         profile_step(args)
         return
-    out = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if args.workload == "cones":
+        out = run_cones(args)
+    else:
+        out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:
         print(json.dumps(out))
 

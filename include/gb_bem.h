@@ -104,7 +104,11 @@ int gb_solve_mEMP(gb_obj *o);
 /* Uip <- Ui, Ui <- Ui0, dUi <- dUi0 (reset_incident_bd, mo_solve.c:398-411) */
 int gb_reset_incident(gb_obj *o);
 /* dst.Ui, dst.dUi += potential scattered by src at dst's exterior nodes
- * (add_scattered_mEMP, mo_solve.c:296-396); fails if a node lies inside src */
+ * (add_scattered_mEMP, mo_solve.c:296-396); fails if a node lies inside src.
+ * The first call for a (src, type) pair fixes the nodes' domains and, when
+ * they fit in a quarter of the free device memory, integrates the
+ * coefficients of src's potential at dst's nodes once; later calls are a
+ * product with src's current boundary values. */
 int gb_add_scattered(gb_obj *dst, gb_obj *src, int type);
 /* sums of the convergence measure over the exterior nodes (ccd_f, mo_solve.c:413-455):
  * out[0] sum of potential changes, out[1] sum of phi changes, out[2] node count */
