@@ -67,6 +67,8 @@ def lib():
     L.gbh_set_quiet.restype = None
     L.gbh_last_iteration.argtypes = [vp, vp]
     L.gbh_last_iteration.restype = None
+    L.gbh_mscene_phase_times.argtypes = [vp]
+    L.gbh_mscene_phase_times.restype = None
     L.gb_ktime_enable.argtypes = [c_int]
     L.gb_ktime_enable.restype = None
     L.gb_ktime_read.argtypes = [vp, vp, vp, vp]
@@ -169,6 +171,13 @@ class MultiScene:
         if lib().gbh_mscene_step(self.h, form, type_, rcp, F.ctypes.data, N.ctypes.data) != 0:
             raise RuntimeError("gbh_mscene_step failed: %s" % last_error())
         return F.reshape(self.n, 3), N.reshape(self.n, 3)
+
+    def phase_times(self):
+        """(assembly, factorisation, iteration + E/H, force) seconds of the last step"""
+        import numpy as np
+        t = np.zeros(4)
+        lib().gbh_mscene_phase_times(t.ctypes.data)
+        return dict(zip(("assembly", "factorisation", "iteration_eh", "force"), t.tolist()))
 
     def iteration(self):
         it, cc = ctypes.c_int(0), ctypes.c_double(0.0)

@@ -7,10 +7,9 @@
 //            nodes of another object)  mo_solve.c:351-396
 //   EH_s_bd (fields on the boundary, own element integrated singularly)
 //                                     d3b1_field.c:238-279
-// One thread per point for the domain id (a sequential solid-angle sum in the
-// reference's element order, so that boundary and region decisions are the
-// reference's), one warp per point for the boundary-integral sums (lanes over
-// source elements).  A lane whose pair needs the GHN fallback
+// One warp per point for the domain id (solid-angle sums over each domain's
+// element list, boundary and region decisions as the reference's) and for the
+// boundary-integral sums (lanes over source elements).  A lane whose pair needs the GHN fallback
 // (|Re dF/dv| > CBD_SDF, d3b1_elem.c:296,314) gets it integrated by the whole
 // warp.
 #include "gb_quad.cuh"
@@ -70,37 +69,46 @@ __device__ double elem_solid_angle(int quad, double r[4][3], int* onb) {
   return om;
 }
 
-// sequential semantics of domain_id: per domain d in order, accumulate the
-// solid angles of its positively listed elements into Og[d] and subtract them
-// from Og[sd]; return at the first boundary hit or after domain d decides
-__device__ int domain_id_pt(const FieldObj& o, const double rt[3]) {
+// Domain of a point (reference domain_id, setup2.c:944-978): per domain d in
+// order, accumulate the solid angles of its positively listed elements into
+// Og[d] and subtract them from Og[sd]; a point on an element of domain d's list
+// belongs to d; after domain d's list, |Og[0]| < 2 pi (d = 0) or Og[d] > 2 pi
+// decides d; no decision: -1.
+// One warp per point, lanes over the elements of each domain's list: a
+// boundary hit anywhere in domain d's list returns d (the sequential loop
+// returns d at its first hit), and the region tests after domain d read the
+// warp-reduced sums Og (their summation order differs from the sequential
+// loop only by rounding).
+__global__ void __launch_bounds__(128) k_domain_id(FieldObj o, int n, const double* rt, int* did) {
+  const int lane = threadIdx.x & 31;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= n) return;
+  const double r0[3] = {rt[3 * p], rt[3 * p + 1], rt[3 * p + 2]};
   double Og[GB_MAXDOM];
   for (int d = 0; d <= o.MN; d++) Og[d] = 0.0;
+  int res = -1;
   for (int d = 0; d <= o.MN; d++) {
     const int* sid = o.sid + o.sb_off[d];
-    for (int i = 1; i <= o.sb_Ne[d]; i++) {
-      int s = sid[i];
+    int hit = 0;
+    for (int i = 1 + lane; i <= o.sb_Ne[d]; i += 32) {
+      const int s = sid[i];
       if (s <= 0) continue;
       double r[4][3];
       for (int j = 0; j < 4; j++)
-        for (int k = 0; k < 3; k++) r[j][k] = o.corner[(size_t)s * 12 + j * 3 + k] - rt[k];
+        for (int k = 0; k < 3; k++) r[j][k] = o.corner[(size_t)s * 12 + j * 3 + k] - r0[k];
       int onb = 0;
-      double om = elem_solid_angle(o.etype[s], r, &onb);
-      if (onb) return d;
+      const double om = elem_solid_angle(o.etype[s], r, &onb);
+      if (onb) { hit = 1; continue; }
       Og[d] += om;
       Og[o.sd[s]] -= om;
     }
-    if (d == 0 && fabs(Og[0]) < 2.0 * GB_PI) return 0;
-    if (Og[d] > 2.0 * GB_PI) return d;
+    if (__any_sync(0xffffffffu, hit)) { res = d; break; }
+    double od = Og[d];
+    for (int off = 16; off > 0; off >>= 1) od += __shfl_xor_sync(0xffffffffu, od, off);
+    if (d == 0 && fabs(od) < 2.0 * GB_PI) { res = 0; break; }
+    if (od > 2.0 * GB_PI) { res = d; break; }
   }
-  return -1;
-}
-
-__global__ void k_domain_id(FieldObj o, int n, const double* rt, int* did) {
-  int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= n) return;
-  double r[3] = {rt[3 * p], rt[3 * p + 1], rt[3 * p + 2]};
-  did[p] = domain_id_pt(o, r);
+  if (lane == 0) did[p] = res;
 }
 
 // ------------------------------------------------------------------ field sums
@@ -536,7 +544,7 @@ extern "C" int gbi_cross_apply(int n, int C, const cplx* Gm, const cplx* Hm, con
 // ------------------------------------------------------------------ launchers
 extern "C" int gbi_domain_id(const FieldObj* o, int n, const double* rt, int* did, cudaStream_t st) {
   if (n <= 0) return 0;
-  k_domain_id<<<(n + 127) / 128, 128, 0, st>>>(*o, n, rt, did);
+  k_domain_id<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(*o, n, rt, did);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;

@@ -35,6 +35,7 @@
 #include "gb_internal.h"
 
 #define LU_NB 64
+#define LU_NBO 256  // outer block: the trailing update's K
 
 // ------------------------------------------------------------------ A build
 struct ABuildArgs {
@@ -844,9 +845,30 @@ static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStre
       k_trsm_right<T><<<nblk, PANEL_THREADS, sm_right, st>>>(A, lda, k, nb, kend, n);
       gbi_count_launch();
       if (cudaGetLastError() != cudaSuccess) { gbi_set_error("LU panel launch failed"); rc = -1; break; }
-      if (trsm_rows<T>(0, A + (size_t)k * lda + k, lda, A + (size_t)k * lda, lda, nb, kend, n, st)) { rc = -1; break; }
-      if (gemm(n - kend, n - kend, nb, A + (size_t)kend * lda + k, lda, A + (size_t)k * lda + kend, lda,
+    }
+    // updates: inside the outer block of LU_NBO columns only, until its last
+    // panel; then the block's columns of U and one trailing update with
+    // K = LU_NBO (a quarter of the C traffic of per-panel updates)
+    const int K0 = (k / LU_NBO) * LU_NBO;
+    const int Kend = (K0 + LU_NBO < n) ? K0 + LU_NBO : n;
+    if (kend < Kend) {
+      if (trsm_rows<T>(0, A + (size_t)k * lda + k, lda, A + (size_t)k * lda, lda, nb, kend, Kend, st)) { rc = -1; break; }
+      if (gemm(n - kend, Kend - kend, nb, A + (size_t)kend * lda + k, lda, A + (size_t)k * lda + kend, lda,
                A + (size_t)kend * lda + kend, lda, st)) { rc = -1; break; }
+    } else if (Kend < n) {
+      // U12 of the outer block: X <- L^-1 X for rows K0..Kend, columns Kend..n,
+      // L the block's unit lower triangle, by its 64-row diagonal blocks
+      for (int i0 = K0; i0 < Kend && !rc; i0 += LU_NB) {
+        const int ib = (Kend - i0 < LU_NB) ? Kend - i0 : LU_NB;
+        if (trsm_rows<T>(0, A + (size_t)i0 * lda + i0, lda, A + (size_t)i0 * lda, lda, ib, Kend, n, st)) rc = -1;
+        else if (i0 + ib < Kend &&
+                 gemm(Kend - i0 - ib, n - Kend, ib, A + (size_t)(i0 + ib) * lda + i0, lda, A + (size_t)i0 * lda + Kend,
+                      lda, A + (size_t)(i0 + ib) * lda + Kend, lda, st))
+          rc = -1;
+      }
+      if (rc) break;
+      if (gemm(n - Kend, n - Kend, Kend - K0, A + (size_t)Kend * lda + K0, lda, A + (size_t)K0 * lda + Kend, lda,
+               A + (size_t)Kend * lda + Kend, lda, st)) { rc = -1; break; }
     }
   }
   cudaFreeAsync(cand, st);
@@ -1036,7 +1058,7 @@ extern "C" int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info,
   if (n <= 0) return 0;
   float* scratch = nullptr;
   int* err = nullptr;
-  size_t need = gbi_tc_scratch_floats(n, n, LU_NB);
+  size_t need = gbi_tc_scratch_floats(n, n, LU_NBO);
   GB_CUDA(cudaMallocAsync((void**)&scratch, need * sizeof(float), st));
   GB_CUDA(cudaMallocAsync((void**)&err, 16, st));
   GB_CUDA(cudaMemsetAsync(err, 0, 4, st));

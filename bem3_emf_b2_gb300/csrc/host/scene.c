@@ -2,6 +2,7 @@
  * scene.c -- single- and multi-object scenes without intermediate files
  * (gb_scene.h).
  */
+#include <time.h>
 #include "gb_host.h"
 #include "gb_scene.h"
 
@@ -121,25 +122,38 @@ MOBJ *gbh_mscene_open(int n,const char *const *medium_files,const char *const *m
   return mo;
 }
 
+static double g_phase[4];
+static double gbh_now(void){ struct timespec t; clock_gettime(CLOCK_MONOTONIC,&t); return t.tv_sec+1e-9*t.tv_nsec; }
+
 int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double *N)
 {
+  double t0=gbh_now(),ta=0.0,tf=0.0;
   for(int m=0;m<mo->N;m++){
     DOMD *md=&mo->md[m];
     gb_obj *o=gb_dev(md);
+    double t1=gbh_now();
     for(int d=0;d<=md->MN;d++)
       if(gb_assemble(o,d,type)){ printf("gbh_mscene_step: %s\n",gb_last_error()); return -1; }
+    double t2=gbh_now();
     if(form==0 ? gb_invA_compute(o) : gb_factor_mixed(o)){ printf("gbh_mscene_step: %s\n",gb_last_error()); return -1; }
+    ta+=t2-t1; tf+=gbh_now()-t2;
     /* matrices and the factors are resident: the iteration reads no .cmat file */
     gb_dev_set_flags(md,GB_F_CMAT|GB_F_INV,GB_F_BV);
   }
+  double t3=gbh_now();
   mo_solve_bv(mo);
+  double t4=gbh_now();
   for(int m=0;m<mo->N;m++){
     double c[3];
     for(int i=0;i<3;i++) c[i]=rc?rc[3*m+i]:mo->md[m].tv[i];
     if(mo_force_FN(F+3*m,N+3*m,c,m,0,mo)<0) return -1;
   }
+  g_phase[0]=ta; g_phase[1]=tf; g_phase[2]=t4-t3; g_phase[3]=gbh_now()-t4;
+  (void)t0;
   return 0;
 }
+
+void gbh_mscene_phase_times(double *t){ for(int i=0;i<4;i++) t[i]=g_phase[i]; }
 
 void gbh_mscene_drop_device(MOBJ *mo){ for(int m=0;m<mo->N;m++) gb_dev_release(&mo->md[m]); }
 

@@ -367,6 +367,7 @@ def run_cones(args):
         if i >= args.warmup:
             times.append(time.perf_counter() - t0)
     it, cc = sc.iteration()
+    phases = sc.phase_times()
     launches = (L.gb_launch_count() - l0) / (args.warmup + args.steps)
     sc.close()
     v = sum(times) / len(times)
@@ -375,7 +376,7 @@ def run_cones(args):
             "dtype": "f64 quadrature, c64 LU + c128 refinement", "data": "synthetic (meshgen cones, seed 7)",
             "config": {"workload": CONES["name"], "elements_per_cone": ne, "form": "mixed",
                        "timing": "host wall clock around each scene step (synchronised)"},
-            "iterations": it, "cc": cc, "force": F.tolist(), "torque": N.tolist(),
+            "iterations": it, "cc": cc, "phases_s": phases, "force": F.tolist(), "torque": N.tolist(),
             "gpu_launches": int(round(launches))}
 
 

@@ -52,6 +52,9 @@ void gbh_mscene_close(MOBJ *mo);
 void gbh_set_quiet(int q);
 /* iteration count and convergence measure cc of the last mo_solve_bv */
 void gbh_last_iteration(int *iter, double *cc);
+/* host wall-clock seconds of the last gbh_mscene_step: assembly, factorisation,
+ * multiple-scattering iteration with E/H (mo_solve_bv), force and torque */
+void gbh_mscene_phase_times(double *t);
 
 #ifdef __cplusplus
 }
