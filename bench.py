@@ -148,7 +148,7 @@ def cpu_baseline(wd, seconds_budget=20.0):
     o = port.Obj(os.path.join(wd, "mesh.msh"), [WORKLOAD["n_obj"]], WORKLOAD["lambda0"], WORKLOAD["n_host"])
     t_asm = 0.0
     nrows_total = 0
-    sample_rows = max(ncpu, 16)
+    sample_rows = max(8 * ncpu, 128)
     for d in range(o.MN + 1):
         N = 4 * (len(o.sids[d]) - 1)
         rows = np.linspace(0, N - 1, sample_rows).astype(np.int32)
@@ -158,7 +158,7 @@ def cpu_baseline(wd, seconds_budget=20.0):
         nrows_total += N
     from scipy.linalg import lapack
     na = 8 * o.NN
-    ns = 1536
+    ns = 3072
     A = (np.random.default_rng(0).standard_normal((ns, ns)) + 1j * np.random.default_rng(1).standard_normal((ns, ns)))
     t0 = time.perf_counter()
     lu, piv, info = lapack.zgetrf(A)
