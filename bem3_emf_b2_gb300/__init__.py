@@ -73,12 +73,29 @@ def lib():
     L.gb_ktime_enable.restype = None
     L.gb_ktime_read.argtypes = [vp, vp, vp, vp]
     L.gb_ktime_read.restype = c_int
+    L.gb_ktime_list.argtypes = [c_int, vp]
+    L.gb_ktime_list.restype = c_int
+    L.gb_form_precision.argtypes = [c_int]
+    L.gb_form_precision.restype = c_int
     _lib = L
     return L
 
 
 def last_error():
     return lib().gb_last_error().decode()
+
+
+def ktime_list():
+    """[(device ms, M, N, K)] of each recorded tensor-core launch (not cleared)"""
+    import numpy as np
+    L = lib()
+    n = L.gb_ktime_list(0, None)
+    if n < 0:
+        raise RuntimeError(last_error())
+    rec = np.zeros(4 * max(n, 1))
+    if L.gb_ktime_list(n, rec.ctypes.data) != n:
+        raise RuntimeError(last_error())
+    return [tuple(rec[4 * i:4 * i + 4]) for i in range(n)]
 
 
 def ktime_read():

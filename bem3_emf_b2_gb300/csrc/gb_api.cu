@@ -327,7 +327,7 @@ extern "C" int gb_assemble(gb_obj* o, int did, int type) { return gb_assemble2(o
 extern "C" int gb_assemble2(gb_obj* o, int did, int type, int precision) {
   if (check_did(o, did)) return -1;
   if (type < 0 || type > 3) { gbi_set_error("gb_assemble: quadrature type %d not in 0..3", type); return -1; }
-  if (precision != 0 && precision != 1) { gbi_set_error("gb_assemble: precision %d not 0 or 1", precision); return -1; }
+  if (precision < 0 || precision > 2) { gbi_set_error("gb_assemble: precision %d not in 0..2", precision); return -1; }
   if (ensure_cmatrix(o, did)) return -1;
   size_t Ne = (size_t)o->m.sb_Ne[did];
   double* Fs = nullptr;
@@ -945,14 +945,20 @@ extern "C" int gb_ir_info(gb_obj* o, int* iters, double* relres) {
   return 0;
 }
 
+// Assembly precision of each scene form: form 1 (the chosen form) integrates
+// the regular pairs in double-float, form 2 the far pairs in FP32, forms 0
+// and 3 everything in FP64.
+extern "C" int gb_form_precision(int form) { return form == 1 ? 2 : (form == 2 ? 1 : 0); }
+
 // One scene step on the device for a single object: assembly of every
-// domain (quadrature type), factorisation of A (form 0: FP64 LU and explicit
-// inverse; form 1: complex FP32 LU + FP64 refinement; form 2: form 1 with the
-// FP32 far-pair assembly of gb_assemble2), boundary values U,dU, then E, H
-// and their normal derivatives.
+// domain (quadrature type, precision gb_form_precision(form)), factorisation
+// of A (form 0: FP64 LU and explicit inverse; forms 1-3: complex FP32 LU +
+// FP64 refinement), boundary values U,dU, then E, H and their normal
+// derivatives.
 extern "C" int gb_scene_step(gb_obj* o, int form, int type) {
+  if (form < 0 || form > 3) { gbi_set_error("gb_scene_step: form %d not in 0..3", form); return -1; }
   for (int d = 0; d <= o->m.MN; d++)
-    if (gb_assemble2(o, d, type, form == 2 ? 1 : 0)) return -1;
+    if (gb_assemble2(o, d, type, gb_form_precision(form))) return -1;
   if (form == 0) { if (gb_invA_compute(o)) return -1; }
   else if (gb_factor_mixed(o)) return -1;
   if (gb_solve_mEMP(o)) return -1;

@@ -430,6 +430,7 @@ namespace {
 struct KtRec {
   cudaEvent_t a, b;
   double flops, bytes;
+  int M, N, K;
 };
 std::mutex g_kt_mu;
 bool g_kt_on = false;
@@ -465,6 +466,27 @@ extern "C" int gb_ktime_read(double* ms, long* launches, double* flops, double* 
   g_kt.clear();
   if (rc) gbi_set_error("gb_ktime_read: event query failed");
   return rc;
+}
+
+// the recorded launches one by one (not cleared): rec[4 i .. 4 i + 3] = device
+// ms, M, N, K of launch i for i < min(cap, count); returns the count or -1
+extern "C" int gb_ktime_list(int cap, double* rec) {
+  std::lock_guard<std::mutex> lk(g_kt_mu);
+  int i = 0;
+  for (auto& r : g_kt) {
+    if (i >= cap) break;
+    float x = 0.f;
+    if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&x, r.a, r.b) != cudaSuccess) {
+      gbi_set_error("gb_ktime_list: event query failed");
+      return -1;
+    }
+    rec[4 * i] = x;
+    rec[4 * i + 1] = r.M;
+    rec[4 * i + 2] = r.N;
+    rec[4 * i + 3] = r.K;
+    i++;
+  }
+  return (int)g_kt.size();
 }
 
 // floats of scratch that gbi_tc_cgemm_sub needs for an M x N x K update
@@ -543,6 +565,9 @@ extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda,
     if (timing) {
       GB_CUDA(cudaEventCreate(&rec.a));
       GB_CUDA(cudaEventCreate(&rec.b));
+      rec.M = M;
+      rec.N = N;
+      rec.K = K;
       rec.flops = 8.0 * M * (double)N * K;
       rec.bytes = 16.0 * M * (double)N + (three ? 2.0 : 1.0) * 4.0 * ((double)M + 2.0 * N) * Kp;
       GB_CUDA(cudaEventRecord(rec.a, st));

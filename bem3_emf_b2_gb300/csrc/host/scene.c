@@ -133,7 +133,7 @@ int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double
     gb_obj *o=gb_dev(md);
     double t1=gbh_now();
     for(int d=0;d<=md->MN;d++)
-      if(gb_assemble(o,d,type)){ printf("gbh_mscene_step: %s\n",gb_last_error()); return -1; }
+      if(gb_assemble2(o,d,type,gb_form_precision(form))){ printf("gbh_mscene_step: %s\n",gb_last_error()); return -1; }
     double t2=gbh_now();
     if(form==0 ? gb_invA_compute(o) : gb_factor_mixed(o)){ printf("gbh_mscene_step: %s\n",gb_last_error()); return -1; }
     ta+=t2-t1; tf+=gbh_now()-t2;

@@ -56,6 +56,9 @@ void *gb_obj_stream(gb_obj *o);
  * and algorithmic HBM bytes since then and clears the record */
 void gb_ktime_enable(int on);
 int gb_ktime_read(double *ms, long *launches, double *flops, double *bytes);
+/* the recorded launches one by one, without clearing: rec[4i..4i+3] = device
+ * ms, M, N, K of launch i (i < cap); returns the number recorded, -1 on error */
+int gb_ktime_list(int cap, double *rec);
 
 int gb_obj_create(const gb_mesh_desc *m, gb_obj **out);
 void gb_obj_destroy(gb_obj *o);
@@ -64,14 +67,19 @@ void gb_obj_destroy(gb_obj *o);
  * N = 4 sb_Ne[did], quadrature type 0..3 (4-point, 9/7-point, GLN, GHN; the
  * reference uses 2).  Replaces create_cmatrix_domain, solve_bieq2.c:98-184. */
 int gb_assemble(gb_obj *o, int did, int type);
-/* as gb_assemble; precision 1: regular pairs of the GLN x GLN rule farther
- * than three element radii integrated in FP32 relative to the source
- * element's centre (FP64 phase at the centre), all other pairs, the GHN
- * fallback and the singular elements in FP64.  Matrix entries then carry
- * ~1e-7 relative error (measured: G 9e-8, dH 2e-7, radiation force up to
- * 8e-7 on the 384-element sphere), so the scene steps use precision 0;
- * precision 1 is an opt-in for large scenes where assembly dominates. */
+/* as gb_assemble (precision 0: all in FP64) with another arithmetic for the
+ * regular pairs of the GLN x GLN rule.
+ * precision 2: regular pairs in double-float (two FP32 numbers, ~48 bits),
+ * pairs that need the GHN fallback and the singular elements in FP64.  The
+ * matrices agree with precision 0 to ~1e-14 relative Frobenius (rounding
+ * level); the chosen scene form uses it.
+ * precision 1: regular pairs farther than three element radii in FP32
+ * relative to the source element's centre (FP64 phase at the centre).
+ * Matrix entries then carry ~1e-7 relative error (measured: G 9e-8, dH 2e-7,
+ * radiation force up to 8e-7 on the 384-element sphere): an opt-in only. */
 int gb_assemble2(gb_obj *o, int did, int type, int precision);
+/* assembly precision of scene form `form` (1 -> 2, 2 -> 1, 0 and 3 -> 0) */
+int gb_form_precision(int form);
 /* copy the resident matrices of domain did to/from host buffers in the
  * reference's .cmat layout (any pointer may be NULL to skip that matrix) */
 int gb_cmatrix_download(gb_obj *o, int did, void *G, void *H, void *dG, void *dH, double *dF);
@@ -156,8 +164,11 @@ int gb_assemble_domain_noalloc(const double *cr, const double *cw, const int *et
  * refinement with those factors (residual b - A x in FP64, relative residual
  * <= 1e-13) instead of applying an explicit inverse.
  * gb_ir_info: corrections and final relative residual of the last solve.
- * gb_scene_step: assembly of every domain + factorisation (form 0: FP64 LU and
- * explicit inverse as in the reference; form 1: mixed) + U, dU + E, H, dE, dH. */
+ * gb_scene_step: assembly of every domain + factorisation + U, dU + E, H,
+ * dE, dH.  form 0: FP64 assembly, FP64 LU and explicit inverse as in the
+ * reference; form 1 (chosen): double-float regular pairs (gb_assemble2
+ * precision 2) and the mixed factorisation; form 2: FP32 far pairs
+ * (precision 1) and mixed; form 3: FP64 assembly and mixed. */
 int gb_factor_mixed(gb_obj *o);
 int gb_ir_info(gb_obj *o, int *iters, double *relres);
 int gb_scene_step(gb_obj *o, int form, int type);

@@ -1,8 +1,10 @@
 """GPU: the chosen (mixed-precision) form against the plain FP64 form and the
-reference.  Complex-FP32 LU + FP64 iterative refinement must reproduce the
-FP64 form's radiation force and torque to <= 1e-6 relative (the north-star
-tolerance of the chosen form) -- in practice the refinement reaches a
-relative residual of 1e-13 -- and the reference's force (golden) too."""
+reference.  Double-float regular-pair assembly + complex-FP32 LU + FP64
+iterative refinement must reproduce the FP64 form's radiation force and
+torque to <= 1e-6 relative (the tolerance of the chosen form) -- in practice
+the refinement reaches a relative residual of 1e-13 and the double-float
+matrices agree with FP64 to ~1e-14 -- and the reference's force (golden)
+too."""
 import os
 
 import numpy as np
@@ -64,3 +66,52 @@ def test_fp32_far_pair_assembly_error(gb_build, tmp_path):
         assert max(errs) <= 3e-7, errs
         assert max(errs) > 0.0  # the FP32 path did run
     sc.close()
+
+
+def _download(L, o, d, N):
+    m = [np.zeros((N, N), complex), np.zeros((N, N), complex), np.zeros((2 * N, N), complex),
+         np.zeros((2 * N, N), complex), np.zeros((N, 3))]
+    assert L.gb_cmatrix_download(o, d, *[x.ctypes.data for x in m]) == 0, L.gb_last_error()
+    return m
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["sphere2", "cone_mix", "cone_tri", "cube1", "sphere_nf6"])
+def test_double_float_assembly_matches_fp64(case, gb_build, tmp_path):
+    """gb_assemble2(precision 2): regular pairs in double-float.  G, H, dG, dH
+    and dF must agree with the FP64 assembly to <= 1e-12 relative Frobenius
+    (measured 3e-15 .. 4e-14), and the chosen scene form (form 1) must give the
+    force and torque of form 3 (same factorisation, FP64 assembly) to 1e-11."""
+    import ctypes
+    from bem3_emf_b2_gb300 import Scene, formats, lib
+    import bench
+    L = lib()
+    vp, ci = ctypes.c_void_p, ctypes.c_int
+    L.gb_assemble2.argtypes = [vp, ci, ci, ci]
+    L.gb_assemble2.restype = ci
+    L.gb_cmatrix_download.argtypes = [vp, ci] + [vp] * 5
+    L.gb_form_precision.argtypes = [ci]
+    L.gb_form_precision.restype = ci
+    assert [L.gb_form_precision(f) for f in range(4)] == [0, 2, 1, 0]
+    wd = str(tmp_path)
+    if case == "sphere_nf6":
+        bench.write_scene(wd, 6)
+        Ns = [4 * 6 * 36] * 2
+    else:
+        meta, _ = load_case(case)
+        write_inputs(meta, wd)
+        Ns = [4 * x for x in meta["sb_Ne"]]
+    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+    o = sc.obj()
+    for d in range(len(Ns)):
+        assert L.gb_assemble2(o, d, 2, 0) == 0, L.gb_last_error()
+        a = _download(L, o, d, Ns[d])
+        assert L.gb_assemble2(o, d, 2, 2) == 0, L.gb_last_error()
+        b = _download(L, o, d, Ns[d])
+        errs = [formats.rel_fro(x, y) for x, y in zip(b, a)]
+        assert max(errs) <= 1e-12, errs
+    F3, N3 = sc.step(form=3)
+    F1, N1 = sc.step(form=1)
+    sc.close()
+    d = np.linalg.norm(np.concatenate([F1 - F3, N1 - N3])) / np.linalg.norm(np.concatenate([F3, N3]))
+    assert d <= 1e-11, "double-float vs FP64 assembly, force/torque %g" % d
