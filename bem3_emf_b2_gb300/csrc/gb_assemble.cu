@@ -109,6 +109,7 @@ struct GbTablesF {
 static __constant__ GbTablesF c_tabf;
 struct GbTablesD {  // GL nodes and weights in double-float (hi, lo)
   float2 x[GB_GLN], w[GB_GLN];
+  float2 xh[GB_GHN], wh[GB_GHN];
 };
 static __constant__ GbTablesD c_tabd;
 
@@ -534,6 +535,180 @@ __global__ void __launch_bounds__(128) k_asm_regular(AsmArgs a) {
   if (work) store_pair(a, N, row, sidx, A);
 }
 
+// ---- double-float set B of the singular pairs (precision 2)
+// The derivative integrals on [DEPS, rm] with the GHN rule (sing_bil_setB /
+// sing_lit_setB of gb_quad.cuh, reference bil_dcoef.c / lit_dcoef.c D-bar_eps
+// parts) take 64 of every ~88 points of a singular row; here they run in
+// double-float.  The geometry along the ray is affine in r (K = Ka + Kb r,
+// W = Wa + Wb r, per direction in FP64), each direction's sums are kept in
+// double-float and added to the FP64 accumulators.
+struct SingAccB {
+  dfc dG[2][4], dH[2][4];
+  df dF[2];
+};
+
+__device__ __forceinline__ void singb_add(const SingAccB& B, SingAcc& A, int nsh, double scale) {
+#pragma unroll
+  for (int d = 0; d < 2; d++) {
+#pragma unroll
+    for (int n = 0; n < 4; n++) {
+      if (n >= nsh) break;
+      A.dG[d][n] += cmk(df_to(B.dG[d][n].re), df_to(B.dG[d][n].im)) * scale;
+      A.dH[d][n] += cmk(df_to(B.dH[d][n].re), df_to(B.dH[d][n].im)) * scale;
+    }
+    A.dF[d] += df_to(B.dF[d]);
+  }
+}
+
+__device__ __forceinline__ void singb_zero(SingAccB& B) {
+  const df z = dfmk(0.0f, 0.0f);
+#pragma unroll
+  for (int d = 0; d < 2; d++) {
+#pragma unroll
+    for (int n = 0; n < 4; n++) { B.dG[d][n] = dfcmk(z, z); B.dH[d][n] = dfcmk(z, z); }
+    B.dF[d] = z;
+  }
+}
+
+static __device__ void sing_bil_setB_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
+  const Elem& E = c.E;
+  const double zs = c.zt * sth + c.et * cth;
+  df Ka[3], Kb[3], Wa[3], Wb[3], vt[2][3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    Ka[d] = df_from(E.cr[d][1] * cth + E.cr[d][2] * sth + E.cr[d][3] * zs);
+    Kb[d] = df_from(E.cr[d][3] * cth * sth);
+    Wa[d] = df_from(E.cw[d][0] + E.cw[d][1] * c.zt + E.cw[d][2] * c.et);
+    Wb[d] = df_from(E.cw[d][1] * cth + E.cw[d][2] * sth);
+    vt[0][d] = df_from(c.vt[0][d]);
+    vt[1][d] = df_from(c.vt[1][d]);
+  }
+  const df hr = df_from(0.5 * (rm - GB_DEPS)), r0 = df_from(0.5 * (rm + GB_DEPS));
+  const df w0 = df_from(wth * 0.5 * (rm - GB_DEPS));
+  const df dzt = df_from(c.zt), det = df_from(c.et), dc = df_from(cth), ds = df_from(sth);
+  const df kr = df_from(c.k.x), ki = df_from(c.k.y);
+  const df cs[2] = {dc, ds}, outer[2] = {ds, dc};
+  const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // 1 / GB_P44_N = sqrt(3)
+  SingAccB B;
+  singb_zero(B);
+  for (int i = 0; i < GB_GHN; i++) {
+    const df rr = df_add(df_mul(hr, dfmk(c_tabd.xh[i].x, c_tabd.xh[i].y)), r0);
+    const df w = df_mul(w0, dfmk(c_tabd.wh[i].x, c_tabd.wh[i].y));
+    df K[3], W[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      K[d] = df_add(Ka[d], df_mul(Kb[d], rr));
+      W[d] = df_add(Wa[d], df_mul(Wb[d], rr));
+    }
+    const df aK2 = dot3d(K, K);
+    const df aK = df_sqrt(aK2), aW = df_sqrt(dot3d(W, W));
+    const df iK = df_rcp(aK), irr = df_rcp(rr);
+    const df x = df_mul(aK, rr);
+    const dfc kR = dfcmk(df_mul(kr, x), df_mul(ki, x));
+    df sn, co;
+    df_sincos(kR.re, &sn, &co);
+    dfc ce = dfcmk(co, sn);
+    if (ki.hi != 0.0f) ce = dfc_scale(ce, df_exp(df_neg(kR.im)));
+    const dfc cb = dfcmk(df_add_f(df_neg(kR.im), -1.0f), kR.re);
+    const df za = df_mul(df_add(dzt, df_mul(rr, dc)), ia), ea = df_mul(df_add(det, df_mul(rr, ds)), ia);
+    const df zm = df_add_f(df_neg(za), 1.0f), zp = df_add_f(za, 1.0f);
+    const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
+    df N[4];
+    N[0] = df_mul_f(df_mul(zm, em), 0.25f);
+    N[1] = df_mul_f(df_mul(zp, em), 0.25f);
+    N[2] = df_mul_f(df_mul(zp, ep), 0.25f);
+    N[3] = df_mul_f(df_mul(zm, ep), 0.25f);
+    const dfc cbce = dfc_mul(cb, ce);
+    const df iK2 = df_sqr(iK);
+    const df gs = df_mul(df_mul(df_mul(w, iK2), df_mul(irr, iK)), aW);
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+      const df KdT = dot3d(K, vt[d]);
+      const dfc g = dfc_scale(cbce, df_mul(gs, KdT));
+#pragma unroll
+      for (int n = 0; n < 4; n++) B.dG[d][n] = dfc_fma_re(B.dG[d][n], g, N[n]);
+    }
+    if (!c.planar) {
+      const dfc t1 = dfc_add(dfc_mul(kR, kR), dfcmk(df_mul_f(cb.re, 3.0f), df_mul_f(cb.im, 3.0f)));
+      const df iK5r = df_mul(df_mul(df_sqr(iK2), iK), irr);
+#pragma unroll
+      for (int d = 0; d < 2; d++) {
+        const df KdT = dot3d(K, vt[d]);
+        const df wo = df_mul(df_mul(w, outer[d]), iK5r);
+        const df kc = df_mul(KdT, cs[d]);
+        const dfc u = dfc_add(dfc_scale(t1, kc), dfc_scale(cb, df_neg(aK2)));
+        const dfc h = dfc_scale(dfc_mul(ce, u), wo);
+#pragma unroll
+        for (int n = 0; n < 4; n++) B.dH[d][n] = dfc_fma_re(B.dH[d][n], h, N[n]);
+        B.dF[d] = df_add(B.dF[d], df_mul(wo, df_sub(df_mul_f(kc, 3.0f), aK2)));
+      }
+    }
+  }
+  singb_add(B, A, 4, 1.0);
+}
+
+// triangle: K is constant along the ray; 3 x the shape functions in
+// double-float, the 1/3 applied in FP64
+static __device__ void sing_lit_setB_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
+  const Elem& E = c.E;
+  double K[3];
+  for (int d = 0; d < 3; d++) K[d] = E.cr[d][1] * cth + E.cr[d][2] * sth;
+  const double aK = norm3(K), iK = 1.0 / aK;
+  const df kv[2] = {df_from(dot3(K, c.vt[0]) * iK), df_from(dot3(K, c.vt[1]) * iK)};
+  const df daK = df_from(aK), iK2 = df_from(iK * iK);
+  const df hr = df_from(0.5 * (rm - GB_DEPS)), r0 = df_from(0.5 * (rm + GB_DEPS));
+  const df w0 = df_from(wth * 0.5 * (rm - GB_DEPS));
+  const df dzt = df_from(c.zt), det = df_from(c.et), dc = df_from(cth), ds = df_from(sth);
+  const df kr = df_from(c.k.x), ki = df_from(c.k.y);
+  const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
+  SingAccB B;
+  singb_zero(B);
+  for (int i = 0; i < GB_GHN; i++) {
+    const df rr = df_add(df_mul(hr, dfmk(c_tabd.xh[i].x, c_tabd.xh[i].y)), r0);
+    const df w = df_mul(w0, dfmk(c_tabd.wh[i].x, c_tabd.wh[i].y));
+    const df x = df_mul(daK, rr);
+    const dfc kR = dfcmk(df_mul(kr, x), df_mul(ki, x));
+    df sn, co;
+    df_sincos(kR.re, &sn, &co);
+    dfc ce = dfcmk(co, sn);
+    if (ki.hi != 0.0f) ce = dfc_scale(ce, df_exp(df_neg(kR.im)));
+    const dfc cb = dfcmk(df_add_f(df_neg(kR.im), -1.0f), kR.re);
+    const df z = df_add(dzt, df_mul(rr, dc)), e = df_add(det, df_mul(rr, ds));
+    const df se = df_mul(s3, e);
+    df N[3];
+    N[0] = df_add_f(df_mul_f(df_add(z, se), -2.5f), 1.0f);
+    N[1] = df_add_f(df_mul_f(z, 5.0f), 1.0f);
+    N[2] = df_add_f(df_mul_f(df_sub(z, se), -2.5f), 1.0f);
+    const dfc base = dfc_scale(dfc_mul(cb, ce), df_mul(df_mul(w, df_rcp(rr)), iK2));
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+      const dfc g = dfc_scale(base, kv[d]);
+#pragma unroll
+      for (int n = 0; n < 3; n++) B.dG[d][n] = dfc_fma_re(B.dG[d][n], g, N[n]);
+    }
+  }
+  singb_add(B, A, 3, 1.0 / 3.0);
+}
+
+// sing_item with set B in double-float
+static __device__ void sing_item_df(const SingCtx& c, int q, SingAcc& A) {
+  const int nA = c.nedge * 2 * GB_GHN;
+  if (q < nA || q >= 2 * nA) {
+    sing_item(c, q, A);
+    return;
+  }
+  const int qq = q - nA;
+  const int j = qq / (2 * GB_GHN), rem = qq % (2 * GB_GHN);
+  const int h = rem / GB_GHN, m = rem % GB_GHN;
+  double th, wth, rm;
+  sing_edge_theta(c, j, h, m, &th, &wth, &rm);
+  double sth, cth;
+  sincos(th, &sth, &cth);
+  if (c.E.quad) sing_bil_setB_df(c, cth, sth, rm, wth, A);
+  else sing_lit_setB_df(c, cth, sth, rm, wth, A);
+}
+
+template <bool DF>
 __global__ void __launch_bounds__(256) k_asm_singular(AsmArgs a) {
   __shared__ double red[51 * 8];
   const int row = blockIdx.x;
@@ -550,7 +725,10 @@ __global__ void __launch_bounds__(256) k_asm_singular(AsmArgs a) {
   SingAcc A;
   singacc_zero(A);
   int nit = sing_items(c, 1);
-  for (int q = threadIdx.x; q < nit; q += blockDim.x) sing_item(c, q, A);
+  for (int q = threadIdx.x; q < nit; q += blockDim.x) {
+    if (DF) sing_item_df(c, q, A);
+    else sing_item(c, q, A);
+  }
   static_assert(sizeof(SingAcc) == 51 * sizeof(double), "SingAcc layout");
   block_reduce<51>((double*)&A, red);
   if (threadIdx.x == 0) {
@@ -654,7 +832,8 @@ extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int p
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   if (redo) GB_CUDA(cudaFreeAsync(redo, st));
-  k_asm_singular<<<(unsigned)N, 256, 0, st>>>(a);
+  if (precision == 2) k_asm_singular<true><<<(unsigned)N, 256, 0, st>>>(a);
+  else k_asm_singular<false><<<(unsigned)N, 256, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   k_asm_rows<<<(unsigned)((N + 127) / 128), 128, 0, st>>>(a);
@@ -675,6 +854,12 @@ extern "C" int gbi_upload_tables_asm(const void* t) {
     g.x[i].y = (float)(d->xli[i] - (double)g.x[i].x);
     g.w[i].x = (float)d->wli[i];
     g.w[i].y = (float)(d->wli[i] - (double)g.w[i].x);
+  }
+  for (int i = 0; i < GB_GHN; i++) {
+    g.xh[i].x = (float)d->xhi[i];
+    g.xh[i].y = (float)(d->xhi[i] - (double)g.xh[i].x);
+    g.wh[i].x = (float)d->whi[i];
+    g.wh[i].y = (float)(d->whi[i] - (double)g.wh[i].x);
   }
   GB_CUDA(cudaMemcpyToSymbol(c_tabd, &g, sizeof(GbTablesD)));
   return 0;
