@@ -1177,50 +1177,113 @@ __global__ void k_gather_rows(const T* X, size_t ldx, int n, int nrhs, const int
   Y[(size_t)i * nrhs + c] = X[(size_t)perm[i] * ldx + c];
 }
 // One cooperative launch per triangular solve.  Row blocks of LU_NB rows are
-// owned by the CTAs (block q by CTA q mod gridDim, in increasing q); a block
-// folds in the contribution of every block it depends on as soon as that
-// block's flag is set, solves its diagonal block (warp per right-hand side,
-// substitution with shuffles), publishes its rows of Y and sets its flag.
-// All CTAs are co-resident (cooperative launch) and every block waits only
-// on blocks of smaller q, so the waits end; each wait is also bounded
+// owned by the CTAs (block q by CTA q mod gridDim, in increasing q).  A CTA
+// streams its block's strip of the factor, LU_NB x LU_NB tiles of block
+// pairs (q, j < q), into shared memory ahead of need (cp.async, two stages:
+// the tiles do not depend on the other blocks), and folds in tile j as soon
+// as block j's flag is set: thread (row i, quarter kq) keeps its partial sums
+// of the block's right-hand sides in registers across all tiles, reduced once
+// at the end.  Then the diagonal block is solved (warp per right-hand side,
+// substitution with shuffles), the block's rows of Y published and its flag
+// set.  All CTAs are co-resident (cooperative launch) and every block waits
+// only on blocks of smaller q, so the waits end; each wait is also bounded
 // (TRSV_SPIN_LIMIT polls): on time-out *err is raised and every CTA returns.
+// Tile layout in shared memory: row i of a tile is 512 B (FP32 complex) or
+// 1 KB (FP64 complex) of 16-byte chunks; chunk c of row i is stored at
+// position c ^ (i & 7), so that 32 lanes reading one chunk of 32 consecutive
+// rows hit every bank once per 8 rows.
 #define TRSV_SPIN_LIMIT (1 << 22)
+#define TRSV_THREADS 256
 __device__ __forceinline__ cplx ldcg_c(const cplx* p) { return cmk(__ldcg(&p->x), __ldcg(&p->y)); }
 __device__ __forceinline__ cplxf ldcg_c(const cplxf* p) { return cmkf(__ldcg(&p->x), __ldcg(&p->y)); }
 
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait0() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+template <class T>
+struct TrsvLayout {
+  static constexpr int CPC = 16 / (int)sizeof(T);      // complex per 16-byte chunk
+  static constexpr int CHUNKS = LU_NB / CPC;           // chunks per tile row
+  static constexpr int TILE = LU_NB * LU_NB;           // complex per tile
+  static constexpr int LDT = LU_NB + 1;                // transposed diagonal block
+  static constexpr size_t SMEM = (size_t)(2 * TILE + LU_NB * LDT + LU_NB + 2 * LU_NB * 8) * sizeof(T);
+};
+
+// stage tile (rows r0.., columns c0..) of the factor into buf (swizzled
+// chunks); rows >= rows_, columns >= cols_ are zero.  vec: 16-byte copies
+// are legal (aligned base and leading dimension)
+template <class T>
+__device__ __forceinline__ void trsv_stage(const T* LU, size_t lda, int r0, int rows_, int c0, int cols_, T* buf,
+                                           bool vec) {
+  typedef TrsvLayout<T> Ly;
+  for (int t = threadIdx.x; t < LU_NB * Ly::CHUNKS; t += blockDim.x) {
+    const int i = t / Ly::CHUNKS, c = t % Ly::CHUNKS;
+    T* dst = buf + i * LU_NB + ((c ^ (i & 7)) * Ly::CPC);
+    const int col = c * Ly::CPC;
+    const T* src = LU + (size_t)(r0 + i) * lda + c0 + col;
+    if (i < rows_ && col + Ly::CPC <= cols_ && vec) {
+      cp_async16(dst, src);
+    } else {
+#pragma unroll
+      for (int e = 0; e < Ly::CPC; e++) {
+        T v;
+        v.x = 0;
+        v.y = 0;
+        if (i < rows_ && col + e < cols_) v = src[e];
+        dst[e] = v;
+      }
+    }
+  }
+}
+
 template <class T, int UPPER>
-__global__ void __launch_bounds__(256) k_trsv_flags(const T* __restrict__ LU, size_t lda, int n, T* Y, int nrhs,
-                                                    int* flags, int* err) {
+__global__ void __launch_bounds__(TRSV_THREADS) k_trsv_flags(const T* __restrict__ LU, size_t lda, int n, T* Y,
+                                                             int nrhs, int* flags, int* err, int vec) {
   typedef typename RealOf<T>::type Rt;
+  typedef TrsvLayout<T> Ly;
   extern __shared__ __align__(16) unsigned char tfraw[];
-  constexpr int LD = LU_NB + 1;
-  T* sT = (T*)tfraw;             // diagonal block, transposed: sT[j * LD + i] = block[i][j]
-  T* sdinv = sT + LU_NB * LD;    // inverted diagonal (UPPER)
-  T* sx = sdinv + LU_NB;         // the block's right-hand sides, LU_NB x 8
+  T* sL = (T*)tfraw;                     // two tile stages
+  T* sT = sL + 2 * Ly::TILE;             // diagonal block, transposed: sT[j * LDT + i] = block[i][j]
+  T* sdinv = sT + LU_NB * Ly::LDT;       // inverted diagonal (UPPER)
+  T* sy = sdinv + LU_NB;                 // right-hand sides of the tile's column block, LU_NB x 8
+  T* sx = sy + LU_NB * 8;                // the block's right-hand sides, LU_NB x 8
   __shared__ int s_abort;
   const int nbk = (n + LU_NB - 1) / LU_NB;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int mi = threadIdx.x & (LU_NB - 1), kq = threadIdx.x / LU_NB;  // row, quarter of the chunks
+  constexpr int QCH = Ly::CHUNKS / 4;
   for (int q = blockIdx.x; q < nbk; q += gridDim.x) {
     const int b = UPPER ? nbk - 1 - q : q;
     const int r0 = b * LU_NB, rows = min(LU_NB, n - r0);
     for (int t = threadIdx.x; t < rows * nrhs; t += blockDim.x) sx[t] = Y[(size_t)r0 * nrhs + t];
     for (int t = threadIdx.x; t < rows * rows; t += blockDim.x) {
       const int i = t / rows, j = t % rows;
-      sT[j * LD + i] = LU[(size_t)(r0 + i) * lda + r0 + j];
+      sT[j * Ly::LDT + i] = LU[(size_t)(r0 + i) * lda + r0 + j];
     }
     if (threadIdx.x == 0) s_abort = 0;
-    __syncthreads();
-    if (UPPER) {
-      for (int j = threadIdx.x; j < rows; j += blockDim.x) {
-        T one;
-        one.x = 1; one.y = 0;
-        sdinv[j] = cdivc(one, sT[j * LD + j]);
-      }
-      __syncthreads();  // the diagonal solve may follow without a dependency round
+    Rt ar[8], ai[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) { ar[c] = 0; ai[c] = 0; }
+    // tiles of the blocks this one depends on, in the order their flags are set
+    if (q > 0) {
+      const int jb0 = UPPER ? nbk - 1 : 0;
+      trsv_stage<T>(LU, lda, r0, rows, jb0 * LU_NB, min(LU_NB, n - jb0 * LU_NB), sL, vec != 0);
     }
+    cp_async_commit();
     for (int jq = 0; jq < q; jq++) {
       const int jb = UPPER ? nbk - 1 - jq : jq;
       const int c0 = jb * LU_NB, cols = min(LU_NB, n - c0);
+      if (jq + 1 < q) {
+        const int jn = UPPER ? nbk - 2 - jq : jq + 1;
+        trsv_stage<T>(LU, lda, r0, rows, jn * LU_NB, min(LU_NB, n - jn * LU_NB), sL + ((jq + 1) & 1) * Ly::TILE,
+                      vec != 0);
+      }
+      cp_async_commit();
       if (threadIdx.x == 0) {
         int it = 0;
         while (*(volatile int*)(flags + jb) == 0) {
@@ -1230,40 +1293,69 @@ __global__ void __launch_bounds__(256) k_trsv_flags(const T* __restrict__ LU, si
         __threadfence();
       }
       __syncthreads();
-      if (s_abort) return;
-      for (int i = w; i < rows; i += nw) {  // sx[i] -= LU[r0+i][c0..] Y[c0..]
-        const T* a = LU + (size_t)(r0 + i) * lda + c0;
-        Rt sr[8], si[8];
+      if (s_abort) {
+        cp_async_wait0();
+        return;
+      }
+      for (int t = threadIdx.x; t < LU_NB * 8; t += blockDim.x) {
+        const int k = t >> 3, c = t & 7;
+        T v;
+        v.x = 0;
+        v.y = 0;
+        if (k < cols && c < nrhs) v = ldcg_c(Y + (size_t)(c0 + k) * nrhs + c);
+        sy[t] = v;
+      }
+      cp_async_wait1();
+      __syncthreads();
+      const T* tile = sL + (jq & 1) * Ly::TILE + mi * LU_NB;
+#pragma unroll 2
+      for (int cc = 0; cc < QCH; cc++) {
+        const int ch = kq * QCH + cc;
+        const T* src = tile + ((ch ^ (mi & 7)) * Ly::CPC);
 #pragma unroll
-        for (int c = 0; c < 8; c++) { sr[c] = 0; si[c] = 0; }
-        for (int k = lane; k < cols; k += 32) {
-          const T av = a[k];
+        for (int e = 0; e < Ly::CPC; e++) {
+          const T av = src[e];
+          const T* yv = sy + (ch * Ly::CPC + e) * 8;
 #pragma unroll
           for (int c = 0; c < 8; c++) {
             if (c < nrhs) {
-              const T yv = ldcg_c(Y + (size_t)(c0 + k) * nrhs + c);
-              sr[c] += av.x * yv.x - av.y * yv.y;
-              si[c] += av.x * yv.y + av.y * yv.x;
+              const T y = yv[c];
+              ar[c] += av.x * y.x - av.y * y.y;
+              ai[c] += av.x * y.y + av.y * y.x;
             }
           }
-        }
-#pragma unroll
-        for (int c = 0; c < 8; c++) {
-          if (c < nrhs) {
-            for (int o = 16; o > 0; o >>= 1) {
-              sr[c] += __shfl_down_sync(0xffffffffu, sr[c], o);
-              si[c] += __shfl_down_sync(0xffffffffu, si[c], o);
-            }
-          }
-        }
-        if (lane == 0) {
-#pragma unroll
-          for (int c = 0; c < 8; c++)
-            if (c < nrhs) { sx[i * nrhs + c].x -= sr[c]; sx[i * nrhs + c].y -= si[c]; }
         }
       }
-      __syncthreads();
+      __syncthreads();  // the stage and sy are rewritten next
     }
+    cp_async_wait0();
+    // reduce the four quarters (the tile stages are free now)
+    if (q > 0) {
+      T* red = sL;  // [4][LU_NB][8]
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+        T v;
+        v.x = ar[c];
+        v.y = ai[c];
+        red[(kq * LU_NB + mi) * 8 + c] = v;
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < rows * nrhs; t += blockDim.x) {
+        const int i = t / nrhs, c = t % nrhs;
+        T sum = red[i * 8 + c];
+        for (int u = 1; u < 4; u++) sum += red[(u * LU_NB + i) * 8 + c];
+        sx[t] -= sum;
+      }
+    }
+    __syncthreads();  // sT, sx complete (no tile loop when q == 0)
+    if (UPPER) {
+      for (int j = threadIdx.x; j < rows; j += blockDim.x) {
+        T one;
+        one.x = 1; one.y = 0;
+        sdinv[j] = cdivc(one, sT[j * Ly::LDT + j]);
+      }
+    }
+    __syncthreads();
     if (w < nrhs) {  // diagonal block: warp w solves right-hand side w
       const int i0 = lane, i1 = lane + 32;
       T x0, x1;
@@ -1276,7 +1368,7 @@ __global__ void __launch_bounds__(256) k_trsv_flags(const T* __restrict__ LU, si
           T xj;
           xj.x = __shfl_sync(0xffffffffu, v.x, j & 31);
           xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
-          const T* col = sT + j * LD;
+          const T* col = sT + j * Ly::LDT;
           if (i0 > j && i0 < rows) x0 -= col[i0] * xj;
           if (i1 > j && i1 < rows) x1 -= col[i1] * xj;
         }
@@ -1288,7 +1380,7 @@ __global__ void __launch_bounds__(256) k_trsv_flags(const T* __restrict__ LU, si
           xj.y = __shfl_sync(0xffffffffu, v.y, j & 31);
           xj = xj * sdinv[j];
           if (lane == (j & 31)) { if (j < 32) x0 = xj; else x1 = xj; }
-          const T* col = sT + j * LD;
+          const T* col = sT + j * Ly::LDT;
           if (i0 < j) x0 -= col[i0] * xj;
           if (i1 < j) x1 -= col[i1] * xj;
         }
@@ -1304,18 +1396,19 @@ __global__ void __launch_bounds__(256) k_trsv_flags(const T* __restrict__ LU, si
 
 template <class T, int UPPER>
 static int trsv_flags(const T* LU, size_t lda, int n, T* Y, int nrhs, int* flags, int* err, cudaStream_t st) {
-  const size_t sm = ((size_t)LU_NB * (LU_NB + 1) + LU_NB + (size_t)LU_NB * 8) * sizeof(T);
+  const size_t sm = TrsvLayout<T>::SMEM;
   GB_CUDA(cudaFuncSetAttribute(k_trsv_flags<T, UPPER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
   int dev = 0, nsm = 0, occ = 0;
   GB_CUDA(cudaGetDevice(&dev));
   GB_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_flags<T, UPPER>, 256, sm));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_flags<T, UPPER>, TRSV_THREADS, sm));
   const int nbk = (n + LU_NB - 1) / LU_NB;
   int grid = nsm * (occ > 0 ? occ : 1);
   if (grid > nbk) grid = nbk;
+  const int vec = ((((uintptr_t)LU) & 15) == 0 && ((lda * sizeof(T)) & 15) == 0) ? 1 : 0;
   GB_CUDA(cudaMemsetAsync(flags, 0, (size_t)nbk * sizeof(int), st));
-  void* args[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&Y, (void*)&nrhs, (void*)&flags, (void*)&err};
-  GB_CUDA(cudaLaunchCooperativeKernel((const void*)k_trsv_flags<T, UPPER>, dim3(grid), dim3(256), args, sm, st));
+  void* args[] = {(void*)&LU, (void*)&lda, (void*)&n, (void*)&Y, (void*)&nrhs, (void*)&flags, (void*)&err, (void*)&vec};
+  GB_CUDA(cudaLaunchCooperativeKernel((const void*)k_trsv_flags<T, UPPER>, dim3(grid), dim3(TRSV_THREADS), args, sm, st));
   gbi_count_launch();
   return 0;
 }

@@ -95,3 +95,41 @@ def test_getrf_factors(n, gb_build):
         assert ipiv.min() >= 0 and ipiv.max() < n and np.all(ipiv >= np.arange(n))
         err = _check_lu(Ad.cpu().numpy().astype(np.complex128), ipiv, A0)
         assert err <= tol, "%s n=%d: %g" % (f.__name__, n, err)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,nrhs,pad", [(1, 1, 0), (63, 4, 0), (300, 6, 1), (1000, 8, 0), (2113, 4, 1), (4096, 4, 0)])
+def test_lu_solve_multi(n, nrhs, pad, gb_build):
+    """gbi_csolve_multi / gbi_zsolve_multi (the triangular solves of the
+    refinement: gather by the pivot permutation, then one cooperative launch
+    per triangle) against numpy's solve with the same factors' matrix; pad
+    makes the leading dimension odd (no 16-byte copies of the factor)."""
+    import torch
+    L = _lib()
+    L.gbi_make_perm.argtypes = [vp, ci, vp, vp]
+    L.gbi_make_perm.restype = ci
+    for f in (L.gbi_csolve_multi, L.gbi_zsolve_multi):
+        f.argtypes = [vp, csz, ci, vp, vp, csz, ci, vp, vp]
+        f.restype = ci
+    rng = np.random.default_rng(n + nrhs)
+    A0 = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 4.0 * np.sqrt(n) * np.eye(n)
+    B0 = rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs))
+    ref = np.linalg.solve(A0, B0)
+    lda = n + pad
+    for dt, getrf, solve, tol in ((torch.complex64, L.gbi_cgetrf, L.gbi_csolve_multi, 1e-4),
+                                  (torch.complex128, L.gbi_zgetrf, L.gbi_zsolve_multi, 1e-12)):
+        Ap = np.zeros((n, lda), complex)
+        Ap[:, :n] = A0
+        Ad = torch.tensor(Ap, dtype=dt, device="cuda")
+        ip = torch.zeros(n, dtype=torch.int64, device="cuda")
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        assert getrf(Ad.data_ptr(), lda, n, ip.data_ptr(), info.data_ptr(), None) == 0, L.gb_last_error()
+        perm = torch.zeros(n, dtype=torch.int32, device="cuda")
+        assert L.gbi_make_perm(ip.data_ptr(), n, perm.data_ptr(), None) == 0
+        Xd = torch.tensor(B0, dtype=dt, device="cuda")
+        Yd = torch.zeros(n, nrhs, dtype=dt, device="cuda")
+        assert solve(Ad.data_ptr(), lda, n, perm.data_ptr(), Xd.data_ptr(), nrhs, nrhs, Yd.data_ptr(), None) == 0, \
+            L.gb_last_error()
+        torch.cuda.synchronize()
+        err = _rel(Yd.cpu().numpy().astype(np.complex128), ref)
+        assert err <= tol, "%s n=%d nrhs=%d: %g" % (solve.__name__, n, nrhs, err)
