@@ -56,6 +56,10 @@ int gbi_resid_finish(const cplx* b, const cplx* y, cplx* r, size_t n, double* nr
 int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cplx* X, int* iters, double* relres, cudaStream_t st);
 int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU32, size_t lda, int n, const int* perm,
                 cudaStream_t st);
+int gbi_ir_step_rbt(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU32, size_t lda, int n, const int* perm,
+                    const float* pu, const float* pv, cudaStream_t st);
+int gbi_rbt_matrix(cplxf* A, size_t lda, int n, const float* pu, const float* pv, cudaStream_t st);
+int gbi_cgetrf_nopiv(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
 int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st);
 int gbi_zsolve_multi(const cplx* LU, size_t lda, int n, const int* perm, const cplx* X, size_t ldx, int nrhs, cplx* Y,
                      cudaStream_t st);
@@ -170,6 +174,12 @@ struct gb_obj {
   int have_lu32;
   int ir_iters;
   double ir_relres;
+  // the FP32 factors are of U^T A V (random butterflies, no interchanges)
+  // when lu_rbt; lu_mode 1 forces tournament pivoting
+  float* rbt;        // [4][na]: U's two levels, then V's
+  int lu_rbt;
+  int lu_mode;
+  int lu_fallbacks;  // refactorisations with interchanges after a stalled refinement
   // boundary values per domain, [(Ne_d+1)][4][4] (U, dU) and [(Ne_d+1)][4][3] (E, dE, H, dH)
   cplx* bU[GB_MAXDOM];
   cplx* bdU[GB_MAXDOM];
@@ -211,7 +221,7 @@ extern "C" void gb_obj_destroy(gb_obj* o) {
     cudaFree(o->rowk[d]);
   }
   cudaFree(o->invA);
-  cudaFree(o->LU32); cudaFree(o->ipiv32); cudaFree(o->perm32);
+  cudaFree(o->LU32); cudaFree(o->ipiv32); cudaFree(o->perm32); cudaFree(o->rbt);
   for (int d = 0; d < GB_MAXDOM; d++) {
     cudaFree(o->bU[d]); cudaFree(o->bdU[d]); cudaFree(o->bE[d]); cudaFree(o->bdE[d]); cudaFree(o->bH[d]); cudaFree(o->bdH[d]);
   }
@@ -234,6 +244,7 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   o->invA = nullptr;
   o->have_invA = 0;
   o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
+  o->rbt = nullptr; o->lu_rbt = 0; o->lu_mode = 0; o->lu_fallbacks = 0;
   for (int d = 0; d < GB_MAXDOM; d++) o->bU[d] = o->bdU[d] = o->bE[d] = o->bdE[d] = o->bH[d] = o->bdH[d] = nullptr;
   o->Ui = o->dUi = o->Ui0 = o->dUi0 = o->Uip = nullptr;
   o->next = 0;
@@ -856,12 +867,33 @@ extern "C" int gb_field_bd(gb_obj* o, int type, int n, const int* did, const int
 // ------------------------------------------------------------------ mixed precision
 // Complex FP32 LU of A (tournament pivoting, tensor-core trailing updates);
 // A is built directly in FP32 into the factor's buffer.
-extern "C" int gb_factor_mixed(gb_obj* o) {
+// butterfly parameters e^{rho/10}, rho uniform in [-1/2, 1/2), from a fixed
+// seed (splitmix64), so that a factorisation is reproducible
+static int ensure_rbt(gb_obj* o) {
+  if (o->rbt) return 0;
+  const size_t n4 = 4 * o->na;
+  std::vector<float> h(n4);
+  uint64_t z = 0x243F6A8885A308D3ull ^ (uint64_t)o->na;
+  for (size_t i = 0; i < n4; i++) {
+    z += 0x9E3779B97F4A7C15ull;
+    uint64_t x = z;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    const double rho = (double)(x >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    h[i] = (float)exp(rho / 10.0);
+  }
+  if (dalloc((void**)&o->rbt, n4 * sizeof(float))) return -1;
+  GB_CUDA(cudaMemcpy(o->rbt, h.data(), n4 * sizeof(float), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+// A (complex FP32) from the resident G, H into LU32 and its factors:
+// randomised (U^T A V) without interchanges when rbt, else tournament
+// pivoting; *hinfo: the first zero pivot (0: none)
+static int factor32(gb_obj* o, bool rbt, int* hinfo) {
   size_t na = o->na;
   int* info = nullptr;
-  if (!o->LU32 && dalloc((void**)&o->LU32, na * na * sizeof(cplxf))) return -1;
-  if (!o->ipiv32 && dalloc((void**)&o->ipiv32, na * sizeof(int64_t))) return -1;
-  if (!o->perm32 && dalloc((void**)&o->perm32, na * sizeof(int))) return -1;
   if (dalloc((void**)&info, sizeof(int))) return -1;
   int rc = 0;
   if (cudaMemsetAsync(o->LU32, 0, na * na * sizeof(cplxf), o->st) != cudaSuccess) { gbi_set_error("memset"); rc = -1; }
@@ -872,18 +904,53 @@ extern "C" int gb_factor_mixed(gb_obj* o) {
                               o->nrows[d], base, na, o->LU32, o->st);
     base += 4 * (size_t)o->nrows[d];
   }
-  if (!rc) rc = gbi_cgetrf(o->LU32, na, (int)na, o->ipiv32, info, o->st);
+  if (rbt) {
+    if (!rc) rc = gbi_rbt_matrix(o->LU32, na, (int)na, o->rbt, o->rbt + 2 * na, o->st);
+    if (!rc) rc = gbi_cgetrf_nopiv(o->LU32, na, (int)na, o->ipiv32, info, o->st);
+  } else if (!rc) {
+    rc = gbi_cgetrf(o->LU32, na, (int)na, o->ipiv32, info, o->st);
+  }
   if (!rc) rc = gbi_make_perm(o->ipiv32, (int)na, o->perm32, o->st);
-  int hinfo = 0;
-  if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
+  *hinfo = 0;
+  if (!rc && (cudaMemcpyAsync(hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
               cudaStreamSynchronize(o->st) != cudaSuccess)) {
     gbi_set_error("gb_factor_mixed: %s", cudaGetErrorString(cudaGetLastError()));
     rc = -1;
   }
-  if (!rc && hinfo) { gbi_set_error("gb_factor_mixed: FP32 factor singular (info=%d)", hinfo); rc = -1; }
   cudaFree(info);
+  if (!rc) o->lu_rbt = rbt ? 1 : 0;
+  return rc;
+}
+
+extern "C" int gb_factor_mixed(gb_obj* o) {
+  size_t na = o->na;
+  if (!o->LU32 && dalloc((void**)&o->LU32, na * na * sizeof(cplxf))) return -1;
+  if (!o->ipiv32 && dalloc((void**)&o->ipiv32, na * sizeof(int64_t))) return -1;
+  if (!o->perm32 && dalloc((void**)&o->perm32, na * sizeof(int))) return -1;
+  const bool rbt = o->lu_mode == 0 && na % 4 == 0;
+  if (rbt && ensure_rbt(o)) return -1;
+  o->have_lu32 = 0;
+  int hinfo = 0;
+  int rc = factor32(o, rbt, &hinfo);
+  if (!rc && rbt && hinfo) {  // a zero pivot without interchanges: factorise with them
+    o->lu_fallbacks++;
+    rc = factor32(o, false, &hinfo);
+  }
+  if (!rc && hinfo) { gbi_set_error("gb_factor_mixed: FP32 factor singular (info=%d)", hinfo); rc = -1; }
   if (!rc) { o->have_lu32 = 1; o->have_invA = 0; }
   return rc;
+}
+
+extern "C" int gb_set_lu_pivoting(gb_obj* o, int mode) {
+  if (mode != 0 && mode != 1) { gbi_set_error("gb_set_lu_pivoting: mode %d not 0 or 1", mode); return -1; }
+  o->lu_mode = mode;
+  return 0;
+}
+
+extern "C" int gb_lu_info(gb_obj* o, int* rbt, int* fallbacks) {
+  *rbt = o->lu_rbt;
+  *fallbacks = o->lu_fallbacks;
+  return 0;
 }
 
 // y = A x in FP64 from G and H (PQ: scratch of 8 N_max complex)
@@ -918,19 +985,36 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
   if (cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess ||
       cudaMemcpyAsync(r, B, na * sizeof(cplx), cudaMemcpyDeviceToDevice, o->st) != cudaSuccess)
     rc = -1;
-  double h[2] = {0.0, 1.0}, rel = 1.0;
-  int it = 0;
-  for (; !rc && it < 31; it++) {
+  double h[2] = {0.0, 1.0}, rel = 1.0, prev = 1.0;
+  int it = 0, since = 0;  // corrections, corrections with the current factors
+  for (; !rc && it < 31; it++, since++) {
     if (it > 0) {
       rc = apply_A(o, X, PQ, y);
       if (!rc) rc = gbi_resid_finish(B, y, r, na, nrm, o->st);
       if (rc) break;
       if (cudaMemcpyAsync(h, nrm, 2 * sizeof(double), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
           cudaStreamSynchronize(o->st) != cudaSuccess) { rc = -1; break; }
+      prev = rel;
       rel = (h[1] > 0.0) ? sqrt(h[0] / h[1]) : 0.0;
       if (rel <= 1e-13) break;
+      // factors without interchanges that do not contract the residual by
+      // 10x per correction (far from the rounding floor), or not within 12
+      // corrections: factorise again with tournament pivoting and go on
+      // from the current x (from x = 0 if it diverged)
+      if (o->lu_rbt && ((since >= 2 && rel > 0.1 * prev && rel > 1e-11) || since >= 12 || !(rel < 1e3))) {
+        int hinfo = 0;
+        o->lu_fallbacks++;
+        rc = factor32(o, false, &hinfo);
+        if (!rc && hinfo) { gbi_set_error("ir_solve: FP32 factor singular (info=%d)", hinfo); rc = -1; }
+        if (rc) break;
+        if (!(rel < 1.0) &&
+            (cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess ||
+             cudaMemcpyAsync(r, B, na * sizeof(cplx), cudaMemcpyDeviceToDevice, o->st) != cudaSuccess)) { rc = -1; break; }
+        since = 0;
+      }
     }
-    rc = gbi_ir_step(X, r, d, d2, o->LU32, na, (int)na, o->perm32, o->st);
+    rc = o->lu_rbt ? gbi_ir_step_rbt(X, r, d, d2, o->LU32, na, (int)na, o->perm32, o->rbt, o->rbt + 2 * na, o->st)
+                   : gbi_ir_step(X, r, d, d2, o->LU32, na, (int)na, o->perm32, o->st);
   }
   o->ir_iters = it;
   o->ir_relres = rel;

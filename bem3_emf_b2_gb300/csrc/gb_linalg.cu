@@ -801,9 +801,21 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_trsm_right(T* A, size_t lda, 
 // sequence across the full row width, as LAPACK's); info (device int)
 // receives LAPACK's info (0: success).  gemm(M, N, K, A, lda, B, ldb, C, ldc,
 // st) performs C -= A B.
+__global__ void k_iota_i64(int64_t* v, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = i;
+}
+
+// pivot == false: no row interchanges at all (ipiv = identity): for a matrix
+// randomised by butterfly transforms (k_rbt_matrix), where the refinement
+// that follows checks the factors
 template <class T, class GEMM>
-static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st, GEMM gemm) {
+static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st, GEMM gemm, bool pivot = true) {
   if (n <= 0) return 0;
+  if (!pivot) {
+    k_iota_i64<<<(n + 255) / 256, 256, 0, st>>>(ipiv, n);
+    gbi_count_launch();
+  }
   const int nsets0 = (n + TS_ROWS - 1) / TS_ROWS;
   int* cand = nullptr;
   GB_CUDA(cudaMallocAsync((void**)&cand, sizeof(int) * (size_t)2 * nsets0 * LU_NB, st));
@@ -822,19 +834,21 @@ static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStre
     int nsets = (n - k + TS_ROWS - 1) / TS_ROWS;
     int* cin = cand;
     int* cout = cand + (size_t)nsets0 * LU_NB;
-    k_tslu_leaf<T><<<nsets, TS_THREADS, 0, st>>>(A, lda, n, k, nb, cin, ipiv);
-    gbi_count_launch();
-    while (nsets > 1) {
-      int nout = (nsets + TS_ARITY - 1) / TS_ARITY;
-      k_tslu_merge<T><<<nout, TS_THREADS, 0, st>>>(A, lda, k, nb, cin, nsets, cout, ipiv);
+    if (pivot) {
+      k_tslu_leaf<T><<<nsets, TS_THREADS, 0, st>>>(A, lda, n, k, nb, cin, ipiv);
       gbi_count_launch();
-      int* t = cin;
-      cin = cout;
-      cout = t;
-      nsets = nout;
+      while (nsets > 1) {
+        int nout = (nsets + TS_ARITY - 1) / TS_ARITY;
+        k_tslu_merge<T><<<nout, TS_THREADS, 0, st>>>(A, lda, k, nb, cin, nsets, cout, ipiv);
+        gbi_count_launch();
+        int* t = cin;
+        cin = cout;
+        cout = t;
+        nsets = nout;
+      }
+      k_laswp_rows<T><<<(n + 255) / 256, 256, 0, st>>>(A, lda, n, k, nb, ipiv);
+      gbi_count_launch();
     }
-    k_laswp_rows<T><<<(n + 255) / 256, 256, 0, st>>>(A, lda, n, k, nb, ipiv);
-    gbi_count_launch();
     k_diag_lu<T><<<1, PANEL_THREADS, sm_diag, st>>>(A, lda, k, nb, info);
     gbi_count_launch();
     if (kend < n) {
@@ -1054,7 +1068,15 @@ extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda,
 // Complex-FP32 LU: the trailing updates on the tensor cores (split TF32, three
 // passes: FP32-level products), scratch and the time-out flag shared by all
 // panels; the flag is read back once at the end.
+static int cgetrf_tc(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st, bool pivot);
 extern "C" int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st) {
+  return cgetrf_tc(A, lda, n, ipiv, info, st, true);
+}
+// as gbi_cgetrf without row interchanges (ipiv = identity)
+extern "C" int gbi_cgetrf_nopiv(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st) {
+  return cgetrf_tc(A, lda, n, ipiv, info, st, false);
+}
+static int cgetrf_tc(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st, bool pivot) {
   if (n <= 0) return 0;
   float* scratch = nullptr;
   int* err = nullptr;
@@ -1064,7 +1086,7 @@ extern "C" int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info,
   GB_CUDA(cudaMemsetAsync(err, 0, 4, st));
   auto tc = [scratch, err](int M, int N, int K, const cplxf* a, size_t la, const cplxf* b, size_t lb, cplxf* c, size_t lc,
                            cudaStream_t s) { return gbi_tc_cgemm_sub(M, N, K, a, la, b, lb, c, lc, 3, scratch, err, s); };
-  int rc = lu_factor<cplxf>(A, lda, n, ipiv, info, st, tc);
+  int rc = lu_factor<cplxf>(A, lda, n, ipiv, info, st, tc, pivot);
   int h = 0;
   if (!rc && (cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
               cudaStreamSynchronize(st) != cudaSuccess)) {
@@ -1130,6 +1152,133 @@ __global__ void k_c128_to_c64_scaled(const cplx* r, cplxf* d, int n) {
 template <class T>
 static int lu_solve_multi(const T* LU, size_t lda, int n, const int* perm, const T* X, size_t ldx, int nrhs, T* Y,
                           cudaStream_t st);
+// ---- random butterfly transforms (RBT)
+// Parker's recursive butterflies of depth 2 as used to avoid pivoting
+// (D. S. Parker, UCLA tech. report CSD-950023, 1995; M. Baboulin, J.
+// Dongarra, J. Herrmann, S. Tomov, ACM TOMS 39 (2013) 16): A_r = U^T A V with
+// U, V = diag(B', B'') B, B = [R0 R1; R0 -R1] / sqrt 2 of size n (R0, R1
+// random diagonal, entries e^{rho/10}, rho uniform in [-1/2, 1/2)), B', B''
+// the same of size n/2.  A_r is factorised without interchanges; then
+// A^-1 b = V A_r^-1 U^T b.  With q = n/4, indices i + a q (a = 0..3) mix only
+// among themselves.  Parameters p[2][n] per side, level 1 (pairs a, a+2) then
+// level 2 (pairs (0,1), (2,3)): for the pair (a, b) the diagonal entries are
+// p[i + a q] and p[i + b q].
+//   transposed butterfly (U^T from the left, V from the right, in the order
+//   level 2 then level 1): x_a' = r_a (x_a + x_b) / sqrt 2,
+//                          x_b' = r_b (x_a - x_b) / sqrt 2
+//   butterfly (V y, level 1 then level 2): x_a' = (r_a x_a + r_b x_b) / sqrt 2,
+//                                          x_b' = (r_a x_a - r_b x_b) / sqrt 2
+template <class C, class R>
+__device__ __forceinline__ void bfly_t(C& xa, C& xb, R ra, R rb) {
+  const R s = (R)0.70710678118654752440;
+  const C u = xa + xb, v = xa - xb;
+  xa = u * (ra * s);
+  xb = v * (rb * s);
+}
+template <class C, class R>
+__device__ __forceinline__ void bfly_f(C& xa, C& xb, R ra, R rb) {
+  const R s = (R)0.70710678118654752440;
+  const C u = xa * (ra * s), v = xb * (rb * s);
+  xa = u + v;
+  xb = u - v;
+}
+template <class C, class R>
+__device__ __forceinline__ void rbt4_t(C x[4], const float* p, int i, int q) {  // U^T x (or the columns of A V)
+  const float* p1 = p;
+  const float* p2 = p + 4 * (size_t)q;
+  bfly_t<C, R>(x[0], x[1], (R)p2[i], (R)p2[i + q]);
+  bfly_t<C, R>(x[2], x[3], (R)p2[i + 2 * q], (R)p2[i + 3 * q]);
+  bfly_t<C, R>(x[0], x[2], (R)p1[i], (R)p1[i + 2 * q]);
+  bfly_t<C, R>(x[1], x[3], (R)p1[i + q], (R)p1[i + 3 * q]);
+}
+template <class C, class R>
+__device__ __forceinline__ void rbt4_f(C x[4], const float* p, int i, int q) {  // V y
+  const float* p1 = p;
+  const float* p2 = p + 4 * (size_t)q;
+  bfly_f<C, R>(x[0], x[2], (R)p1[i], (R)p1[i + 2 * q]);
+  bfly_f<C, R>(x[1], x[3], (R)p1[i + q], (R)p1[i + 3 * q]);
+  bfly_f<C, R>(x[0], x[1], (R)p2[i], (R)p2[i + q]);
+  bfly_f<C, R>(x[2], x[3], (R)p2[i + 2 * q], (R)p2[i + 3 * q]);
+}
+
+// A <- U^T A V in place (n divisible by 4); thread per index pair (i, j) of
+// [0, n/4)^2: the 16 entries A[i + a q][j + b q]
+__global__ void k_rbt_matrix(cplxf* A, size_t lda, int n, const float* pu, const float* pv) {
+  const int q = n / 4;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)q * q) return;
+  const int i = (int)(t / q), j = (int)(t % q);
+  cplxf x[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) x[a][b] = A[(size_t)(i + a * q) * lda + j + b * q];
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    cplxf c[4] = {x[0][b], x[1][b], x[2][b], x[3][b]};
+    rbt4_t<cplxf, float>(c, pu, i, q);
+#pragma unroll
+    for (int a = 0; a < 4; a++) x[a][b] = c[a];
+  }
+#pragma unroll
+  for (int a = 0; a < 4; a++) rbt4_t<cplxf, float>(x[a], pv, j, q);
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) A[(size_t)(i + a * q) * lda + j + b * q] = x[a][b];
+}
+// d = U^T r in FP64, rounded to FP32
+__global__ void k_rbt_ut(const cplx* r, cplxf* d, int n, const float* pu) {
+  const int q = n / 4;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= q) return;
+  cplx x[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) x[a] = r[i + a * q];
+  rbt4_t<cplx, double>(x, pu, i, q);
+#pragma unroll
+  for (int a = 0; a < 4; a++) d[i + a * q] = cmkf((float)x[a].x, (float)x[a].y);
+}
+// x += V y in FP64
+__global__ void k_rbt_axpy_v(cplx* x, const cplxf* y, int n, const float* pv) {
+  const int q = n / 4;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= q) return;
+  cplx v[4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) v[a] = cmk((double)y[i + a * q].x, (double)y[i + a * q].y);
+  rbt4_f<cplx, double>(v, pv, i, q);
+#pragma unroll
+  for (int a = 0; a < 4; a++) x[i + a * q] += v[a];
+}
+extern "C" int gbi_rbt_matrix(cplxf* A, size_t lda, int n, const float* pu, const float* pv, cudaStream_t st) {
+  if (n % 4) { gbi_set_error("gbi_rbt_matrix: n = %d not divisible by 4", n); return -1; }
+  const size_t qq = (size_t)(n / 4) * (n / 4);
+  if (qq == 0) return 0;
+  k_rbt_matrix<<<(unsigned)((qq + 255) / 256), 256, 0, st>>>(A, lda, n, pu, pv);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+template <class T>
+static int lu_solve_multi(const T* LU, size_t lda, int n, const int* perm, const T* X, size_t ldx, int nrhs, T* Y,
+                          cudaStream_t st);
+// x += V LU32^-1 U^T r for the factors of the randomised matrix (no
+// interchanges; perm = identity)
+extern "C" int gbi_ir_step_rbt(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU32, size_t lda, int n,
+                               const int* perm, const float* pu, const float* pv, cudaStream_t st) {
+  const int q = n / 4;
+  k_rbt_ut<<<(q + 255) / 256, 256, 0, st>>>(r, d, n, pu);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  if (lu_solve_multi<cplxf>(LU32, lda, n, perm, d, 1, 1, d2, st)) return -1;
+  k_rbt_axpy_v<<<(q + 255) / 256, 256, 0, st>>>(x, d2, n, pv);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
 // x += LU32^-1 P r (r converted to FP32; d, d2: n-element FP32 work vectors)
 extern "C" int gbi_ir_step(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU32, size_t lda, int n,
                            const int* perm, cudaStream_t st) {

@@ -171,6 +171,17 @@ int gb_assemble_domain_noalloc(const double *cr, const double *cw, const int *et
  * (precision 1) and mixed; form 3: FP64 assembly and mixed. */
 int gb_factor_mixed(gb_obj *o);
 int gb_ir_info(gb_obj *o, int *iters, double *relres);
+/* Row interchanges of the FP32 factorisation.  mode 0 (default): A is
+ * randomised by two-sided recursive butterfly transforms of depth 2
+ * (U^T A V, random diagonal entries e^{rho/10}, fixed seed; Parker 1995,
+ * Baboulin et al. 2013) and factorised without interchanges, when na is
+ * divisible by 4; a zero pivot, or a refinement that does not contract the
+ * residual 10x per correction, makes the object factorise again with
+ * tournament pivoting.  mode 1: tournament pivoting always.
+ * gb_lu_info: rbt = 1 if the current factors are of the randomised matrix;
+ * fallbacks = such refactorisations so far. */
+int gb_set_lu_pivoting(gb_obj *o, int mode);
+int gb_lu_info(gb_obj *o, int *rbt, int *fallbacks);
 int gb_scene_step(gb_obj *o, int form, int type);
 
 /* Dense complex FP64 LU solve of a host system: A (n x n, row-major) X = B

@@ -133,3 +133,65 @@ def test_lu_solve_multi(n, nrhs, pad, gb_build):
         torch.cuda.synchronize()
         err = _rel(Yd.cpu().numpy().astype(np.complex128), ref)
         assert err <= tol, "%s n=%d nrhs=%d: %g" % (solve.__name__, n, nrhs, err)
+
+
+def _butterfly_t(p, n):
+    """dense matrix of the depth-2 transposed recursive butterfly U^T for the
+    parameters p[2][n] (level 1, level 2), as defined for gbi_rbt_matrix"""
+    q = n // 4
+    s = 1.0 / np.sqrt(2.0)
+    p1, p2 = p[:n], p[n:]
+
+    def level(pairs, pp):
+        M = np.zeros((n, n))
+        for i in range(q):
+            for a, b in pairs:
+                ia, ib = i + a * q, i + b * q
+                M[ia, ia] = M[ia, ib] = pp[ia] * s
+                M[ib, ia] = pp[ib] * s
+                M[ib, ib] = -pp[ib] * s
+        return M
+    L2 = level([(0, 1), (2, 3)], p2)
+    L1 = level([(0, 2), (1, 3)], p1)
+    return L1 @ L2  # level 2 first
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [4, 64, 512])
+def test_rbt_transform_matches_dense_model(n, gb_build):
+    """gbi_rbt_matrix: A <- U^T A V with U^T, V^T the depth-2 transposed
+    butterflies of the parameters (the dense model above); the unpivoted LU
+    of the randomised matrix solves the original system as x = V A_r^-1 U^T b."""
+    import torch
+    L = _lib()
+    L.gbi_rbt_matrix.argtypes = [vp, csz, ci, vp, vp, vp]
+    L.gbi_rbt_matrix.restype = ci
+    L.gbi_cgetrf_nopiv.argtypes = [vp, csz, ci, vp, vp, vp]
+    L.gbi_cgetrf_nopiv.restype = ci
+    rng = np.random.default_rng(n)
+    A0 = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))).astype(np.complex64)
+    pu = np.exp(rng.uniform(-0.5, 0.5, 2 * n) / 10).astype(np.float32)
+    pv = np.exp(rng.uniform(-0.5, 0.5, 2 * n) / 10).astype(np.float32)
+    Ut = _butterfly_t(pu.astype(float), n)
+    V = _butterfly_t(pv.astype(float), n).T
+    ref = Ut @ A0.astype(np.complex128) @ V
+    Ad = torch.tensor(A0, device="cuda")
+    pud = torch.tensor(pu, device="cuda")
+    pvd = torch.tensor(pv, device="cuda")
+    assert L.gbi_rbt_matrix(Ad.data_ptr(), n, n, pud.data_ptr(), pvd.data_ptr(), None) == 0, L.gb_last_error()
+    torch.cuda.synchronize()
+    Ar = Ad.cpu().numpy().astype(np.complex128)
+    assert _rel(Ar, ref) <= 2e-6
+    ip = torch.zeros(n, dtype=torch.int64, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert L.gbi_cgetrf_nopiv(Ad.data_ptr(), n, n, ip.data_ptr(), info.data_ptr(), None) == 0, L.gb_last_error()
+    torch.cuda.synchronize()
+    assert int(info.item()) == 0
+    assert np.array_equal(ip.cpu().numpy(), np.arange(n))
+    LU = Ad.cpu().numpy().astype(np.complex128)
+    Lm = np.tril(LU, -1) + np.eye(n)
+    U = np.triu(LU)
+    assert _rel(Lm @ U, Ar) <= 1e-4
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    x = V @ np.linalg.solve(Lm @ U, Ut @ b)
+    assert _rel(A0.astype(np.complex128) @ x, b) <= 1e-3 * max(1.0, np.linalg.cond(A0) / 1e3)

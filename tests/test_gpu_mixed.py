@@ -115,3 +115,39 @@ def test_double_float_assembly_matches_fp64(case, gb_build, tmp_path):
     sc.close()
     d = np.linalg.norm(np.concatenate([F1 - F3, N1 - N3])) / np.linalg.norm(np.concatenate([F3, N3]))
     assert d <= 1e-11, "double-float vs FP64 assembly, force/torque %g" % d
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["sphere2", "cone_mix", "cone_tri", "cube1"])
+def test_butterfly_lu_matches_tournament_lu(case, gb_build, tmp_path):
+    """The chosen form factorises the randomised matrix U^T A V without
+    interchanges (gb_set_lu_pivoting 0, the default); with tournament
+    pivoting (mode 1) the same refinement must give the same force and torque
+    to the refinement's accuracy, and the randomised factors must have been
+    used without a fallback on these scenes."""
+    import ctypes
+    from bem3_emf_b2_gb300 import Scene, lib
+    L = lib()
+    vp, ci = ctypes.c_void_p, ctypes.c_int
+    L.gb_set_lu_pivoting.argtypes = [vp, ci]
+    L.gb_set_lu_pivoting.restype = ci
+    L.gb_lu_info.argtypes = [vp, vp, vp]
+    L.gb_lu_info.restype = ci
+    meta, _ = load_case(case)
+    wd = str(tmp_path)
+    write_inputs(meta, wd)
+    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+    o = sc.obj()
+    F0, N0 = sc.step(form=1)
+    rbt, fb = ctypes.c_int(), ctypes.c_int()
+    L.gb_lu_info(o, ctypes.byref(rbt), ctypes.byref(fb))
+    it0, rr0 = sc.ir_info()
+    assert rbt.value == 1 and fb.value == 0, (rbt.value, fb.value)
+    assert rr0 <= 1e-13
+    assert L.gb_set_lu_pivoting(o, 1) == 0
+    F1, N1 = sc.step(form=1)
+    L.gb_lu_info(o, ctypes.byref(rbt), ctypes.byref(fb))
+    assert rbt.value == 0
+    sc.close()
+    d = np.linalg.norm(np.concatenate([F1 - F0, N1 - N0])) / np.linalg.norm(np.concatenate([F0, N0]))
+    assert d <= 1e-11, "butterfly vs tournament LU, force/torque %g" % d
