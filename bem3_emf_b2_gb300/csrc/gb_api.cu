@@ -60,6 +60,7 @@ int gbi_ir_step_rbt(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU
                     const float* pu, const float* pv, cudaStream_t st);
 int gbi_rbt_matrix(cplxf* A, size_t lda, int n, const float* pu, const float* pv, cudaStream_t st);
 int gbi_cgetrf_nopiv(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
+void gbi_rbt_params(int n, float* h);
 int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st);
 int gbi_zsolve_multi(const cplx* LU, size_t lda, int n, const int* perm, const cplx* X, size_t ldx, int nrhs, cplx* Y,
                      cudaStream_t st);
@@ -867,22 +868,12 @@ extern "C" int gb_field_bd(gb_obj* o, int type, int n, const int* did, const int
 // ------------------------------------------------------------------ mixed precision
 // Complex FP32 LU of A (tournament pivoting, tensor-core trailing updates);
 // A is built directly in FP32 into the factor's buffer.
-// butterfly parameters e^{rho/10}, rho uniform in [-1/2, 1/2), from a fixed
-// seed (splitmix64), so that a factorisation is reproducible
+// butterfly parameters of the object's order (gbi_rbt_params)
 static int ensure_rbt(gb_obj* o) {
   if (o->rbt) return 0;
   const size_t n4 = 4 * o->na;
   std::vector<float> h(n4);
-  uint64_t z = 0x243F6A8885A308D3ull ^ (uint64_t)o->na;
-  for (size_t i = 0; i < n4; i++) {
-    z += 0x9E3779B97F4A7C15ull;
-    uint64_t x = z;
-    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
-    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
-    x ^= x >> 31;
-    const double rho = (double)(x >> 11) * (1.0 / 9007199254740992.0) - 0.5;
-    h[i] = (float)exp(rho / 10.0);
-  }
+  gbi_rbt_params((int)o->na, h.data());
   if (dalloc((void**)&o->rbt, n4 * sizeof(float))) return -1;
   GB_CUDA(cudaMemcpy(o->rbt, h.data(), n4 * sizeof(float), cudaMemcpyHostToDevice));
   return 0;

@@ -33,6 +33,7 @@
 // two blocked triangular solves whose updates use the same GEMM kernel.
 #include "gb_common.cuh"
 #include "gb_internal.h"
+#include <vector>
 
 #define LU_NB 64
 #define LU_NBO 256  // outer block: the trailing update's K
@@ -1227,29 +1228,51 @@ __global__ void k_rbt_matrix(cplxf* A, size_t lda, int n, const float* pu, const
 #pragma unroll
     for (int b = 0; b < 4; b++) A[(size_t)(i + a * q) * lda + j + b * q] = x[a][b];
 }
-// d = U^T r in FP64, rounded to FP32
-__global__ void k_rbt_ut(const cplx* r, cplxf* d, int n, const float* pu) {
+// d = U^T r in FP64, rounded to FP32 (n x nrhs, packed rows)
+__global__ void k_rbt_ut(const cplx* r, cplxf* d, int n, int nrhs, const float* pu) {
   const int q = n / 4;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= q) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= q * nrhs) return;
+  const int i = t / nrhs, c = t % nrhs;
   cplx x[4];
 #pragma unroll
-  for (int a = 0; a < 4; a++) x[a] = r[i + a * q];
+  for (int a = 0; a < 4; a++) x[a] = r[(size_t)(i + a * q) * nrhs + c];
   rbt4_t<cplx, double>(x, pu, i, q);
 #pragma unroll
-  for (int a = 0; a < 4; a++) d[i + a * q] = cmkf((float)x[a].x, (float)x[a].y);
+  for (int a = 0; a < 4; a++) d[(size_t)(i + a * q) * nrhs + c] = cmkf((float)x[a].x, (float)x[a].y);
 }
-// x += V y in FP64
-__global__ void k_rbt_axpy_v(cplx* x, const cplxf* y, int n, const float* pv) {
+// x += V y in FP64 (n x nrhs, packed rows)
+__global__ void k_rbt_axpy_v(cplx* x, const cplxf* y, int n, int nrhs, const float* pv) {
   const int q = n / 4;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= q) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= q * nrhs) return;
+  const int i = t / nrhs, c = t % nrhs;
   cplx v[4];
 #pragma unroll
-  for (int a = 0; a < 4; a++) v[a] = cmk((double)y[i + a * q].x, (double)y[i + a * q].y);
+  for (int a = 0; a < 4; a++) {
+    const cplxf w = y[(size_t)(i + a * q) * nrhs + c];
+    v[a] = cmk((double)w.x, (double)w.y);
+  }
   rbt4_f<cplx, double>(v, pv, i, q);
 #pragma unroll
-  for (int a = 0; a < 4; a++) x[i + a * q] += v[a];
+  for (int a = 0; a < 4; a++) x[(size_t)(i + a * q) * nrhs + c] += v[a];
+}
+
+// butterfly parameters for order n: 4 n floats (U's two levels, then V's),
+// e^{rho/10} with rho uniform in [-1/2, 1/2) from splitmix64 with a fixed
+// seed, so that a factorisation is reproducible
+extern "C" void gbi_rbt_params(int n, float* h) {
+  const size_t n4 = 4 * (size_t)n;
+  uint64_t z = 0x243F6A8885A308D3ull ^ (uint64_t)n;
+  for (size_t i = 0; i < n4; i++) {
+    z += 0x9E3779B97F4A7C15ull;
+    uint64_t x = z;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    x ^= x >> 31;
+    const double rho = (double)(x >> 11) * (1.0 / 9007199254740992.0) - 0.5;
+    h[i] = (float)exp(rho / 10.0);
+  }
 }
 extern "C" int gbi_rbt_matrix(cplxf* A, size_t lda, int n, const float* pu, const float* pv, cudaStream_t st) {
   if (n % 4) { gbi_set_error("gbi_rbt_matrix: n = %d not divisible by 4", n); return -1; }
@@ -1269,11 +1292,11 @@ static int lu_solve_multi(const T* LU, size_t lda, int n, const int* perm, const
 extern "C" int gbi_ir_step_rbt(cplx* x, const cplx* r, cplxf* d, cplxf* d2, const cplxf* LU32, size_t lda, int n,
                                const int* perm, const float* pu, const float* pv, cudaStream_t st) {
   const int q = n / 4;
-  k_rbt_ut<<<(q + 255) / 256, 256, 0, st>>>(r, d, n, pu);
+  k_rbt_ut<<<(q + 255) / 256, 256, 0, st>>>(r, d, n, 1, pu);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   if (lu_solve_multi<cplxf>(LU32, lda, n, perm, d, 1, 1, d2, st)) return -1;
-  k_rbt_axpy_v<<<(q + 255) / 256, 256, 0, st>>>(x, d2, n, pv);
+  k_rbt_axpy_v<<<(q + 255) / 256, 256, 0, st>>>(x, d2, n, 1, pv);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
@@ -1631,6 +1654,34 @@ __global__ void k_resid_multi(const cplx* __restrict__ A, int n, const cplx* __r
     }
 }
 
+// FP32 factors of A (n x n, FP64 input) into A32: randomised without
+// interchanges (rbt: butterfly parameters on the device) or with tournament
+// pivoting; *hinfo: first zero pivot (0: none)
+static int factor32_dense(const cplx* A, int n, cplxf* A32, int64_t* ipiv, int* perm, int* info, const float* rbt,
+                          int* hinfo, cudaStream_t st) {
+  const size_t nn = (size_t)n * n;
+  int rc = gbi_to_c64(A, A32, nn, st);
+  if (rbt) {
+    if (!rc) rc = gbi_rbt_matrix(A32, n, n, rbt, rbt + 2 * (size_t)n, st);
+    if (!rc) rc = gbi_cgetrf_nopiv(A32, n, n, ipiv, info, st);
+  } else if (!rc) {
+    rc = gbi_cgetrf(A32, n, n, ipiv, info, st);
+  }
+  if (!rc) rc = gbi_make_perm(ipiv, n, perm, st);
+  *hinfo = 0;
+  if (!rc && (cudaMemcpyAsync(hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaStreamSynchronize(st) != cudaSuccess)) {
+    gbi_set_error("gbi_zgesv_mixed: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
+  }
+  return rc;
+}
+
+// A X = B (FP64, n x n, nrhs <= 8 packed columns) by FP32 factors and FP64
+// refinement to a relative residual of 1e-13; the factors are of the
+// butterfly-randomised matrix without interchanges when n is divisible by 4,
+// with tournament pivoting after a zero pivot or a refinement that does not
+// contract the residual 10x per correction (and when n is not)
 extern "C" int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cplx* X, int* iters, double* relres,
                                cudaStream_t st) {
   if (nrhs < 1 || nrhs > 8) { gbi_set_error("gbi_zgesv_mixed: nrhs %d not in 1..8", nrhs); return -1; }
@@ -1640,6 +1691,7 @@ extern "C" int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cp
   int64_t* ipiv = nullptr;
   int *perm = nullptr, *info = nullptr;
   double* nrm = nullptr;
+  float* rbt = nullptr;
   GB_CUDA(cudaMallocAsync((void**)&A32, nn * sizeof(cplxf), st));
   GB_CUDA(cudaMallocAsync((void**)&D, nb * sizeof(cplxf), st));
   GB_CUDA(cudaMallocAsync((void**)&Y, nb * sizeof(cplxf), st));
@@ -1648,23 +1700,29 @@ extern "C" int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cp
   GB_CUDA(cudaMallocAsync((void**)&perm, (size_t)n * sizeof(int), st));
   GB_CUDA(cudaMallocAsync((void**)&info, sizeof(int), st));
   GB_CUDA(cudaMallocAsync((void**)&nrm, 2 * sizeof(double), st));
-  int rc = gbi_to_c64(A, A32, nn, st);
-  if (!rc) rc = gbi_cgetrf(A32, n, n, ipiv, info, st);
-  if (!rc) rc = gbi_make_perm(ipiv, n, perm, st);
+  int rc = 0;
+  if (n % 4 == 0 && n >= 4) {
+    std::vector<float> h(4 * (size_t)n);
+    gbi_rbt_params(n, h.data());
+    GB_CUDA(cudaMallocAsync((void**)&rbt, h.size() * sizeof(float), st));
+    if (cudaMemcpyAsync(rbt, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
+  }
   int hinfo = 0;
-  if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
-              cudaStreamSynchronize(st) != cudaSuccess)) {
-    gbi_set_error("gbi_zgesv_mixed: %s", cudaGetErrorString(cudaGetLastError()));
-    rc = -1;
+  if (!rc) rc = factor32_dense(A, n, A32, ipiv, perm, info, rbt, &hinfo, st);
+  if (!rc && rbt && hinfo) {
+    cudaFreeAsync(rbt, st);
+    rbt = nullptr;
+    rc = factor32_dense(A, n, A32, ipiv, perm, info, nullptr, &hinfo, st);
   }
   if (!rc && hinfo) { gbi_set_error("mixed solve: FP32 factor singular (info=%d)", hinfo); rc = -1; }
   if (!rc && (cudaMemsetAsync(X, 0, nb * sizeof(cplx), st) != cudaSuccess ||
               cudaMemcpyAsync(R, B, nb * sizeof(cplx), cudaMemcpyDeviceToDevice, st) != cudaSuccess))
     rc = -1;
-  double rel = 1.0;
-  int it = 0;
+  double rel = 1.0, prev = 1.0;
+  int it = 0, since = 0;
   const unsigned gb = (unsigned)((nb + 255) / 256);
-  for (; !rc && it < 31; it++) {
+  for (; !rc && it < 31; it++, since++) {
     if (it > 0) {
       // R = B - A X (FP64)
       k_resid_multi<<<(unsigned)(((size_t)n * 32 + 255) / 256), 256, 0, st>>>(A, n, X, B, nrhs, R);
@@ -1677,15 +1735,37 @@ extern "C" int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cp
       double h[2];
       if (cudaMemcpyAsync(h, nrm, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess) { rc = -1; break; }
+      prev = rel;
       rel = (h[1] > 0.0) ? sqrt(h[0] / h[1]) : 0.0;
       if (rel <= 1e-13) break;
+      if (rbt && ((since >= 2 && rel > 0.1 * prev && rel > 1e-11) || since >= 12 || !(rel < 1e3))) {
+        cudaFreeAsync(rbt, st);
+        rbt = nullptr;
+        rc = factor32_dense(A, n, A32, ipiv, perm, info, nullptr, &hinfo, st);
+        if (!rc && hinfo) { gbi_set_error("mixed solve: FP32 factor singular (info=%d)", hinfo); rc = -1; }
+        if (rc) break;
+        if (!(rel < 1.0) &&
+            (cudaMemsetAsync(X, 0, nb * sizeof(cplx), st) != cudaSuccess ||
+             cudaMemcpyAsync(R, B, nb * sizeof(cplx), cudaMemcpyDeviceToDevice, st) != cudaSuccess)) { rc = -1; break; }
+        since = 0;
+      }
     }
-    k_c128_to_c64_scaled<<<gb, 256, 0, st>>>(R, D, (int)nb);
-    gbi_count_launch();
-    if (lu_solve_multi<cplxf>(A32, n, n, perm, D, nrhs, nrhs, Y, st)) { rc = -1; break; }
-    k_axpy_c64<<<gb, 256, 0, st>>>(X, Y, (int)nb);
-    gbi_count_launch();
+    const int q = n / 4;
+    if (rbt) {
+      k_rbt_ut<<<(unsigned)(((size_t)q * nrhs + 255) / 256), 256, 0, st>>>(R, D, n, nrhs, rbt);
+      gbi_count_launch();
+      if (lu_solve_multi<cplxf>(A32, n, n, perm, D, nrhs, nrhs, Y, st)) { rc = -1; break; }
+      k_rbt_axpy_v<<<(unsigned)(((size_t)q * nrhs + 255) / 256), 256, 0, st>>>(X, Y, n, nrhs, rbt + 2 * (size_t)n);
+      gbi_count_launch();
+    } else {
+      k_c128_to_c64_scaled<<<gb, 256, 0, st>>>(R, D, (int)nb);
+      gbi_count_launch();
+      if (lu_solve_multi<cplxf>(A32, n, n, perm, D, nrhs, nrhs, Y, st)) { rc = -1; break; }
+      k_axpy_c64<<<gb, 256, 0, st>>>(X, Y, (int)nb);
+      gbi_count_launch();
+    }
   }
+  cudaFreeAsync(rbt, st);
   if (iters) *iters = it;
   if (relres) *relres = rel;
   if (!rc && rel > 1e-10) { gbi_set_error("mixed solve: refinement stalled at relative residual %g", rel); rc = -1; }

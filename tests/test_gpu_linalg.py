@@ -195,3 +195,29 @@ def test_rbt_transform_matches_dense_model(n, gb_build):
     b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     x = V @ np.linalg.solve(Lm @ U, Ut @ b)
     assert _rel(A0.astype(np.complex128) @ x, b) <= 1e-3 * max(1.0, np.linalg.cond(A0) / 1e3)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,nrhs", [(6, 6), (64, 1), (258, 6), (1536, 6), (1001, 3)])
+def test_zgesv_mixed(n, nrhs, gb_build):
+    """gbi_zgesv_mixed (the dE/dn, dH/dn solve of the chosen form): FP32
+    factors of the butterfly-randomised matrix (n divisible by 4) or with
+    tournament pivoting (otherwise) and FP64 refinement to 1e-13: the FP64
+    solution of numpy to that level."""
+    import torch
+    L = _lib()
+    L.gbi_zgesv_mixed.argtypes = [vp, ci, vp, ci, vp, vp, vp, vp]
+    L.gbi_zgesv_mixed.restype = ci
+    rng = np.random.default_rng(n * 3 + nrhs)
+    A0 = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) + 2.0 * np.sqrt(n) * np.eye(n)
+    B0 = rng.standard_normal((n, nrhs)) + 1j * rng.standard_normal((n, nrhs))
+    ref = np.linalg.solve(A0, B0)
+    Ad = torch.tensor(A0, dtype=torch.complex128, device="cuda")
+    Bd = torch.tensor(B0, dtype=torch.complex128, device="cuda")
+    Xd = torch.zeros(n, nrhs, dtype=torch.complex128, device="cuda")
+    it, rr = ctypes.c_int(), ctypes.c_double()
+    assert L.gbi_zgesv_mixed(Ad.data_ptr(), n, Bd.data_ptr(), nrhs, Xd.data_ptr(), ctypes.byref(it), ctypes.byref(rr),
+                             None) == 0, L.gb_last_error()
+    torch.cuda.synchronize()
+    assert rr.value <= 1e-13 and 1 <= it.value <= 8, (it.value, rr.value)
+    assert _rel(Xd.cpu().numpy(), ref) <= 1e-11
