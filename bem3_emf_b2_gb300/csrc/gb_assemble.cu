@@ -302,10 +302,10 @@ struct AccD {
 };
 
 __device__ __forceinline__ df dot3d(const df a[3], const df b[3]) {
-  return df_add(df_add(df_mul(a[0], b[0]), df_mul(a[1], b[1])), df_mul(a[2], b[2]));
+  return df_fma(df_fma(df_mul(a[0], b[0]), a[1], b[1]), a[2], b[2]);
 }
 __device__ __forceinline__ dfc dfc_fma_re(dfc acc, dfc v, df s) {  // acc + v s
-  return dfcmk(df_add(acc.re, df_mul(v.re, s)), df_add(acc.im, df_mul(v.im, s)));
+  return dfcmk(df_fma(acc.re, v.re, s), df_fma(acc.im, v.im, s));
 }
 
 struct PairD {
@@ -321,9 +321,9 @@ __device__ __forceinline__ void reg_point_df(const PairD& P, bool quad, df z, df
   const df ze = df_mul(z, e);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
-    d[i] = df_add(df_add(df_mul(P.c1[i], z), df_mul(P.c2[i], e)), df_mul(P.c3[i], ze));
+    d[i] = df_fma(df_fma(df_mul(P.c1[i], z), P.c2[i], e), P.c3[i], ze);
     R[i] = df_add(P.R0[i], d[i]);
-    W[i] = df_add(df_add(P.w0[i], df_mul(P.w1[i], z)), df_mul(P.w2[i], e));
+    W[i] = df_fma(df_fma(P.w0[i], P.w1[i], z), P.w2[i], e);
   }
   const df aR = df_sqrt(dot3d(R, R));
   const df iR = df_rcp(aR);
@@ -364,7 +364,7 @@ __device__ __forceinline__ void reg_point_df(const PairD& P, bool quad, df z, df
     A.G[n] = dfc_fma_re(A.G[n], g, N[n]);
     A.H[n] = dfc_fma_re(A.H[n], h, N[n]);
   }
-  A.F = df_add(A.F, df_mul(w, tD));
+  A.F = df_fma(A.F, w, tD);
   const dfc t1 = dfc_add(dfc_mul(kR, kR), dfcmk(df_mul_f(cb.re, 3.0f), df_mul_f(cb.im, 3.0f)));
   const df iR3w = df_mul(df_mul(iR2, iR), w);
 #pragma unroll
@@ -379,7 +379,7 @@ __device__ __forceinline__ void reg_point_df(const PairD& P, bool quad, df z, df
       A.dG[q][n] = dfc_fma_re(A.dG[q][n], dg, N[n]);
       A.dH[q][n] = dfc_fma_re(A.dH[q][n], dh, N[n]);
     }
-    A.dF[q] = df_add(A.dF[q], df_mul(iR3w, df_sub(df_mul_f(df_mul(rdv, rdW), 3.0f), Wdv)));
+    A.dF[q] = df_fma(A.dF[q], iR3w, df_sub(df_mul_f(df_mul(rdv, rdW), 3.0f), Wdv));
   }
 }
 
@@ -570,81 +570,275 @@ __device__ __forceinline__ void singb_zero(SingAccB& B) {
   }
 }
 
-static __device__ void sing_bil_setB_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
+// per-direction geometry of a ray from (zt, et) in direction (cth, sth) of a
+// bilinear element, affine in the distance r: K = Ka + Kb r, W = Wa + Wb r
+struct RayD {
+  df Ka[3], Kb[3], Wa[3], Wb[3], vt[2][3];
+  df zt, et, c, s, kr, ki;
+};
+__device__ __forceinline__ void ray_geom_df(const SingCtx& c, double cth, double sth, RayD& g) {
   const Elem& E = c.E;
   const double zs = c.zt * sth + c.et * cth;
-  df Ka[3], Kb[3], Wa[3], Wb[3], vt[2][3];
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    Ka[d] = df_from(E.cr[d][1] * cth + E.cr[d][2] * sth + E.cr[d][3] * zs);
-    Kb[d] = df_from(E.cr[d][3] * cth * sth);
-    Wa[d] = df_from(E.cw[d][0] + E.cw[d][1] * c.zt + E.cw[d][2] * c.et);
-    Wb[d] = df_from(E.cw[d][1] * cth + E.cw[d][2] * sth);
-    vt[0][d] = df_from(c.vt[0][d]);
-    vt[1][d] = df_from(c.vt[1][d]);
+    g.Ka[d] = df_from(E.cr[d][1] * cth + E.cr[d][2] * sth + E.cr[d][3] * zs);
+    g.Kb[d] = df_from(E.cr[d][3] * cth * sth);
+    g.Wa[d] = df_from(E.cw[d][0] + E.cw[d][1] * c.zt + E.cw[d][2] * c.et);
+    g.Wb[d] = df_from(E.cw[d][1] * cth + E.cw[d][2] * sth);
+    g.vt[0][d] = df_from(c.vt[0][d]);
+    g.vt[1][d] = df_from(c.vt[1][d]);
   }
+  g.zt = df_from(c.zt);
+  g.et = df_from(c.et);
+  g.c = df_from(cth);
+  g.s = df_from(sth);
+  g.kr = df_from(c.k.x);
+  g.ki = df_from(c.k.y);
+}
+// point at signed distance rr (sg = -1: the opposite ray, whose K keeps the
+// +direction terms except the r-term, as the reference's principal-value
+// pairing): K, W and the bilinear shape functions
+__device__ __forceinline__ void ray_point_df(const RayD& g, df rr, float sg, df K[3], df W[3], df N[4]) {
+  const df r = df_mul_f(rr, sg);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    K[d] = df_fma(g.Ka[d], g.Kb[d], r);
+    W[d] = df_fma(g.Wa[d], g.Wb[d], r);
+  }
+  const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // 1 / GB_P44_N = sqrt(3)
+  const df za = df_mul(df_fma(g.zt, r, g.c), ia), ea = df_mul(df_fma(g.et, r, g.s), ia);
+  const df zm = df_add_f(df_neg(za), 1.0f), zp = df_add_f(za, 1.0f);
+  const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
+  N[0] = df_mul_f(df_mul(zm, em), 0.25f);
+  N[1] = df_mul_f(df_mul(zp, em), 0.25f);
+  N[2] = df_mul_f(df_mul(zp, ep), 0.25f);
+  N[3] = df_mul_f(df_mul(zm, ep), 0.25f);
+}
+
+static __device__ void sing_bil_setB_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
+  RayD g;
+  ray_geom_df(c, cth, sth, g);
   const df hr = df_from(0.5 * (rm - GB_DEPS)), r0 = df_from(0.5 * (rm + GB_DEPS));
   const df w0 = df_from(wth * 0.5 * (rm - GB_DEPS));
-  const df dzt = df_from(c.zt), det = df_from(c.et), dc = df_from(cth), ds = df_from(sth);
-  const df kr = df_from(c.k.x), ki = df_from(c.k.y);
-  const df cs[2] = {dc, ds}, outer[2] = {ds, dc};
-  const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // 1 / GB_P44_N = sqrt(3)
+  const df cs[2] = {g.c, g.s}, outer[2] = {g.s, g.c};
   SingAccB B;
   singb_zero(B);
   for (int i = 0; i < GB_GHN; i++) {
-    const df rr = df_add(df_mul(hr, dfmk(c_tabd.xh[i].x, c_tabd.xh[i].y)), r0);
+    const df rr = df_fma(r0, hr, dfmk(c_tabd.xh[i].x, c_tabd.xh[i].y));
     const df w = df_mul(w0, dfmk(c_tabd.wh[i].x, c_tabd.wh[i].y));
-    df K[3], W[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      K[d] = df_add(Ka[d], df_mul(Kb[d], rr));
-      W[d] = df_add(Wa[d], df_mul(Wb[d], rr));
-    }
+    df K[3], W[3], N[4];
+    ray_point_df(g, rr, 1.0f, K, W, N);
     const df aK2 = dot3d(K, K);
     const df aK = df_sqrt(aK2), aW = df_sqrt(dot3d(W, W));
     const df iK = df_rcp(aK), irr = df_rcp(rr);
     const df x = df_mul(aK, rr);
-    const dfc kR = dfcmk(df_mul(kr, x), df_mul(ki, x));
-    df sn, co;
-    df_sincos(kR.re, &sn, &co);
-    dfc ce = dfcmk(co, sn);
-    if (ki.hi != 0.0f) ce = dfc_scale(ce, df_exp(df_neg(kR.im)));
+    const dfc kR = dfcmk(df_mul(g.kr, x), df_mul(g.ki, x));
+    const dfc ce = dfc_expik(g.kr, g.ki, x);
     const dfc cb = dfcmk(df_add_f(df_neg(kR.im), -1.0f), kR.re);
-    const df za = df_mul(df_add(dzt, df_mul(rr, dc)), ia), ea = df_mul(df_add(det, df_mul(rr, ds)), ia);
-    const df zm = df_add_f(df_neg(za), 1.0f), zp = df_add_f(za, 1.0f);
-    const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
-    df N[4];
-    N[0] = df_mul_f(df_mul(zm, em), 0.25f);
-    N[1] = df_mul_f(df_mul(zp, em), 0.25f);
-    N[2] = df_mul_f(df_mul(zp, ep), 0.25f);
-    N[3] = df_mul_f(df_mul(zm, ep), 0.25f);
     const dfc cbce = dfc_mul(cb, ce);
     const df iK2 = df_sqr(iK);
     const df gs = df_mul(df_mul(df_mul(w, iK2), df_mul(irr, iK)), aW);
 #pragma unroll
     for (int d = 0; d < 2; d++) {
-      const df KdT = dot3d(K, vt[d]);
-      const dfc g = dfc_scale(cbce, df_mul(gs, KdT));
+      const df KdT = dot3d(K, g.vt[d]);
+      const dfc gg = dfc_scale(cbce, df_mul(gs, KdT));
 #pragma unroll
-      for (int n = 0; n < 4; n++) B.dG[d][n] = dfc_fma_re(B.dG[d][n], g, N[n]);
+      for (int n = 0; n < 4; n++) B.dG[d][n] = dfc_fma_re(B.dG[d][n], gg, N[n]);
     }
     if (!c.planar) {
       const dfc t1 = dfc_add(dfc_mul(kR, kR), dfcmk(df_mul_f(cb.re, 3.0f), df_mul_f(cb.im, 3.0f)));
       const df iK5r = df_mul(df_mul(df_sqr(iK2), iK), irr);
 #pragma unroll
       for (int d = 0; d < 2; d++) {
-        const df KdT = dot3d(K, vt[d]);
+        const df KdT = dot3d(K, g.vt[d]);
         const df wo = df_mul(df_mul(w, outer[d]), iK5r);
         const df kc = df_mul(KdT, cs[d]);
         const dfc u = dfc_add(dfc_scale(t1, kc), dfc_scale(cb, df_neg(aK2)));
         const dfc h = dfc_scale(dfc_mul(ce, u), wo);
 #pragma unroll
         for (int n = 0; n < 4; n++) B.dH[d][n] = dfc_fma_re(B.dH[d][n], h, N[n]);
-        B.dF[d] = df_add(B.dF[d], df_mul(wo, df_sub(df_mul_f(kc, 3.0f), aK2)));
+        B.dF[d] = df_fma(B.dF[d], wo, df_sub(df_mul_f(kc, 3.0f), aK2));
       }
     }
   }
   singb_add(B, A, 4, 1.0);
+}
+
+// set A: G, H, F on [0, rm] with the GLN rule (sing_bil_setA)
+static __device__ void sing_bil_setA_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
+  RayD g;
+  ray_geom_df(c, cth, sth, g);
+  const df hr = df_from(0.5 * rm), w0 = df_from(wth * 0.5 * rm), csn = df_from(cth * sth);
+  const df zero = dfmk(0.0f, 0.0f);
+  dfc Gs[4], Hs[4];
+  df Fs = zero;
+#pragma unroll
+  for (int n = 0; n < 4; n++) { Gs[n] = dfcmk(zero, zero); Hs[n] = dfcmk(zero, zero); }
+  for (int i = 0; i < GB_GLN; i++) {
+    const df rr = df_mul(hr, df_add_f(dfmk(c_tabd.x[i].x, c_tabd.x[i].y), 1.0f));
+    const df w = df_mul(w0, dfmk(c_tabd.w[i].x, c_tabd.w[i].y));
+    df K[3], W[3], N[4];
+    ray_point_df(g, rr, 1.0f, K, W, N);
+    const df aK = df_sqrt(dot3d(K, K)), aW = df_sqrt(dot3d(W, W));
+    const df iK = df_rcp(aK);
+    const df x = df_mul(aK, rr);
+    const dfc ce = dfc_expik(g.kr, g.ki, x);
+    const dfc gg = dfc_scale(ce, df_mul(df_mul(w, aW), iK));
+#pragma unroll
+    for (int n = 0; n < 4; n++) Gs[n] = dfc_fma_re(Gs[n], gg, N[n]);
+    if (!c.planar) {
+      const df wk = df_mul(df_mul(w, df_mul(df_sqr(iK), iK)), csn);
+      const dfc kR = dfcmk(df_mul(g.kr, x), df_mul(g.ki, x));
+      const dfc cb = dfcmk(df_add_f(df_neg(kR.im), -1.0f), kR.re);
+      const dfc h = dfc_scale(dfc_mul(cb, ce), wk);
+#pragma unroll
+      for (int n = 0; n < 4; n++) Hs[n] = dfc_fma_re(Hs[n], h, N[n]);
+      Fs = df_add(Fs, wk);
+    }
+  }
+#pragma unroll
+  for (int n = 0; n < 4; n++) {
+    A.G[n] += cmk(df_to(Gs[n].re), df_to(Gs[n].im));
+    A.H[n] += cmk(df_to(Hs[n].re), df_to(Hs[n].im));
+  }
+  A.F += df_to(Fs);
+}
+
+// set C: the disc D_eps, r in [0, DEPS] with the GLN rule (sing_bil_setC)
+static __device__ void sing_bil_setC_df(const SingCtx& c, double cth, double sth, double wth, SingAcc& A) {
+  RayD g;
+  ray_geom_df(c, cth, sth, g);
+  const df hr = df_from(0.5 * GB_DEPS), w0 = df_from(wth * 0.5 * GB_DEPS);
+  const df cs[2] = {g.c, g.s}, outer[2] = {g.s, g.c};
+  const dfc k = dfcmk(g.kr, g.ki), ik = dfcmk(df_neg(g.ki), g.kr);
+  const dfc ik3 = dfcmk(df_mul_f(ik.re, 3.0f), df_mul_f(ik.im, 3.0f));
+  SingAccB B;
+  singb_zero(B);
+  for (int i = 0; i < GB_GLN; i++) {
+    const df rr = df_mul(hr, df_add_f(dfmk(c_tabd.x[i].x, c_tabd.x[i].y), 1.0f));
+    const df w = df_mul(w0, dfmk(c_tabd.w[i].x, c_tabd.w[i].y));
+    df K[3], W[3], N[4];
+    ray_point_df(g, rr, 1.0f, K, W, N);
+    const df aK2 = dot3d(K, K);
+    const df aK = df_sqrt(aK2), aW = df_sqrt(dot3d(W, W));
+    const df iK = df_rcp(aK), irr = df_rcp(rr);
+    const df x = df_mul(aK, rr);
+    const dfc kR = dfcmk(df_mul(g.kr, x), df_mul(g.ki, x));
+    const dfc cb = dfcmk(df_add_f(df_neg(kR.im), -1.0f), kR.re);
+    dfc cc, sn;
+    dfc_cossin(kR, &cc, &sn);
+    const dfc ce = dfc_expik(g.kr, g.ki, x);
+    const dfc gbase = dfc_muli(dfc_add(dfc_mul(cb, sn), dfc_mul(kR, cc)));
+    const df gs = df_mul(df_mul(df_mul(w, df_sqr(iK)), df_mul(irr, iK)), aW);
+    const df iK4 = df_sqr(df_sqr(iK));
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+      const df KdT = dot3d(K, g.vt[d]);
+      const dfc gg = dfc_scale(gbase, df_mul(gs, KdT));
+#pragma unroll
+      for (int n = 0; n < 4; n++) B.dG[d][n] = dfc_fma_re(B.dG[d][n], gg, N[n]);
+      if (!c.planar) {
+        const df wo = df_mul(w, outer[d]);
+        const df kc = df_mul(KdT, cs[d]);
+        const dfc u = dfc_sub(dfc_scale(dfc_add(dfc_mul(k, kR), ik3), kc), dfc_scale(ik, aK2));
+        const dfc v0 = dfc_scale(dfc_mul(ce, u), iK4);
+        const dfc v1 = dfc_scale(sn, df_mul(df_mul(df_sub(df_mul_f(kc, 3.0f), aK2), df_mul(iK4, iK)), irr));
+        const dfc h = dfc_scale(dfc_sub(v0, dfc_muli(v1)), wo);
+#pragma unroll
+        for (int n = 0; n < 4; n++) B.dH[d][n] = dfc_fma_re(B.dH[d][n], h, N[n]);
+      }
+    }
+  }
+  singb_add(B, A, 4, 1.0);
+}
+
+// set D: principal-value pairing of +r and -r, r in [0, DEPS] (sing_bil_setD)
+static __device__ void sing_bil_setD_df(const SingCtx& c, double cth, double sth, double wth, SingAcc& A) {
+  RayD g;
+  ray_geom_df(c, cth, sth, g);
+  const df hr = df_from(0.5 * GB_DEPS), w0 = df_from(wth * 0.5 * GB_DEPS);
+  const df cs[2] = {g.c, g.s}, outer[2] = {g.s, g.c};
+  SingAccB B;
+  singb_zero(B);
+  for (int i = 0; i < GB_GLN; i++) {
+    const df rr = df_mul(hr, df_add_f(dfmk(c_tabd.x[i].x, c_tabd.x[i].y), 1.0f));
+    const df w = df_mul(w0, dfmk(c_tabd.w[i].x, c_tabd.w[i].y));
+    df Kp[3], Wp[3], Np[4], Km[3], Wm[3], Nm[4];
+    ray_point_df(g, rr, 1.0f, Kp, Wp, Np);
+    ray_point_df(g, rr, -1.0f, Km, Wm, Nm);
+    const df aKp2 = dot3d(Kp, Kp), aKm2 = dot3d(Km, Km);
+    const df aKp = df_sqrt(aKp2), aWp = df_sqrt(dot3d(Wp, Wp));
+    const df aKm = df_sqrt(aKm2), aWm = df_sqrt(dot3d(Wm, Wm));
+    const df iKp = df_rcp(aKp), iKm = df_rcp(aKm), ir = df_rcp(rr);
+    const df xp = df_mul(aKp, rr), xm = df_neg(df_mul(aKm, rr));
+    dfc ccp, snp, ccm, snm;
+    dfc_cossin(dfcmk(df_mul(g.kr, xp), df_mul(g.ki, xp)), &ccp, &snp);
+    dfc_cossin(dfcmk(df_mul(g.kr, xm), df_mul(g.ki, xm)), &ccm, &snm);
+    const df iKp2 = df_sqr(iKp), iKm2 = df_sqr(iKm);
+    const df iKp5 = df_mul(df_sqr(iKp2), iKp), iKm5 = df_mul(df_sqr(iKm2), iKm);
+    const df gsp = df_mul(df_mul(df_mul(w, ir), df_mul(iKp2, iKp)), aWp);
+    const df gsm = df_mul(df_mul(df_mul(w, ir), df_mul(iKm2, iKm)), aWm);
+#pragma unroll
+    for (int d = 0; d < 2; d++) {
+      const df KpdT = dot3d(Kp, g.vt[d]), KmdT = dot3d(Km, g.vt[d]);
+      const dfc gp = dfc_scale(ccp, df_mul(gsp, KpdT));
+      const dfc gm = dfc_scale(ccm, df_mul(gsm, KmdT));
+#pragma unroll
+      for (int n = 0; n < 4; n++) {
+        const dfc t = dfc_sub(dfcmk(df_mul(gp.re, Np[n]), df_mul(gp.im, Np[n])),
+                              dfcmk(df_mul(gm.re, Nm[n]), df_mul(gm.im, Nm[n])));
+        B.dG[d][n] = dfc_sub(B.dG[d][n], t);
+      }
+      if (!c.planar) {
+        const df wo = df_mul(df_mul(w, outer[d]), ir);
+        const df fp = df_mul(iKp5, df_sub(df_mul_f(df_mul(KpdT, cs[d]), 3.0f), aKp2));
+        const df fm = df_mul(iKm5, df_sub(df_mul_f(df_mul(KmdT, cs[d]), 3.0f), aKm2));
+        const dfc hp = dfc_scale(ccp, df_mul(wo, fp)), hm = dfc_scale(ccm, df_mul(wo, fm));
+#pragma unroll
+        for (int n = 0; n < 4; n++) {
+          const dfc t = dfc_sub(dfcmk(df_mul(hp.re, Np[n]), df_mul(hp.im, Np[n])),
+                                dfcmk(df_mul(hm.re, Nm[n]), df_mul(hm.im, Nm[n])));
+          B.dH[d][n] = dfc_sub(B.dH[d][n], t);
+        }
+        B.dF[d] = df_fma(B.dF[d], wo, df_sub(fp, fm));
+      }
+    }
+  }
+  singb_add(B, A, 4, 1.0);
+}
+
+// triangle set A: G on [0, rm] with the GLN rule; K is constant along the
+// ray; 3 x the shape functions, the 1/3 applied in FP64
+static __device__ void sing_lit_setA_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
+  const Elem& E = c.E;
+  double K[3];
+  for (int d = 0; d < 3; d++) K[d] = E.cr[d][1] * cth + E.cr[d][2] * sth;
+  const double aK = norm3(K);
+  const df daK = df_from(aK), iaK = df_from(1.0 / aK);
+  const df hr = df_from(0.5 * rm), w0 = df_from(wth * 0.5 * rm);
+  const df dzt = df_from(c.zt), det = df_from(c.et), dc = df_from(cth), ds = df_from(sth);
+  const df kr = df_from(c.k.x), ki = df_from(c.k.y);
+  const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
+  const df zero = dfmk(0.0f, 0.0f);
+  dfc Gs[3];
+#pragma unroll
+  for (int n = 0; n < 3; n++) Gs[n] = dfcmk(zero, zero);
+  for (int i = 0; i < GB_GLN; i++) {
+    const df rr = df_mul(hr, df_add_f(dfmk(c_tabd.x[i].x, c_tabd.x[i].y), 1.0f));
+    const df w = df_mul(w0, dfmk(c_tabd.w[i].x, c_tabd.w[i].y));
+    const dfc ce = dfc_expik(kr, ki, df_mul(daK, rr));
+    const df z = df_fma(dzt, rr, dc), e = df_fma(det, rr, ds);
+    const df se = df_mul(s3, e);
+    df N[3];
+    N[0] = df_add_f(df_mul_f(df_add(z, se), -2.5f), 1.0f);
+    N[1] = df_add_f(df_mul_f(z, 5.0f), 1.0f);
+    N[2] = df_add_f(df_mul_f(df_sub(z, se), -2.5f), 1.0f);
+    const dfc gg = dfc_scale(ce, df_mul(w, iaK));
+#pragma unroll
+    for (int n = 0; n < 3; n++) Gs[n] = dfc_fma_re(Gs[n], gg, N[n]);
+  }
+#pragma unroll
+  for (int n = 0; n < 3; n++) A.G[n] += cmk(df_to(Gs[n].re), df_to(Gs[n].im)) * (1.0 / 3.0);
 }
 
 // triangle: K is constant along the ray; 3 x the shape functions in
@@ -664,7 +858,7 @@ static __device__ void sing_lit_setB_df(const SingCtx& c, double cth, double sth
   SingAccB B;
   singb_zero(B);
   for (int i = 0; i < GB_GHN; i++) {
-    const df rr = df_add(df_mul(hr, dfmk(c_tabd.xh[i].x, c_tabd.xh[i].y)), r0);
+    const df rr = df_fma(r0, hr, dfmk(c_tabd.xh[i].x, c_tabd.xh[i].y));
     const df w = df_mul(w0, dfmk(c_tabd.wh[i].x, c_tabd.wh[i].y));
     const df x = df_mul(daK, rr);
     const dfc kR = dfcmk(df_mul(kr, x), df_mul(ki, x));
@@ -673,7 +867,7 @@ static __device__ void sing_lit_setB_df(const SingCtx& c, double cth, double sth
     dfc ce = dfcmk(co, sn);
     if (ki.hi != 0.0f) ce = dfc_scale(ce, df_exp(df_neg(kR.im)));
     const dfc cb = dfcmk(df_add_f(df_neg(kR.im), -1.0f), kR.re);
-    const df z = df_add(dzt, df_mul(rr, dc)), e = df_add(det, df_mul(rr, ds));
+    const df z = df_fma(dzt, rr, dc), e = df_fma(det, rr, ds);
     const df se = df_mul(s3, e);
     df N[3];
     N[0] = df_add_f(df_mul_f(df_add(z, se), -2.5f), 1.0f);
@@ -690,22 +884,52 @@ static __device__ void sing_lit_setB_df(const SingCtx& c, double cth, double sth
   singb_add(B, A, 3, 1.0 / 3.0);
 }
 
-// sing_item with set B in double-float
+// sing_item with the point sets in double-float (the triangle's analytic
+// sets C and D stay FP64: one evaluation per direction)
 static __device__ void sing_item_df(const SingCtx& c, int q, SingAcc& A) {
   const int nA = c.nedge * 2 * GB_GHN;
-  if (q < nA || q >= 2 * nA) {
+  if (q < 2 * nA) {
+    const int setB = q >= nA;
+    const int qq = setB ? q - nA : q;
+    const int j = qq / (2 * GB_GHN), rem = qq % (2 * GB_GHN);
+    const int h = rem / GB_GHN, m = rem % GB_GHN;
+    double th, wth, rm;
+    sing_edge_theta(c, j, h, m, &th, &wth, &rm);
+    double sth, cth;
+    sincos(th, &sth, &cth);
+    if (c.E.quad) {
+      if (setB) sing_bil_setB_df(c, cth, sth, rm, wth, A);
+      else sing_bil_setA_df(c, cth, sth, rm, wth, A);
+    } else {
+      if (setB) sing_lit_setB_df(c, cth, sth, rm, wth, A);
+      else sing_lit_setA_df(c, cth, sth, rm, wth, A);
+    }
+    return;
+  }
+  if (!c.E.quad) {
     sing_item(c, q, A);
     return;
   }
-  const int qq = q - nA;
-  const int j = qq / (2 * GB_GHN), rem = qq % (2 * GB_GHN);
-  const int h = rem / GB_GHN, m = rem % GB_GHN;
-  double th, wth, rm;
-  sing_edge_theta(c, j, h, m, &th, &wth, &rm);
-  double sth, cth;
-  sincos(th, &sth, &cth);
-  if (c.E.quad) sing_bil_setB_df(c, cth, sth, rm, wth, A);
-  else sing_lit_setB_df(c, cth, sth, rm, wth, A);
+  q -= 2 * nA;
+  if (q < 4 * GB_GHN) {  // set C: theta over (-pi, pi] in four quarters
+    const int quarter = q / GB_GHN, m = q % GB_GHN;
+    const double off[4] = {-0.75 * GB_PI, -0.25 * GB_PI, 0.25 * GB_PI, 0.75 * GB_PI};
+    const double th = 0.25 * GB_PI * c_tab.xhi[m] + off[quarter];
+    const double wth = 0.25 * GB_PI * c_tab.whi[m];
+    double sth, cth;
+    sincos(th, &sth, &cth);
+    sing_bil_setC_df(c, cth, sth, wth, A);
+    return;
+  }
+  q -= 4 * GB_GHN;
+  {  // set D: theta over (0, pi) in two halves
+    const int half = q / GB_GHN, m = q % GB_GHN;
+    const double th = 0.25 * GB_PI * c_tab.xhi[m] + (half == 0 ? 0.25 * GB_PI : 0.75 * GB_PI);
+    const double wth = 0.25 * GB_PI * c_tab.whi[m];
+    double sth, cth;
+    sincos(th, &sth, &cth);
+    sing_bil_setD_df(c, cth, sth, wth, A);
+  }
 }
 
 template <bool DF>

@@ -62,24 +62,54 @@ __device__ __forceinline__ df df_mul_f(df a, float b) {
   p.lo = fmaf(a.lo, b, p.lo);
   return quick_two_sum(p.hi, p.lo);
 }
+// c + a b with one rounding error of the double-float format: the product's
+// error terms folded into the sum's (two_sum of the high parts, then one
+// renormalisation); about half the instructions of df_add(c, df_mul(a, b))
+__device__ __forceinline__ df df_fma(df c, df a, df b) {
+  const float p = a.hi * b.hi;
+  float pe = fmaf(a.hi, b.hi, -p);
+  pe = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, pe));
+  const float s = c.hi + p;
+  const float bb = s - c.hi;
+  const float e = (c.hi - (s - bb)) + (p - bb);
+  return quick_two_sum(s, e + (c.lo + pe));
+}
 __device__ __forceinline__ df df_sqr(df a) {
   df p = two_prod(a.hi, a.hi);
   p.lo = fmaf(2.0f * a.hi, a.lo, p.lo);
   return quick_two_sum(p.hi, p.lo);
 }
+__device__ __forceinline__ float rcp_approx(float x) {  // hardware reciprocal estimate (about 1 ulp)
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float rsqrt_approx(float x) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+// 1 / b: the FP32 estimate q1 and one Newton correction with the residual
+// 1 - b q1 formed exactly enough by fused multiply-adds (relative error
+// about 2^-46; b normal, not zero)
+__device__ __forceinline__ df df_rcp(df b) {
+  const float q1 = rcp_approx(b.hi);
+  float r = fmaf(-b.hi, q1, 1.0f);
+  r = fmaf(-b.lo, q1, r);
+  return quick_two_sum(q1, r * q1);
+}
 // a / b: a first quotient, its remainder, a correction
 __device__ __forceinline__ df df_div(df a, df b) {
-  const float q1 = a.hi / b.hi;
+  const float ib = rcp_approx(b.hi);
+  const float q1 = a.hi * ib;
   const df r = df_sub(a, df_mul_f(b, q1));
-  const float q2 = r.hi / b.hi;
-  return quick_two_sum(q1, q2);
+  return quick_two_sum(q1, r.hi * ib);
 }
-__device__ __forceinline__ df df_rcp(df b) { return df_div(dfmk(1.0f, 0.0f), b); }
 // sqrt(a), a > 0: the FP32 root corrected by one Newton step in double-float
 __device__ __forceinline__ df df_sqrt(df a) {
   const float s = sqrtf(a.hi);
   const df e = df_sub(a, two_prod(s, s));
-  return quick_two_sum(s, e.hi / (2.0f * s));
+  return quick_two_sum(s, e.hi * (0.5f * rsqrt_approx(a.hi)));
 }
 
 // complex double-float
@@ -89,7 +119,7 @@ struct dfc {
 __device__ __forceinline__ dfc dfcmk(df r, df i) { dfc c; c.re = r; c.im = i; return c; }
 __device__ __forceinline__ dfc dfc_add(dfc a, dfc b) { return dfcmk(df_add(a.re, b.re), df_add(a.im, b.im)); }
 __device__ __forceinline__ dfc dfc_mul(dfc a, dfc b) {
-  return dfcmk(df_sub(df_mul(a.re, b.re), df_mul(a.im, b.im)), df_add(df_mul(a.re, b.im), df_mul(a.im, b.re)));
+  return dfcmk(df_fma(df_mul(a.re, b.re), df_neg(a.im), b.im), df_fma(df_mul(a.re, b.im), a.im, b.re));
 }
 __device__ __forceinline__ dfc dfc_scale(dfc a, df s) { return dfcmk(df_mul(a.re, s), df_mul(a.im, s)); }
 
@@ -131,14 +161,14 @@ __device__ __forceinline__ void df_sincos(df x, df* s, df* c) {
   df sp = df_ld(g_df_sin_c, 7), cp = df_ld(g_df_cos_c, 7);
 #pragma unroll
   for (int m = 6; m >= 0; m--) {
-    sp = df_add(df_mul(sp, mu), df_ld(g_df_sin_c, m));
-    cp = df_add(df_mul(cp, mu), df_ld(g_df_cos_c, m));
+    sp = df_fma(df_ld(g_df_sin_c, m), sp, mu);
+    cp = df_fma(df_ld(g_df_cos_c, m), cp, mu);
   }
   const df st = df_mul(sp, t), ct = cp;
   const int j = ((int)jf) & 15;
   const df ca = df_ld(g_df_cos_j, j), sa = df_ld(g_df_cos_j, (j + 12) & 15);  // sin(a) = cos(a - pi/2)
-  *s = df_add(df_mul(st, ca), df_mul(ct, sa));
-  *c = df_sub(df_mul(ct, ca), df_mul(st, sa));
+  *s = df_fma(df_mul(st, ca), ct, sa);
+  *c = df_fma(df_mul(ct, ca), df_neg(st), sa);
 }
 
 // exp(y) in double-float, |y| < 80: y = n ln2 + r, |r| <= ln2 / 2 (ln 2 in
@@ -161,7 +191,55 @@ __device__ __forceinline__ df df_exp(df y) {
   r = df_add_f(r, -nf * L3);
   df e = df_ld(g_df_exp_c, 15);
 #pragma unroll
-  for (int k = 14; k >= 0; k--) e = df_add(df_mul(e, r), df_ld(g_df_exp_c, k));
+  for (int k = 14; k >= 0; k--) e = df_fma(df_ld(g_df_exp_c, k), e, r);
   const float sc = ldexpf(1.0f, (int)nf);
   return dfmk(e.hi * sc, e.lo * sc);
 }
+
+// e^{i k x} for k = kr + i ki
+__device__ __forceinline__ dfc dfc_expik(df kr, df ki, df x) {
+  df sn, cs;
+  df_sincos(df_mul(kr, x), &sn, &cs);
+  dfc r = dfcmk(cs, sn);
+  if (ki.hi != 0.0f) r = dfc_scale(r, df_exp(df_neg(df_mul(ki, x))));
+  return r;
+}
+
+// cosh and sinh of b: Taylor polynomials to b^15 for |b| < 1/2 (truncation
+// below 1e-22), exponentials otherwise
+__device__ __forceinline__ void df_coshsinh(df b, df* ch, df* sh) {
+  if (fabsf(b.hi) < 0.5f) {
+    const df t = df_sqr(b);
+    df sp = df_ld(g_df_sin_c, 7), cp = df_ld(g_df_cos_c, 7);
+#pragma unroll
+    for (int m = 6; m >= 0; m--) {
+      sp = df_fma(df_ld(g_df_sin_c, m), sp, t);
+      cp = df_fma(df_ld(g_df_cos_c, m), cp, t);
+    }
+    *sh = df_mul(sp, b);
+    *ch = cp;
+  } else {
+    const df e = df_exp(b), ei = df_rcp(e);
+    *ch = df_mul_f(df_add(e, ei), 0.5f);
+    *sh = df_mul_f(df_sub(e, ei), 0.5f);
+  }
+}
+
+// cos z and sin z of a complex argument
+__device__ __forceinline__ void dfc_cossin(dfc z, dfc* cz, dfc* sz) {
+  df s, c;
+  df_sincos(z.re, &s, &c);
+  if (z.im.hi == 0.0f) {
+    const df zero = dfmk(0.0f, 0.0f);
+    *cz = dfcmk(c, zero);
+    *sz = dfcmk(s, zero);
+    return;
+  }
+  df ch, sh;
+  df_coshsinh(z.im, &ch, &sh);
+  *cz = dfcmk(df_mul(c, ch), df_neg(df_mul(s, sh)));
+  *sz = dfcmk(df_mul(s, ch), df_mul(c, sh));
+}
+
+__device__ __forceinline__ dfc dfc_sub(dfc a, dfc b) { return dfcmk(df_sub(a.re, b.re), df_sub(a.im, b.im)); }
+__device__ __forceinline__ dfc dfc_muli(dfc a) { return dfcmk(df_neg(a.im), a.re); }  // i a
