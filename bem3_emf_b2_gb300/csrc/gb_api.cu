@@ -142,6 +142,7 @@ extern "C" int gb_device_count(void) {
 struct CrossCache {
   unsigned long long src_uid;
   int type;
+  int prec;  // field_prec of the source when built
   int n, C;
   int* did;
   int bad;  // first invalid domain id (+1000), 0 if all nodes are outside the source
@@ -181,6 +182,10 @@ struct gb_obj {
   int lu_rbt;
   int lu_mode;
   int lu_fallbacks;  // refactorisations with interchanges after a stalled refinement
+  // arithmetic of the regular pairs of the field kernels (potentials at
+  // points, fields on the boundary, cross operators): 2 double-float after a
+  // precision-2 assembly, else FP64
+  int field_prec;
   // boundary values per domain, [(Ne_d+1)][4][4] (U, dU) and [(Ne_d+1)][4][3] (E, dE, H, dH)
   cplx* bU[GB_MAXDOM];
   cplx* bdU[GB_MAXDOM];
@@ -245,7 +250,7 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   o->invA = nullptr;
   o->have_invA = 0;
   o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
-  o->rbt = nullptr; o->lu_rbt = 0; o->lu_mode = 0; o->lu_fallbacks = 0;
+  o->rbt = nullptr; o->lu_rbt = 0; o->lu_mode = 0; o->lu_fallbacks = 0; o->field_prec = 0;
   for (int d = 0; d < GB_MAXDOM; d++) o->bU[d] = o->bdU[d] = o->bE[d] = o->bdE[d] = o->bH[d] = o->bdH[d] = nullptr;
   o->Ui = o->dUi = o->Ui0 = o->dUi0 = o->Uip = nullptr;
   o->next = 0;
@@ -352,6 +357,7 @@ extern "C" int gb_assemble2(gb_obj* o, int did, int type, int precision) {
   if (e != cudaSuccess) { gbi_set_error("gb_assemble: %s", cudaGetErrorString(e)); return -1; }
   o->have_invA = 0;
   o->have_lu32 = 0;
+  o->field_prec = precision == 2 ? 2 : 0;
   return 0;
 }
 
@@ -636,6 +642,7 @@ static FieldObj field_view(gb_obj* o) {
   f.sb_off[o->m.MN + 1] = o->m.sb_off[o->m.MN + 1];
   f.MN = o->m.MN;
   f.lambda0 = o->lambda0;
+  f.prec = o->field_prec;
   return f;
 }
 
@@ -644,11 +651,12 @@ static FieldObj field_view(gb_obj* o) {
 
 static CrossCache* cross_entry(gb_obj* dst, gb_obj* src, int type) {
   for (auto& e : dst->xc)
-    if (e.src_uid == src->uid && e.type == type) return &e;
+    if (e.src_uid == src->uid && e.type == type && e.prec == src->field_prec) return &e;
   CrossCache e;
   memset(&e, 0, sizeof(e));
   e.src_uid = src->uid;
   e.type = type;
+  e.prec = src->field_prec;
   e.n = dst->next;
   e.C = 4 * src->m.sb_Ne[0];
   if (dalloc((void**)&e.did, (size_t)e.n * sizeof(int))) return nullptr;

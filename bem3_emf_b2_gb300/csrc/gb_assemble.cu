@@ -36,7 +36,7 @@
 #include "gb_quad.cuh"
 #include "gb_reduce.cuh"
 #include "gb_internal.h"
-#include "gb_df64.cuh"
+#include "gb_quad_df.cuh"
 #include <mutex>
 
 
@@ -107,11 +107,6 @@ struct GbTablesF {
   float xli[GB_GLN], wli[GB_GLN];
 };
 static __constant__ GbTablesF c_tabf;
-struct GbTablesD {  // GL nodes and weights in double-float (hi, lo)
-  float2 x[GB_GLN], w[GB_GLN];
-  float2 xh[GB_GHN], wh[GB_GHN];
-};
-static __constant__ GbTablesD c_tabd;
 
 // per-pair constants in FP32, relative to the source element's point (0, 0)
 struct PairF {
@@ -288,101 +283,10 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, uint8_t* red
 }
 
 // ------------------------------------------------------------------ double-float regular pairs
-// Precision 2: the GLN x GLN rule of the regular pairs in double-float (about
-// 48 significant bits, gb_df64.cuh) on the FP32 pipes, relative to the source
-// element's point (0,0); the common factor e^{ik|R0|} is applied in FP64 to
-// the sums.  Pairs whose |Re dF/dt| is within 0.05 of the CBD_SDF decision
-// (or not finite) are redone by the FP64 kernel, which decides GLN/GHN exactly
-// as the reference.
-struct AccD {
-  dfc G[4], H[4];
-  df F;
-  dfc dG[2][4], dH[2][4];
-  df dF[2];
-};
-
-__device__ __forceinline__ df dot3d(const df a[3], const df b[3]) {
-  return df_fma(df_fma(df_mul(a[0], b[0]), a[1], b[1]), a[2], b[2]);
-}
-__device__ __forceinline__ dfc dfc_fma_re(dfc acc, dfc v, df s) {  // acc + v s
-  return dfcmk(df_fma(acc.re, v.re, s), df_fma(acc.im, v.im, s));
-}
-
-struct PairD {
-  df R0[3], a0;
-  df c1[3], c2[3], c3[3];
-  df w0[3], w1[3], w2[3];
-  df vt[2][3];
-  df kr, ki;
-};
-
-__device__ __forceinline__ void reg_point_df(const PairD& P, bool quad, df z, df e, df w, AccD& A) {
-  df d[3], R[3], W[3];
-  const df ze = df_mul(z, e);
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    d[i] = df_fma(df_fma(df_mul(P.c1[i], z), P.c2[i], e), P.c3[i], ze);
-    R[i] = df_add(P.R0[i], d[i]);
-    W[i] = df_fma(df_fma(P.w0[i], P.w1[i], z), P.w2[i], e);
-  }
-  const df aR = df_sqrt(dot3d(R, R));
-  const df iR = df_rcp(aR);
-  const df aW = df_sqrt(dot3d(W, W));
-  const df dl = df_sub(aR, P.a0);
-  df sn, cs;
-  df_sincos(df_mul(P.kr, dl), &sn, &cs);
-  dfc ph = dfcmk(cs, sn);  // e^{ik(|R| - |R0|)}
-  if (P.ki.hi != 0.0f) ph = dfc_scale(ph, df_exp(df_neg(df_mul(P.ki, dl))));
-  const dfc kR = dfcmk(df_mul(P.kr, aR), df_mul(P.ki, aR));
-  const dfc cb = dfcmk(df_add_f(df_neg(kR.im), -1.0f), kR.re);  // i k R - 1
-  const df iR2 = df_sqr(iR);
-  const df rdW = df_mul(dot3d(R, W), iR);
-  const df tD = df_mul(rdW, iR2);
-  df N[4];
-  if (quad) {
-    const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // 1 / GB_P44_N = sqrt(3)
-    const df za = df_mul(z, ia), ea = df_mul(e, ia);
-    const df zm = df_add_f(df_neg(za), 1.0f), zp = df_add_f(za, 1.0f);
-    const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
-    N[0] = df_mul_f(df_mul(zm, em), 0.25f);
-    N[1] = df_mul_f(df_mul(zp, em), 0.25f);
-    N[2] = df_mul_f(df_mul(zp, ep), 0.25f);
-    N[3] = df_mul_f(df_mul(zm, ep), 0.25f);
-  } else {  // 3 x the shape functions (0.5 / GB_P34_N0 = 2.5 exactly); the 1/3 is applied in FP64
-    const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
-    const df se = df_mul(s3, e);
-    N[0] = df_add_f(df_mul_f(df_add(z, se), -2.5f), 1.0f);
-    N[1] = df_add_f(df_mul_f(z, 5.0f), 1.0f);
-    N[2] = df_add_f(df_mul_f(df_sub(z, se), -2.5f), 1.0f);
-    N[3] = dfmk(0.0f, 0.0f);
-  }
-  const dfc g = dfc_scale(ph, df_mul(df_mul(iR, aW), w));
-  const dfc cbe = dfc_mul(cb, ph);
-  const dfc h = dfc_scale(cbe, df_mul(tD, w));
-#pragma unroll
-  for (int n = 0; n < 4; n++) {
-    A.G[n] = dfc_fma_re(A.G[n], g, N[n]);
-    A.H[n] = dfc_fma_re(A.H[n], h, N[n]);
-  }
-  A.F = df_fma(A.F, w, tD);
-  const dfc t1 = dfc_add(dfc_mul(kR, kR), dfcmk(df_mul_f(cb.re, 3.0f), df_mul_f(cb.im, 3.0f)));
-  const df iR3w = df_mul(df_mul(iR2, iR), w);
-#pragma unroll
-  for (int q = 0; q < 2; q++) {
-    const df rdv = df_mul(dot3d(R, P.vt[q]), iR);
-    const df Wdv = dot3d(W, P.vt[q]);
-    const dfc dg = dfc_scale(cbe, df_mul(df_mul(iR2, rdv), df_mul(aW, w)));
-    const dfc u = dfc_add(dfc_scale(t1, df_mul(rdv, rdW)), dfc_scale(cb, df_neg(Wdv)));
-    const dfc dh = dfc_scale(dfc_mul(ph, u), iR3w);
-#pragma unroll
-    for (int n = 0; n < 4; n++) {
-      A.dG[q][n] = dfc_fma_re(A.dG[q][n], dg, N[n]);
-      A.dH[q][n] = dfc_fma_re(A.dH[q][n], dh, N[n]);
-    }
-    A.dF[q] = df_fma(A.dF[q], iR3w, df_sub(df_mul_f(df_mul(rdv, rdW), 3.0f), Wdv));
-  }
-}
-
+// Precision 2: the GLN x GLN rule of the regular pairs in double-float
+// (reg_integrate_dn, gb_quad_df.cuh); pairs whose |Re dF/dt| is within 0.05
+// of the CBD_SDF decision (or not finite) are flagged and redone by the FP64
+// kernel, which decides GLN/GHN exactly as the reference.
 __global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo) {
   const size_t N = (size_t)a.Ne * 4;
   const size_t npair = N * (size_t)a.Ne;
@@ -401,81 +305,11 @@ __global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo
   double rt[3], vt[2][3];
   for (int d = 0; d < 3; d++) rt[d] = __ldg(a.ren + (size_t)atd * 12 + tn * 3 + d);
   node_tangents(T, tn, vt);
-  PairD P;
-  double R0[3];
-  for (int d = 0; d < 3; d++) {
-    R0[d] = S.cr[d][0] - rt[d];
-    P.R0[d] = df_from(R0[d]);
-    P.c1[d] = df_from(S.cr[d][1]); P.c2[d] = df_from(S.cr[d][2]); P.c3[d] = df_from(S.cr[d][3]);
-    P.w0[d] = df_from(S.cw[d][0]); P.w1[d] = df_from(S.cw[d][1]); P.w2[d] = df_from(S.cw[d][2]);
-    P.vt[0][d] = df_from(vt[0][d]); P.vt[1][d] = df_from(vt[1][d]);
-  }
-  const double a0 = norm3(R0);
-  P.a0 = df_from(a0);
-  P.kr = df_from(a.k.x);
-  P.ki = df_from(a.k.y);
-  const cplx E0 = cexpik(a.k, a0);
-  AccD A;
-  const df zero = dfmk(0.0f, 0.0f);
-#pragma unroll
-  for (int n = 0; n < 4; n++) {
-    A.G[n] = dfcmk(zero, zero); A.H[n] = dfcmk(zero, zero);
-    for (int q = 0; q < 2; q++) { A.dG[q][n] = dfcmk(zero, zero); A.dH[q][n] = dfcmk(zero, zero); }
-  }
-  A.F = zero; A.dF[0] = zero; A.dF[1] = zero;
-  double S0;
-  if (S.quad) {
-    S0 = GB_I_FP;
-    for (int i = 0; i < GB_GLN; i++) {
-      const df x = dfmk(c_tabd.x[i].x, c_tabd.x[i].y), wx = dfmk(c_tabd.w[i].x, c_tabd.w[i].y);
-      for (int j = 0; j < GB_GLN; j++) {
-        const df y = dfmk(c_tabd.x[j].x, c_tabd.x[j].y), wy = dfmk(c_tabd.w[j].x, c_tabd.w[j].y);
-        reg_point_df(P, true, x, y, df_mul(wx, wy), A);
-      }
-    }
-  } else {
-    S0 = 0.0625 * GB_SQ3 * GB_I_SPSQ3;
-    const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
-    for (int i = 0; i < GB_GLN; i++) {
-      const df x = dfmk(c_tabd.x[i].x, c_tabd.x[i].y), wx = dfmk(c_tabd.w[i].x, c_tabd.w[i].y);
-      for (int j = 0; j < GB_GLN; j++) {
-        const df y = dfmk(c_tabd.x[j].x, c_tabd.x[j].y), wy = dfmk(c_tabd.w[j].x, c_tabd.w[j].y);
-        // w = wx wy (1 + x/4 + y/4); the three sub-quadrangle maps of the reference
-        const df w = df_mul(df_mul(wx, wy), df_add_f(df_mul_f(df_add(x, y), 0.25f), 1.0f));
-        const df xy = df_mul(x, y);
-        const df z1 = df_mul_f(df_add(df_add_f(df_mul_f(df_add(x, y), 2.0f), 3.0f), xy), 0.125f);
-        const df e1 = df_mul_f(df_mul(s3, df_sub(y, x)), 0.125f);
-        const df z2 = df_mul_f(df_sub(df_add_f(df_sub(x, df_mul_f(y, 5.0f)), -3.0f), xy), 0.0625f);
-        const df e2 = df_mul_f(df_mul(s3, df_add(df_add_f(df_add(df_mul_f(x, 3.0f), y), 3.0f), xy)), 0.0625f);
-        const df z3 = df_mul_f(df_sub(df_add_f(df_sub(y, df_mul_f(x, 5.0f)), -3.0f), xy), 0.0625f);
-        const df e3 = df_mul_f(df_mul(s3, df_sub(df_add_f(df_neg(df_add(x, df_mul_f(y, 3.0f))), -3.0f), xy)), 0.0625f);
-        reg_point_df(P, false, z1, e1, w, A);
-        reg_point_df(P, false, z2, e2, w, A);
-        reg_point_df(P, false, z3, e3, w, A);
-      }
-    }
-  }
-  const double sh = sd < 0 ? -S0 : S0;
-  const double s3n = S.quad ? 1.0 : 1.0 / 3.0;
-  const double dF0 = df_to(A.dF[0]) * sh, dF1 = df_to(A.dF[1]) * sh;
-  if (!(fabs(dF0) <= GB_CBD_SDF - 0.05 && fabs(dF1) <= GB_CBD_SDF - 0.05)) {
+  RegAcc<2> D;
+  if (!reg_integrate_dn<2>(S, rt, vt, a.k, sd < 0, D)) {
     redo[p] = 1;
     return;
   }
-  RegAcc<2> D;
-  const cplx eS = E0 * (S0 * s3n), eH = E0 * (sh * s3n), eDG = E0 * (-S0 * s3n);
-#pragma unroll
-  for (int n = 0; n < 4; n++) {
-    D.G[n] = cmk(df_to(A.G[n].re), df_to(A.G[n].im)) * eS;
-    D.H[n] = cmk(df_to(A.H[n].re), df_to(A.H[n].im)) * eH;
-    for (int q = 0; q < 2; q++) {
-      D.dG[q][n] = cmk(df_to(A.dG[q][n].re), df_to(A.dG[q][n].im)) * eDG;
-      D.dH[q][n] = cmk(df_to(A.dH[q][n].re), df_to(A.dH[q][n].im)) * eH;
-    }
-  }
-  D.F = df_to(A.F) * sh;
-  D.dF[0] = dF0;
-  D.dF[1] = dF1;
   store_pair(a, N, row, sidx, D);
 }
 
@@ -1072,23 +906,8 @@ extern "C" int gbi_upload_tables_asm(const void* t) {
   GbTablesF f;
   for (int i = 0; i < GB_GLN; i++) { f.xli[i] = (float)d->xli[i]; f.wli[i] = (float)d->wli[i]; }
   GB_CUDA(cudaMemcpyToSymbol(c_tabf, &f, sizeof(GbTablesF)));
-  GbTablesD g;
-  for (int i = 0; i < GB_GLN; i++) {
-    g.x[i].x = (float)d->xli[i];
-    g.x[i].y = (float)(d->xli[i] - (double)g.x[i].x);
-    g.w[i].x = (float)d->wli[i];
-    g.w[i].y = (float)(d->wli[i] - (double)g.w[i].x);
-  }
-  for (int i = 0; i < GB_GHN; i++) {
-    g.xh[i].x = (float)d->xhi[i];
-    g.xh[i].y = (float)(d->xhi[i] - (double)g.xh[i].x);
-    g.wh[i].x = (float)d->whi[i];
-    g.wh[i].y = (float)(d->whi[i] - (double)g.wh[i].x);
-  }
-  GB_CUDA(cudaMemcpyToSymbol(c_tabd, &g, sizeof(GbTablesD)));
-  return 0;
+  return gbi_upload_tabd(d);
 }
-
 // ==================================================================== no allocation
 // Allocation-free variant of the domain assembly (gb_assemble_domain_noalloc
 // in gb_bem.h).  Some callers cannot allocate device memory: an application

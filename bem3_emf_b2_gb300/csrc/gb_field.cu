@@ -12,14 +12,24 @@
 // boundary-integral sums (lanes over source elements).  A lane whose pair needs the GHN fallback
 // (|Re dF/dv| > CBD_SDF, d3b1_elem.c:296,314) gets it integrated by the whole
 // warp.
-#include "gb_quad.cuh"
+#include "gb_quad_df.cuh"
 #include "gb_reduce.cuh"
 #include "gb_internal.h"
 #include "gb_fieldobj.cuh"
 
 extern "C" int gbi_upload_tables_field(const void* t) {
   GB_CUDA(cudaMemcpyToSymbol(c_tab, t, sizeof(GbTables)));
-  return 0;
+  return gbi_upload_tabd((const GbTables*)t);
+}
+
+// the regular integral of one (point, source element) pair: in double-float
+// when DF and the rule is GLN (falling back to FP64 near the CBD_SDF
+// decision), else FP64 -- the same values to ~1e-14
+template <bool DF, int NDIR>
+__device__ __forceinline__ void reg_pair(const Elem& S, int type, const double rt[3], const double (*vt)[3], cplx k,
+                                         bool neg, RegAcc<NDIR>& A) {
+  if (DF && type == 2 && reg_integrate_dn<NDIR>(S, rt, vt, k, neg, A)) return;
+  reg_integrate<NDIR>(S, type, rt, vt, k, neg, A);
 }
 
 // ------------------------------------------------------------------ domain id
@@ -148,6 +158,7 @@ struct FieldArgs {
 
 // one warp per point; the point's domain (and therefore its source list and
 // wave number) is uniform across the warp
+template <bool DF>
 __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
   const int lane = threadIdx.x & 31;
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -179,7 +190,7 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
     if (a.mode == FM_MEMP || a.mode == FM_EH) {
       if (!act) continue;
       RegAcc<0> A;
-      reg_integrate<0>(S, a.type, rt, nullptr, k, neg, A);
+      reg_pair<DF, 0>(S, a.type, rt, nullptr, k, neg, A);
       acc[0] += A.F;
       if (a.mode == FM_MEMP) {
         for (int n = 0; n < 4; n++)
@@ -205,7 +216,7 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
       RegAcc<1> A;
       bool fb = false;
       if (act) {
-        reg_integrate<1>(S, a.type, rt, vt, k, neg, A);
+        reg_pair<DF, 1>(S, a.type, rt, vt, k, neg, A);
         fb = a.type < 3 && fabs(A.dF[0]) > GB_CBD_SDF;
       }
       warp_fallback<1>(fb, S, rt, vt, k, neg, A);
@@ -247,6 +258,7 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
 // FM_EH_MEMP (reference EH_mEMP_s): U and the x,y,z derivatives of all four
 // potential components; separate kernel because it needs 2 + 3 + 8 + 24
 // accumulators.
+template <bool DF>
 __global__ void __launch_bounds__(128) k_field_eh_memp(FieldArgs a) {
   const int lane = threadIdx.x & 31;
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -274,7 +286,7 @@ __global__ void __launch_bounds__(128) k_field_eh_memp(FieldArgs a) {
     RegAcc<3> A;
     bool fb[3] = {false, false, false};
     if (act) {
-      reg_integrate<3>(S, a.type, rt, vt, k, neg, A);
+      reg_pair<DF, 3>(S, a.type, rt, vt, k, neg, A);
       if (a.type < 3)
         for (int d = 0; d < 3; d++) fb[d] = fabs(A.dF[d]) > GB_CBD_SDF;
     }
@@ -339,6 +351,7 @@ struct BdArgs {
   cplx* out;         // [n][6]: E, H
 };
 
+template <bool DF>
 __global__ void __launch_bounds__(128) k_field_bd(BdArgs a) {
   const int lane = threadIdx.x & 31;
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -370,7 +383,7 @@ __global__ void __launch_bounds__(128) k_field_bd(BdArgs a) {
     Elem S;
     load_elem(S, o.cr, o.cw, o.etype, abs(sd));
     RegAcc<0> A;
-    reg_integrate<0>(S, a.type, rt, nullptr, k, sd < 0, A);
+    reg_pair<DF, 0>(S, a.type, rt, nullptr, k, sd < 0, A);
     acc[0] += A.F;
     for (int n = 0; n < 4; n++)
       for (int l = 0; l < 3; l++) {
@@ -438,6 +451,7 @@ struct CrossArgs {
   double* Fp;        // [n][2]: F, dF
 };
 
+template <bool DF>
 __global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
   const int lane = threadIdx.x & 31;
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -461,7 +475,7 @@ __global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
     RegAcc<1> A;
     bool fb = false;
     if (act) {
-      reg_integrate<1>(S, a.type, rt, vt, k, neg, A);
+      reg_pair<DF, 1>(S, a.type, rt, vt, k, neg, A);
       fb = a.type < 3 && fabs(A.dF[0]) > GB_CBD_SDF;
     }
     warp_fallback<1>(fb, S, rt, vt, k, neg, A);
@@ -526,7 +540,8 @@ extern "C" int gbi_cross_build(const FieldObj* o, int type, int n, const double*
   CrossArgs a;
   a.o = *o; a.type = type; a.n = n; a.C = C; a.rt = rt; a.v = v;
   a.Gm = Gm; a.Hm = Hm; a.dGm = dGm; a.dHm = dHm; a.Fp = Fp;
-  k_cross_build<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(a);
+  if (o->prec == 2) k_cross_build<true><<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(a);
+  else k_cross_build<false><<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
@@ -564,8 +579,14 @@ extern "C" int gbi_field(const FieldObj* o, int mode, int type, int n, const dou
   a.out = out;
   a.flag = flag;
   unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
-  if (mode == FM_EH_MEMP) k_field_eh_memp<<<nb, 128, 0, st>>>(a);
-  else k_field<<<nb, 128, 0, st>>>(a);
+  const bool dfp = o->prec == 2;
+  if (mode == FM_EH_MEMP) {
+    if (dfp) k_field_eh_memp<true><<<nb, 128, 0, st>>>(a);
+    else k_field_eh_memp<false><<<nb, 128, 0, st>>>(a);
+  } else {
+    if (dfp) k_field<true><<<nb, 128, 0, st>>>(a);
+    else k_field<false><<<nb, 128, 0, st>>>(a);
+  }
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
@@ -583,7 +604,8 @@ extern "C" int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, 
   a.zt = zt;
   a.out = out;
   unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
-  k_field_bd<<<nb, 128, 0, st>>>(a);
+  if (o->prec == 2) k_field_bd<true><<<nb, 128, 0, st>>>(a);
+  else k_field_bd<false><<<nb, 128, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;

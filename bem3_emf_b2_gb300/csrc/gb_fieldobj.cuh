@@ -22,5 +22,6 @@ struct FieldObj {
   const cplx* H[GB_MAXDOM];
   const cplx* dH[GB_MAXDOM];
   double lambda0;
+  int prec;  // 2: regular GLN pairs in double-float (gb_quad_df.cuh), else FP64
 };
 

@@ -72,7 +72,10 @@ int gb_assemble(gb_obj *o, int did, int type);
  * precision 2: regular pairs in double-float (two FP32 numbers, ~48 bits),
  * pairs that need the GHN fallback and the singular elements in FP64.  The
  * matrices agree with precision 0 to ~1e-14 relative Frobenius (rounding
- * level); the chosen scene form uses it.
+ * level); the chosen scene form uses it.  The object's field kernels
+ * (gb_field_points, gb_field_bd, gb_add_scattered) then integrate their
+ * regular GLN pairs in double-float too; any other precision sets them back
+ * to FP64.
  * precision 1: regular pairs farther than three element radii in FP32
  * relative to the source element's centre (FP64 phase at the centre).
  * Matrix entries then carry ~1e-7 relative error (measured: G 9e-8, dH 2e-7,

@@ -151,3 +151,68 @@ def test_butterfly_lu_matches_tournament_lu(case, gb_build, tmp_path):
     sc.close()
     d = np.linalg.norm(np.concatenate([F1 - F0, N1 - N0])) / np.linalg.norm(np.concatenate([F0, N0]))
     assert d <= 1e-11, "butterfly vs tournament LU, force/torque %g" % d
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["sphere2", "cone_mix"])
+def test_double_float_field_kernels_match_fp64(case, gb_build, tmp_path):
+    """After a precision-2 assembly the object's field kernels (potentials and
+    fields at points: modes 0-3; fields on the boundary) integrate the regular
+    GLN pairs in double-float.  With the same boundary values they must give
+    the FP64 kernels' values to <= 1e-11 relative (vector norm)."""
+    import ctypes
+    from bem3_emf_b2_gb300 import Scene, lib
+    L = lib()
+    vp, ci = ctypes.c_void_p, ctypes.c_int
+    L.gb_assemble2.argtypes = [vp, ci, ci, ci]
+    L.gb_assemble2.restype = ci
+    L.gb_domain_id.argtypes = [vp, ci, vp, vp]
+    L.gb_domain_id.restype = ci
+    L.gb_field_points.argtypes = [vp, ci, ci, ci, vp, vp, vp, vp, vp]
+    L.gb_field_points.restype = ci
+    L.gb_field_bd.argtypes = [vp, ci, ci, vp, vp, vp, vp]
+    L.gb_field_bd.restype = ci
+    meta, _ = load_case(case)
+    wd = str(tmp_path)
+    write_inputs(meta, wd)
+    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+    o = sc.obj()
+    sc.step(form=0)  # boundary values; the field kernels are FP64 after a precision-0 assembly
+    rng = np.random.default_rng(5)
+    n = 256
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d, axis=1)[:, None]
+    rt = np.ascontiguousarray(d * rng.uniform(0.3, 3.0, n)[:, None])
+    v = np.ascontiguousarray(rng.standard_normal((n, 3)))
+    did = np.zeros(n, np.int32)
+    assert L.gb_domain_id(o, n, rt.ctypes.data, did.ctypes.data) == 0, L.gb_last_error()
+    keep = did >= 0
+    rt, v, did = np.ascontiguousarray(rt[keep]), np.ascontiguousarray(v[keep]), np.ascontiguousarray(did[keep])
+    n = len(did)
+    ne = meta["sb_Ne"][0]
+    t = np.ascontiguousarray(rng.integers(1, ne + 1, 64).astype(np.int32))
+    zt = np.ascontiguousarray(rng.uniform(-0.3, 0.3, (64, 2)))
+    dbd = np.zeros(64, np.int32)
+
+    def fields():
+        res = []
+        for mode, width in ((0, 4), (1, 6), (2, 6), (3, 8)):
+            out = np.zeros((n, width), complex)
+            flag = np.zeros(n, np.int32)
+            assert L.gb_field_points(o, mode, 2, n, rt.ctypes.data, v.ctypes.data, did.ctypes.data, out.ctypes.data,
+                                     flag.ctypes.data) == 0, L.gb_last_error()
+            res.append(out)
+        out = np.zeros((64, 6), complex)
+        assert L.gb_field_bd(o, 2, 64, dbd.ctypes.data, t.ctypes.data, zt.ctypes.data, out.ctypes.data) == 0, \
+            L.gb_last_error()
+        res.append(out)
+        return res
+    f64 = fields()
+    for dd in range(len(meta["sb_Ne"])):
+        assert L.gb_assemble2(o, dd, 2, 2) == 0, L.gb_last_error()
+    fdf = fields()
+    sc.close()
+    for a, b in zip(fdf, f64):
+        err = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert err <= 1e-11, err
+        assert np.array_equal(a == 0, b == 0)  # the same near-boundary cutoffs
