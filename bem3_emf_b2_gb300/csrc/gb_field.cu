@@ -449,6 +449,11 @@ struct CrossArgs {
   cplx* dGm;
   cplx* dHm;
   double* Fp;        // [n][2]: F, dF
+  // two-pass build (double-float first): only the pairs flagged in `only`
+  // ([n][Ne]) are integrated, and their F, dF go to Fs ([n][Ne][2]) instead
+  // of the per-point sums
+  const uint8_t* only;
+  double* Fs;
 };
 
 template <bool DF>
@@ -472,14 +477,19 @@ __global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
     Elem S;
     load_elem(S, o.cr, o.cw, o.etype, abs(sd));
     const bool neg = sd < 0;
+    const bool todo = act && (!a.only || a.only[(size_t)p * Ne + s - 1]);
     RegAcc<1> A;
     bool fb = false;
-    if (act) {
+    if (todo) {
       reg_pair<DF, 1>(S, a.type, rt, vt, k, neg, A);
       fb = a.type < 3 && fabs(A.dF[0]) > GB_CBD_SDF;
     }
     warp_fallback<1>(fb, S, rt, vt, k, neg, A);
-    if (!act) continue;
+    if (!todo) continue;
+    if (a.Fs) {
+      a.Fs[((size_t)p * Ne + s - 1) * 2] = A.F;
+      a.Fs[((size_t)p * Ne + s - 1) * 2 + 1] = A.dF[0];
+    }
     F += A.F;
     dF += A.dF[0];
     const size_t c = row + (size_t)(s - 1) * 4;
@@ -494,7 +504,53 @@ __global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
     F += __shfl_down_sync(0xffffffffu, F, o2);
     dF += __shfl_down_sync(0xffffffffu, dF, o2);
   }
-  if (lane == 0) { a.Fp[2 * p] = F; a.Fp[2 * p + 1] = dF; }
+  if (lane == 0 && !a.Fs) { a.Fp[2 * p] = F; a.Fp[2 * p + 1] = dF; }
+}
+
+// double-float pass of the two-pass build: one thread per (point, source
+// element) pair, the GLN rule in double-float (reg_integrate_dn); pairs it
+// declines (near the CBD_SDF decision) are flagged for the FP64 pass
+__global__ void __launch_bounds__(128) k_cross_build_df(CrossArgs a, uint8_t* redo) {
+  const FieldObj& o = a.o;
+  const int Ne = o.sb_Ne[0];
+  const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= (size_t)a.n * Ne) return;
+  const int p = (int)(q / Ne), s = 1 + (int)(q % Ne);
+  const double rt[3] = {a.rt[3 * p], a.rt[3 * p + 1], a.rt[3 * p + 2]};
+  const double vt[1][3] = {{a.v[3 * p], a.v[3 * p + 1], a.v[3 * p + 2]}};
+  const cplx k = cmk(o.kn[0], o.kn[1]);
+  const int sd = o.sid[o.sb_off[0] + s];
+  Elem S;
+  load_elem(S, o.cr, o.cw, o.etype, abs(sd));
+  RegAcc<1> A;
+  if (!reg_integrate_dn<1>(S, rt, vt, k, sd < 0, A)) {
+    redo[q] = 1;
+    return;
+  }
+  redo[q] = 0;
+  const size_t c = (size_t)p * a.C + (size_t)(s - 1) * 4;
+#pragma unroll
+  for (int nn = 0; nn < 4; nn++) {
+    a.Gm[c + nn] = A.G[nn];
+    a.Hm[c + nn] = A.H[nn];
+    a.dGm[c + nn] = A.dG[0][nn];
+    a.dHm[c + nn] = A.dH[0][nn];
+  }
+  a.Fs[2 * q] = A.F;
+  a.Fs[2 * q + 1] = A.dF[0];
+}
+
+// per point: F, dF summed over the source elements in their order
+__global__ void k_cross_fsum(int n, int Ne, const double* Fs, double* Fp) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= n) return;
+  double F = 0.0, dF = 0.0;
+  for (int s = 0; s < Ne; s++) {
+    F += Fs[((size_t)p * Ne + s) * 2];
+    dF += Fs[((size_t)p * Ne + s) * 2 + 1];
+  }
+  Fp[2 * p] = F;
+  Fp[2 * p + 1] = dF;
 }
 
 // one warp per point: out[p][0..3] = u, out[p][4..7] = du (layout of k_field's mode 3)
@@ -540,8 +596,31 @@ extern "C" int gbi_cross_build(const FieldObj* o, int type, int n, const double*
   CrossArgs a;
   a.o = *o; a.type = type; a.n = n; a.C = C; a.rt = rt; a.v = v;
   a.Gm = Gm; a.Hm = Hm; a.dGm = dGm; a.dHm = dHm; a.Fp = Fp;
-  if (o->prec == 2) k_cross_build<true><<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(a);
-  else k_cross_build<false><<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(a);
+  a.only = nullptr; a.Fs = nullptr;
+  const unsigned nbw = (unsigned)(((size_t)n * 32 + 127) / 128);
+  const int Ne = o->sb_Ne[0];
+  if (o->prec == 2 && type == 2 && Ne > 0) {
+    // double-float pass over all pairs, FP64 pass over the declined ones,
+    // then the per-point sums in element order
+    const size_t np = (size_t)n * Ne;
+    uint8_t* redo = nullptr;
+    double* Fs = nullptr;
+    GB_CUDA(cudaMallocAsync((void**)&redo, np, st));
+    GB_CUDA(cudaMallocAsync((void**)&Fs, np * 2 * sizeof(double), st));
+    a.Fs = Fs;
+    k_cross_build_df<<<(unsigned)((np + 127) / 128), 128, 0, st>>>(a, redo);
+    gbi_count_launch();
+    a.only = redo;
+    k_cross_build<false><<<nbw, 128, 0, st>>>(a);
+    gbi_count_launch();
+    k_cross_fsum<<<(n + 127) / 128, 128, 0, st>>>(n, Ne, Fs, Fp);
+    gbi_count_launch();
+    GB_CUDA(cudaGetLastError());
+    cudaFreeAsync(redo, st);
+    cudaFreeAsync(Fs, st);
+    return 0;
+  }
+  k_cross_build<false><<<nbw, 128, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
