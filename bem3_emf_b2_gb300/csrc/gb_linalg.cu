@@ -353,14 +353,27 @@ template <class T, int UPPER>
 __global__ void __launch_bounds__(256) k_trsm_rows(const T* Lsrc, size_t ldl, T* X, size_t ldx, int nb, int c0,
                                                    int c1) {
   extern __shared__ __align__(16) unsigned char sLraw[];
-  const int ld = nb + 1;
+  // lower: the strictly lower triangle zero-padded to LU_NB x LU_NB (no
+  // predicates in the substitution); upper: the nb x nb triangle
+  const int ld = UPPER ? nb + 1 : LU_NB + 1;
   T* sT = (T*)sLraw;           // sT[j * ld + i] = triangle[i][j]
-  T* dinv = sT + nb * ld;      // LU_NB
+  T* dinv = sT + (UPPER ? nb : LU_NB) * ld;  // LU_NB
   T* Xs = dinv + LU_NB;        // LU_NB x (TRSM_COLS + 1)
   constexpr int XL = TRSM_COLS + 1;
-  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
-    int i = t / nb, j = t % nb;
-    sT[j * ld + i] = Lsrc[(size_t)i * ldl + j];
+  if (UPPER) {
+    for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) {
+      int i = t / nb, j = t % nb;
+      sT[j * ld + i] = Lsrc[(size_t)i * ldl + j];
+    }
+  } else {
+    for (int t = threadIdx.x; t < LU_NB * LU_NB; t += blockDim.x) {
+      const int i = t / LU_NB, j = t % LU_NB;
+      T v;
+      v.x = 0;
+      v.y = 0;
+      if (i > j && i < nb) v = Lsrc[(size_t)i * ldl + j];
+      sT[j * ld + i] = v;
+    }
   }
   const int cb = c0 + blockIdx.x * TRSM_COLS;
   for (int t = threadIdx.x; t < nb * TRSM_COLS; t += blockDim.x) {
@@ -377,7 +390,49 @@ __global__ void __launch_bounds__(256) k_trsm_rows(const T* Lsrc, size_t ldl, T*
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
   const int i0 = lane, i1 = lane + 32;
-  for (int c = w; c < TRSM_COLS; c += nw) {
+  if (!UPPER) {
+    // two columns per warp (two independent chains); the second half of the
+    // steps touches only rows 32..63
+    for (int c = w; c < TRSM_COLS; c += 2 * nw) {
+      const int cB = c + nw;
+      if (cb + c >= c1) break;  // warp-uniform
+      const bool okB = cB < TRSM_COLS && cb + cB < c1;
+      T zero;
+      zero.x = 0;
+      zero.y = 0;
+      T xa0 = i0 < nb ? Xs[i0 * XL + c] : zero, xa1 = i1 < nb ? Xs[i1 * XL + c] : zero;
+      T xb0 = (okB && i0 < nb) ? Xs[i0 * XL + cB] : zero, xb1 = (okB && i1 < nb) ? Xs[i1 * XL + cB] : zero;
+#pragma unroll 8
+      for (int j = 0; j < 32; j++) {
+        T va, vb;
+        va.x = __shfl_sync(0xffffffffu, xa0.x, j);
+        va.y = __shfl_sync(0xffffffffu, xa0.y, j);
+        vb.x = __shfl_sync(0xffffffffu, xb0.x, j);
+        vb.y = __shfl_sync(0xffffffffu, xb0.y, j);
+        const T l0 = sT[j * ld + i0], l1 = sT[j * ld + i1];
+        xa0 -= l0 * va;
+        xa1 -= l1 * va;
+        xb0 -= l0 * vb;
+        xb1 -= l1 * vb;
+      }
+#pragma unroll 8
+      for (int j = 32; j < LU_NB; j++) {
+        T va, vb;
+        va.x = __shfl_sync(0xffffffffu, xa1.x, j - 32);
+        va.y = __shfl_sync(0xffffffffu, xa1.y, j - 32);
+        vb.x = __shfl_sync(0xffffffffu, xb1.x, j - 32);
+        vb.y = __shfl_sync(0xffffffffu, xb1.y, j - 32);
+        const T l1 = sT[j * ld + i1];
+        xa1 -= l1 * va;
+        xb1 -= l1 * vb;
+      }
+      if (i0 < nb) Xs[i0 * XL + c] = xa0;
+      if (i1 < nb) Xs[i1 * XL + c] = xa1;
+      if (okB && i0 < nb) Xs[i0 * XL + cB] = xb0;
+      if (okB && i1 < nb) Xs[i1 * XL + cB] = xb1;
+    }
+  }
+  for (int c = w; c < TRSM_COLS && UPPER; c += nw) {
     if (cb + c >= c1) break;  // warp-uniform
     T x0, x1;
     x0.x = 0; x0.y = 0; x1 = x0;
@@ -492,7 +547,8 @@ static int gemm_sub(int M, int N, int K, const cplx* A, size_t lda, const cplx* 
 template <class T>
 static int trsm_rows(int upper, const T* L, size_t ldl, T* X, size_t ldx, int nb, int c0, int c1, cudaStream_t st) {
   if (c1 <= c0) return 0;
-  size_t sm = ((size_t)nb * (nb + 1) + LU_NB + (size_t)LU_NB * (TRSM_COLS + 1)) * sizeof(T);
+  const size_t tri = upper ? (size_t)nb * (nb + 1) : (size_t)LU_NB * (LU_NB + 1);
+  size_t sm = (tri + LU_NB + (size_t)LU_NB * (TRSM_COLS + 1)) * sizeof(T);
   unsigned nblk = (unsigned)((c1 - c0 + TRSM_COLS - 1) / TRSM_COLS);
   if (upper) {
     GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -512,6 +568,7 @@ static int trsm_rows(int upper, const T* L, size_t ldl, T* X, size_t ldx, int nb
 #define TS_ROWS (TS_ARITY * LU_NB)   // rows of a leaf set and of a merge
 #define TS_THREADS 1024              // elimination blocks: 32 warps, 8 rows each
 #define PANEL_THREADS 256
+#define DIAG_THREADS 1024            // k_diag_lu: 32 warps, two rows of the block each
 
 __device__ __forceinline__ cplxf to_c64(cplx a) { return cmkf((float)a.x, (float)a.y); }
 __device__ __forceinline__ cplxf to_c64(cplxf a) { return a; }
@@ -724,7 +781,7 @@ __global__ void k_laswp_rows(T* A, size_t lda, int ncol, int k, int nb, const in
 // L11 U11 = A[k:k+nb][k:k+nb] in place, without interchanges; info[0] = k + j + 1
 // at the first exactly zero pivot (LAPACK's convention)
 template <class T>
-__global__ void __launch_bounds__(PANEL_THREADS) k_diag_lu(T* A, size_t lda, int k, int nb, int* info) {
+__global__ void __launch_bounds__(DIAG_THREADS) k_diag_lu(T* A, size_t lda, int k, int nb, int* info) {
   extern __shared__ __align__(16) unsigned char tsraw[];
   T* M = (T*)tsraw;
   const int ld = nb + 1;
@@ -732,7 +789,7 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_diag_lu(T* A, size_t lda, int
   __syncthreads();
   T one, zero;
   one.x = 1; one.y = 0; zero.x = 0; zero.y = 0;
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = PANEL_THREADS / 32;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = DIAG_THREADS / 32;
   const int c0 = lane, c1 = lane + 32;
   for (int j = 0; j < nb; j++) {
     const T piv = M[j * ld + j];
@@ -757,43 +814,77 @@ __global__ void __launch_bounds__(PANEL_THREADS) k_diag_lu(T* A, size_t lda, int
 }
 
 // rows [r0, r1), columns k..k+nb-1: X <- X U11^-1 (U11 non-unit upper of
-// A[k:k+nb][k:k+nb]); one warp per row, lane l holds columns l and l + 32
+// A[k:k+nb][k:k+nb]).  Column-oriented substitution per row with the rows of
+// U11 pre-divided by their diagonal and zero-padded to 64 x 64 in shared
+// memory (W[j][c] = U[j][c] / U[j][j] for j < c < nb, else 0): at step j every
+// lane subtracts a_j W[j][c] from its columns without a predicate, and a_j
+// stays untouched from step j on, so x_j = a_j / U[j][j] is applied once at
+// the end.  A warp holds two rows (lanes: columns l and l + 32), two
+// independent chains; the second half of the steps touches only the upper
+// 32 columns.
 template <class T>
 __global__ void __launch_bounds__(PANEL_THREADS) k_trsm_right(T* A, size_t lda, int k, int nb, int r0, int r1) {
   extern __shared__ __align__(16) unsigned char tsraw[];
-  T* U = (T*)tsraw;  // nb x nb
-  T* dinv = U + nb * nb;
-  for (int t = threadIdx.x; t < nb * nb; t += blockDim.x) U[t] = A[(size_t)(k + t / nb) * lda + k + t % nb];
+  T* W = (T*)tsraw;  // LU_NB x LU_NB
+  T* dinv = W + LU_NB * LU_NB;
+  T zero;
+  zero.x = 0;
+  zero.y = 0;
+  for (int t = threadIdx.x; t < LU_NB * LU_NB; t += blockDim.x) {
+    const int j = t / LU_NB, c = t % LU_NB;
+    W[t] = (j < nb && c < nb) ? A[(size_t)(k + j) * lda + k + c] : zero;
+  }
   __syncthreads();
-  for (int j = threadIdx.x; j < nb; j += blockDim.x) {
-    T d = U[j * nb + j];
+  for (int j = threadIdx.x; j < LU_NB; j += blockDim.x) {
+    const T d = W[j * LU_NB + j];
     T one;
     one.x = 1;
     one.y = 0;
-    dinv[j] = (d.x == 0 && d.y == 0) ? d : cdivc(one, d);
+    dinv[j] = (j >= nb || (d.x == 0 && d.y == 0)) ? zero : cdivc(one, d);
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < LU_NB * LU_NB; t += blockDim.x) {
+    const int j = t / LU_NB, c = t % LU_NB;
+    W[t] = (c > j) ? W[t] * dinv[j] : zero;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
-  for (int r = r0 + blockIdx.x * wpb + (threadIdx.x >> 5); r < r1; r += gridDim.x * wpb) {
-    T* row = A + (size_t)r * lda + k;
-    T a0, a1;
-    a0.x = 0; a0.y = 0; a1 = a0;
-    if (lane < nb) a0 = row[lane];
-    if (lane + 32 < nb) a1 = row[lane + 32];
-    for (int j = 0; j < nb; j++) {
-      const int owner = j & 31;
-      T v = (j < 32) ? a0 : a1;
-      T x;
-      x.x = __shfl_sync(0xffffffffu, v.x, owner);
-      x.y = __shfl_sync(0xffffffffu, v.y, owner);
-      x = x * dinv[j];
-      if (lane == owner) { if (j < 32) a0 = x; else a1 = x; }
-      if (lane > j && lane < nb) a0 -= x * U[j * nb + lane];
-      if (lane + 32 > j && lane + 32 < nb) a1 -= x * U[j * nb + lane + 32];
+  const int stride = 2 * gridDim.x * wpb;
+  for (int r = r0 + 2 * (blockIdx.x * wpb + (threadIdx.x >> 5)); r < r1; r += stride) {
+    const bool hasB = r + 1 < r1;
+    T* rowA = A + (size_t)r * lda + k;
+    T* rowB = rowA + lda;
+    T a0 = zero, a1 = zero, b0 = zero, b1 = zero;
+    if (lane < nb) { a0 = rowA[lane]; if (hasB) b0 = rowB[lane]; }
+    if (lane + 32 < nb) { a1 = rowA[lane + 32]; if (hasB) b1 = rowB[lane + 32]; }
+#pragma unroll 8
+    for (int j = 0; j < 32; j++) {
+      T va, vb;
+      va.x = __shfl_sync(0xffffffffu, a0.x, j);
+      va.y = __shfl_sync(0xffffffffu, a0.y, j);
+      vb.x = __shfl_sync(0xffffffffu, b0.x, j);
+      vb.y = __shfl_sync(0xffffffffu, b0.y, j);
+      const T w0 = W[j * LU_NB + lane], w1 = W[j * LU_NB + lane + 32];
+      a0 -= va * w0;
+      a1 -= va * w1;
+      b0 -= vb * w0;
+      b1 -= vb * w1;
     }
-    if (lane < nb) row[lane] = a0;
-    if (lane + 32 < nb) row[lane + 32] = a1;
+#pragma unroll 8
+    for (int j = 32; j < LU_NB; j++) {
+      T va, vb;
+      va.x = __shfl_sync(0xffffffffu, a1.x, j - 32);
+      va.y = __shfl_sync(0xffffffffu, a1.y, j - 32);
+      vb.x = __shfl_sync(0xffffffffu, b1.x, j - 32);
+      vb.y = __shfl_sync(0xffffffffu, b1.y, j - 32);
+      const T w1 = W[j * LU_NB + lane + 32];
+      a1 -= va * w1;
+      b1 -= vb * w1;
+    }
+    const T d0 = dinv[lane], d1 = dinv[lane + 32];
+    if (lane < nb) { rowA[lane] = a0 * d0; if (hasB) rowB[lane] = b0 * d0; }
+    if (lane + 32 < nb) { rowA[lane + 32] = a1 * d1; if (hasB) rowB[lane + 32] = b1 * d1; }
   }
 }
 
@@ -822,7 +913,7 @@ static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStre
   GB_CUDA(cudaMallocAsync((void**)&cand, sizeof(int) * (size_t)2 * nsets0 * LU_NB, st));
   GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), st));
   const size_t sm_diag = (size_t)LU_NB * (LU_NB + 1) * sizeof(T);
-  const size_t sm_right = (size_t)LU_NB * LU_NB * sizeof(T) + LU_NB * sizeof(T);
+  const size_t sm_right = (size_t)LU_NB * LU_NB * sizeof(T) + LU_NB * sizeof(T);  // W, dinv
   int rc = 0;
   int dev = 0, nsm = 0;
   GB_CUDA(cudaGetDevice(&dev));
@@ -850,12 +941,12 @@ static int lu_factor(T* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStre
       k_laswp_rows<T><<<(n + 255) / 256, 256, 0, st>>>(A, lda, n, k, nb, ipiv);
       gbi_count_launch();
     }
-    k_diag_lu<T><<<1, PANEL_THREADS, sm_diag, st>>>(A, lda, k, nb, info);
+    k_diag_lu<T><<<1, DIAG_THREADS, sm_diag, st>>>(A, lda, k, nb, info);
     gbi_count_launch();
     if (kend < n) {
       int rows = n - kend;
       int wpb = PANEL_THREADS / 32;
-      int nblk = (rows + wpb - 1) / wpb;
+      int nblk = (rows + 2 * wpb - 1) / (2 * wpb);
       if (nblk > 2 * nsm) nblk = 2 * nsm;
       k_trsm_right<T><<<nblk, PANEL_THREADS, sm_right, st>>>(A, lda, k, nb, kend, n);
       gbi_count_launch();
