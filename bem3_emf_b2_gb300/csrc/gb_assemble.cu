@@ -404,30 +404,79 @@ __device__ __forceinline__ void singb_zero(SingAccB& B) {
   }
 }
 
-// per-direction geometry of a ray from (zt, et) in direction (cth, sth) of a
+// Per-row constants in double-float, set once per block from the FP64
+// polar decomposition (sing_setup): along a ray in direction (c, s) from
+// (zt, et), K = Ka + Kb r with Ka = a1 c + a2 s (a1 = cr1 + cr3 et,
+// a2 = cr2 + cr3 zt; triangles: cr1, cr2) and Kb = cr3 c s, and
+// W = Wa + (w1 c + w2 s) r; per edge j the end angles t0, t1 with their
+// cosines and sines, the end radii r0, r1 and sin(t1 - t0), so that the
+// distance to the edge along theta, r0 r1 sin(t1 - t0) / (r0 sin(theta - t0)
+// - r1 sin(theta - t1)), needs no further transcendental.
+struct RowD {
+  df a1[3], a2[3], c3[3], Wa[3], w1[3], w2[3], vt[2][3];
+  df zt, et, kr, ki;
+  df t0[4], dt[4], ct0[4], st0[4], ct1[4], st1[4], r0[4], r1[4], sdt[4];
+};
+__device__ void row_setup_df(const SingCtx& c, RowD& R) {
+  const Elem& E = c.E;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (E.quad) {
+      R.a1[d] = df_from(E.cr[d][1] + E.cr[d][3] * c.et);
+      R.a2[d] = df_from(E.cr[d][2] + E.cr[d][3] * c.zt);
+      R.c3[d] = df_from(E.cr[d][3]);
+    } else {
+      R.a1[d] = df_from(E.cr[d][1]);
+      R.a2[d] = df_from(E.cr[d][2]);
+      R.c3[d] = dfmk(0.0f, 0.0f);
+    }
+    R.Wa[d] = df_from(E.cw[d][0] + E.cw[d][1] * c.zt + E.cw[d][2] * c.et);
+    R.w1[d] = df_from(E.cw[d][1]);
+    R.w2[d] = df_from(E.cw[d][2]);
+    R.vt[0][d] = df_from(c.vt[0][d]);
+    R.vt[1][d] = df_from(c.vt[1][d]);
+  }
+  R.zt = df_from(c.zt);
+  R.et = df_from(c.et);
+  R.kr = df_from(c.k.x);
+  R.ki = df_from(c.k.y);
+  for (int j = 0; j < c.nedge; j++) {
+    const double t0 = c.th[j], t1 = c.th[j + 1];
+    R.t0[j] = df_from(t0);
+    R.dt[j] = df_from(t1 - t0);
+    R.ct0[j] = df_from(cos(t0));
+    R.st0[j] = df_from(sin(t0));
+    R.ct1[j] = df_from(cos(t1));
+    R.st1[j] = df_from(sin(t1));
+    R.r0[j] = df_from(c.r[j]);
+    R.r1[j] = df_from(c.r[j + 1]);
+    R.sdt[j] = df_from(sin(t1 - t0));
+  }
+}
+
+// per-direction geometry of a ray from (zt, et) in direction (c, s) of a
 // bilinear element, affine in the distance r: K = Ka + Kb r, W = Wa + Wb r
 struct RayD {
   df Ka[3], Kb[3], Wa[3], Wb[3], vt[2][3];
   df zt, et, c, s, kr, ki;
 };
-__device__ __forceinline__ void ray_geom_df(const SingCtx& c, double cth, double sth, RayD& g) {
-  const Elem& E = c.E;
-  const double zs = c.zt * sth + c.et * cth;
+__device__ __forceinline__ void ray_geom_df(const RowD& R, df cth, df sth, RayD& g) {
+  const df cs = df_mul(cth, sth);
 #pragma unroll
   for (int d = 0; d < 3; d++) {
-    g.Ka[d] = df_from(E.cr[d][1] * cth + E.cr[d][2] * sth + E.cr[d][3] * zs);
-    g.Kb[d] = df_from(E.cr[d][3] * cth * sth);
-    g.Wa[d] = df_from(E.cw[d][0] + E.cw[d][1] * c.zt + E.cw[d][2] * c.et);
-    g.Wb[d] = df_from(E.cw[d][1] * cth + E.cw[d][2] * sth);
-    g.vt[0][d] = df_from(c.vt[0][d]);
-    g.vt[1][d] = df_from(c.vt[1][d]);
+    g.Ka[d] = df_fma(df_mul(R.a1[d], cth), R.a2[d], sth);
+    g.Kb[d] = df_mul(R.c3[d], cs);
+    g.Wa[d] = R.Wa[d];
+    g.Wb[d] = df_fma(df_mul(R.w1[d], cth), R.w2[d], sth);
+    g.vt[0][d] = R.vt[0][d];
+    g.vt[1][d] = R.vt[1][d];
   }
-  g.zt = df_from(c.zt);
-  g.et = df_from(c.et);
-  g.c = df_from(cth);
-  g.s = df_from(sth);
-  g.kr = df_from(c.k.x);
-  g.ki = df_from(c.k.y);
+  g.zt = R.zt;
+  g.et = R.et;
+  g.c = cth;
+  g.s = sth;
+  g.kr = R.kr;
+  g.ki = R.ki;
 }
 // point at signed distance rr (sg = -1: the opposite ray, whose K keeps the
 // +direction terms except the r-term, as the reference's principal-value
@@ -449,11 +498,13 @@ __device__ __forceinline__ void ray_point_df(const RayD& g, df rr, float sg, df 
   N[3] = df_mul_f(df_mul(zm, ep), 0.25f);
 }
 
-static __device__ void sing_bil_setB_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
+static __device__ void sing_bil_setB_df(const SingCtx& c, const RowD& R, df cth, df sth, df rm, df wth,
+                                        SingAcc& A) {
   RayD g;
-  ray_geom_df(c, cth, sth, g);
-  const df hr = df_from(0.5 * (rm - GB_DEPS)), r0 = df_from(0.5 * (rm + GB_DEPS));
-  const df w0 = df_from(wth * 0.5 * (rm - GB_DEPS));
+  ray_geom_df(R, cth, sth, g);
+  const df deps = dfmk(0.1f, -1.4901161415892261e-09f);  // GB_DEPS = 0.1 in double-float
+  const df hr = df_mul_f(df_sub(rm, deps), 0.5f), r0 = df_mul_f(df_add(rm, deps), 0.5f);
+  const df w0 = df_mul(wth, hr);
   const df cs[2] = {g.c, g.s}, outer[2] = {g.s, g.c};
   SingAccB B;
   singb_zero(B);
@@ -499,10 +550,11 @@ static __device__ void sing_bil_setB_df(const SingCtx& c, double cth, double sth
 }
 
 // set A: G, H, F on [0, rm] with the GLN rule (sing_bil_setA)
-static __device__ void sing_bil_setA_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
+static __device__ void sing_bil_setA_df(const SingCtx& c, const RowD& R, df cth, df sth, df rm, df wth,
+                                        SingAcc& A) {
   RayD g;
-  ray_geom_df(c, cth, sth, g);
-  const df hr = df_from(0.5 * rm), w0 = df_from(wth * 0.5 * rm), csn = df_from(cth * sth);
+  ray_geom_df(R, cth, sth, g);
+  const df hr = df_mul_f(rm, 0.5f), w0 = df_mul(wth, hr), csn = df_mul(cth, sth);
   const df zero = dfmk(0.0f, 0.0f);
   dfc Gs[4], Hs[4];
   df Fs = zero;
@@ -539,10 +591,10 @@ static __device__ void sing_bil_setA_df(const SingCtx& c, double cth, double sth
 }
 
 // set C: the disc D_eps, r in [0, DEPS] with the GLN rule (sing_bil_setC)
-static __device__ void sing_bil_setC_df(const SingCtx& c, double cth, double sth, double wth, SingAcc& A) {
+static __device__ void sing_bil_setC_df(const SingCtx& c, const RowD& R, df cth, df sth, df wth, SingAcc& A) {
   RayD g;
-  ray_geom_df(c, cth, sth, g);
-  const df hr = df_from(0.5 * GB_DEPS), w0 = df_from(wth * 0.5 * GB_DEPS);
+  ray_geom_df(R, cth, sth, g);
+  const df hr = df_from(0.5 * GB_DEPS), w0 = df_mul(wth, hr);
   const df cs[2] = {g.c, g.s}, outer[2] = {g.s, g.c};
   const dfc k = dfcmk(g.kr, g.ki), ik = dfcmk(df_neg(g.ki), g.kr);
   const dfc ik3 = dfcmk(df_mul_f(ik.re, 3.0f), df_mul_f(ik.im, 3.0f));
@@ -587,10 +639,10 @@ static __device__ void sing_bil_setC_df(const SingCtx& c, double cth, double sth
 }
 
 // set D: principal-value pairing of +r and -r, r in [0, DEPS] (sing_bil_setD)
-static __device__ void sing_bil_setD_df(const SingCtx& c, double cth, double sth, double wth, SingAcc& A) {
+static __device__ void sing_bil_setD_df(const SingCtx& c, const RowD& R, df cth, df sth, df wth, SingAcc& A) {
   RayD g;
-  ray_geom_df(c, cth, sth, g);
-  const df hr = df_from(0.5 * GB_DEPS), w0 = df_from(wth * 0.5 * GB_DEPS);
+  ray_geom_df(R, cth, sth, g);
+  const df hr = df_from(0.5 * GB_DEPS), w0 = df_mul(wth, hr);
   const df cs[2] = {g.c, g.s}, outer[2] = {g.s, g.c};
   SingAccB B;
   singb_zero(B);
@@ -643,15 +695,15 @@ static __device__ void sing_bil_setD_df(const SingCtx& c, double cth, double sth
 
 // triangle set A: G on [0, rm] with the GLN rule; K is constant along the
 // ray; 3 x the shape functions, the 1/3 applied in FP64
-static __device__ void sing_lit_setA_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
-  const Elem& E = c.E;
-  double K[3];
-  for (int d = 0; d < 3; d++) K[d] = E.cr[d][1] * cth + E.cr[d][2] * sth;
-  const double aK = norm3(K);
-  const df daK = df_from(aK), iaK = df_from(1.0 / aK);
-  const df hr = df_from(0.5 * rm), w0 = df_from(wth * 0.5 * rm);
-  const df dzt = df_from(c.zt), det = df_from(c.et), dc = df_from(cth), ds = df_from(sth);
-  const df kr = df_from(c.k.x), ki = df_from(c.k.y);
+static __device__ void sing_lit_setA_df(const SingCtx& c, const RowD& R, df dc, df ds, df rm, df wth,
+                                        SingAcc& A) {
+  df K[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) K[d] = df_fma(df_mul(R.a1[d], dc), R.a2[d], ds);
+  const df daK = df_sqrt(dot3d(K, K)), iaK = df_rcp(daK);
+  const df hr = df_mul_f(rm, 0.5f), w0 = df_mul(wth, hr);
+  const df dzt = R.zt, det = R.et;
+  const df kr = R.kr, ki = R.ki;
   const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
   const df zero = dfmk(0.0f, 0.0f);
   dfc Gs[3];
@@ -677,17 +729,19 @@ static __device__ void sing_lit_setA_df(const SingCtx& c, double cth, double sth
 
 // triangle: K is constant along the ray; 3 x the shape functions in
 // double-float, the 1/3 applied in FP64
-static __device__ void sing_lit_setB_df(const SingCtx& c, double cth, double sth, double rm, double wth, SingAcc& A) {
-  const Elem& E = c.E;
-  double K[3];
-  for (int d = 0; d < 3; d++) K[d] = E.cr[d][1] * cth + E.cr[d][2] * sth;
-  const double aK = norm3(K), iK = 1.0 / aK;
-  const df kv[2] = {df_from(dot3(K, c.vt[0]) * iK), df_from(dot3(K, c.vt[1]) * iK)};
-  const df daK = df_from(aK), iK2 = df_from(iK * iK);
-  const df hr = df_from(0.5 * (rm - GB_DEPS)), r0 = df_from(0.5 * (rm + GB_DEPS));
-  const df w0 = df_from(wth * 0.5 * (rm - GB_DEPS));
-  const df dzt = df_from(c.zt), det = df_from(c.et), dc = df_from(cth), ds = df_from(sth);
-  const df kr = df_from(c.k.x), ki = df_from(c.k.y);
+static __device__ void sing_lit_setB_df(const SingCtx& c, const RowD& R, df dc, df ds, df rm, df wth,
+                                        SingAcc& A) {
+  df K[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) K[d] = df_fma(df_mul(R.a1[d], dc), R.a2[d], ds);
+  const df daK = df_sqrt(dot3d(K, K)), iK = df_rcp(daK);
+  const df kv[2] = {df_mul(dot3d(K, R.vt[0]), iK), df_mul(dot3d(K, R.vt[1]), iK)};
+  const df iK2 = df_sqr(iK);
+  const df deps = dfmk(0.1f, -1.4901161415892261e-09f);  // GB_DEPS = 0.1 in double-float
+  const df hr = df_mul_f(df_sub(rm, deps), 0.5f), r0 = df_mul_f(df_add(rm, deps), 0.5f);
+  const df w0 = df_mul(wth, hr);
+  const df dzt = R.zt, det = R.et;
+  const df kr = R.kr, ki = R.ki;
   const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
   SingAccB B;
   singb_zero(B);
@@ -718,25 +772,32 @@ static __device__ void sing_lit_setB_df(const SingCtx& c, double cth, double sth
   singb_add(B, A, 3, 1.0 / 3.0);
 }
 
-// sing_item with the point sets in double-float (the triangle's analytic
-// sets C and D stay FP64: one evaluation per direction)
-static __device__ void sing_item_df(const SingCtx& c, int q, SingAcc& A) {
+// sing_item with the point sets in double-float, the directions too: theta,
+// its weight, cos and sin and the distance to the edge from the row's
+// double-float constants (the triangle's analytic sets C and D stay FP64:
+// one evaluation per direction)
+static __device__ void sing_item_df(const SingCtx& c, const RowD& R, int q, SingAcc& A) {
   const int nA = c.nedge * 2 * GB_GHN;
   if (q < 2 * nA) {
     const int setB = q >= nA;
     const int qq = setB ? q - nA : q;
     const int j = qq / (2 * GB_GHN), rem = qq % (2 * GB_GHN);
     const int h = rem / GB_GHN, m = rem % GB_GHN;
-    double th, wth, rm;
-    sing_edge_theta(c, j, h, m, &th, &wth, &rm);
-    double sth, cth;
-    sincos(th, &sth, &cth);
+    const df x = dfmk(c_tabd.xh[m].x, c_tabd.xh[m].y), wx = dfmk(c_tabd.wh[m].x, c_tabd.wh[m].y);
+    // theta = t0 + dt (x/4 + 1/4) (first half of the edge) or + dt (x/4 + 3/4)
+    const df th = df_fma(R.t0[j], R.dt[j], df_add_f(df_mul_f(x, 0.25f), h == 0 ? 0.25f : 0.75f));
+    const df wth = df_mul_f(df_mul(R.dt[j], wx), 0.25f);
+    df sn, cs;
+    df_sincos(th, &sn, &cs);
+    const df den = df_sub(df_mul(R.r0[j], df_fma(df_mul(sn, R.ct0[j]), df_neg(cs), R.st0[j])),
+                          df_mul(R.r1[j], df_fma(df_mul(sn, R.ct1[j]), df_neg(cs), R.st1[j])));
+    const df rm = df_div(df_mul(df_mul(R.r0[j], R.r1[j]), R.sdt[j]), den);
     if (c.E.quad) {
-      if (setB) sing_bil_setB_df(c, cth, sth, rm, wth, A);
-      else sing_bil_setA_df(c, cth, sth, rm, wth, A);
+      if (setB) sing_bil_setB_df(c, R, cs, sn, rm, wth, A);
+      else sing_bil_setA_df(c, R, cs, sn, rm, wth, A);
     } else {
-      if (setB) sing_lit_setB_df(c, cth, sth, rm, wth, A);
-      else sing_lit_setA_df(c, cth, sth, rm, wth, A);
+      if (setB) sing_lit_setB_df(c, R, cs, sn, rm, wth, A);
+      else sing_lit_setA_df(c, R, cs, sn, rm, wth, A);
     }
     return;
   }
@@ -745,24 +806,24 @@ static __device__ void sing_item_df(const SingCtx& c, int q, SingAcc& A) {
     return;
   }
   q -= 2 * nA;
-  if (q < 4 * GB_GHN) {  // set C: theta over (-pi, pi] in four quarters
+  const df qpi = dfmk(0.7853981852531433f, -2.1855694143368964e-08f);  // pi / 4
+  if (q < 4 * GB_GHN) {  // set C: theta over (-pi, pi] in four quarters, centres -3pi/4 .. 3pi/4
     const int quarter = q / GB_GHN, m = q % GB_GHN;
-    const double off[4] = {-0.75 * GB_PI, -0.25 * GB_PI, 0.25 * GB_PI, 0.75 * GB_PI};
-    const double th = 0.25 * GB_PI * c_tab.xhi[m] + off[quarter];
-    const double wth = 0.25 * GB_PI * c_tab.whi[m];
-    double sth, cth;
-    sincos(th, &sth, &cth);
-    sing_bil_setC_df(c, cth, sth, wth, A);
+    const df x = dfmk(c_tabd.xh[m].x, c_tabd.xh[m].y), wx = dfmk(c_tabd.wh[m].x, c_tabd.wh[m].y);
+    const df th = df_mul(qpi, df_add_f(x, (float)(2 * quarter - 3)));
+    df sn, cs;
+    df_sincos(th, &sn, &cs);
+    sing_bil_setC_df(c, R, cs, sn, df_mul(qpi, wx), A);
     return;
   }
   q -= 4 * GB_GHN;
-  {  // set D: theta over (0, pi) in two halves
+  {  // set D: theta over (0, pi) in two halves, centres pi/4 and 3pi/4
     const int half = q / GB_GHN, m = q % GB_GHN;
-    const double th = 0.25 * GB_PI * c_tab.xhi[m] + (half == 0 ? 0.25 * GB_PI : 0.75 * GB_PI);
-    const double wth = 0.25 * GB_PI * c_tab.whi[m];
-    double sth, cth;
-    sincos(th, &sth, &cth);
-    sing_bil_setD_df(c, cth, sth, wth, A);
+    const df x = dfmk(c_tabd.xh[m].x, c_tabd.xh[m].y), wx = dfmk(c_tabd.wh[m].x, c_tabd.wh[m].y);
+    const df th = df_mul(qpi, df_add_f(x, half == 0 ? 1.0f : 3.0f));
+    df sn, cs;
+    df_sincos(th, &sn, &cs);
+    sing_bil_setD_df(c, R, cs, sn, df_mul(qpi, wx), A);
   }
 }
 
@@ -783,9 +844,13 @@ __global__ void __launch_bounds__(256) k_asm_singular(AsmArgs a) {
   SingAcc A;
   singacc_zero(A);
   int nit = sing_items(c, 1);
-  for (int q = threadIdx.x; q < nit; q += blockDim.x) {
-    if (DF) sing_item_df(c, q, A);
-    else sing_item(c, q, A);
+  if (DF) {
+    __shared__ RowD R;
+    if (threadIdx.x == 0) row_setup_df(c, R);
+    __syncthreads();
+    for (int q = threadIdx.x; q < nit; q += blockDim.x) sing_item_df(c, R, q, A);
+  } else {
+    for (int q = threadIdx.x; q < nit; q += blockDim.x) sing_item(c, q, A);
   }
   static_assert(sizeof(SingAcc) == 51 * sizeof(double), "SingAcc layout");
   block_reduce<51>((double*)&A, red);
