@@ -62,6 +62,7 @@ int gbi_rbt_matrix(cplxf* A, size_t lda, int n, const float* pu, const float* pv
 int gbi_cgetrf_nopiv(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
 void gbi_rbt_params(int n, float* h);
 int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st);
+int gbi_perm_identity(int n, int* perm, cudaStream_t st);
 int gbi_zsolve_multi(const cplx* LU, size_t lda, int n, const int* perm, const cplx* X, size_t ldx, int nrhs, cplx* Y,
                      cudaStream_t st);
 }
@@ -758,6 +759,21 @@ extern "C" int gb_solve_EH(gb_obj* o) {
     cplx *Ac = nullptr, *Bc = nullptr, *Yc = nullptr;
     int64_t* ipiv = nullptr;
     int *info = nullptr, *perm = nullptr;
+    if (o->have_lu32) {
+      // chosen form: complex-FP32 factors + FP64 refinement (as for A);
+      // stream-ordered buffers (no device-wide synchronisation)
+      GB_CUDA(cudaMallocAsync((void**)&Ac, (size_t)nn * nn * sizeof(cplx), o->st));
+      GB_CUDA(cudaMallocAsync((void**)&Bc, (size_t)nn * 6 * sizeof(cplx), o->st));
+      GB_CUDA(cudaMallocAsync((void**)&Yc, (size_t)nn * 6 * sizeof(cplx), o->st));
+      rc = gbi_deh_build(o->G[d], o->H[d], o->rowk[d], Ne, nn, o->bE[d], o->bH[d], Ac, Bc, o->st);
+      if (!rc) rc = gbi_zgesv_mixed(Ac, nn, Bc, 6, Yc, nullptr, nullptr, o->st);
+      if (!rc) rc = gbi_deh_scatter(Yc, o->rowk[d], Ne, o->bdE[d], o->bdH[d], o->st);
+      cudaFreeAsync(Ac, o->st);
+      cudaFreeAsync(Bc, o->st);
+      cudaFreeAsync(Yc, o->st);
+      if (!rc) rc = sync_obj(o, "gb_solve_EH");
+      continue;
+    }
     if (dalloc((void**)&Ac, (size_t)nn * nn * sizeof(cplx)) || dalloc((void**)&Bc, (size_t)nn * 6 * sizeof(cplx)) ||
         dalloc((void**)&Yc, (size_t)nn * 6 * sizeof(cplx)) || dalloc((void**)&perm, (size_t)nn * sizeof(int)) ||
         dalloc((void**)&ipiv, (size_t)nn * sizeof(int64_t)) || dalloc((void**)&info, sizeof(int))) {
@@ -765,14 +781,6 @@ extern "C" int gb_solve_EH(gb_obj* o) {
       return -1;
     }
     rc = gbi_deh_build(o->G[d], o->H[d], o->rowk[d], Ne, nn, o->bE[d], o->bH[d], Ac, Bc, o->st);
-    if (!rc && o->have_lu32) {
-      // chosen form: complex-FP32 factors + FP64 refinement (as for A)
-      rc = gbi_zgesv_mixed(Ac, nn, Bc, 6, Yc, nullptr, nullptr, o->st);
-      if (!rc) rc = gbi_deh_scatter(Yc, o->rowk[d], Ne, o->bdE[d], o->bdH[d], o->st);
-      if (!rc) rc = sync_obj(o, "gb_solve_EH");
-      cudaFree(Ac); cudaFree(Bc); cudaFree(Yc); cudaFree(perm); cudaFree(ipiv); cudaFree(info);
-      continue;
-    }
     if (!rc) rc = gbi_zgetrf(Ac, nn, nn, ipiv, info, o->st);
     int hinfo = 0;
     if (!rc && (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
@@ -909,7 +917,7 @@ static int factor32(gb_obj* o, bool rbt, int* hinfo) {
   } else if (!rc) {
     rc = gbi_cgetrf(o->LU32, na, (int)na, o->ipiv32, info, o->st);
   }
-  if (!rc) rc = gbi_make_perm(o->ipiv32, (int)na, o->perm32, o->st);
+  if (!rc) rc = rbt ? gbi_perm_identity((int)na, o->perm32, o->st) : gbi_make_perm(o->ipiv32, (int)na, o->perm32, o->st);
   *hinfo = 0;
   if (!rc && (cudaMemcpyAsync(hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
               cudaStreamSynchronize(o->st) != cudaSuccess)) {

@@ -1424,6 +1424,18 @@ __global__ void k_make_perm(const int64_t* ipiv, int n, int* perm) {
   if (v != perm)
     for (int i = threadIdx.x; i < n; i += blockDim.x) perm[i] = v[i];
 }
+__global__ void k_iota_i32(int* v, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) v[i] = i;
+}
+// the identity permutation (factors without interchanges)
+extern "C" int gbi_perm_identity(int n, int* perm, cudaStream_t st) {
+  if (n <= 0) return 0;
+  k_iota_i32<<<(n + 255) / 256, 256, 0, st>>>(perm, n);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
 extern "C" int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st) {
   size_t sm = (n <= PERM_SMEM_MAX) ? (size_t)n * sizeof(int) : 0;
   GB_CUDA(cudaFuncSetAttribute(k_make_perm, cudaFuncAttributeMaxDynamicSharedMemorySize, PERM_SMEM_MAX * (int)sizeof(int)));
@@ -1758,7 +1770,7 @@ static int factor32_dense(const cplx* A, int n, cplxf* A32, int64_t* ipiv, int* 
   } else if (!rc) {
     rc = gbi_cgetrf(A32, n, n, ipiv, info, st);
   }
-  if (!rc) rc = gbi_make_perm(ipiv, n, perm, st);
+  if (!rc) rc = rbt ? gbi_perm_identity(n, perm, st) : gbi_make_perm(ipiv, n, perm, st);
   *hinfo = 0;
   if (!rc && (cudaMemcpyAsync(hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
               cudaStreamSynchronize(st) != cudaSuccess)) {
