@@ -6,6 +6,8 @@
 #include <algorithm>
 #include <mutex>
 #include <vector>
+#include <thread>
+#include <string>
 #include "gb_common.cuh"
 #include "gb_internal.h"
 #include "gb_bem.h"
@@ -187,6 +189,7 @@ struct gb_obj {
   // points, fields on the boundary, cross operators): 2 double-float after a
   // precision-2 assembly, else FP64
   int field_prec;
+  cudaStream_t st_dom[GB_MAXDOM];  // per-domain streams of the concurrent dE/dn solves
   // boundary values per domain, [(Ne_d+1)][4][4] (U, dU) and [(Ne_d+1)][4][3] (E, dE, H, dH)
   cplx* bU[GB_MAXDOM];
   cplx* bdU[GB_MAXDOM];
@@ -234,6 +237,8 @@ extern "C" void gb_obj_destroy(gb_obj* o) {
   }
   cudaFree(o->Ui); cudaFree(o->dUi); cudaFree(o->Ui0); cudaFree(o->dUi0); cudaFree(o->Uip);
   cudaFree(o->m.corner); cudaFree(o->ext_r); cudaFree(o->ext_v); cudaFree(o->ext_idx);
+  for (int d = 0; d < GB_MAXDOM; d++)
+    if (o->st_dom[d]) cudaStreamDestroy(o->st_dom[d]);
   if (o->st) cudaStreamDestroy(o->st);
   delete o;
 }
@@ -252,6 +257,7 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   o->have_invA = 0;
   o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
   o->rbt = nullptr; o->lu_rbt = 0; o->lu_mode = 0; o->lu_fallbacks = 0; o->field_prec = 0;
+  for (int d = 0; d < GB_MAXDOM; d++) o->st_dom[d] = nullptr;
   for (int d = 0; d < GB_MAXDOM; d++) o->bU[d] = o->bdU[d] = o->bE[d] = o->bdE[d] = o->bH[d] = o->bdH[d] = nullptr;
   o->Ui = o->dUi = o->Ui0 = o->dUi0 = o->Uip = nullptr;
   o->next = 0;
@@ -746,9 +752,60 @@ extern "C" int gb_ccd_sums(gb_obj* o, double* hout) {
   return rc;
 }
 
+// dE/dn, dH/dn of domain d in the chosen form on stream st: the system of
+// solve_deh_bv built from G, H, E, H, solved by FP32 factors + FP64
+// refinement, scattered back; synchronises st
+static int deh_mixed(gb_obj* o, int d, cudaStream_t st) {
+  const int Ne = o->m.sb_Ne[d], nn = o->nrows[d];
+  cplx *Ac = nullptr, *Bc = nullptr, *Yc = nullptr;
+  GB_CUDA(cudaMallocAsync((void**)&Ac, (size_t)nn * nn * sizeof(cplx), st));
+  GB_CUDA(cudaMallocAsync((void**)&Bc, (size_t)nn * 6 * sizeof(cplx), st));
+  GB_CUDA(cudaMallocAsync((void**)&Yc, (size_t)nn * 6 * sizeof(cplx), st));
+  int rc = gbi_deh_build(o->G[d], o->H[d], o->rowk[d], Ne, nn, o->bE[d], o->bH[d], Ac, Bc, st);
+  if (!rc) rc = gbi_zgesv_mixed(Ac, nn, Bc, 6, Yc, nullptr, nullptr, st);
+  if (!rc) rc = gbi_deh_scatter(Yc, o->rowk[d], Ne, o->bdE[d], o->bdH[d], st);
+  cudaFreeAsync(Ac, st);
+  cudaFreeAsync(Bc, st);
+  cudaFreeAsync(Yc, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  if (!rc && e != cudaSuccess) { gbi_set_error("gb_solve_EH: %s", cudaGetErrorString(e)); rc = -1; }
+  return rc;
+}
+
 extern "C" int gb_solve_EH(gb_obj* o) {
   if (ensure_bv(o)) return -1;
   int rc = 0;
+  if (o->have_lu32) {
+    // chosen form: E, H of every domain, then the domains' dE/dn systems at
+    // once, one host thread and stream each (each solve is a chain of small
+    // dependent launches that leaves most SMs idle)
+    for (int d = 0; d <= o->m.MN; d++) {
+      if (o->m.sb_Ne[d] == 0) continue;
+      if (!o->G[d]) { gbi_set_error("gb_solve_EH: domain %d has no coefficient matrices", d); return -1; }
+      if (gbi_eh_bv(o->dG[d], o->dH[d], o->dF[d], &o->m, d, o->lambda0, o->bU[d], o->bdU[d], o->bE[d], o->bH[d], o->st))
+        return -1;
+    }
+    if (sync_obj(o, "gb_solve_EH")) return -1;
+    int dev = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    for (int d = 0; d <= o->m.MN; d++)
+      if (!o->st_dom[d]) GB_CUDA(cudaStreamCreateWithFlags(&o->st_dom[d], cudaStreamNonBlocking));
+    std::vector<int> rcs((size_t)o->m.MN + 1, 0);
+    std::vector<std::string> msg((size_t)o->m.MN + 1);
+    std::vector<std::thread> th;
+    for (int d = 0; d <= o->m.MN; d++) {
+      if (o->m.sb_Ne[d] == 0) continue;
+      th.emplace_back([o, d, dev, &rcs, &msg]() {
+        if (cudaSetDevice(dev) != cudaSuccess) { rcs[d] = -1; msg[d] = "cudaSetDevice failed"; return; }
+        rcs[d] = deh_mixed(o, d, o->st_dom[d]);
+        if (rcs[d]) msg[d] = gb_last_error();
+      });
+    }
+    for (auto& t : th) t.join();
+    for (int d = 0; d <= o->m.MN; d++)
+      if (rcs[d]) { gbi_set_error("%s", msg[d].c_str()); return -1; }
+    return 0;
+  }
   for (int d = 0; d <= o->m.MN && !rc; d++) {
     int Ne = o->m.sb_Ne[d];
     if (Ne == 0) continue;
@@ -759,21 +816,6 @@ extern "C" int gb_solve_EH(gb_obj* o) {
     cplx *Ac = nullptr, *Bc = nullptr, *Yc = nullptr;
     int64_t* ipiv = nullptr;
     int *info = nullptr, *perm = nullptr;
-    if (o->have_lu32) {
-      // chosen form: complex-FP32 factors + FP64 refinement (as for A);
-      // stream-ordered buffers (no device-wide synchronisation)
-      GB_CUDA(cudaMallocAsync((void**)&Ac, (size_t)nn * nn * sizeof(cplx), o->st));
-      GB_CUDA(cudaMallocAsync((void**)&Bc, (size_t)nn * 6 * sizeof(cplx), o->st));
-      GB_CUDA(cudaMallocAsync((void**)&Yc, (size_t)nn * 6 * sizeof(cplx), o->st));
-      rc = gbi_deh_build(o->G[d], o->H[d], o->rowk[d], Ne, nn, o->bE[d], o->bH[d], Ac, Bc, o->st);
-      if (!rc) rc = gbi_zgesv_mixed(Ac, nn, Bc, 6, Yc, nullptr, nullptr, o->st);
-      if (!rc) rc = gbi_deh_scatter(Yc, o->rowk[d], Ne, o->bdE[d], o->bdH[d], o->st);
-      cudaFreeAsync(Ac, o->st);
-      cudaFreeAsync(Bc, o->st);
-      cudaFreeAsync(Yc, o->st);
-      if (!rc) rc = sync_obj(o, "gb_solve_EH");
-      continue;
-    }
     if (dalloc((void**)&Ac, (size_t)nn * nn * sizeof(cplx)) || dalloc((void**)&Bc, (size_t)nn * 6 * sizeof(cplx)) ||
         dalloc((void**)&Yc, (size_t)nn * 6 * sizeof(cplx)) || dalloc((void**)&perm, (size_t)nn * sizeof(int)) ||
         dalloc((void**)&ipiv, (size_t)nn * sizeof(int64_t)) || dalloc((void**)&info, sizeof(int))) {
