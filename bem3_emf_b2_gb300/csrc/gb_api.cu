@@ -976,7 +976,7 @@ extern "C" int gb_factor_mixed(gb_obj* o) {
   if (!o->LU32 && dalloc((void**)&o->LU32, na * na * sizeof(cplxf))) return -1;
   if (!o->ipiv32 && dalloc((void**)&o->ipiv32, na * sizeof(int64_t))) return -1;
   if (!o->perm32 && dalloc((void**)&o->perm32, na * sizeof(int))) return -1;
-  const bool rbt = o->lu_mode == 0 && na % 4 == 0;
+  const bool rbt = o->lu_mode != 1 && na % 4 == 0;
   if (rbt && ensure_rbt(o)) return -1;
   o->have_lu32 = 0;
   int hinfo = 0;
@@ -991,7 +991,7 @@ extern "C" int gb_factor_mixed(gb_obj* o) {
 }
 
 extern "C" int gb_set_lu_pivoting(gb_obj* o, int mode) {
-  if (mode != 0 && mode != 1) { gbi_set_error("gb_set_lu_pivoting: mode %d not 0 or 1", mode); return -1; }
+  if (mode < 0 || mode > 2) { gbi_set_error("gb_set_lu_pivoting: mode %d not in 0..2", mode); return -1; }
   o->lu_mode = mode;
   return 0;
 }
@@ -1050,7 +1050,8 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
       // 10x per correction (far from the rounding floor), or not within 12
       // corrections: factorise again with tournament pivoting and go on
       // from the current x (from x = 0 if it diverged)
-      if (o->lu_rbt && ((since >= 2 && rel > 0.1 * prev && rel > 1e-11) || since >= 12 || !(rel < 1e3))) {
+      const bool forced = o->lu_mode == 2 && o->lu_rbt;  // diagnostic mode: take the fallback at the first check
+      if (o->lu_rbt && (forced || (since >= 2 && rel > 0.1 * prev && rel > 1e-11) || since >= 12 || !(rel < 1e3))) {
         int hinfo = 0;
         o->lu_fallbacks++;
         rc = factor32(o, false, &hinfo);

@@ -180,7 +180,9 @@ int gb_ir_info(gb_obj *o, int *iters, double *relres);
  * Baboulin et al. 2013) and factorised without interchanges, when na is
  * divisible by 4; a zero pivot, or a refinement that does not contract the
  * residual 10x per correction, makes the object factorise again with
- * tournament pivoting.  mode 1: tournament pivoting always.
+ * tournament pivoting.  mode 1: tournament pivoting always.  mode 2
+ * (diagnostic): as mode 0, but the first refinement check takes the
+ * fallback, so that the refactorisation path can be exercised.
  * gb_lu_info: rbt = 1 if the current factors are of the randomised matrix;
  * fallbacks = such refactorisations so far. */
 int gb_set_lu_pivoting(gb_obj *o, int mode);

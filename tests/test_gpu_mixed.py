@@ -148,9 +148,20 @@ def test_butterfly_lu_matches_tournament_lu(case, gb_build, tmp_path):
     F1, N1 = sc.step(form=1)
     L.gb_lu_info(o, ctypes.byref(rbt), ctypes.byref(fb))
     assert rbt.value == 0
+    # the fallback path: butterfly factors, refinement declared stalled at its
+    # first check, tournament refactorisation, refinement continued
+    assert L.gb_set_lu_pivoting(o, 2) == 0
+    F2, N2 = sc.step(form=1)
+    L.gb_lu_info(o, ctypes.byref(rbt), ctypes.byref(fb))
+    it2, rr2 = sc.ir_info()
+    assert rbt.value == 0 and fb.value == 1, (rbt.value, fb.value)
+    assert rr2 <= 1e-13
+    assert L.gb_set_lu_pivoting(o, 3) != 0
     sc.close()
     d = np.linalg.norm(np.concatenate([F1 - F0, N1 - N0])) / np.linalg.norm(np.concatenate([F0, N0]))
     assert d <= 1e-11, "butterfly vs tournament LU, force/torque %g" % d
+    d2 = np.linalg.norm(np.concatenate([F2 - F0, N2 - N0])) / np.linalg.norm(np.concatenate([F0, N0]))
+    assert d2 <= 1e-11, "after the fallback, force/torque %g" % d2
 
 
 @pytest.mark.gpu
