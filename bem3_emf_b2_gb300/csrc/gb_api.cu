@@ -1100,3 +1100,12 @@ extern "C" int gb_scene_step(gb_obj* o, int form, int type) {
 }
 
 extern "C" void* gb_obj_stream(gb_obj* o) { return (void*)o->st; }
+
+extern "C" int gb_current_device(void) {
+  int d = 0;
+  return cudaGetDevice(&d) == cudaSuccess ? d : -1;
+}
+extern "C" int gb_use_device(int dev) {
+  if (cudaSetDevice(dev) != cudaSuccess) { gbi_set_error("cudaSetDevice(%d) failed", dev); return -1; }
+  return 0;
+}

@@ -3,6 +3,7 @@
  * (gb_scene.h).
  */
 #include <time.h>
+#include <pthread.h>
 #include "gb_host.h"
 #include "gb_scene.h"
 
@@ -125,21 +126,53 @@ MOBJ *gbh_mscene_open(int n,const char *const *medium_files,const char *const *m
 static double g_phase[4];
 static double gbh_now(void){ struct timespec t; clock_gettime(CLOCK_MONOTONIC,&t); return t.tv_sec+1e-9*t.tv_nsec; }
 
+/* assembly and factorisation of one object (its own gb_obj and stream), run
+ * for all objects at once from one host thread each: the objects are
+ * independent until the multiple-scattering iteration, and one object's
+ * quadrature fills the SMs that another's LU panel chain leaves idle */
+struct mscene_job { gb_obj *o; int MN,form,type,dev,rc; double ta,tf; char err[256]; };
+
+static void *mscene_worker(void *p)
+{
+  struct mscene_job *j=(struct mscene_job *)p;
+  if(gb_use_device(j->dev)){ j->rc=-1; snprintf(j->err,sizeof(j->err),"%s",gb_last_error()); return NULL; }
+  double t1=gbh_now();
+  for(int d=0;d<=j->MN && !j->rc;d++)
+    if(gb_assemble2(j->o,d,j->type,gb_form_precision(j->form))) j->rc=-1;
+  double t2=gbh_now();
+  if(!j->rc && (j->form==0 ? gb_invA_compute(j->o) : gb_factor_mixed(j->o))) j->rc=-1;
+  if(j->rc) snprintf(j->err,sizeof(j->err),"%s",gb_last_error());
+  j->ta=t2-t1; j->tf=gbh_now()-t2;
+  return NULL;
+}
+
 int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double *N)
 {
   double t0=gbh_now(),ta=0.0,tf=0.0;
-  for(int m=0;m<mo->N;m++){
-    DOMD *md=&mo->md[m];
-    gb_obj *o=gb_dev(md);
-    double t1=gbh_now();
-    for(int d=0;d<=md->MN;d++)
-      if(gb_assemble2(o,d,type,gb_form_precision(form))){ printf("gbh_mscene_step: %s\n",gb_last_error()); return -1; }
-    double t2=gbh_now();
-    if(form==0 ? gb_invA_compute(o) : gb_factor_mixed(o)){ printf("gbh_mscene_step: %s\n",gb_last_error()); return -1; }
-    ta+=t2-t1; tf+=gbh_now()-t2;
-    /* matrices and the factors are resident: the iteration reads no .cmat file */
-    gb_dev_set_flags(md,GB_F_CMAT|GB_F_INV,GB_F_BV);
+  struct mscene_job *jobs=(struct mscene_job *)calloc(mo->N,sizeof(struct mscene_job));
+  pthread_t *th=(pthread_t *)calloc(mo->N,sizeof(pthread_t));
+  int dev=gb_current_device();
+  for(int m=0;m<mo->N;m++){  /* device copies first (host tables, sequential) */
+    jobs[m].o=gb_dev(&mo->md[m]);
+    jobs[m].MN=mo->md[m].MN; jobs[m].form=form; jobs[m].type=type; jobs[m].dev=dev;
   }
+  double tw=gbh_now();
+  for(int m=0;m<mo->N;m++)
+    if(pthread_create(&th[m],NULL,mscene_worker,&jobs[m])){ jobs[m].rc=-2; }
+  int bad=-1;
+  for(int m=0;m<mo->N;m++){
+    if(jobs[m].rc!=-2) pthread_join(th[m],NULL);
+    else mscene_worker(&jobs[m]);  /* no thread available: run here */
+    if(jobs[m].rc && bad<0) bad=m;
+    ta+=jobs[m].ta; tf+=jobs[m].tf;
+  }
+  double tw2=gbh_now();
+  if(bad>=0){ printf("gbh_mscene_step: %s\n",jobs[bad].err); free(jobs); free(th); return -1; }
+  free(jobs); free(th);
+  /* the two phases overlap across objects: report their shares of the wall time */
+  if(ta+tf>0.0){ double w=tw2-tw; double sa=ta/(ta+tf); ta=w*sa; tf=w-ta; }
+  /* matrices and the factors are resident: the iteration reads no .cmat file */
+  for(int m=0;m<mo->N;m++) gb_dev_set_flags(&mo->md[m],GB_F_CMAT|GB_F_INV,GB_F_BV);
   double t3=gbh_now();
   mo_solve_bv(mo);
   double t4=gbh_now();

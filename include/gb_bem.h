@@ -50,6 +50,10 @@ int gb_device_count(void);
 unsigned long long gb_launch_count(void);
 /* the CUDA stream (cudaStream_t) the object's work runs on */
 void *gb_obj_stream(gb_obj *o);
+/* the calling host thread's current device, and setting it (for host
+ * threads that drive objects created on another thread) */
+int gb_current_device(void);
+int gb_use_device(int dev);
 /* live timing of the tensor-core trailing-update kernel (roofline figures):
  * enable(1) starts recording (CUDA events around every launch on its stream),
  * read() returns total device ms, launches, complex-equivalent flops (8 M N K)
