@@ -20,10 +20,20 @@
 // Per-pair solid-angle terms go through a scratch array Fs[N][Ne][3] so the
 // row sums are deterministic.
 //
-// Opt-in FP32 regular pairs (precision 1; the scene steps use precision 0
-// because the per-pair FP32 constants -- wave number, scale, weights --
-// bias every far entry alike by ~1e-7, which moves the radiation force by up
-// to ~1e-6): k_asm_regular_f32 integrates the GLN x GLN rule
+// Precision 0: the kernels above in FP64.  Precision 2 (the chosen form):
+//   k_asm_regular_df     the GLN x GLN rule of the regular pairs in
+//                        double-float on the FP32 pipes (gb_quad_df.cuh);
+//                        pairs near the CBD_SDF switch are flagged and
+//                        integrated by k_asm_regular (FP64)
+//   k_asm_singular<1>    all point sets of the singular integrals in
+//                        double-float, the directions from per-row
+//                        double-float constants
+// with matrices that agree with precision 0 to ~1e-14.
+//
+// Opt-in FP32 regular pairs (precision 1, not used by the scene forms that
+// are measured, because the per-pair FP32 constants -- wave number, scale,
+// weights -- bias every far entry alike by ~1e-7, which moves the radiation
+// force by up to ~1e-6): k_asm_regular_f32 integrates the GLN x GLN rule
 // of every regular pair in FP32, relative to the source element's centre
 // (the phase e^{ikR} = e^{ik|R0|} e^{ik(|R|-|R0|)}, the first factor in FP64
 // once per pair, the second from the stably computed difference

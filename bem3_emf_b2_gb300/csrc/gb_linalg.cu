@@ -1,4 +1,5 @@
-// gb_linalg.cu -- dense complex linear algebra of the BEM hot path (FP64).
+// gb_linalg.cu -- dense complex linear algebra of the BEM hot path (FP64 and
+// the chosen form's complex FP32 with FP64 refinement).
 //
 // Replaces, on the GPU:
 //   create_Amatrix_csr(_dac)  reference solve_bieq2.c:186-341 (coupled matrix A;
@@ -31,6 +32,12 @@
 // solve the same system to rounding.
 // The inverse solves A X = I through the factors: X = U^-1 (L^-1 (P I)),
 // two blocked triangular solves whose updates use the same GEMM kernel.
+// The chosen form's FP32 factors are of the butterfly-randomised matrix
+// U^T A V (k_rbt_matrix) without interchanges (lu_factor with pivot =
+// false: the tournament kernels are skipped); the tournament is its fallback.
+// Panels are blocked two-level: 64-column panels update only their
+// 256-column outer block, the trailing matrix is updated once per outer
+// block with K = 256.
 #include "gb_common.cuh"
 #include "gb_internal.h"
 #include <vector>
