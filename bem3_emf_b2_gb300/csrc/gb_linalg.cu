@@ -802,7 +802,13 @@ __global__ void __launch_bounds__(DIAG_THREADS) k_diag_lu(T* A, size_t lda, int 
     const T piv = M[j * ld + j];
     const bool nz = !(piv.x == 0 && piv.y == 0);
     if (!nz && threadIdx.x == 0 && info[0] == 0) info[0] = k + j + 1;
-    const T pinv = nz ? cdivc(one, piv) : zero;
+    // 1 / piv through one real division
+    typedef typename RealOf<T>::type Rt;
+    const Rt d2 = piv.x * piv.x + piv.y * piv.y;
+    const Rt id = nz ? (Rt)1 / d2 : (Rt)0;
+    T pinv;
+    pinv.x = piv.x * id;
+    pinv.y = -piv.y * id;
     // warp w: rows j + 1 + ((w - j - 1) mod nw) + nw i; lanes: columns c0, c1 > j
     const bool u0 = c0 > j && c0 < nb, u1 = c1 > j && c1 < nb;
     const T p0 = u0 ? M[j * ld + c0] : zero;

@@ -66,16 +66,11 @@ struct PairDN {
   df kr, ki;
 };
 
+// the integrand at one point (R = r - rt, W = the surface vector, shape
+// functions N, weight w) added to the sums
 template <int NDIR>
-__device__ __forceinline__ void reg_point_dn(const PairDN<NDIR>& P, bool quad, df z, df e, df w, AccDN<NDIR>& A) {
-  df d[3], R[3], W[3];
-  const df ze = df_mul(z, e);
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    d[i] = df_fma(df_fma(df_mul(P.c1[i], z), P.c2[i], e), P.c3[i], ze);
-    R[i] = df_add(P.R0[i], d[i]);
-    W[i] = df_fma(df_fma(P.w0[i], P.w1[i], z), P.w2[i], e);
-  }
+__device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[3], const df W[3], const df N[4], df w,
+                                              AccDN<NDIR>& A) {
   const df aR = df_sqrt(dot3d(R, R));
   const df iR = df_rcp(aR);
   const df aW = df_sqrt(dot3d(W, W));
@@ -89,24 +84,6 @@ __device__ __forceinline__ void reg_point_dn(const PairDN<NDIR>& P, bool quad, d
   const df iR2 = df_sqr(iR);
   const df rdW = df_mul(dot3d(R, W), iR);
   const df tD = df_mul(rdW, iR2);
-  df N[4];
-  if (quad) {
-    const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // 1 / GB_P44_N = sqrt(3)
-    const df za = df_mul(z, ia), ea = df_mul(e, ia);
-    const df zm = df_add_f(df_neg(za), 1.0f), zp = df_add_f(za, 1.0f);
-    const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
-    N[0] = df_mul_f(df_mul(zm, em), 0.25f);
-    N[1] = df_mul_f(df_mul(zp, em), 0.25f);
-    N[2] = df_mul_f(df_mul(zp, ep), 0.25f);
-    N[3] = df_mul_f(df_mul(zm, ep), 0.25f);
-  } else {  // 3 x the shape functions (0.5 / GB_P34_N0 = 2.5 exactly); the 1/3 is applied in FP64
-    const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
-    const df se = df_mul(s3, e);
-    N[0] = df_add_f(df_mul_f(df_add(z, se), -2.5f), 1.0f);
-    N[1] = df_add_f(df_mul_f(z, 5.0f), 1.0f);
-    N[2] = df_add_f(df_mul_f(df_sub(z, se), -2.5f), 1.0f);
-    N[3] = dfmk(0.0f, 0.0f);
-  }
   const dfc g = dfc_scale(ph, df_mul(df_mul(iR, aW), w));
   const dfc cbe = dfc_mul(cb, ph);
   const dfc h = dfc_scale(cbe, df_mul(tD, w));
@@ -134,6 +111,78 @@ __device__ __forceinline__ void reg_point_dn(const PairDN<NDIR>& P, bool quad, d
       A.dF[q] = df_fma(A.dF[q], iR3w, df_sub(df_mul_f(df_mul(rdv, rdW), 3.0f), Wdv));
     }
   }
+}
+
+
+template <int NDIR>
+__device__ __forceinline__ void reg_point_dn(const PairDN<NDIR>& P, bool quad, df z, df e, df w, AccDN<NDIR>& A) {
+  df d[3], R[3], W[3];
+  const df ze = df_mul(z, e);
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    d[i] = df_fma(df_fma(df_mul(P.c1[i], z), P.c2[i], e), P.c3[i], ze);
+    R[i] = df_add(P.R0[i], d[i]);
+    W[i] = df_fma(df_fma(P.w0[i], P.w1[i], z), P.w2[i], e);
+  }
+  df N[4];
+  if (quad) {
+    const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // 1 / GB_P44_N = sqrt(3)
+    const df za = df_mul(z, ia), ea = df_mul(e, ia);
+    const df zm = df_add_f(df_neg(za), 1.0f), zp = df_add_f(za, 1.0f);
+    const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
+    N[0] = df_mul_f(df_mul(zm, em), 0.25f);
+    N[1] = df_mul_f(df_mul(zp, em), 0.25f);
+    N[2] = df_mul_f(df_mul(zp, ep), 0.25f);
+    N[3] = df_mul_f(df_mul(zm, ep), 0.25f);
+  } else {  // 3 x the shape functions (0.5 / GB_P34_N0 = 2.5 exactly); the 1/3 is applied in FP64
+    const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
+    const df se = df_mul(s3, e);
+    N[0] = df_add_f(df_mul_f(df_add(z, se), -2.5f), 1.0f);
+    N[1] = df_add_f(df_mul_f(z, 5.0f), 1.0f);
+    N[2] = df_add_f(df_mul_f(df_sub(z, se), -2.5f), 1.0f);
+    N[3] = dfmk(0.0f, 0.0f);
+  }
+  reg_kernel_dn<NDIR>(P, R, W, N, w, A);
+}
+
+// quadrangle, one row z of the tensor rule: the point's geometry is affine in
+// e with row constants R = aR + bR e (aR = R0 + c1 z, bR = c2 + c3 z),
+// W = aW + w2 e (aW = w0 + w1 z), and the shape functions factor into row
+// factors zm/4, zp/4 and (1 -+ sqrt(3) e)
+struct RowQ {
+  df aR[3], bR[3], aW[3];
+  df zm4, zp4;
+};
+template <int NDIR>
+__device__ __forceinline__ void reg_rowq_dn(const PairDN<NDIR>& P, df z, RowQ& Q) {
+  const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // 1 / GB_P44_N = sqrt(3)
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    Q.aR[i] = df_fma(P.R0[i], P.c1[i], z);
+    Q.bR[i] = df_fma(P.c2[i], P.c3[i], z);
+    Q.aW[i] = df_fma(P.w0[i], P.w1[i], z);
+  }
+  const df za = df_mul(z, ia);
+  Q.zm4 = df_mul_f(df_add_f(df_neg(za), 1.0f), 0.25f);
+  Q.zp4 = df_mul_f(df_add_f(za, 1.0f), 0.25f);
+}
+template <int NDIR>
+__device__ __forceinline__ void reg_point_dnq(const PairDN<NDIR>& P, const RowQ& Q, df e, df w, AccDN<NDIR>& A) {
+  df R[3], W[3];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    R[i] = df_fma(Q.aR[i], Q.bR[i], e);
+    W[i] = df_fma(Q.aW[i], P.w2[i], e);
+  }
+  const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
+  const df ea = df_mul(e, ia);
+  const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
+  df N[4];
+  N[0] = df_mul(Q.zm4, em);
+  N[1] = df_mul(Q.zp4, em);
+  N[2] = df_mul(Q.zp4, ep);
+  N[3] = df_mul(Q.zm4, ep);
+  reg_kernel_dn<NDIR>(P, R, W, N, w, A);
 }
 
 // GLN x GLN integrals of source element S at the observation point rt (with
@@ -176,9 +225,11 @@ __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double
     S0 = GB_I_FP;
     for (int i = 0; i < GB_GLN; i++) {
       const df x = dfmk(c_tabd.x[i].x, c_tabd.x[i].y), wx = dfmk(c_tabd.w[i].x, c_tabd.w[i].y);
+      RowQ Q;
+      reg_rowq_dn<NDIR>(P, x, Q);
       for (int j = 0; j < GB_GLN; j++) {
         const df y = dfmk(c_tabd.x[j].x, c_tabd.x[j].y), wy = dfmk(c_tabd.w[j].x, c_tabd.w[j].y);
-        reg_point_dn<NDIR>(P, true, x, y, df_mul(wx, wy), A);
+        reg_point_dnq<NDIR>(P, Q, y, df_mul(wx, wy), A);
       }
     }
   } else {
