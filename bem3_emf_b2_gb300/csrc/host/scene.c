@@ -162,7 +162,7 @@ int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double
   int bad=-1;
   for(int m=0;m<mo->N;m++){
     if(jobs[m].rc!=-2) pthread_join(th[m],NULL);
-    else mscene_worker(&jobs[m]);  /* no thread available: run here */
+    else { jobs[m].rc=0; mscene_worker(&jobs[m]); }  /* no thread available: run here */
     if(jobs[m].rc && bad<0) bad=m;
     ta+=jobs[m].ta; tf+=jobs[m].tf;
   }
