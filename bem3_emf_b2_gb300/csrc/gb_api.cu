@@ -795,11 +795,16 @@ extern "C" int gb_solve_EH(gb_obj* o) {
     std::vector<std::thread> th;
     for (int d = 0; d <= o->m.MN; d++) {
       if (o->m.sb_Ne[d] == 0) continue;
-      th.emplace_back([o, d, dev, &rcs, &msg]() {
+      auto job = [o, d, dev, &rcs, &msg]() {
         if (cudaSetDevice(dev) != cudaSuccess) { rcs[d] = -1; msg[d] = "cudaSetDevice failed"; return; }
         rcs[d] = deh_mixed(o, d, o->st_dom[d]);
         if (rcs[d]) msg[d] = gb_last_error();
-      });
+      };
+      try {
+        th.emplace_back(job);
+      } catch (...) {
+        job();  // no thread available: solve this domain here
+      }
     }
     for (auto& t : th) t.join();
     for (int d = 0; d <= o->m.MN; d++)
