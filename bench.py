@@ -8,15 +8,20 @@ sphere of radius 1 (lengths in vacuum wavelengths), n = 1.5 in n = 1.33,
 cubed sphere with 8 x 8 bilinear quadrangles per face (384 elements,
 na = 12,288 unknowns), x-polarised plane wave along +z.
 
-  value        chosen form (complex-FP32 LU + FP64 iterative refinement to a
-               relative residual of 1e-13), inputs resident in HBM, CUDA events
-               on the library's stream
+  value        chosen form (double-float quadrature on the FP32 pipes; A
+               randomised by recursive butterflies, complex-FP32 LU without
+               interchanges with tensor-core trailing updates, FP64
+               iterative refinement to a relative residual of 1e-13), inputs
+               resident in HBM, CUDA events on the library's stream
   e2e          same step through the C ABI from host memory: device copy
                re-created from host arrays (H2D) and boundary values read back
                (D2H) every step
-  fp64_form    the plain FP64 form (FP64 LU + explicit inverse, as the
-               reference) timed the same way, and the relative force/torque
-               difference between the two forms
+  fp64_form    the plain FP64 form (FP64 quadrature, FP64 LU + explicit
+               inverse, as the reference) timed the same way, and the
+               relative force/torque difference between the two forms
+  roofline     the tensor-core trailing update of the LU, timed live per
+               launch: its outer-block launches (tensor-bound) and, nested,
+               its inner-panel launches (HBM-bound)
   cpu_baseline the CPU oracle (oracle/port: C restatement of the quadrature,
                LAPACK for the LU) on this host, on a bounded sample scaled to
                one scene
@@ -247,7 +252,7 @@ def run_gpu(args):
         cpu = cpu_baseline(wd) if (ws == 1 and not args.no_cpu) else None
         out = {"metric": METRIC, "value": value, "unit": "s/scene", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": 1000.0 * tmax / args.steps, "higher_is_better": False,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f64 quadrature, c64 LU + c128 refinement",
+               "scaling": "weak", "vs_baseline": None, "dtype": "double-float (f32 pairs) quadrature, c64 LU + c128 refinement",
                "data": "synthetic (meshgen cubed sphere, seeded by construction)",
                "config": {"workload": WORKLOAD["name"], "elements": 384, "na": 12288, "form": "mixed",
                           "parallelism": "replicas x%d" % ws,
@@ -405,7 +410,7 @@ def run_cones(args):
     v = sum(times) / len(times)
     return {"metric": METRIC, "value": v, "unit": "s/scene", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1000.0 * v, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64 quadrature, c64 LU + c128 refinement", "data": "synthetic (meshgen cones, seed 7)",
+            "dtype": "double-float (f32 pairs) quadrature, c64 LU + c128 refinement", "data": "synthetic (meshgen cones, seed 7)",
             "config": {"workload": CONES["name"], "elements_per_cone": ne, "form": "mixed",
                        "timing": "host wall clock around each scene step (synchronised)"},
             "iterations": it, "cc": cc, "phases_s": phases, "force": F.tolist(), "torque": N.tolist(),
