@@ -351,35 +351,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (threadIdx.x == 0 && *s_fail) atomicExch(err, 1);
 }
 
-// A (m x kc complex, lda) -> hi, lo [m][Kp] floats (columns >= 2 kc zero)
-__global__ void k_tc_split_a(const cplxf* __restrict__ A, size_t lda, int m, int kc, int Kp, float* hi, float* lo) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)m * Kp) return;
-  int i = (int)(t / Kp), q = (int)(t % Kp);
-  float v = 0.f;
-  if (q < 2 * kc) {
-    cplxf a = A[(size_t)i * lda + (q >> 1)];
-    v = (q & 1) ? a.y : a.x;
+// The operands as TF32 hi (and lo) parts in the layouts the TMA loads:
+//   A (m x kc complex, lda) -> [m][Kp] floats, row i = (re, im) of A[i][*]
+//   B (kc x n complex, ldb) -> Bt [2n][Kp]: Bt[2j+e][2l+f] = re, im, -im, re
+//     of B[l][j] for (e, f) = (0,0), (1,0), (0,1), (1,1), so that the real
+//     GEMM on interleaved storage gives re and im of the complex product
+// (columns >= 2 kc zero).  Both in one launch: blocks [0, nba) split A, the
+// rest build Bt (independent; one launch instead of two per update).
+__global__ void k_tc_prep(const cplxf* __restrict__ A, size_t lda, int m, const cplxf* __restrict__ B, size_t ldb,
+                          int n, int kc, int Kp, unsigned nba, float* ahi, float* alo, float* bhi, float* blo) {
+  if (blockIdx.x < nba) {
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)m * Kp) return;
+    const int i = (int)(t / Kp), q = (int)(t % Kp);
+    float v = 0.f;
+    if (q < 2 * kc) {
+      const cplxf a = A[(size_t)i * lda + (q >> 1)];
+      v = (q & 1) ? a.y : a.x;
+    }
+    const float h = tf32_round(v);
+    ahi[t] = h;
+    if (alo) alo[t] = v - h;
+  } else {
+    const size_t t = (size_t)(blockIdx.x - nba) * blockDim.x + threadIdx.x;
+    if (t >= (size_t)2 * n * Kp) return;
+    const int cp = (int)(t / Kp), q = (int)(t % Kp);
+    float v = 0.f;
+    if (q < 2 * kc) {
+      const cplxf b = B[(size_t)(q >> 1) * ldb + (cp >> 1)];
+      const int e = cp & 1, f = q & 1;
+      v = f == 0 ? (e == 0 ? b.x : b.y) : (e == 0 ? -b.y : b.x);
+    }
+    const float h = tf32_round(v);
+    bhi[t] = h;
+    if (blo) blo[t] = v - h;
   }
-  float h = tf32_round(v);
-  hi[t] = h;
-  if (lo) lo[t] = v - h;
-}
-
-// B (kc x n complex, ldb) -> Bt hi, lo [2n][Kp] floats
-__global__ void k_tc_build_bt(const cplxf* __restrict__ B, size_t ldb, int kc, int n, int Kp, float* hi, float* lo) {
-  size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)2 * n * Kp) return;
-  int cp = (int)(t / Kp), q = (int)(t % Kp);
-  float v = 0.f;
-  if (q < 2 * kc) {
-    cplxf b = B[(size_t)(q >> 1) * ldb + (cp >> 1)];
-    int e = cp & 1, f = q & 1;
-    v = f == 0 ? (e == 0 ? b.x : b.y) : (e == 0 ? -b.y : b.x);
-  }
-  float h = tf32_round(v);
-  hi[t] = h;
-  if (lo) lo[t] = v - h;
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -523,9 +529,9 @@ extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda,
   float* blo = bhi + (size_t)2 * N * Kp;
   const bool three = passes == 3;
   size_t ta = (size_t)M * Kp, tb = (size_t)2 * N * Kp;
-  k_tc_split_a<<<(unsigned)((ta + 255) / 256), 256, 0, st>>>(A, lda, M, K, Kp, ahi, three ? alo : nullptr);
-  gbi_count_launch();
-  k_tc_build_bt<<<(unsigned)((tb + 255) / 256), 256, 0, st>>>(B, ldb, K, N, Kp, bhi, three ? blo : nullptr);
+  const unsigned nba = (unsigned)((ta + 255) / 256), nbb = (unsigned)((tb + 255) / 256);
+  k_tc_prep<<<nba + nbb, 256, 0, st>>>(A, lda, M, B, ldb, N, K, Kp, nba, ahi, three ? alo : nullptr, bhi,
+                                       three ? blo : nullptr);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   CUtensorMap mAhi, mAlo, mBhi, mBlo;
