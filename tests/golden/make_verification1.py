@@ -22,11 +22,9 @@ def cnum(re_s, im_s):
     return [float(re_s), float(im_s)]
 
 
-def main():
-    os.makedirs(DST, exist_ok=True)
-    for f in FILES:
-        shutil.copyfile(os.path.join(SRC, f), os.path.join(DST, f))
-    log = open(os.path.join(SRC, "example1.log")).read()
+def extract(src=SRC):
+    """the values printed by the reference's verification1 run"""
+    log = open(os.path.join(src, "example1.log")).read()
     exp = {"point": [0.3, 0.0, 1.1], "fields": {}, "force": {}, "absorb": {}}
     # total field blocks: one per type, Ex..Hz
     blocks = re.split(r"type=(\d) setting", log.split("Total electromagnetic field")[1].split("Radiation force")[0])
@@ -47,9 +45,16 @@ def main():
         t = int(parts[i])
         for oid, P in re.findall(r"object id = (\d)\s*\nP = ([-+0-9.e]+)", parts[i + 1]):
             exp["absorb"]["%s_%d" % (oid, t)] = float(P)
-    bv = open(os.path.join(SRC, "d3b2_bv_solver.log")).read()
+    bv = open(os.path.join(src, "d3b2_bv_solver.log")).read()
     exp["cc"] = [float(x) for x in re.findall(r"cc = ([0-9.eE+-]+)", bv)]
-    json.dump(exp, open(os.path.join(DST, "expected.json"), "w"), indent=1)
+    return exp
+
+
+def main():
+    os.makedirs(DST, exist_ok=True)
+    for f in FILES:
+        shutil.copyfile(os.path.join(SRC, f), os.path.join(DST, f))
+    json.dump(extract(), open(os.path.join(DST, "expected.json"), "w"), indent=1)
 
 
 if __name__ == "__main__":

@@ -38,3 +38,22 @@ def test_ref_reproduces_shipped_logs(dat, log, tmp_path):
     for t in range(2):
         err = np.linalg.norm(mine[t] - ref[t]) / np.linalg.norm(ref[t])
         assert err < 1e-13, "type %d relative difference %g" % (t, err)
+
+
+@pytest.mark.skipif(not os.path.isdir(REFSRC), reason="reference sources not present")
+def test_verification1_fixture_matches_reference():
+    """The committed verification1 fixture (inputs and the printed values)
+    is what make_verification1.py extracts from the reference's own files."""
+    import filecmp
+    import importlib.util
+    import json
+    spec = importlib.util.spec_from_file_location("mkv1", os.path.join(ROOT, "tests", "golden", "make_verification1.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    committed = json.load(open(os.path.join(ROOT, "tests", "golden", "verification1", "expected.json")))
+    assert mod.extract() == committed
+    assert len(committed["fields"]) == 2 and len(committed["force"]) == 4 and len(committed["absorb"]) == 4
+    assert len(committed["cc"]) == 10
+    for f in mod.FILES:
+        assert filecmp.cmp(os.path.join(mod.SRC, f), os.path.join(ROOT, "tests", "golden", "verification1", f),
+                           shallow=False), f
