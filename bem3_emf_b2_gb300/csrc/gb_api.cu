@@ -189,7 +189,7 @@ struct gb_obj {
   // points, fields on the boundary, cross operators): 2 double-float after a
   // precision-2 assembly, else FP64
   int field_prec;
-  cudaStream_t st_dom[GB_MAXDOM];  // per-domain streams of the concurrent dE/dn solves
+  cudaStream_t st_dom[GB_MAXDOM];  // per-domain streams (concurrent assembly and dE/dn solves)
   // boundary values per domain, [(Ne_d+1)][4][4] (U, dU) and [(Ne_d+1)][4][3] (E, dE, H, dH)
   cplx* bU[GB_MAXDOM];
   cplx* bdU[GB_MAXDOM];
@@ -348,23 +348,71 @@ static int check_did(gb_obj* o, int did) {
 
 extern "C" int gb_assemble(gb_obj* o, int did, int type) { return gb_assemble2(o, did, type, 0); }
 
-extern "C" int gb_assemble2(gb_obj* o, int did, int type, int precision) {
-  if (check_did(o, did)) return -1;
-  if (type < 0 || type > 3) { gbi_set_error("gb_assemble: quadrature type %d not in 0..3", type); return -1; }
-  if (precision < 0 || precision > 2) { gbi_set_error("gb_assemble: precision %d not in 0..2", precision); return -1; }
-  if (ensure_cmatrix(o, did)) return -1;
-  size_t Ne = (size_t)o->m.sb_Ne[did];
+// domain did into its (allocated) matrices on stream st, scratch
+// stream-ordered; synchronises st
+static int assemble_on(gb_obj* o, int did, int type, int precision, cudaStream_t st) {
+  const size_t Ne = (size_t)o->m.sb_Ne[did];
   double* Fs = nullptr;
-  if (dalloc((void**)&Fs, 3 * 4 * Ne * Ne * sizeof(double))) return -1;
-  int rc = gbi_assemble_domain2(&o->m, did, type, precision, o->G[did], o->H[did], o->dG[did], o->dH[did], o->dF[did],
-                                Fs, o->st);
-  cudaError_t e = cudaStreamSynchronize(o->st);
-  cudaFree(Fs);
+  GB_CUDA(cudaMallocAsync((void**)&Fs, 3 * 4 * Ne * Ne * sizeof(double), st));
+  const int rc = gbi_assemble_domain2(&o->m, did, type, precision, o->G[did], o->H[did], o->dG[did], o->dH[did],
+                                      o->dF[did], Fs, st);
+  cudaFreeAsync(Fs, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
   if (rc) return -1;
   if (e != cudaSuccess) { gbi_set_error("gb_assemble: %s", cudaGetErrorString(e)); return -1; }
+  return 0;
+}
+
+static int check_asm_args(int type, int precision) {
+  if (type < 0 || type > 3) { gbi_set_error("gb_assemble: quadrature type %d not in 0..3", type); return -1; }
+  if (precision < 0 || precision > 2) { gbi_set_error("gb_assemble: precision %d not in 0..2", precision); return -1; }
+  return 0;
+}
+
+static void assembled(gb_obj* o, int precision) {
   o->have_invA = 0;
   o->have_lu32 = 0;
   o->field_prec = precision == 2 ? 2 : 0;
+}
+
+extern "C" int gb_assemble2(gb_obj* o, int did, int type, int precision) {
+  if (check_did(o, did) || check_asm_args(type, precision)) return -1;
+  if (ensure_cmatrix(o, did)) return -1;
+  if (assemble_on(o, did, type, precision, o->st)) return -1;
+  assembled(o, precision);
+  return 0;
+}
+
+extern "C" int gb_assemble_all(gb_obj* o, int type, int precision) {
+  if (check_asm_args(type, precision)) return -1;
+  for (int d = 0; d <= o->m.MN; d++)
+    if (ensure_cmatrix(o, d)) return -1;
+  int dev = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  for (int d = 0; d <= o->m.MN; d++)
+    if (!o->st_dom[d]) GB_CUDA(cudaStreamCreateWithFlags(&o->st_dom[d], cudaStreamNonBlocking));
+  // o->st may hold earlier work on these matrices: the domain streams start after it
+  GB_CUDA(cudaStreamSynchronize(o->st));
+  std::vector<int> rcs((size_t)o->m.MN + 1, 0);
+  std::vector<std::string> msg((size_t)o->m.MN + 1);
+  std::vector<std::thread> th;
+  for (int d = 0; d <= o->m.MN; d++) {
+    if (o->m.sb_Ne[d] == 0) continue;
+    auto job = [o, d, dev, type, precision, &rcs, &msg]() {
+      if (cudaSetDevice(dev) != cudaSuccess) { rcs[d] = -1; msg[d] = "cudaSetDevice failed"; return; }
+      rcs[d] = assemble_on(o, d, type, precision, o->st_dom[d]);
+      if (rcs[d]) msg[d] = gb_last_error();
+    };
+    try {
+      th.emplace_back(job);
+    } catch (...) {
+      job();  // no thread available: assemble this domain here
+    }
+  }
+  for (auto& t : th) t.join();
+  for (int d = 0; d <= o->m.MN; d++)
+    if (rcs[d]) { gbi_set_error("%s", msg[d].c_str()); return -1; }
+  assembled(o, precision);
   return 0;
 }
 
@@ -1096,8 +1144,7 @@ extern "C" int gb_form_precision(int form) { return form == 1 ? 2 : (form == 2 ?
 // derivatives.
 extern "C" int gb_scene_step(gb_obj* o, int form, int type) {
   if (form < 0 || form > 3) { gbi_set_error("gb_scene_step: form %d not in 0..3", form); return -1; }
-  for (int d = 0; d <= o->m.MN; d++)
-    if (gb_assemble2(o, d, type, gb_form_precision(form))) return -1;
+  if (gb_assemble_all(o, type, gb_form_precision(form))) return -1;
   if (form == 0) { if (gb_invA_compute(o)) return -1; }
   else if (gb_factor_mixed(o)) return -1;
   if (gb_solve_mEMP(o)) return -1;

@@ -137,8 +137,7 @@ static void *mscene_worker(void *p)
   struct mscene_job *j=(struct mscene_job *)p;
   if(gb_use_device(j->dev)){ j->rc=-1; snprintf(j->err,sizeof(j->err),"%s",gb_last_error()); return NULL; }
   double t1=gbh_now();
-  for(int d=0;d<=j->MN && !j->rc;d++)
-    if(gb_assemble2(j->o,d,j->type,gb_form_precision(j->form))) j->rc=-1;
+  if(gb_assemble_all(j->o,j->type,gb_form_precision(j->form))) j->rc=-1;
   double t2=gbh_now();
   if(!j->rc && (j->form==0 ? gb_invA_compute(j->o) : gb_factor_mixed(j->o))) j->rc=-1;
   if(j->rc) snprintf(j->err,sizeof(j->err),"%s",gb_last_error());

@@ -85,6 +85,9 @@ int gb_assemble(gb_obj *o, int did, int type);
  * Matrix entries then carry ~1e-7 relative error (measured: G 9e-8, dH 2e-7,
  * radiation force up to 8e-7 on the 384-element sphere): an opt-in only. */
 int gb_assemble2(gb_obj *o, int did, int type, int precision);
+/* every domain of the object, as gb_assemble2, the domains at once (one host
+ * thread and stream each) */
+int gb_assemble_all(gb_obj *o, int type, int precision);
 /* assembly precision of scene form `form` (1 -> 2, 2 -> 1, 0 and 3 -> 0) */
 int gb_form_precision(int form);
 /* copy the resident matrices of domain did to/from host buffers in the
