@@ -73,3 +73,25 @@ def test_host_setup_without_gpu(gb_build, tmp_path):
     sc.close()
     o = port.Obj(os.path.join(wd, "m.msh"), [1.5 + 0.05j], 1.0, 1.33)
     assert o.NN == 12 * 3 + 12 * 4 and o.Ne == 24
+
+
+def test_butterfly_parameters(gb_build):
+    """gbi_rbt_params (host code of the library, no GPU needed): 4 n
+    parameters e^{rho/10}, rho in [-1/2, 1/2), reproducible for an order and
+    different across orders (the factorisations are reproducible)."""
+    import numpy as np
+    lib = ctypes.CDLL(os.path.join(gb_build, "libbem3gb.so"))
+    lib.gbi_rbt_params.argtypes = [ctypes.c_int, ctypes.c_void_p]
+    lib.gbi_rbt_params.restype = None
+
+    def params(n):
+        h = np.zeros(4 * n, np.float32)
+        lib.gbi_rbt_params(n, h.ctypes.data)
+        return h
+    a, b, c = params(1024), params(1024), params(2048)
+    assert np.array_equal(a, b)
+    assert not np.array_equal(a, c[:4096])
+    lo, hi = np.float32(np.exp(-0.05)), np.float32(np.exp(0.05))
+    assert a.min() >= lo * (1 - 1e-6) and a.max() <= hi * (1 + 1e-6)
+    rho = 10.0 * np.log(a.astype(np.float64))
+    assert abs(rho.mean()) < 0.03 and 0.25 < rho.std() < 0.32  # uniform on [-1/2, 1/2): std 0.289
