@@ -35,7 +35,38 @@ struct BArgs {
   cplx* B;
 };
 
-__global__ void k_build_B(BArgs a) {
+// per source element of the domain, the constants k_build_B needs: the
+// interface factors of its (main, sub) media and the unit normals at its
+// nodes (the same operations as before, done once per element instead of
+// once per row and component)
+struct BElem {
+  cplx delt, beps, sigm;
+  double vn[4][3];
+  int asd, nl, active;
+};
+__global__ void k_build_B_prep(BArgs a, BElem* E) {
+  const int s = 1 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (s > a.Ne) return;
+  BElem e;
+  const int sd = a.sid[s], asd = abs(sd);
+  const int mdid = a.md[asd], sdid = a.sd[asd];
+  e.asd = asd;
+  e.nl = a.etype[asd] ? 4 : 3;
+  e.active = !(a.did == mdid || mdid != 0);
+  const cplx k1 = cmk(a.kn[2 * mdid], a.kn[2 * mdid + 1]), k2 = cmk(a.kn[2 * sdid], a.kn[2 * sdid + 1]);
+  const cplx k12 = k1 * k1, k22 = k2 * k2;
+  e.delt = k12 - k22;
+  e.beps = cdivc(k12, k22);
+  e.sigm = cmk(1.0, 0.0) - e.beps;
+  for (int l = 0; l < 4; l++) {
+    double vn[3] = {0.0, 0.0, 0.0};
+    if (l < e.nl) unit_normal(a.wen, asd, l, vn);
+    for (int d = 0; d < 3; d++) e.vn[l][d] = vn[d];
+  }
+  E[s - 1] = e;
+}
+
+__global__ void k_build_B(BArgs a, const BElem* __restrict__ E) {
   const int lane = threadIdx.x & 31;
   size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   size_t N = (size_t)a.Ne * 4;
@@ -47,16 +78,12 @@ __global__ void k_build_B(BArgs a) {
   const cplx* h = a.H + (size_t)row * N;
   double br = 0.0, bi = 0.0;
   for (int s = 1 + lane; s <= a.Ne; s += 32) {
-    int sd = a.sid[s], asd = abs(sd);
-    int mdid = a.md[asd], sdid = a.sd[asd];
-    if (a.did == mdid || mdid != 0) continue;
-    cplx k1 = cmk(a.kn[2 * mdid], a.kn[2 * mdid + 1]), k2 = cmk(a.kn[2 * sdid], a.kn[2 * sdid + 1]);
-    cplx k12 = k1 * k1, k22 = k2 * k2;
-    cplx delt = k12 - k22, beps = cdivc(k12, k22), sigm = cmk(1.0, 0.0) - beps;
-    int nl = a.etype[asd] ? 4 : 3;
+    const BElem& e = E[s - 1];
+    if (!e.active) continue;
+    const int asd = e.asd, nl = e.nl;
+    const cplx delt = e.delt, beps = e.beps, sigm = e.sigm;
     for (int l = 0; l < nl; l++) {
-      double vn[3];
-      unit_normal(a.wen, asd, l, vn);
+      const double vn[3] = {e.vn[l][0], e.vn[l][1], e.vn[l][2]};
       cplx tg = g[(size_t)(s - 1) * 4 + l], th = h[(size_t)(s - 1) * 4 + l];
       const cplx* ui = a.Ui + ((size_t)asd * 4 + l) * 4;
       const cplx* dui = a.dUi + ((size_t)asd * 4 + l) * 4;
@@ -86,8 +113,13 @@ extern "C" int gbi_build_B(const cplx* G, const cplx* H, const int* sid, const i
   a.kn = kn_dev; a.Ui = Ui; a.dUi = dUi; a.Ne = m->sb_Ne[did]; a.did = did; a.nrows = nrows; a.base = base; a.B = B;
   size_t warps = 4 * 4 * (size_t)a.Ne;
   if (warps == 0) return 0;
-  k_build_B<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(a);
+  BElem* E = nullptr;
+  GB_CUDA(cudaMallocAsync((void**)&E, (size_t)a.Ne * sizeof(BElem), st));
+  k_build_B_prep<<<(unsigned)((a.Ne + 127) / 128), 128, 0, st>>>(a, E);
   gbi_count_launch();
+  k_build_B<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(a, E);
+  gbi_count_launch();
+  cudaFreeAsync(E, st);
   GB_CUDA(cudaGetLastError());
   return 0;
 }
