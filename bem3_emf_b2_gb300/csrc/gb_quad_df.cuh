@@ -5,8 +5,10 @@
 // Same points, weights, shape functions and scalings as reg_integrate
 // (reference bil_dcoef_v2_GL, lit_dcoef_v2_GL) for the GLN x GLN rule, the
 // geometry relative to the source element's point (0, 0): R = R0 + d with
-// d = c1 z + c2 e + c3 z e; the common factor e^{ik|R0|} is taken out of the
-// sums and applied in FP64, so the double-float phase is e^{ik(|R| - |R0|)}.
+// d = c1 z + c2 e + c3 z e (for a quadrangle's tensor rule evaluated row by
+// row: affine in e with per-row constants); the common factor e^{ik|R0|} is
+// taken out of the sums and applied in FP64, so the double-float phase is
+// e^{ik(|R| - |R0|)}.
 // The GLN/GHN decision of the reference (|Re dF/dv| > CBD_SDF) belongs to the
 // FP64 path: reg_integrate_dn declines (returns false) when a |dF| lies
 // within 0.05 of CBD_SDF or is not finite, and the caller integrates the pair
