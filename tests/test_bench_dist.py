@@ -37,3 +37,25 @@ def test_two_rank_max_reduction():
         p.join(timeout=60)
     assert [r[:2] for r in res] == [(0, 2), (1, 2)]
     assert all(abs(r[2] - 1.0) < 1e-15 for r in res)
+
+
+def test_roofline_classes_and_arithmetic():
+    """bench.roofline_live on a synthetic launch list: outer-block launches
+    (K = 256) form the tensor-bound entry, inner ones (K <= 64) the nested
+    HBM-bound entry; achieved = algorithmic work / device time."""
+    sys.path.insert(0, ROOT)
+    import bench
+    M = N = 4096
+    klist = [(2.0, M, N, 256), (1.0, M, N, 256), (0.5, M, 128, 64), (0.5, 200, N, 64)]
+    r = bench.roofline_live(klist, step_seconds=0.1, steps=1)
+    assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s"
+    flops = 2 * 8.0 * M * N * 256
+    assert abs(r["achieved"] - flops / 3.0e-3 / 1e12) < 1e-9 * r["achieved"]
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12
+    assert r["launches_per_step"] == 2 and abs(r["kernel_share_of_timed_steps"] - 0.03) < 1e-12
+    inner = r["inner_launches"]
+    assert inner["bound"] == "hbm" and inner["unit"] == "GB/s" and inner["launches_per_step"] == 2
+    Kp = 128
+    nbytes = (16.0 * M * 128 + 8.0 * (M + 256) * Kp) + (16.0 * 200 * N + 8.0 * (200 + 2 * N) * Kp)
+    assert abs(inner["achieved"] - nbytes / 1.0e-3 / 1e9) < 1e-9 * inner["achieved"]
+    assert bench.roofline_live([], 0.1, 1) is None
