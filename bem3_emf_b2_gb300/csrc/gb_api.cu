@@ -67,6 +67,12 @@ int gbi_make_perm(const int64_t* ipiv, int n, int* perm, cudaStream_t st);
 int gbi_perm_identity(int n, int* perm, cudaStream_t st);
 int gbi_zsolve_multi(const cplx* LU, size_t lda, int n, const int* perm, const cplx* X, size_t ldx, int nrhs, cplx* Y,
                      cudaStream_t st);
+struct GbSchur;
+int gbi_schur_create(int n, GbSchur** out);
+void gbi_schur_destroy(GbSchur* s);
+int gbi_schur_factor(GbSchur* s, const GbMeshDev* m, const cplx* G0, const cplx* H0, const cplx* G1, const cplx* H1,
+                     const int* sid0, const int* sid1, const int* rowk0, const int* rowk1, cudaStream_t st);
+int gbi_schur_apply(GbSchur* s, const cplx* r, cplx* x, cudaStream_t st);
 }
 
 // ------------------------------------------------------------------ errors
@@ -185,6 +191,11 @@ struct gb_obj {
   int lu_rbt;
   int lu_mode;
   int lu_fallbacks;  // refactorisations with interchanges after a stalled refinement
+  // block elimination (lu_mode 3) for an object with one interface: the
+  // correction solve through node-sized FP32 inverses (gb_schur.cu)
+  GbSchur* schur;
+  int schur_ok;  // every element between domain 0 (outside) and 1 (inside)
+  int lu_schur;  // the current factors are the block ones
   // arithmetic of the regular pairs of the field kernels (potentials at
   // points, fields on the boundary, cross operators): 2 double-float after a
   // precision-2 assembly, else FP64
@@ -232,6 +243,7 @@ extern "C" void gb_obj_destroy(gb_obj* o) {
   }
   cudaFree(o->invA);
   cudaFree(o->LU32); cudaFree(o->ipiv32); cudaFree(o->perm32); cudaFree(o->rbt);
+  gbi_schur_destroy(o->schur);
   for (int d = 0; d < GB_MAXDOM; d++) {
     cudaFree(o->bU[d]); cudaFree(o->bdU[d]); cudaFree(o->bE[d]); cudaFree(o->bdE[d]); cudaFree(o->bH[d]); cudaFree(o->bdH[d]);
   }
@@ -257,6 +269,7 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   o->have_invA = 0;
   o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
   o->rbt = nullptr; o->lu_rbt = 0; o->lu_mode = 0; o->lu_fallbacks = 0; o->field_prec = 0;
+  o->schur = nullptr; o->schur_ok = 0; o->lu_schur = 0;
   for (int d = 0; d < GB_MAXDOM; d++) o->st_dom[d] = nullptr;
   for (int d = 0; d < GB_MAXDOM; d++) o->bU[d] = o->bdU[d] = o->bE[d] = o->bdE[d] = o->bH[d] = o->bdH[d] = nullptr;
   o->Ui = o->dUi = o->Ui0 = o->dUi0 = o->Uip = nullptr;
@@ -325,6 +338,12 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
     gbi_set_error("gb_obj_create: inconsistent mesh (rows %zu != 8 NN = %zu)", na, 8 * (size_t)md->NN);
     gb_obj_destroy(o);
     return -1;
+  }
+  if (md->MN == 1 && md->sb_Ne[0] == md->Ne && md->sb_Ne[1] == md->Ne && o->nrows[0] == md->NN &&
+      o->nrows[1] == md->NN) {
+    o->schur_ok = 1;
+    for (int e = 1; e <= md->Ne && o->schur_ok; e++)
+      if (md->md[e] != 0 || md->sd[e] != 1) o->schur_ok = 0;
   }
   *out = o;
   return 0;
@@ -1024,14 +1043,40 @@ static int factor32(gb_obj* o, bool rbt, int* hinfo) {
   return rc;
 }
 
-extern "C" int gb_factor_mixed(gb_obj* o) {
+static int alloc_lu32(gb_obj* o) {
   size_t na = o->na;
   if (!o->LU32 && dalloc((void**)&o->LU32, na * na * sizeof(cplxf))) return -1;
   if (!o->ipiv32 && dalloc((void**)&o->ipiv32, na * sizeof(int64_t))) return -1;
   if (!o->perm32 && dalloc((void**)&o->perm32, na * sizeof(int))) return -1;
-  const bool rbt = o->lu_mode != 1 && na % 4 == 0;
-  if (rbt && ensure_rbt(o)) return -1;
+  return 0;
+}
+
+// block factors (gb_schur.cu): 0, 1 after a zero pivot, -1 on error
+static int factor_schur(gb_obj* o) {
+  if (!o->G[0] || !o->G[1]) { gbi_set_error("coupled matrix: a domain has no coefficient matrices"); return -1; }
+  if (!o->schur && gbi_schur_create(o->m.NN, &o->schur)) return -1;
+  return gbi_schur_factor(o->schur, &o->m, o->G[0], o->H[0], o->G[1], o->H[1], o->m.sid + o->m.sb_off[0],
+                          o->m.sid + o->m.sb_off[1], o->rowk[0], o->rowk[1], o->st);
+}
+
+extern "C" int gb_factor_mixed(gb_obj* o) {
+  size_t na = o->na;
   o->have_lu32 = 0;
+  if (o->lu_mode == 3 && o->schur_ok) {
+    const int r = factor_schur(o);
+    if (r < 0) return -1;
+    if (r == 0) {
+      o->lu_schur = 1;
+      o->have_lu32 = 1;
+      o->have_invA = 0;
+      return 0;
+    }
+    o->lu_fallbacks++;  // a zero pivot in the block factors: the dense factors instead
+  }
+  o->lu_schur = 0;
+  if (alloc_lu32(o)) return -1;
+  const bool rbt = (o->lu_mode == 0 || o->lu_mode == 2 || o->lu_mode == 3) && na % 4 == 0;
+  if (rbt && ensure_rbt(o)) return -1;
   int hinfo = 0;
   int rc = factor32(o, rbt, &hinfo);
   if (!rc && rbt && hinfo) {  // a zero pivot without interchanges: factorise with them
@@ -1044,13 +1089,13 @@ extern "C" int gb_factor_mixed(gb_obj* o) {
 }
 
 extern "C" int gb_set_lu_pivoting(gb_obj* o, int mode) {
-  if (mode < 0 || mode > 2) { gbi_set_error("gb_set_lu_pivoting: mode %d not in 0..2", mode); return -1; }
+  if (mode < 0 || mode > 3) { gbi_set_error("gb_set_lu_pivoting: mode %d not in 0..3", mode); return -1; }
   o->lu_mode = mode;
   return 0;
 }
 
 extern "C" int gb_lu_info(gb_obj* o, int* rbt, int* fallbacks) {
-  *rbt = o->lu_rbt;
+  *rbt = o->lu_schur ? 2 : o->lu_rbt;
   *fallbacks = o->lu_fallbacks;
   return 0;
 }
@@ -1104,10 +1149,13 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
       // corrections: factorise again with tournament pivoting and go on
       // from the current x (from x = 0 if it diverged)
       const bool forced = o->lu_mode == 2 && o->lu_rbt;  // diagnostic mode: take the fallback at the first check
-      if (o->lu_rbt && (forced || (since >= 2 && rel > 0.1 * prev && rel > 1e-11) || since >= 12 || !(rel < 1e3))) {
+      if ((o->lu_rbt || o->lu_schur) &&
+          (forced || (since >= 2 && rel > 0.1 * prev && rel > 1e-11) || since >= 12 || !(rel < 1e3))) {
         int hinfo = 0;
         o->lu_fallbacks++;
-        rc = factor32(o, false, &hinfo);
+        o->lu_schur = 0;
+        rc = alloc_lu32(o);
+        if (!rc) rc = factor32(o, false, &hinfo);
         if (!rc && hinfo) { gbi_set_error("ir_solve: FP32 factor singular (info=%d)", hinfo); rc = -1; }
         if (rc) break;
         if (!(rel < 1.0) &&
@@ -1116,8 +1164,11 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
         since = 0;
       }
     }
-    rc = o->lu_rbt ? gbi_ir_step_rbt(X, r, d, d2, o->LU32, na, (int)na, o->perm32, o->rbt, o->rbt + 2 * na, o->st)
-                   : gbi_ir_step(X, r, d, d2, o->LU32, na, (int)na, o->perm32, o->st);
+    if (o->lu_schur)
+      rc = gbi_schur_apply(o->schur, r, X, o->st);
+    else
+      rc = o->lu_rbt ? gbi_ir_step_rbt(X, r, d, d2, o->LU32, na, (int)na, o->perm32, o->rbt, o->rbt + 2 * na, o->st)
+                     : gbi_ir_step(X, r, d, d2, o->LU32, na, (int)na, o->perm32, o->st);
   }
   o->ir_iters = it;
   o->ir_relres = rel;

@@ -1890,3 +1890,78 @@ extern "C" int gbi_zgesv_mixed(const cplx* A, int n, const cplx* B, int nrhs, cp
   if (!rc) GB_CUDA(cudaGetLastError());
   return rc;
 }
+
+// ------------------------------------------------------------------ FP32 inverse
+// X = P I for the permutation of gbi_make_perm: row i of X is e_perm[i]
+__global__ void k_perm_identity_c64(cplxf* X, size_t ldx, int n, const int* perm) {
+  size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (size_t)n * n) return;
+  const int i = (int)(p / n), j = (int)(p % n);
+  X[(size_t)i * ldx + j] = cmkf(j == perm[i] ? 1.0f : 0.0f, 0.0f);
+}
+
+// X <- U^-1 L^-1 X (X n x nrhs, row-major) with the factors of an LU in LU;
+// two-level blocking as in lu_factor: inside an outer block of LU_NBO rows the
+// LU_NB-row diagonal blocks are solved by k_trsm_rows and update only the
+// outer block (K = LU_NB), the rows beyond it are updated once per outer block
+// (K = LU_NBO).  gemm(M, N, K, A, lda, B, ldb, C, ldc, st): C -= A B.
+template <class T, class GEMM>
+static int lu_solve_blocked(const T* LU, size_t lda, int n, T* X, size_t ldx, int nrhs, cudaStream_t st, GEMM gemm) {
+  for (int K0 = 0; K0 < n; K0 += LU_NBO) {  // forward: L Y = X
+    const int Kend = (K0 + LU_NBO < n) ? K0 + LU_NBO : n;
+    for (int i0 = K0; i0 < Kend; i0 += LU_NB) {
+      const int ib = (Kend - i0 < LU_NB) ? Kend - i0 : LU_NB;
+      if (trsm_rows<T>(0, LU + (size_t)i0 * lda + i0, lda, X + (size_t)i0 * ldx, ldx, ib, 0, nrhs, st)) return -1;
+      if (i0 + ib < Kend && gemm(Kend - i0 - ib, nrhs, ib, LU + (size_t)(i0 + ib) * lda + i0, lda, X + (size_t)i0 * ldx,
+                                 ldx, X + (size_t)(i0 + ib) * ldx, ldx, st))
+        return -1;
+    }
+    if (Kend < n && gemm(n - Kend, nrhs, Kend - K0, LU + (size_t)Kend * lda + K0, lda, X + (size_t)K0 * ldx, ldx,
+                         X + (size_t)Kend * ldx, ldx, st))
+      return -1;
+  }
+  for (int K0 = ((n - 1) / LU_NBO) * LU_NBO; K0 >= 0; K0 -= LU_NBO) {  // backward: U X = Y
+    const int Kend = (K0 + LU_NBO < n) ? K0 + LU_NBO : n;
+    for (int i0 = K0 + ((Kend - 1 - K0) / LU_NB) * LU_NB; i0 >= K0; i0 -= LU_NB) {
+      const int ib = (Kend - i0 < LU_NB) ? Kend - i0 : LU_NB;
+      if (trsm_rows<T>(1, LU + (size_t)i0 * lda + i0, lda, X + (size_t)i0 * ldx, ldx, ib, 0, nrhs, st)) return -1;
+      if (i0 > K0 && gemm(i0 - K0, nrhs, ib, LU + (size_t)K0 * lda + i0, lda, X + (size_t)i0 * ldx, ldx,
+                          X + (size_t)K0 * ldx, ldx, st))
+        return -1;
+    }
+    if (K0 > 0 && gemm(K0, nrhs, Kend - K0, LU + K0, lda, X + (size_t)K0 * ldx, ldx, X, ldx, st)) return -1;
+  }
+  return 0;
+}
+
+// X = A^-1 (complex FP32, n x n) from the factors of gbi_cgetrf (LU, perm of
+// gbi_make_perm), the updates on the tensor cores (split TF32, three passes)
+extern "C" int gbi_cinverse_tc(const cplxf* LU, size_t lda, int n, const int* perm, cplxf* X, size_t ldx,
+                               cudaStream_t st) {
+  if (n <= 0) return 0;
+  const size_t nn = (size_t)n * n;
+  k_perm_identity_c64<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(X, ldx, n, perm);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  float* scratch = nullptr;
+  int* err = nullptr;
+  GB_CUDA(cudaMallocAsync((void**)&scratch, gbi_tc_scratch_floats(n, n, LU_NBO) * sizeof(float), st));
+  GB_CUDA(cudaMallocAsync((void**)&err, 16, st));
+  GB_CUDA(cudaMemsetAsync(err, 0, 4, st));
+  auto tc = [scratch, err](int M, int N, int K, const cplxf* a, size_t la, const cplxf* b, size_t lb, cplxf* c, size_t lc,
+                           cudaStream_t s) { return gbi_tc_cgemm_sub(M, N, K, a, la, b, lb, c, lc, 3, scratch, err, s); };
+  int rc = lu_solve_blocked<cplxf>(LU, lda, n, X, ldx, n, st, tc);
+  int h = 0;
+  if (!rc && (cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+              cudaStreamSynchronize(st) != cudaSuccess)) {
+    gbi_set_error("FP32 inverse: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
+  }
+  cudaFreeAsync(scratch, st);
+  cudaFreeAsync(err, st);
+  if (!rc && h) {
+    gbi_set_error("FP32 inverse: a tensor-core pipeline wait timed out");
+    rc = -1;
+  }
+  return rc;
+}

@@ -156,7 +156,7 @@ def test_butterfly_lu_matches_tournament_lu(case, gb_build, tmp_path):
     it2, rr2 = sc.ir_info()
     assert rbt.value == 0 and fb.value == 1, (rbt.value, fb.value)
     assert rr2 <= 1e-13
-    assert L.gb_set_lu_pivoting(o, 3) != 0
+    assert L.gb_set_lu_pivoting(o, 4) != 0
     sc.close()
     d = np.linalg.norm(np.concatenate([F1 - F0, N1 - N0])) / np.linalg.norm(np.concatenate([F0, N0]))
     assert d <= 1e-11, "butterfly vs tournament LU, force/torque %g" % d
