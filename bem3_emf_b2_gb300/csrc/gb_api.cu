@@ -270,6 +270,10 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
   o->rbt = nullptr; o->lu_rbt = 0; o->lu_mode = 0; o->lu_fallbacks = 0; o->field_prec = 0;
   o->schur = nullptr; o->schur_ok = 0; o->lu_schur = 0;
+  {  // GB_LU_MODE: the objects' initial gb_set_lu_pivoting mode (0..3)
+    const char* e = getenv("GB_LU_MODE");
+    if (e && e[0] >= '0' && e[0] <= '3' && e[1] == 0) o->lu_mode = e[0] - '0';
+  }
   for (int d = 0; d < GB_MAXDOM; d++) o->st_dom[d] = nullptr;
   for (int d = 0; d < GB_MAXDOM; d++) o->bU[d] = o->bdU[d] = o->bE[d] = o->bdE[d] = o->bH[d] = o->bdH[d] = nullptr;
   o->Ui = o->dUi = o->Ui0 = o->dUi0 = o->Uip = nullptr;

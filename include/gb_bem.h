@@ -189,9 +189,19 @@ int gb_ir_info(gb_obj *o, int *iters, double *relres);
  * residual 10x per correction, makes the object factorise again with
  * tournament pivoting.  mode 1: tournament pivoting always.  mode 2
  * (diagnostic): as mode 0, but the first refinement check takes the
- * fallback, so that the refactorisation path can be exercised.
- * gb_lu_info: rbt = 1 if the current factors are of the randomised matrix;
- * fallbacks = such refactorisations so far. */
+ * fallback, so that the refactorisation path can be exercised.  mode 3:
+ * block elimination for an object whose elements all separate domain 0
+ * (outside) from domain 1 (inside): the corrections go through complex-FP32
+ * inverses of order NN (G0^-1, G1^-1, G0^-1 H0, and those of the two Schur
+ * complements) instead of factors of the 8 NN x 8 NN matrix A -- about 43x
+ * fewer flop and 5 NN^2 instead of 64 NN^2 elements; the FP64 refinement on
+ * A is unchanged.  Other objects are factorised as in mode 0; a zero pivot
+ * or a stalled refinement falls back to tournament-pivoted dense factors.
+ * The environment variable GB_LU_MODE (0..3) sets the mode objects are
+ * created with (default 0).
+ * gb_lu_info: rbt = 1 if the current factors are of the randomised matrix,
+ * 2 if they are the block factors of mode 3; fallbacks = refactorisations
+ * after a zero pivot or a stalled refinement so far. */
 int gb_set_lu_pivoting(gb_obj *o, int mode);
 int gb_lu_info(gb_obj *o, int *rbt, int *fallbacks);
 int gb_scene_step(gb_obj *o, int form, int type);

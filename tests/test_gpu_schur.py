@@ -97,3 +97,33 @@ def test_block_elimination_sphere384(gb_build, tmp_path):
     assert res[3][3][1] <= 1e-13
     d = _rel(res[3][0], res[3][1], res[0][0], res[0][1])
     assert d <= 1e-11, d
+
+
+@pytest.mark.gpu
+def test_block_elimination_sphere1536(gb_build, tmp_path):
+    """The 1,536-element sphere (49,152 unknowns, 16 x 16 quadrangles per
+    face): the dense FP32 factors need 19 GB and (8/3) (8 NN)^3 flop, the block
+    factors 5 NN^2 complex FP32 and about 32 NN^3 -- same force and torque."""
+    from bem3_emf_b2_gb300 import Scene
+    L = _lib()
+    wd = str(tmp_path)
+    nodes, elems = meshgen.cubed_sphere(16, 1.0)
+    meshgen.write_mesh(os.path.join(wd, "mesh.msh"), nodes, elems)
+    meshgen.write_medium(os.path.join(wd, "medium.txt"), [1.5])
+    meshgen.write_ipw(os.path.join(wd, "ipw.txt"), [dict(lambda0=1.0, ni=1.33, power=1.0, e0x=1.0, e0y=0.0,
+                                                          theta=0.0, phi=0.0)])
+    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+    o = sc.obj()
+    res = {}
+    for mode in (3, 0):
+        assert L.gb_set_lu_pivoting(o, mode) == 0
+        t0 = time.perf_counter()
+        F, N = sc.step(form=1)
+        res[mode] = (F, N, time.perf_counter() - t0, sc.ir_info(), _lu_info(L, o))
+    sc.close()
+    print("sphere1536 step s: block %.3f  dense %.3f  (refinement %s / %s)" %
+          (res[3][2], res[0][2], res[3][3], res[0][3]))
+    assert res[3][4] == (2, 0)
+    assert res[3][3][1] <= 1e-13
+    d = _rel(res[3][0], res[3][1], res[0][0], res[0][1])
+    assert d <= 1e-10, d
