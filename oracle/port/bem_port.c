@@ -724,3 +724,39 @@ void port_field_c(const port_mesh_args *a, int mode, int type, int n, const doub
   for (int p = 0; p < n; p++)
     ret[p] = port_field(&m, mode, type, rt + 3 * p, v ? v + 3 * p : NULL, lambda0, bU, bdU, bE, bdE, bH, bdH, (cd *)out + (size_t)nout * p);
 }
+
+/* ---- labels of the learned near-singular quadrature -------------------------
+ * G (CC[0..3]) and H (CC[4..7]) of bilinear elements given by their corners
+ * (corner[p][4][3], the mesh's corner order) at observation points rt[p], by
+ * the rule `type` (3: the GHN 64 x 64 Gauss-Legendre rule that the reference's
+ * fallback bil_dcoef_v2_GH, bil_dcoef_v2.c:235-326, integrates with).  The
+ * element coefficients cr, cw are the reference's (setup2.c:666-745).
+ * out[p][16]: re, im of G_0..G_3 then of H_0..H_3. */
+void port_quad_labels_c(int n, const double *corner, const double *rt, const double *k, int type, double *out) {
+  tables();
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int p = 0; p < n; p++) {
+    const double *c = corner + (size_t)p * 12;
+    double rc[3][4];
+    for (int j = 0; j < 4; j++)
+      for (int d = 0; d < 3; d++) rc[d][j] = c[j * 3 + d];
+    pelem E;
+    E.quad = 1;
+    for (int d = 0; d < 3; d++) {
+      E.cr[d][0] = 0.25 * (rc[d][0] + rc[d][1] + rc[d][2] + rc[d][3]);
+      E.cr[d][1] = 0.25 * (-rc[d][0] + rc[d][1] + rc[d][2] - rc[d][3]);
+      E.cr[d][2] = 0.25 * (-rc[d][0] - rc[d][1] + rc[d][2] + rc[d][3]);
+      E.cr[d][3] = 0.25 * (rc[d][0] - rc[d][1] + rc[d][2] - rc[d][3]);
+      const int a = (d + 1) % 3, b = (d + 2) % 3;
+      E.cw[d][0] = 0.125 * ((rc[a][0] - rc[a][2]) * (rc[b][1] - rc[b][3]) - (rc[a][1] - rc[a][3]) * (rc[b][0] - rc[b][2]));
+      E.cw[d][1] = 0.125 * ((rc[a][2] - rc[a][3]) * (rc[b][0] - rc[b][1]) - (rc[a][0] - rc[a][1]) * (rc[b][2] - rc[b][3]));
+      E.cw[d][2] = 0.125 * ((rc[a][1] - rc[a][2]) * (rc[b][0] - rc[b][3]) - (rc[a][0] - rc[a][3]) * (rc[b][1] - rc[b][2]));
+    }
+    cd CC[9], dC[1][9];
+    port_reg(&E, type, rt + (size_t)p * 3, 0, NULL, k[2 * (size_t)p] + I * k[2 * (size_t)p + 1], 0, CC, dC);
+    for (int i = 0; i < 8; i++) {
+      out[(size_t)p * 16 + 2 * i] = creal(CC[i]);
+      out[(size_t)p * 16 + 2 * i + 1] = cimag(CC[i]);
+    }
+  }
+}
