@@ -51,7 +51,7 @@ def _declared(header):
 def test_library_exports_every_declared_entry_point(gb_build):
     lib = ctypes.CDLL(os.path.join(gb_build, "libbem3gb.so"))
     missing = []
-    for h in ("gb_bem.h", "gb_scene.h", "bem3_emf_b2.h", "d3b1_elem.h", "multi_fbeam.h", "ipw.h", "my_utils.h",
+    for h in ("gb_bem.h", "gb_scene.h", "gb_mlp.h", "bem3_emf_b2.h", "d3b1_elem.h", "multi_fbeam.h", "ipw.h", "my_utils.h",
               "gauleg.h", "osu_mksa.h"):
         for name in _declared(h):
             if not hasattr(lib, name):
