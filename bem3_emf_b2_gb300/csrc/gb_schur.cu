@@ -285,22 +285,26 @@ extern "C" int gbi_schur_factor(GbSchur* s, const GbMeshDev* m, const cplx* G0, 
   int64_t* ipiv = nullptr;
   int *perm = nullptr, *info = nullptr, *err = nullptr;
   float* scratch = nullptr;
-  GB_CUDA(cudaMallocAsync((void**)&P0, nn * sizeof(cplxf), st));
-  GB_CUDA(cudaMallocAsync((void**)&P1, nn * sizeof(cplxf), st));
-  GB_CUDA(cudaMallocAsync((void**)&Q0, nn * sizeof(cplxf), st));
-  GB_CUDA(cudaMallocAsync((void**)&Q1, nn * sizeof(cplxf), st));
-  GB_CUDA(cudaMallocAsync((void**)&ipiv, (size_t)n * sizeof(int64_t), st));
-  GB_CUDA(cudaMallocAsync((void**)&perm, (size_t)n * sizeof(int), st));
-  GB_CUDA(cudaMallocAsync((void**)&info, 4 * sizeof(int), st));
-  GB_CUDA(cudaMallocAsync((void**)&err, 16, st));
-  GB_CUDA(cudaMallocAsync((void**)&scratch, gbi_tc_scratch_floats(n, n, n) * sizeof(float), st));
-  GB_CUDA(cudaMemsetAsync(err, 0, 16, st));
   int rc = 0;
+  // temporaries (freed on every path below; a failed allocation leaves null)
+  if (cudaMallocAsync((void**)&P0, nn * sizeof(cplxf), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&P1, nn * sizeof(cplxf), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&Q0, nn * sizeof(cplxf), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&Q1, nn * sizeof(cplxf), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&ipiv, (size_t)n * sizeof(int64_t), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&perm, (size_t)n * sizeof(int), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&info, 4 * sizeof(int), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&err, 16, st) != cudaSuccess ||
+      cudaMallocAsync((void**)&scratch, gbi_tc_scratch_floats(n, n, n) * sizeof(float), st) != cudaSuccess ||
+      cudaMemsetAsync(err, 0, 16, st) != cudaSuccess) {
+    gbi_set_error("block elimination: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
+  }
   const unsigned gq = (unsigned)(((size_t)N * N + 255) / 256), gn = (unsigned)((nn + 255) / 256);
-  if (cudaMemsetAsync(P0, 0, nn * sizeof(cplxf), st) != cudaSuccess ||
-      cudaMemsetAsync(P1, 0, nn * sizeof(cplxf), st) != cudaSuccess ||
-      cudaMemsetAsync(Q0, 0, nn * sizeof(cplxf), st) != cudaSuccess ||
-      cudaMemsetAsync(Q1, 0, nn * sizeof(cplxf), st) != cudaSuccess) {
+  if (!rc && (cudaMemsetAsync(P0, 0, nn * sizeof(cplxf), st) != cudaSuccess ||
+              cudaMemsetAsync(P1, 0, nn * sizeof(cplxf), st) != cudaSuccess ||
+              cudaMemsetAsync(Q0, 0, nn * sizeof(cplxf), st) != cudaSuccess ||
+              cudaMemsetAsync(Q1, 0, nn * sizeof(cplxf), st) != cudaSuccess)) {
     gbi_set_error("block elimination: memset");
     rc = -1;
   }
@@ -339,9 +343,9 @@ extern "C" int gbi_schur_factor(GbSchur* s, const GbMeshDev* m, const cplx* G0, 
     gbi_set_error("block elimination: %s", cudaGetErrorString(cudaGetLastError()));
     rc = -1;
   }
-  cudaFreeAsync(P0, st); cudaFreeAsync(P1, st); cudaFreeAsync(Q0, st); cudaFreeAsync(Q1, st);
-  cudaFreeAsync(ipiv, st); cudaFreeAsync(perm, st); cudaFreeAsync(info, st); cudaFreeAsync(err, st);
-  cudaFreeAsync(scratch, st);
+  void* tmp[9] = {P0, P1, Q0, Q1, ipiv, perm, info, err, scratch};
+  for (void* t : tmp)
+    if (t) cudaFreeAsync(t, st);
   if (!rc && h[4]) { gbi_set_error("block elimination: a tensor-core pipeline wait timed out"); rc = -1; }
   if (!rc && (h[0] || h[1] || h[2] || h[3])) rc = 1;
   return rc;
