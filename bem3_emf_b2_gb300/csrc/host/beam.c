@@ -44,7 +44,8 @@ void read_data_mfb(Bobj *obj)
     }
   }
   if(wn==0){
-    printf("read_data_mfb() No beam defined, check beam data file : %s.\n",fn_ipw);
+    printf("read_data_mfb() No beam defined, check beam data file : %s, %s, %s, %s, %s, %s.\n",fn_ipw,other[0],other[1],
+           other[2],other[3],other[4]);
     exit(1);
   }
 }
