@@ -95,3 +95,16 @@ def test_reference_network_gradient_by_finite_differences():
                 P[idx] = old
                 fd = (lp - lm) / (2 * eps)
                 assert abs(fd - grads[li][which][idx]) <= 1e-7 * max(1.0, abs(fd)), (li, which, idx)
+
+
+def test_bar_for_a_learned_rule_on_sphere_pairs():
+    """The bar a learned replacement of the 64 x 64 fallback rule has to
+    beat: on a cubed sphere's near-singular pairs (the rules differ by more
+    than 1e-6) the plain 12 x 12 rule stays within 1e-3 of the 64 x 64 rule
+    (relative, per pair over G_p, H_p)."""
+    from oracle import lq_accuracy
+    c, rt, k = lq_accuracy.sphere_near_pairs(3)
+    gl, gh = lq.labels(c, rt, k, 2), lq.labels(c, rt, k, 3)
+    e = np.linalg.norm(gl - gh, axis=1) / np.linalg.norm(gh, axis=1)
+    assert len(c) > 100
+    assert e.max() <= 1e-3, e.max()
