@@ -66,6 +66,58 @@ def sample_pairs(n, seed, aspect=(1.0, 4.0), dist=(0.0, 3.0), warp=0.05, jitter=
     return corners, rt, k
 
 
+def sample_mesh_pairs(n, seed, aspect=(1.0, 2.0), fold=0.5, jitter=0.05, kh=(0.0, 2.5), kh_imag=(0.0, 0.1)):
+    """Seeded (element, node) pairs placed the way a surface mesh places its
+    near-singular pairs: the observation point is a collocation node
+    (zeta, eta = +-1/sqrt 3) of a neighbouring quadrangle that shares an edge
+    with the element (or, for a quarter of the pairs, only a corner), folded
+    about the shared edge (or tilted about the corner) by up to `fold`
+    radians.  Element: rectangle of aspect ratio U[aspect], corners jittered
+    by up to `jitter`; the pair then rotated, scaled and placed at random.
+    Returns corners (n, 4, 3), rt (n, 3), k (n,) complex."""
+    rng = np.random.default_rng(seed)
+    a = rng.uniform(*aspect, n)
+    sx, sy = np.sqrt(a), 1.0 / np.sqrt(a)
+    base = np.array([[-0.5, -0.5], [0.5, -0.5], [0.5, 0.5], [-0.5, 0.5]])
+    c = np.zeros((n, 4, 3))
+    c[:, :, 0] = base[None, :, 0] * sx[:, None]
+    c[:, :, 1] = base[None, :, 1] * sy[:, None]
+    c[:, :, :2] += rng.uniform(-jitter, jitter, (n, 4, 2))
+    g = 0.5773502691896257645091
+    zn = rng.choice([-g, g], n)
+    en = rng.choice([-g, g], n)
+    rt = np.zeros((n, 3))
+    corner = rng.random(n) < 0.25
+    ang = rng.uniform(-fold, fold, n)
+    for i in range(n):
+        # neighbour rectangle of the same size, its local point (in the
+        # element's plane before folding): shifted by one element along x,
+        # or diagonally for a corner neighbour
+        side = rng.integers(4)
+        dx, dy = [(1, 0), (-1, 0), (0, 1), (0, -1)][side]
+        if corner[i]:
+            dx, dy = rng.choice([-1, 1]), rng.choice([-1, 1])
+        p = np.array([dx * sx[i] + 0.5 * zn[i] * sx[i], dy * sy[i] + 0.5 * en[i] * sy[i], 0.0])
+        # fold about the shared edge (or tilt about the shared corner)
+        pivot = np.array([0.5 * dx * sx[i], 0.5 * dy * sy[i], 0.0])
+        axis = np.array([-dy, dx, 0.0]) if not corner[i] else np.array([-dy * sy[i], dx * sx[i], 0.0])
+        axis /= np.linalg.norm(axis)
+        v = p - pivot
+        ca, sa = np.cos(ang[i]), np.sin(ang[i])
+        v = v * ca + np.cross(axis, v) * sa + axis * np.dot(axis, v) * (1 - ca)
+        rt[i] = pivot + v
+    scale = np.exp(rng.uniform(np.log(0.05), np.log(2.0), n))
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    R = _quat_to_rot(q)
+    shift = rng.uniform(-5.0, 5.0, (n, 3))
+    corners = np.einsum("nij,nkj->nki", R, c) * scale[:, None, None] + shift[:, None, :]
+    rt = np.einsum("nij,nj->ni", R, rt) * scale[:, None] + shift
+    h = element_size(corners)
+    k = (rng.uniform(*kh, n) + 1j * rng.uniform(*kh_imag, n)) / h
+    return corners, rt, k
+
+
 def _quat_to_rot(q):
     w, x, y, z = q.T
     return np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], -1),

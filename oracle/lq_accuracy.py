@@ -9,7 +9,10 @@ relative error per pair (|Y - T| / |T| over the 16 outputs).  Then, on the
 near-singular pairs of cubed spheres (4 and 8 quadrangles per face), it
 compares the network and the plain 12 x 12 rule against the 64 x 64 rule.
 
-    python -m oracle.lq_accuracy [training pairs] [steps]
+    python -m oracle.lq_accuracy [training pairs] [steps] [uniform | mesh]
+
+(mesh: training pairs from lq.sample_mesh_pairs, placed as a surface mesh
+places its near-singular pairs).
 """
 import sys
 import time
@@ -19,15 +22,15 @@ import numpy as np
 from oracle import lq
 
 
-def data(n, seed):
-    c, rt, k = lq.sample_pairs(n, seed)
+def data(n, seed, sampler="uniform"):
+    c, rt, k = (lq.sample_mesh_pairs if sampler == "mesh" else lq.sample_pairs)(n, seed)
     X, h = lq.features(c, rt, k)
     return X, lq.targets(lq.labels(c, rt, k, 3), h)
 
 
-def run(ntr=20480, steps=3000, batch=512, lr0=1e-3, seed=3):
-    X, T = data(ntr, 4)
-    Xv, Tv = data(2048, 5)
+def run(ntr=20480, steps=3000, batch=512, lr0=1e-3, seed=3, sampler="uniform"):
+    X, T = data(ntr, 4, sampler)
+    Xv, Tv = data(2048, 5, sampler)
     mu, sd = T.mean(0), T.std(0)
     Tn = (T - mu) / sd
     flat = lq.pack(lq.init_params(seed)).astype(np.float64)
@@ -91,10 +94,11 @@ def compare_on_sphere(model, nface=4):
 if __name__ == "__main__":
     ntr = int(sys.argv[1]) if len(sys.argv) > 1 else 20480
     steps = int(sys.argv[2]) if len(sys.argv) > 2 else 3000
+    sampler = sys.argv[3] if len(sys.argv) > 3 else "uniform"
     t0 = time.time()
-    q, tot, model = run(ntr, steps)
-    print("pairs %d steps %d (%.0f s): held-out relative error per pair median %.3g, 90%% %.3g, max %.3g; overall %.3g"
-          % (ntr, steps, time.time() - t0, q[0], q[1], q[2], tot))
+    q, tot, model = run(ntr, steps, sampler=sampler)
+    print("%s pairs %d steps %d (%.0f s): held-out relative error per pair median %.3g, 90%% %.3g, max %.3g; overall %.3g"
+          % (sampler, ntr, steps, time.time() - t0, q[0], q[1], q[2], tot))
     for nface in (4, 8):
         n, e_net, e_gl = compare_on_sphere(model, nface)
         print("cubed sphere %d x %d per face: %d near-singular pairs; error against the 64 x 64 rule "

@@ -108,3 +108,17 @@ def test_bar_for_a_learned_rule_on_sphere_pairs():
     e = np.linalg.norm(gl - gh, axis=1) / np.linalg.norm(gh, axis=1)
     assert len(c) > 100
     assert e.max() <= 1e-3, e.max()
+
+
+def test_mesh_like_pairs():
+    """lq.sample_mesh_pairs: the observation point is a neighbouring
+    quadrangle's collocation node -- off the element, within about two
+    element sizes of its centre -- and, like the sphere's near-singular
+    pairs, mostly integrated to better than 1e-3 by the 12 x 12 rule."""
+    c, rt, k = lq.sample_mesh_pairs(400, 21)
+    X, h = lq.features(c, rt, k)
+    d = np.linalg.norm(rt - c.mean(1), axis=1) / h
+    assert d.min() > 0.5 and d.max() < 2.5, (d.min(), d.max())
+    gl, gh = lq.labels(c, rt, k, 2), lq.labels(c, rt, k, 3)
+    e = np.linalg.norm(gl - gh, axis=1) / np.linalg.norm(gh, axis=1)
+    assert np.quantile(e, 0.9) < 1e-3
