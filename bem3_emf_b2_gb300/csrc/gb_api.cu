@@ -68,7 +68,7 @@ int gbi_perm_identity(int n, int* perm, cudaStream_t st);
 int gbi_zsolve_multi(const cplx* LU, size_t lda, int n, const int* perm, const cplx* X, size_t ldx, int nrhs, cplx* Y,
                      cudaStream_t st);
 struct GbSchur;
-int gbi_schur_create(int n, GbSchur** out);
+int gbi_schur_create(int n, int fp64, GbSchur** out);
 void gbi_schur_destroy(GbSchur* s);
 int gbi_schur_factor(GbSchur* s, const GbMeshDev* m, const cplx* G0, const cplx* H0, const cplx* G1, const cplx* H1,
                      const int* sid0, const int* sid1, const int* rowk0, const int* rowk1, cudaStream_t st);
@@ -196,6 +196,11 @@ struct gb_obj {
   GbSchur* schur;
   int schur_ok;  // every element between domain 0 (outside) and 1 (inside)
   int lu_schur;  // the current factors are the block ones
+  // plain FP64 form of such an object (lu_mode 3): complex FP64 block
+  // factors; solves refine in FP64 with them (one correction reaches the
+  // rounding level) -- the FP64 form of objects whose dense inverse does not fit
+  GbSchur* schur64;
+  int have_blk64;
   // arithmetic of the regular pairs of the field kernels (potentials at
   // points, fields on the boundary, cross operators): 2 double-float after a
   // precision-2 assembly, else FP64
@@ -244,6 +249,7 @@ extern "C" void gb_obj_destroy(gb_obj* o) {
   cudaFree(o->invA);
   cudaFree(o->LU32); cudaFree(o->ipiv32); cudaFree(o->perm32); cudaFree(o->rbt);
   gbi_schur_destroy(o->schur);
+  gbi_schur_destroy(o->schur64);
   for (int d = 0; d < GB_MAXDOM; d++) {
     cudaFree(o->bU[d]); cudaFree(o->bdU[d]); cudaFree(o->bE[d]); cudaFree(o->bdE[d]); cudaFree(o->bH[d]); cudaFree(o->bdH[d]);
   }
@@ -270,6 +276,8 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
   o->rbt = nullptr; o->lu_rbt = 0; o->lu_mode = 0; o->lu_fallbacks = 0; o->field_prec = 0;
   o->schur = nullptr; o->schur_ok = 0; o->lu_schur = 0;
+  o->schur64 = nullptr; o->have_blk64 = 0;
+  o->lu_mode = 3;  // block elimination where the object allows it
   {  // GB_LU_MODE: the objects' initial gb_set_lu_pivoting mode (0..3)
     const char* e = getenv("GB_LU_MODE");
     if (e && e[0] >= '0' && e[0] <= '3' && e[1] == 0) o->lu_mode = e[0] - '0';
@@ -395,6 +403,7 @@ static int check_asm_args(int type, int precision) {
 static void assembled(gb_obj* o, int precision) {
   o->have_invA = 0;
   o->have_lu32 = 0;
+  o->have_blk64 = 0;
   o->field_prec = precision == 2 ? 2 : 0;
 }
 
@@ -525,7 +534,7 @@ extern "C" int gb_invA_compute(gb_obj* o) {
     rc = -1;
   }
   cudaFree(A); cudaFree(ipiv); cudaFree(info);
-  if (!rc) o->have_invA = 1;
+  if (!rc) { o->have_invA = 1; o->have_lu32 = 0; o->have_blk64 = 0; }
   return rc;
 }
 
@@ -539,6 +548,8 @@ extern "C" int gb_invA_upload(gb_obj* o, const void* invA) {
   if (!o->invA && dalloc((void**)&o->invA, o->na * o->na * sizeof(cplx))) return -1;
   GB_CUDA(cudaMemcpy(o->invA, invA, o->na * o->na * sizeof(cplx), cudaMemcpyHostToDevice));
   o->have_invA = 1;
+  o->have_lu32 = 0;
+  o->have_blk64 = 0;
   return 0;
 }
 
@@ -675,7 +686,10 @@ static int sync_obj(gb_obj* o, const char* what) {
 static int ir_solve(gb_obj* o, const cplx* B, cplx* X);
 
 extern "C" int gb_solve_mEMP(gb_obj* o) {
-  if (!o->have_invA && !o->have_lu32) { gbi_set_error("gb_solve_mEMP: A is neither inverted nor factorised"); return -1; }
+  if (!o->have_invA && !o->have_lu32 && !o->have_blk64) {
+    gbi_set_error("gb_solve_mEMP: A is neither inverted nor factorised");
+    return -1;
+  }
   if (ensure_bv(o)) return -1;
   size_t na = o->na;
   cplx *B = nullptr, *X = nullptr;
@@ -1058,7 +1072,7 @@ static int alloc_lu32(gb_obj* o) {
 // block factors (gb_schur.cu): 0, 1 after a zero pivot, -1 on error
 static int factor_schur(gb_obj* o) {
   if (!o->G[0] || !o->G[1]) { gbi_set_error("coupled matrix: a domain has no coefficient matrices"); return -1; }
-  if (!o->schur && gbi_schur_create(o->m.NN, &o->schur)) return -1;
+  if (!o->schur && gbi_schur_create(o->m.NN, 0, &o->schur)) return -1;
   return gbi_schur_factor(o->schur, &o->m, o->G[0], o->H[0], o->G[1], o->H[1], o->m.sid + o->m.sb_off[0],
                           o->m.sid + o->m.sb_off[1], o->rowk[0], o->rowk[1], o->st);
 }
@@ -1066,6 +1080,7 @@ static int factor_schur(gb_obj* o) {
 extern "C" int gb_factor_mixed(gb_obj* o) {
   size_t na = o->na;
   o->have_lu32 = 0;
+  o->have_blk64 = 0;
   if (o->lu_mode == 3 && o->schur_ok) {
     const int r = factor_schur(o);
     if (r < 0) return -1;
@@ -1099,7 +1114,7 @@ extern "C" int gb_set_lu_pivoting(gb_obj* o, int mode) {
 }
 
 extern "C" int gb_lu_info(gb_obj* o, int* rbt, int* fallbacks) {
-  *rbt = o->lu_schur ? 2 : o->lu_rbt;
+  *rbt = o->have_blk64 ? 3 : (o->lu_schur ? 2 : o->lu_rbt);
   *fallbacks = o->lu_fallbacks;
   return 0;
 }
@@ -1153,7 +1168,7 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
       // corrections: factorise again with tournament pivoting and go on
       // from the current x (from x = 0 if it diverged)
       const bool forced = o->lu_mode == 2 && o->lu_rbt;  // diagnostic mode: take the fallback at the first check
-      if ((o->lu_rbt || o->lu_schur) &&
+      if (!o->have_blk64 && (o->lu_rbt || o->lu_schur) &&
           (forced || (since >= 2 && rel > 0.1 * prev && rel > 1e-11) || since >= 12 || !(rel < 1e3))) {
         int hinfo = 0;
         o->lu_fallbacks++;
@@ -1168,7 +1183,9 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
         since = 0;
       }
     }
-    if (o->lu_schur)
+    if (o->have_blk64)
+      rc = gbi_schur_apply(o->schur64, r, X, o->st);
+    else if (o->lu_schur)
       rc = gbi_schur_apply(o->schur, r, X, o->st);
     else
       rc = o->lu_rbt ? gbi_ir_step_rbt(X, r, d, d2, o->LU32, na, (int)na, o->perm32, o->rbt, o->rbt + 2 * na, o->st)
@@ -1197,10 +1214,30 @@ extern "C" int gb_form_precision(int form) { return form == 1 ? 2 : (form == 2 ?
 // of A (form 0: FP64 LU and explicit inverse; forms 1-3: complex FP32 LU +
 // FP64 refinement), boundary values U,dU, then E, H and their normal
 // derivatives.
+// Plain FP64 factorisation: the FP64 block factors for an object with one
+// interface in LU mode 3 (the default), else the dense LU and explicit
+// inverse of A as the reference (gb_invA_compute).
+extern "C" int gb_factor_fp64(gb_obj* o) {
+  o->have_lu32 = 0;
+  o->have_blk64 = 0;
+  if (o->lu_mode == 3 && o->schur_ok) {
+    if (!o->G[0] || !o->G[1]) { gbi_set_error("coupled matrix: a domain has no coefficient matrices"); return -1; }
+    if (!o->schur64 && gbi_schur_create(o->m.NN, 1, &o->schur64)) return -1;
+    const int r = gbi_schur_factor(o->schur64, &o->m, o->G[0], o->H[0], o->G[1], o->H[1], o->m.sid + o->m.sb_off[0],
+                                   o->m.sid + o->m.sb_off[1], o->rowk[0], o->rowk[1], o->st);
+    if (r < 0) return -1;
+    if (r > 0) { gbi_set_error("gb_factor_fp64: a node matrix is singular"); return -1; }
+    o->have_blk64 = 1;
+    o->have_invA = 0;
+    return 0;
+  }
+  return gb_invA_compute(o);
+}
+
 extern "C" int gb_scene_step(gb_obj* o, int form, int type) {
   if (form < 0 || form > 3) { gbi_set_error("gb_scene_step: form %d not in 0..3", form); return -1; }
   if (gb_assemble_all(o, type, gb_form_precision(form))) return -1;
-  if (form == 0) { if (gb_invA_compute(o)) return -1; }
+  if (form == 0) { if (gb_factor_fp64(o)) return -1; }
   else if (gb_factor_mixed(o)) return -1;
   if (gb_solve_mEMP(o)) return -1;
   return gb_solve_EH(o);

@@ -1388,6 +1388,43 @@ extern "C" int gbi_rbt_matrix(cplxf* A, size_t lda, int n, const float* pu, cons
   return 0;
 }
 
+// X <- V X U^T in place: the inverse of A from the inverse X of the
+// randomised U^T A V.  Column groups take the butterfly V (rbt4_f, pv), row
+// groups the butterfly U (row . U^T = (U row^T)^T: rbt4_f, pu).
+__global__ void k_rbt_inverse(cplxf* X, size_t ldx, int n, const float* pu, const float* pv) {
+  const int q = n / 4;
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)q * q) return;
+  const int i = (int)(t / q), j = (int)(t % q);
+  cplxf x[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) x[a][b] = X[(size_t)(i + a * q) * ldx + j + b * q];
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    cplxf c[4] = {x[0][b], x[1][b], x[2][b], x[3][b]};
+    rbt4_f<cplxf, float>(c, pv, i, q);
+#pragma unroll
+    for (int a = 0; a < 4; a++) x[a][b] = c[a];
+  }
+#pragma unroll
+  for (int a = 0; a < 4; a++) rbt4_f<cplxf, float>(x[a], pu, j, q);
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) X[(size_t)(i + a * q) * ldx + j + b * q] = x[a][b];
+}
+extern "C" int gbi_rbt_inverse(cplxf* X, size_t ldx, int n, const float* pu, const float* pv, cudaStream_t st) {
+  if (n % 4) { gbi_set_error("gbi_rbt_inverse: n = %d not divisible by 4", n); return -1; }
+  const size_t qq = (size_t)(n / 4) * (n / 4);
+  if (qq == 0) return 0;
+  k_rbt_inverse<<<(unsigned)((qq + 255) / 256), 256, 0, st>>>(X, ldx, n, pu, pv);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
 template <class T>
 static int lu_solve_multi(const T* LU, size_t lda, int n, const int* perm, const T* X, size_t ldx, int nrhs, T* Y,
                           cudaStream_t st);

@@ -139,7 +139,7 @@ static void *mscene_worker(void *p)
   double t1=gbh_now();
   if(gb_assemble_all(j->o,j->type,gb_form_precision(j->form))) j->rc=-1;
   double t2=gbh_now();
-  if(!j->rc && (j->form==0 ? gb_invA_compute(j->o) : gb_factor_mixed(j->o))) j->rc=-1;
+  if(!j->rc && (j->form==0 ? gb_factor_fp64(j->o) : gb_factor_mixed(j->o))) j->rc=-1;
   if(j->rc) snprintf(j->err,sizeof(j->err),"%s",gb_last_error());
   j->ta=t2-t1; j->tf=gbh_now()-t2;
   return NULL;

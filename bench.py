@@ -1,34 +1,41 @@
 """Benchmark of the GB300 BEM hot path: seconds per scene.
 
-One step = one scene solved on the GPU: coefficient-matrix assembly of both
-domains (GLN x GLN quadrature, GHN fallback, singular self terms), the coupled
-matrix A and its factorisation, the boundary values (potentials, E, H and
-normal derivatives), and the radiation force and torque.  Workload: dielectric
-sphere of radius 1 (lengths in vacuum wavelengths), n = 1.5 in n = 1.33,
-cubed sphere with 8 x 8 bilinear quadrangles per face (384 elements,
-na = 12,288 unknowns), x-polarised plane wave along +z.
+One step = one scene solved on the GPU: coefficient-matrix assembly of every
+domain of every object (GLN x GLN quadrature, GHN fallback, singular self
+terms), the factorisation of each object's coupled system, the multiple-
+scattering iteration (reference mo_solve_bv: scattered potentials of the other
+objects, right-hand sides, refined solves, the reference's convergence rule),
+the E/H boundary values and normal derivatives, and the radiation force and
+torque of every object.
 
-  value        chosen form (double-float quadrature on the FP32 pipes; A
-               randomised by recursive butterflies, complex-FP32 LU without
-               interchanges with tensor-core trailing updates, FP64
-               iterative refinement to a relative residual of 1e-13), inputs
-               resident in HBM, CUDA events on the library's stream
-  e2e          same step through the C ABI from host memory: device copy
+Default workload (--workload cones): two right circular cones (base radius
+0.5, height 1, n = 1.59 in n = 1.33, lengths in vacuum wavelengths), 3,072
+linear triangles each (na = 73,728 unknowns per cone), cone 2 rotated pi about
+x and shifted 1.5 along x, right-circularly polarised plane wave along +z.
+This is the largest of the reference-defined configurations that fits one
+GPU.  --workload sphere: the 384-element dielectric sphere (single object).
+
+  value        chosen form: double-float quadrature on the FP32 pipes, block
+               elimination with complex-FP32 node inverses (butterfly-
+               randomised LUs, tensor-core updates), FP64 refinement; inputs
+               resident in HBM; CUDA events with a device-wide synchronise on
+               both sides of each step (the step spans several streams)
+  e2e          same step through the C ABI from host memory: device copies
                re-created from host arrays (H2D) and boundary values read back
                (D2H) every step
-  fp64_form    the plain FP64 form (FP64 quadrature, FP64 LU + explicit
-               inverse, as the reference) timed the same way, and the
-               relative force/torque difference between the two forms
-  roofline     the tensor-core trailing update of the LU, timed live per
-               launch: its outer-block launches (tensor-bound) and, nested,
-               its inner-panel launches (HBM-bound)
+  fp64_form    the plain FP64 form (FP64 quadrature; FP64 block elimination
+               for one-interface objects, else FP64 LU + explicit inverse)
+               timed the same way, and the relative force/torque difference
+  roofline     the tensor-core update kernel of the factorisation, timed per
+               launch in a separate instrumented step (not inside the timed
+               steps)
   cpu_baseline the CPU oracle (oracle/port: C restatement of the quadrature,
-               LAPACK for the LU) on this host, on a bounded sample scaled to
-               one scene
+               LAPACK for the dense LU/inverse) on this host's cores: a
+               bounded sample scaled to one scene ("estimated": true)
 With torchrun (N > 1) every rank solves its own copy of the scene (replicas;
 the path has no exchange step): value = max-over-ranks time / scenes.
-`--impl reference` times the CPU implementation of the path (oracle port) on
-the host cores and prints the same line with "impl": "reference".
+`--impl reference` times the CPU implementation of the path on the host cores
+when it can finish a scene inside the run, else prints its `unavailable` line.
 """
 import argparse
 import json
@@ -37,7 +44,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 import numpy as np
@@ -46,18 +52,63 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "assembly+LU+solve s per scene; chosen vs FP64 GPU at 1e-6 force/torque rel err"
-WORKLOAD = dict(name="sphere r=1, cubed 8x8 quads/face (384 elements, na=12288), n=1.5 in 1.33, lambda0=1, "
-                     "x-pol plane wave +z, single object",
-                faces_n=8, radius=1.0, n_obj=1.5, n_host=1.33, lambda0=1.0)
+SPHERE = dict(name="sphere r=1, cubed 8x8 quads/face (384 elements, na=12288), n=1.5 in 1.33, lambda0=1, "
+                   "x-pol plane wave +z, single object",
+              faces_n=8, radius=1.0, n_obj=1.5, n_host=1.33, lambda0=1.0)
+CONES = dict(name="two cones (base radius 0.5, height 1, n = 1.59 in 1.33, lambda0 = 1), 12 m^2 linear triangles "
+                  "each (m = 16: 3,072 triangles, na = 73,728 per cone, node jitter 5 % of the ring spacing, "
+                  "seed 7); cone 2 rotated pi about x and shifted 1.5 along x; right-circularly polarised plane "
+                  "wave along +z; multiple-scattering iteration to the reference's convergence rule",
+             m=16, radius=0.5, height=1.0, n_obj=1.59, n_host=1.33, lambda0=1.0, seed=7)
+VS_BASELINE_NOTE = "no published number for this metric (BASELINE.md: the reference publishes no benchmark)"
 
 
-def write_scene(wd, n_face=8):
+def write_sphere(wd, n_face=8):
     from bem3_emf_b2_gb300 import meshgen
-    nodes, elems = meshgen.cubed_sphere(n_face, WORKLOAD["radius"])
+    nodes, elems = meshgen.cubed_sphere(n_face, SPHERE["radius"])
     meshgen.write_mesh(os.path.join(wd, "mesh.msh"), nodes, elems)
-    meshgen.write_medium(os.path.join(wd, "medium.txt"), [WORKLOAD["n_obj"]])
-    meshgen.write_ipw(os.path.join(wd, "ipw.txt"), [dict(lambda0=WORKLOAD["lambda0"], ni=WORKLOAD["n_host"], power=1.0,
+    meshgen.write_medium(os.path.join(wd, "medium.txt"), [SPHERE["n_obj"]])
+    meshgen.write_ipw(os.path.join(wd, "ipw.txt"), [dict(lambda0=SPHERE["lambda0"], ni=SPHERE["n_host"], power=1.0,
                                                           e0x=1.0, e0y=0.0)])
+    return len(elems)
+
+
+def write_cones(wd, m=None):
+    from bem3_emf_b2_gb300 import meshgen
+    m = m or CONES["m"]
+    nodes, elems = meshgen.cone_tri(m, CONES["radius"], CONES["height"], jitter=0.05, seed=CONES["seed"])
+    meshgen.write_mesh(os.path.join(wd, "cone.msh"), nodes, elems)
+    meshgen.write_medium(os.path.join(wd, "medium.txt"), [CONES["n_obj"]])
+    meshgen.write_ipw(os.path.join(wd, "ipw.txt"), [dict(lambda0=CONES["lambda0"], ni=CONES["n_host"], power=1.0,
+                                                          e0x=1.0, e0y=1j)])
+    return len(elems)
+
+
+CONE_RV = np.array([[1.0, 0.0, 0.0], [1.0, 0.0, 0.0]])
+CONE_TH = np.array([0.0, np.pi])
+CONE_TV = np.array([[0.0, 0.0, 0.0], [1.5, 0.0, 0.0]])
+
+
+def open_workload(args, wd):
+    """(scene, description dict) of the chosen workload, set up from its input files"""
+    from bem3_emf_b2_gb300 import MultiScene, Scene
+    if args.workload == "cones":
+        ne = write_cones(wd, args.cone_m)
+        med = [os.path.join(wd, "medium.txt")] * 2
+        msh = [os.path.join(wd, "cone.msh")] * 2
+        sc = MultiScene(med, msh, os.path.join(wd, "ipw.txt"), rv=CONE_RV, th=CONE_TH, tv=CONE_TV)
+        m = args.cone_m or CONES["m"]
+        name = CONES["name"] if m == CONES["m"] else CONES["name"].replace("m = 16: 3,072", "m = %d: %d" % (m, ne))
+        return sc, dict(workload=name, objects=2, elements_per_object=ne, na_per_object=8 * 3 * ne)
+    ne = write_sphere(wd, args.faces)
+    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+    name = SPHERE["name"] if args.faces == 8 else "sphere r=1, cubed %dx%d quads/face (%d elements)" % (
+        args.faces, args.faces, ne)
+    return sc, dict(workload=name, objects=1, elements_per_object=ne, na_per_object=8 * 4 * ne)
+
+
+def force_vec(F, N):
+    return np.concatenate([np.asarray(F, float).ravel(), np.asarray(N, float).ravel()])
 
 
 # ---------------------------------------------------------------- distributed
@@ -143,38 +194,75 @@ def flush_l2():
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_baseline(wd, seconds_budget=20.0):
-    """Oracle port on the host cores: a sample of assembly rows of both
-    domains and a LAPACK zgetrf+zgetri at a reduced order, scaled to one
-    scene (rows x N, and (na / n_sample)^3)."""
+def _lapack_rate(ns=3072):
+    """seconds of LAPACK zgetrf + zgetri at order ns on this host"""
+    from scipy.linalg import lapack
+    rng = np.random.default_rng(0)
+    A = rng.standard_normal((ns, ns)) + 1j * rng.standard_normal((ns, ns))
+    t0 = time.perf_counter()
+    lu, piv, info = lapack.zgetrf(A)
+    lapack.zgetri(lu, piv)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(args, wd, iterations=11):
+    """Oracle port on the host cores, a bounded sample scaled to one scene
+    (an estimate, not a timing of a whole scene):
+      assembly   sampled rows of every domain, scaled by rows;
+      LU+inverse LAPACK zgetrf + zgetri at order 3,072, scaled by (na/3072)^3
+                 (the reference inverts A densely, solve_bieq2.c:343-408);
+      iteration  (multi-object scenes) sampled scattered-potential points of
+                 add_scattered_mEMP (oracle field mode 3) scaled to every
+                 exterior node of every object, times the GPU run's iteration
+                 count, plus one invA b product (8 na^2 flop) per object and
+                 iteration at the host's measured LAPACK rate."""
     from oracle import port
     ncpu = os.cpu_count() or 1
     os.environ.setdefault("OMP_NUM_THREADS", str(ncpu))
-    o = port.Obj(os.path.join(wd, "mesh.msh"), [WORKLOAD["n_obj"]], WORKLOAD["lambda0"], WORKLOAD["n_host"])
+    if args.workload == "cones":
+        objs = [port.Obj(os.path.join(wd, "cone.msh"), [CONES["n_obj"]], CONES["lambda0"], CONES["n_host"])]
+        nobj = 2
+    else:
+        objs = [port.Obj(os.path.join(wd, "mesh.msh"), [SPHERE["n_obj"]], SPHERE["lambda0"], SPHERE["n_host"])]
+        nobj = 1
+    o = objs[0]
     t_asm = 0.0
-    nrows_total = 0
-    sample_rows = max(8 * ncpu, 128)
+    sample_rows = max(4 * ncpu, 64)
     for d in range(o.MN + 1):
         N = 4 * (len(o.sids[d]) - 1)
         rows = np.linspace(0, N - 1, sample_rows).astype(np.int32)
         t0 = time.perf_counter()
         o.rows(d, rows)
         t_asm += (time.perf_counter() - t0) * N / len(rows)
-        nrows_total += N
-    from scipy.linalg import lapack
+    t_asm *= nobj
     na = 8 * o.NN
     ns = 3072
-    A = (np.random.default_rng(0).standard_normal((ns, ns)) + 1j * np.random.default_rng(1).standard_normal((ns, ns)))
-    t0 = time.perf_counter()
-    lu, piv, info = lapack.zgetrf(A)
-    inv, info = lapack.zgetri(lu, piv)
-    t_lu = (time.perf_counter() - t0) * (na / ns) ** 3
-    total = t_asm + t_lu
-    return dict(value=total, unit="s/scene", cores=ncpu, kind="port",
-                sample="assembly: %d rows per domain of %d (scaled by N/rows), LU+inverse: LAPACK zgetrf+zgetri at "
-                       "n=%d scaled by (%d/%d)^3; estimate %.1f s assembly + %.1f s LU" % (
-                           sample_rows, nrows_total // (o.MN + 1), ns, na, ns, t_asm, t_lu),
-                assembly_s=t_asm, lu_s=t_lu)
+    t_ns = _lapack_rate(ns)
+    t_lu = nobj * t_ns * (na / ns) ** 3
+    t_it = 0.0
+    if nobj > 1:
+        # scattered potential of one object at sampled exterior nodes of the other
+        ext = o.ren[1:, :3, :].reshape(-1, 3) + np.array([1.5, 0.0, 0.0])
+        npts = max(2 * ncpu, 32)
+        pts = ext[np.linspace(0, len(ext) - 1, npts).astype(int)]
+        v = np.tile([0.0, 0.0, 1.0], (npts, 1))
+        bv = [dict(U=np.zeros((len(o.sids[d]), 4, 4), complex), dU=np.zeros((len(o.sids[d]), 4, 4), complex),
+                   E=np.zeros((len(o.sids[d]), 4, 3), complex), dE=np.zeros((len(o.sids[d]), 4, 3), complex),
+                   H=np.zeros((len(o.sids[d]), 4, 3), complex), dH=np.zeros((len(o.sids[d]), 4, 3), complex))
+              for d in range(o.MN + 1)]
+        t0 = time.perf_counter()
+        o.field(3, 2, pts, bv, v)
+        t_pt = (time.perf_counter() - t0) / npts
+        matvec = t_ns / (8.0 * ns ** 3) * 8.0 * na * na  # invA b at the LAPACK flop rate
+        t_it = iterations * nobj * (t_pt * o.NN + matvec)
+    total = t_asm + t_lu + t_it
+    return dict(value=total, unit="s/scene", cores=ncpu, kind="port", estimated=True,
+                sample="oracle port on %d cores: %d assembly rows per domain (scaled by rows), LAPACK zgetrf+zgetri at "
+                       "n=%d scaled by (%d/%d)^3 per object%s; estimate %.1f s assembly + %.1f s LU/inverse + %.1f s "
+                       "iteration (E/H stage and force not included)" % (
+                           ncpu, sample_rows, ns, na, ns,
+                           (", %d add_scattered points scaled to %d nodes x %d iterations" % (npts, o.NN, iterations))
+                           if nobj > 1 else "", t_asm, t_lu, t_it))
 
 
 # ---------------------------------------------------------------- GPU arm
@@ -182,60 +270,64 @@ def rel_vec(a, b):
     return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / max(np.linalg.norm(b), 1e-300))
 
 
+def timed_steps(sc, form, steps, warmup, dist=None):
+    """warm-up steps, then `steps` steps each bracketed by a device-wide
+    synchronise and CUDA events on the current stream (the step spans several
+    streams and host threads); L2 flushed before each step"""
+    import torch
+    for _ in range(warmup):
+        sc.step(form=form)
+    st = torch.cuda.current_stream()
+    times = []
+    F = N = None
+    torch.cuda.synchronize()
+    dist_barrier(dist)
+    for _ in range(steps):
+        flush_l2()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        F, N = sc.step(form=form)
+        torch.cuda.synchronize()
+        e1.record(st)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) / 1000.0)
+    dist_barrier(dist)
+    return times, F, N
+
+
 def run_gpu(args):
     import torch
     dist, rank, ws = dist_init()
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
-    from bem3_emf_b2_gb300 import Scene, build, lib, ktime_list, ktime_read
+    from bem3_emf_b2_gb300 import build, ktime_list, ktime_read, lib
     build.build()
-    wd = tempfile.mkdtemp(prefix="bench_")
-    write_scene(wd)
-    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
     L = lib()
+    wd = tempfile.mkdtemp(prefix="bench_")
+    sc, desc = open_workload(args, wd)
+    cones = args.workload == "cones"
 
-    def timed(form, steps, warmup, ktime=False):
-        for _ in range(warmup):
-            sc.step(form=form)
-        st = torch.cuda.ExternalStream(sc.stream())
-        times = []
-        F = N = None
-        torch.cuda.synchronize()
-        dist_barrier(dist)
-        l0 = L.gb_launch_count()
-        if ktime:
-            L.gb_ktime_enable(1)
-        for _ in range(steps):
-            flush_l2()
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            F, N = sc.step(form=form)
-            e1.record(st)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1) / 1000.0)
-        torch.cuda.synchronize()
-        launches = (L.gb_launch_count() - l0) / steps
-        kt = None
-        if ktime:
-            kt = ktime_list()
-            ktime_read()
-            L.gb_ktime_enable(0)
-        dist_barrier(dist)
-        return times, F, N, launches, kt
-
-    # plain FP64 form (reference-equivalent), then the chosen form
-    t64, F64, N64, _, _ = timed(0, max(1, min(args.steps, 2)), 1)
+    # chosen form: warm-up, then exactly K timed steps (launch count over them)
+    for _ in range(args.warmup):
+        sc.step(form=1)
+    l0 = L.gb_launch_count()
     with ClockSampler(local) as clk:
-        t32, F32, N32, launches, kt = timed(1, args.steps, args.warmup, ktime=True)
+        t32, F32, N32 = timed_steps(sc, 1, args.steps, 0, dist)
+    launches = (L.gb_launch_count() - l0) / args.steps
     tsum = sum(t32)
     tmax = dist_max(dist, tsum)
     value = tmax / (args.steps * ws)
-    # e2e: device copy rebuilt from host memory every step (H2D), results read back (D2H)
+    phases = sc.phase_times() if cones else None
+    iters = sc.iteration() if cones else None
+    # plain FP64 form (after the chosen form: its allocations are not in the line's steps)
+    n64 = 1 if cones else max(1, min(args.steps, 2))
+    t64, F64, N64 = timed_steps(sc, 0, n64, 0, dist)
+    # e2e: device copies rebuilt from host memory every step (H2D), results read back (D2H)
     h2d, d2h = sc.h2d_bytes(), sc.d2h_bytes()
     te = []
-    for _ in range(max(1, min(args.steps, 3))):
+    for _ in range(max(1, min(args.steps, 2 if cones else 3))):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         sc.drop_device()
@@ -243,28 +335,48 @@ def run_gpu(args):
         torch.cuda.synchronize()
         te.append(time.perf_counter() - t0)
     e2e = dist_max(dist, sum(te)) / (len(te) * ws)
-    # relative difference of the combined force/torque vector (a component that
-    # vanishes by symmetry is rounding noise and is not a meaningful ratio)
-    force_err = rel_vec(np.concatenate([F32, N32]), np.concatenate([F64, N64]))
+    # instrumented step for the roofline (per-launch events), outside the timed steps
+    L.gb_ktime_enable(1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sc.step(form=1)
+    torch.cuda.synchronize()
+    t_instr = time.perf_counter() - t0
+    kt = ktime_list()
+    ktime_read()
+    L.gb_ktime_enable(0)
+    force_err = rel_vec(force_vec(F32, N32), force_vec(F64, N64))
     out = None
     if rank == 0:
-        roof = roofline_live(kt, tsum, args.steps)
-        cpu = cpu_baseline(wd) if (ws == 1 and not args.no_cpu) else None
+        roof = roofline_live(kt, t_instr, 1)
+        cpu = cpu_baseline(args, wd, iters[0] if iters else 11) if (ws == 1 and not args.no_cpu) else None
+        cfg = {"workload": desc["workload"], "objects": desc["objects"],
+               "elements_per_object": desc["elements_per_object"], "na_per_object": desc["na_per_object"],
+               "form": "chosen (double-float quadrature, FP32 block elimination + FP64 refinement)",
+               "parallelism": "replicas x%d" % ws,
+               "l2": "working set larger than L2 (coefficient matrices %s) and a 256 MB L2 flush before each step" % (
+                   "2 x 29 GB" if cones else "0.45 GB"),
+               "timing": "CUDA events on the current stream with a device-wide synchronise on both sides of each step"}
         out = {"metric": METRIC, "value": value, "unit": "s/scene", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": 1000.0 * tmax / args.steps, "higher_is_better": False,
-               "scaling": "weak", "vs_baseline": None, "dtype": "double-float (f32 pairs) quadrature, c64 LU + c128 refinement",
-               "data": "synthetic (meshgen cubed sphere, seeded by construction)",
-               "config": {"workload": WORKLOAD["name"], "elements": 384, "na": 12288, "form": "mixed",
-                          "parallelism": "replicas x%d" % ws,
-                          "l2": "working set larger than L2 (A: 2.4 GB FP64) and a 256 MB L2 flush before each step"},
-               "fp64_form": {"s_per_scene": sum(t64) / len(t64), "force_torque_rel_diff_vs_chosen": force_err},
-               "force": list(map(float, F32)), "torque": list(map(float, N32)),
+               "scaling": "weak", "vs_baseline": None, "vs_baseline_note": VS_BASELINE_NOTE,
+               "dtype": "double-float (f32 pairs) quadrature, c64 block LU + c128 refinement",
+               "data": "synthetic (meshgen %s, seeded)" % ("cones, seed 7" if cones else "cubed sphere"),
+               "config": cfg,
+               "fp64_form": {"s_per_scene": sum(t64) / len(t64), "steps": len(t64),
+                             "force_torque_rel_diff_vs_chosen": force_err,
+                             "form": "FP64 quadrature, FP64 block elimination (node LUs + inverses), FP64 E/H"},
+               "force": np.asarray(F32).tolist(), "torque": np.asarray(N32).tolist(),
                "e2e": {"value": e2e, "unit": "s/scene", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                "gpu_launches": int(round(launches)), "clocks": clk.summary()}
+        if phases:
+            out["phases_s_last_step"] = phases
+        if iters:
+            out["iterations"] = {"count": iters[0], "cc": iters[1]}
         if roof:
             out["roofline"] = roof
         if cpu:
-            out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+            out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "estimated")}
     sc.close()
     if dist is not None:
         dist.destroy_process_group()
@@ -275,18 +387,18 @@ TRAFFIC_FILE = os.path.join(ROOT, "profiles", "tc_cgemm_traffic.json")
 
 
 def roofline_live(klist, step_seconds, steps):
-    """Roofline of the dominant kernel of the complex-FP32 LU -- the tensor-core
-    trailing update k_tc_cgemm_sub (tcgen05, TF32 in three passes for FP32
-    accuracy) -- from CUDA events around each of its launches on the library's
-    stream inside the timed steps.  Per launch M x N x K (complex):
-    algorithmic flops 8 M N K (complex-equivalent), algorithmic HBM bytes
-    16 M N (C read and written) + the split operands 2 x 4 (M + 2N) Kp.
-    Two classes: the outer-block updates (K = 256: 128 complex flop per byte,
-    above the ridge, tensor-bound) and the inner-panel updates (K <= 64,
-    HBM-bound).  The tensor figures are against the measured dense bf16 peak;
-    tcgen05 kind::tf32 issues at 1.1/2.25 of the kind::f16 rate and the FP32-
-    accurate split needs three passes, so the ceiling this arithmetic can reach
-    is bf16 x (1.1 / 2.25) / 3, reported beside it."""
+    """Roofline of the factorisation's tensor-core update kernel
+    k_tc_cgemm_sub (tcgen05, TF32 in three passes for FP32 accuracy) from
+    CUDA events around each of its launches on the library's streams in one
+    instrumented step.  Per launch M x N x K (complex): algorithmic flops
+    8 M N K (complex-equivalent), algorithmic HBM bytes 16 M N (C read and
+    written) + the split operands 2 x 4 (M + 2N) Kp.  Two classes: launches
+    with K >= 128 (outer-block updates and the block elimination's products:
+    >= 64 complex flop per byte, tensor-bound) and the inner-panel updates
+    (K <= 64, HBM-bound).  The tensor figures are against the measured dense
+    bf16 peak; tcgen05 kind::tf32 issues at 1.1/2.25 of the kind::f16 rate and
+    the FP32-accurate split needs three passes, so the ceiling this
+    arithmetic can reach is bf16 x (1.1 / 2.25) / 3, reported beside it."""
     if not klist:
         return None
     peaks = {}
@@ -312,7 +424,7 @@ def roofline_live(klist, step_seconds, steps):
         dt = o[1] / 1000.0
         ach = o[2] / dt / 1e12
         ratio = tr.get("outer", {}).get("dram_bytes_per_algorithmic_byte")
-        out = {"kernel": "k_tc_cgemm_sub (tcgen05 TF32 x3 complex trailing update), outer-block launches (K = 256)",
+        out = {"kernel": "k_tc_cgemm_sub (tcgen05 TF32 x3 complex update), launches with K >= 128",
                "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16,
                "peak_source": src + " bf16_tflops",
                "traffic": ratio * o[3] / o[0] if ratio else None,
@@ -338,99 +450,44 @@ def roofline_live(klist, step_seconds, steps):
 
 # ---------------------------------------------------------------- reference arm
 def run_reference(args):
+    """The reference's CPU path on this host.  Its dense inverse of each
+    object's coupled matrix (zgetrf + zgetri of na = 8 NN, solve_bieq2.c:343-408)
+    is what bounds a CPU scene: for the two-cone scene that is two inverses of
+    order 73,728 (87 GB of complex128 each, ~3.2e15 flop each), hours on the
+    host's cores -- it cannot finish inside this run, so the arm prints its
+    `unavailable` line with the sampled estimate of cpu_baseline beside it."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
     wd = tempfile.mkdtemp(prefix="bench_ref_")
-    write_scene(wd)
-    vals = []
-    cpu = None
-    for _ in range(max(1, args.steps)):
-        cpu = cpu_baseline(wd)
-        vals.append(cpu["value"])
-    v = statistics.median(vals)
-    return {"metric": METRIC, "value": v, "unit": "s/scene", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * v, "higher_is_better": False,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic",
-            "impl": "reference",
-            "config": {"workload": WORKLOAD["name"], "elements": 384, "na": 12288, "form": "CPU oracle port"},
-            "cpu_baseline": {"value": v, "unit": "s/scene", "cores": cpu["cores"], "kind": cpu["kind"],
-                             "sample": cpu["sample"]},
-            "e2e": {"value": v, "unit": "s/scene", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-
-
-CONES = dict(name="two cones (base radius 0.5, height 1, n = 1.59 in 1.33, lambda0 = 1), 12 m^2 linear triangles "
-                   "each (m = 16: 3,072 triangles, na = 73,728 per cone, node jitter 5 % of the ring spacing, "
-                   "seed 7); cone 2 rotated pi about x and shifted 1.5 along x; right-circularly polarised plane "
-                   "wave along +z; multiple-scattering iteration to the reference's convergence rule",
-             m=16, radius=0.5, height=1.0, n_obj=1.59, n_host=1.33, lambda0=1.0, seed=7)
-
-
-def write_cones(wd, m=None):
-    from bem3_emf_b2_gb300 import meshgen
-    m = m or CONES["m"]
-    nodes, elems = meshgen.cone_tri(m, CONES["radius"], CONES["height"], jitter=0.05, seed=CONES["seed"])
-    meshgen.write_mesh(os.path.join(wd, "cone.msh"), nodes, elems)
-    meshgen.write_medium(os.path.join(wd, "medium.txt"), [CONES["n_obj"]])
-    meshgen.write_ipw(os.path.join(wd, "ipw.txt"), [dict(lambda0=CONES["lambda0"], ni=CONES["n_host"], power=1.0,
-                                                          e0x=1.0, e0y=1j)])
-    return len(elems)
-
-
-def run_cones(args):
-    """The two-cone scene in the chosen form (one GPU): seconds per scene and
-    force/torque on each cone.  Its plain FP64 form (an FP64 LU and inverse of
-    na = 73,728 per cone, ~3e15 flop each) is not timed here."""
-    import torch
-    from bem3_emf_b2_gb300 import MultiScene, build, lib
-    build.build()
-    L = lib()
-    wd = tempfile.mkdtemp(prefix="cones_")
-    ne = write_cones(wd, args.cone_m)
-    med = [os.path.join(wd, "medium.txt")] * 2
-    msh = [os.path.join(wd, "cone.msh")] * 2
-    rv = np.array([[1.0, 0.0, 0.0], [1.0, 0.0, 0.0]])
-    th = np.array([0.0, np.pi])
-    tv = np.array([[0.0, 0.0, 0.0], [1.5, 0.0, 0.0]])
-    sc = MultiScene(med, msh, os.path.join(wd, "ipw.txt"), rv=rv, th=th, tv=tv)
-    times = []
-    F = N = None
-    l0 = L.gb_launch_count()
-    for i in range(args.warmup + args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        F, N = sc.step(form=1)
-        torch.cuda.synchronize()
-        if i >= args.warmup:
-            times.append(time.perf_counter() - t0)
-    it, cc = sc.iteration()
-    phases = sc.phase_times()
-    launches = (L.gb_launch_count() - l0) / (args.warmup + args.steps)
-    sc.close()
-    v = sum(times) / len(times)
-    return {"metric": METRIC, "value": v, "unit": "s/scene", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1000.0 * v, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "double-float (f32 pairs) quadrature, c64 LU + c128 refinement", "data": "synthetic (meshgen cones, seed 7)",
-            "config": {"workload": CONES["name"], "elements_per_cone": ne, "form": "mixed",
-                       "timing": "host wall clock around each scene step (synchronised)"},
-            "iterations": it, "cc": cc, "phases_s": phases, "force": F.tolist(), "torque": N.tolist(),
-            "gpu_launches": int(round(launches))}
+    if args.workload == "cones":
+        write_cones(wd, args.cone_m)
+    else:
+        write_sphere(wd, args.faces)
+    cpu = cpu_baseline(args, wd)
+    reason = ("the reference CPU path inverts each object's coupled matrix densely (zgetrf+zgetri, "
+              "solve_bieq2.c:343-408); for this workload that is %s and cannot finish a scene inside this run; "
+              "sampled estimate %.0f s/scene on %d cores" % (
+                  "2 x order 73,728 (87 GB c128 each, ~3.2e15 flop each)" if args.workload == "cones"
+                  else "order 12,288 plus the E/H stage and force that the CPU restatement does not cover",
+                  cpu["value"], cpu["cores"]))
+    return {"impl": "reference", "unavailable": reason,
+            "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "estimated")}}
 
 
 def profile_step(args):
     """Warm-up steps then exactly one chosen-form step (for ncu launch lists)."""
     import torch
-    from bem3_emf_b2_gb300 import Scene, build
+    from bem3_emf_b2_gb300 import build
     build.build()
     wd = tempfile.mkdtemp(prefix="prof_")
-    write_scene(wd, args.faces)
-    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+    sc, desc = open_workload(args, wd)
     for _ in range(args.warmup):
         sc.step(form=1)
     torch.cuda.synchronize()
     F, N = sc.step(form=1)
     torch.cuda.synchronize()
-    print("profile step done: faces=%d force=%s" % (args.faces, F))
+    print("profile step done: %s force=%s" % (desc["workload"][:40], np.asarray(F).ravel()))
     sc.close()
 
 
@@ -443,18 +500,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--profile-step", action="store_true",
                     help="profiling run: one chosen-form scene step after --warmup steps, nothing else, no JSON line")
-    ap.add_argument("--faces", type=int, default=8, help="quadrangles per cube face of the profiling scene")
-    ap.add_argument("--workload", choices=["sphere", "cones"], default="sphere",
-                    help="sphere: the bench line (both forms); cones: the two-cone scene, chosen form only")
+    ap.add_argument("--workload", choices=["cones", "sphere"], default="cones",
+                    help="cones: the two-cone scene (default); sphere: the 384-element sphere")
+    ap.add_argument("--faces", type=int, default=8, help="quadrangles per cube face of the sphere workload")
     ap.add_argument("--cone-m", type=int, default=None, help="rings per cone surface (12 m^2 triangles per cone)")
     args = ap.parse_args()
     if args.profile_step:
         profile_step(args)
         return
-    if args.workload == "cones":
-        out = run_cones(args)
-    else:
-        out = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:
         print(json.dumps(out))
 

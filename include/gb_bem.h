@@ -175,8 +175,8 @@ int gb_assemble_domain_noalloc(const double *cr, const double *cw, const int *et
  * <= 1e-13) instead of applying an explicit inverse.
  * gb_ir_info: corrections and final relative residual of the last solve.
  * gb_scene_step: assembly of every domain + factorisation + U, dU + E, H,
- * dE, dH.  form 0: FP64 assembly, FP64 LU and explicit inverse as in the
- * reference; form 1 (chosen): double-float regular pairs (gb_assemble2
+ * dE, dH.  form 0: FP64 assembly and FP64 factorisation (gb_factor_fp64);
+ * form 1 (chosen): double-float regular pairs (gb_assemble2
  * precision 2) and the mixed factorisation; form 2: FP32 far pairs
  * (precision 1) and mixed; form 3: FP64 assembly and mixed. */
 int gb_factor_mixed(gb_obj *o);
@@ -189,21 +189,30 @@ int gb_ir_info(gb_obj *o, int *iters, double *relres);
  * residual 10x per correction, makes the object factorise again with
  * tournament pivoting.  mode 1: tournament pivoting always.  mode 2
  * (diagnostic): as mode 0, but the first refinement check takes the
- * fallback, so that the refactorisation path can be exercised.  mode 3:
- * block elimination for an object whose elements all separate domain 0
- * (outside) from domain 1 (inside): the corrections go through complex-FP32
- * inverses of order NN (G0^-1, G1^-1, G0^-1 H0, and those of the two Schur
- * complements) instead of factors of the 8 NN x 8 NN matrix A -- about 43x
- * fewer flop and 5 NN^2 instead of 64 NN^2 elements; the FP64 refinement on
- * A is unchanged.  Other objects are factorised as in mode 0; a zero pivot
- * or a stalled refinement falls back to tournament-pivoted dense factors.
- * The environment variable GB_LU_MODE (0..3) sets the mode objects are
- * created with (default 0).
+ * fallback, so that the refactorisation path can be exercised.  mode 3 (the
+ * default): block elimination for an object whose elements all separate
+ * domain 0 (outside) from domain 1 (inside): the corrections go through
+ * complex-FP32 inverses of order NN (G0^-1, G1^-1, G0^-1 H0, and those of the
+ * two Schur complements; each node matrix randomised by butterflies and
+ * factorised without interchanges) instead of factors of the 8 NN x 8 NN
+ * matrix A -- about 43x fewer flop and 5 NN^2 instead of 64 NN^2 elements;
+ * the FP64 refinement on A is unchanged.  Other objects are factorised as in
+ * mode 0; a zero pivot or a stalled refinement falls back to
+ * tournament-pivoted dense factors.  The environment variable GB_LU_MODE
+ * (0..3) sets the mode objects are created with (default 3).
  * gb_lu_info: rbt = 1 if the current factors are of the randomised matrix,
- * 2 if they are the block factors of mode 3; fallbacks = refactorisations
- * after a zero pivot or a stalled refinement so far. */
+ * 2 if they are the FP32 block factors of mode 3, 3 if they are the FP64
+ * block factors of gb_factor_fp64; fallbacks = refactorisations after a zero
+ * pivot or a stalled refinement so far.
+ * gb_factor_fp64: the plain FP64 form's factorisation.  For an object with
+ * one interface in mode 3 the same block elimination in complex FP64 (node
+ * LUs with tournament pivoting, FP64 inverses and products; later solves
+ * take one FP64 correction and confirm the residual from G, H); otherwise
+ * the dense LU and explicit inverse of A as the reference's lu_dec_A
+ * (gb_invA_compute). */
 int gb_set_lu_pivoting(gb_obj *o, int mode);
 int gb_lu_info(gb_obj *o, int *rbt, int *fallbacks);
+int gb_factor_fp64(gb_obj *o);
 int gb_scene_step(gb_obj *o, int form, int type);
 
 /* Dense complex FP64 LU solve of a host system: A (n x n, row-major) X = B

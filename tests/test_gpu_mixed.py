@@ -121,7 +121,7 @@ def test_double_float_assembly_matches_fp64(case, gb_build, tmp_path):
 @pytest.mark.parametrize("case", ["sphere2", "cone_mix", "cone_tri", "cube1"])
 def test_butterfly_lu_matches_tournament_lu(case, gb_build, tmp_path):
     """The chosen form factorises the randomised matrix U^T A V without
-    interchanges (gb_set_lu_pivoting 0, the default); with tournament
+    interchanges (gb_set_lu_pivoting 0); with tournament
     pivoting (mode 1) the same refinement must give the same force and torque
     to the refinement's accuracy, and the randomised factors must have been
     used without a fallback on these scenes."""
@@ -138,6 +138,7 @@ def test_butterfly_lu_matches_tournament_lu(case, gb_build, tmp_path):
     write_inputs(meta, wd)
     sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
     o = sc.obj()
+    assert L.gb_set_lu_pivoting(o, 0) == 0  # dense butterfly factors (the default is block elimination)
     F0, N0 = sc.step(form=1)
     rbt, fb = ctypes.c_int(), ctypes.c_int()
     L.gb_lu_info(o, ctypes.byref(rbt), ctypes.byref(fb))

@@ -1,4 +1,4 @@
-"""Block elimination of the coupled system (gb_set_lu_pivoting mode 3).
+"""Block elimination of the coupled system (gb_set_lu_pivoting mode 3, the default).
 
 For an object whose elements all separate the exterior domain 0 from the
 interior domain 1, the chosen form's corrections can go through node-sized
@@ -49,6 +49,8 @@ def test_block_elimination_matches_dense_factors(case, gb_build, tmp_path):
     write_inputs(meta, wd)
     sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
     o = sc.obj()
+    assert _lu_info(L, o) == (0, 0)
+    assert L.gb_set_lu_pivoting(o, 0) == 0
     F0, N0 = sc.step(form=1)
     assert _lu_info(L, o)[0] == 1
     assert L.gb_set_lu_pivoting(o, 3) == 0
@@ -127,3 +129,54 @@ def test_block_elimination_sphere1536(gb_build, tmp_path):
     assert res[3][3][1] <= 1e-13
     d = _rel(res[3][0], res[3][1], res[0][0], res[0][1])
     assert d <= 1e-10, d
+
+
+def _bv(L, sc, meta):
+    """U, dU of every domain of the scene's object (reference layout)."""
+    o = sc.obj()
+    out = []
+    for d, ne in enumerate(meta["sb_Ne"]):
+        U = np.zeros((ne + 1, 4, 4), complex)
+        dU = np.zeros((ne + 1, 4, 4), complex)
+        assert L.gb_bv_download(o, d, U.ctypes.data, dU.ctypes.data, None, None, None, None) == 0
+        out += [U[1:], dU[1:]]
+    return out
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["sphere2", "cube1", "cone_mix", "cone_tri"])
+def test_fp64_block_elimination_matches_dense_inverse(case, gb_build, tmp_path):
+    """The plain FP64 form of a one-interface object factorises by the same
+    block elimination in complex FP64 (gb_factor_fp64); its boundary values
+    must equal those of the dense FP64 inverse (the reference's lu_dec_A) to
+    <= 1e-10 relative, force and torque to <= 1e-11, and both must reproduce
+    the reference's golden force."""
+    from bem3_emf_b2_gb300 import Scene
+    from tests._scenes import parse_analysis
+    L = _lib()
+    vp, ci = ctypes.c_void_p, ctypes.c_int
+    L.gb_bv_download.argtypes = [vp, ci] + [vp] * 6
+    L.gb_bv_download.restype = ci
+    meta, _ = load_case(case)
+    wd = str(tmp_path)
+    write_inputs(meta, wd)
+    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+    o = sc.obj()
+    assert L.gb_set_lu_pivoting(o, 0) == 0
+    F0, N0 = sc.step(form=0)
+    assert _lu_info(L, o)[0] == 0  # dense inverse
+    b0 = _bv(L, sc, meta)
+    assert L.gb_set_lu_pivoting(o, 3) == 0
+    F3, N3 = sc.step(form=0)
+    assert _lu_info(L, o) == (3, 0)
+    it, rr = sc.ir_info()
+    assert rr <= 1e-13 and it <= 3, (it, rr)
+    b3 = _bv(L, sc, meta)
+    sc.close()
+    for x, y in zip(b3, b0):
+        e = np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300)
+        assert e <= 1e-10, e
+    assert _rel(F3, N3, F0, N0) <= 1e-11
+    ref = parse_analysis(meta["analysis"])["force_0_0"]
+    err = np.linalg.norm(np.concatenate([F3, N3]) - ref) / np.linalg.norm(ref)
+    assert err <= 1e-9, err
