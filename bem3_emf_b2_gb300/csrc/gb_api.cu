@@ -105,6 +105,11 @@ static int ensure_tables() {
   memset(&t, 0, sizeof(t));
   gauleg(-1.0, 1.0, t.xli, t.wli, GB_GLN);
   gauleg(-1.0, 1.0, t.xhi, t.whi, GB_GHN);
+  for (int n = 1; n < GB_GLN; n++) gauleg(-1.0, 1.0, t.xn + n * (n - 1) / 2, t.wn + n * (n - 1) / 2, n);
+  for (int i = 0; i < GB_GLN; i++) {  // the GLN rule itself: the reference's table
+    t.xn[GB_GLN * (GB_GLN - 1) / 2 + i] = t.xli[i];
+    t.wn[GB_GLN * (GB_GLN - 1) / 2 + i] = t.wli[i];
+  }
   const double a = GB_P44_N;
   const double z44[4] = {-a, a, a, -a}, e44[4] = {-a, -a, a, a};
   const double n9 = 0.7745966692414833770359;
@@ -396,7 +401,7 @@ static int assemble_on(gb_obj* o, int did, int type, int precision, cudaStream_t
 
 static int check_asm_args(int type, int precision) {
   if (type < 0 || type > 3) { gbi_set_error("gb_assemble: quadrature type %d not in 0..3", type); return -1; }
-  if (precision < 0 || precision > 2) { gbi_set_error("gb_assemble: precision %d not in 0..2", precision); return -1; }
+  if (precision < 0 || precision > 3) { gbi_set_error("gb_assemble: precision %d not in 0..3", precision); return -1; }
   return 0;
 }
 
@@ -404,7 +409,7 @@ static void assembled(gb_obj* o, int precision) {
   o->have_invA = 0;
   o->have_lu32 = 0;
   o->have_blk64 = 0;
-  o->field_prec = precision == 2 ? 2 : 0;
+  o->field_prec = precision >= 2 ? precision : 0;
 }
 
 extern "C" int gb_assemble2(gb_obj* o, int did, int type, int precision) {
@@ -457,6 +462,28 @@ extern "C" int gb_cmatrix_download(gb_obj* o, int did, void* G, void* H, void* d
   if (dG) GB_CUDA(cudaMemcpy(dG, o->dG[did], 2 * N * N * sizeof(cplx), cudaMemcpyDeviceToHost));
   if (dH) GB_CUDA(cudaMemcpy(dH, o->dH[did], 2 * N * N * sizeof(cplx), cudaMemcpyDeviceToHost));
   if (dF) GB_CUDA(cudaMemcpy(dF, o->dF[did], 3 * N * sizeof(double), cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int gb_cmatrix_rows(gb_obj* o, int did, int nrows, const int* rows, void* G, void* H, void* dG, void* dH,
+                               double* dF) {
+  if (check_did(o, did)) return -1;
+  if (!o->G[did]) { gbi_set_error("gb_cmatrix_rows: domain %d not assembled", did); return -1; }
+  const size_t N = (size_t)o->m.sb_Ne[did] * 4;
+  for (int i = 0; i < nrows; i++)
+    if (rows[i] < 0 || (size_t)rows[i] >= N) { gbi_set_error("gb_cmatrix_rows: row %d out of range", rows[i]); return -1; }
+  for (int i = 0; i < nrows; i++) {
+    const size_t r = (size_t)rows[i];
+    cplx* g = (cplx*)G;
+    cplx* h = (cplx*)H;
+    cplx* dg = (cplx*)dG;
+    cplx* dh = (cplx*)dH;
+    if (G) GB_CUDA(cudaMemcpy(g + i * N, o->G[did] + r * N, N * sizeof(cplx), cudaMemcpyDeviceToHost));
+    if (H) GB_CUDA(cudaMemcpy(h + i * N, o->H[did] + r * N, N * sizeof(cplx), cudaMemcpyDeviceToHost));
+    if (dG) GB_CUDA(cudaMemcpy(dg + 2 * i * N, o->dG[did] + 2 * r * N, 2 * N * sizeof(cplx), cudaMemcpyDeviceToHost));
+    if (dH) GB_CUDA(cudaMemcpy(dh + 2 * i * N, o->dH[did] + 2 * r * N, 2 * N * sizeof(cplx), cudaMemcpyDeviceToHost));
+    if (dF) GB_CUDA(cudaMemcpy(dF + 3 * i, o->dF[did] + 3 * r, 3 * sizeof(double), cudaMemcpyDeviceToHost));
+  }
   return 0;
 }
 
@@ -1205,9 +1232,10 @@ extern "C" int gb_ir_info(gb_obj* o, int* iters, double* relres) {
 }
 
 // Assembly precision of each scene form: form 1 (the chosen form) integrates
-// the regular pairs in double-float, form 2 the far pairs in FP32, forms 0
-// and 3 everything in FP64.
-extern "C" int gb_form_precision(int form) { return form == 1 ? 2 : (form == 2 ? 1 : 0); }
+// the regular pairs in double-float with the distance-adaptive order
+// (precision 3), form 2 the far pairs in FP32, forms 0 and 3 everything in
+// FP64.
+extern "C" int gb_form_precision(int form) { return form == 1 ? 3 : (form == 2 ? 1 : 0); }
 
 // One scene step on the device for a single object: assembly of every
 // domain (quadrature type, precision gb_form_precision(form)), factorisation

@@ -68,6 +68,7 @@ struct AsmArgs {
   double* dF;
   double* Fs;      // scratch [N][Ne][3]
   const uint8_t* only;  // non-null: k_asm_regular integrates only the pairs flagged here
+  int adapt;       // k_asm_regular_df: the distance-adaptive order (precision 3)
 };
 
 // unit tangents at collocation node tn of element |td| (reference tz_te_bd_node d3b1_elem.c:122-143)
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo
   for (int d = 0; d < 3; d++) rt[d] = __ldg(a.ren + (size_t)atd * 12 + tn * 3 + d);
   node_tangents(T, tn, vt);
   RegAcc<2> D;
-  if (!reg_integrate_dn<2>(S, rt, vt, a.k, sd < 0, D)) {
+  if (!reg_integrate_dn<2>(S, rt, vt, a.k, sd < 0, D, a.adapt != 0)) {
     redo[p] = 1;
     return;
   }
@@ -916,7 +917,9 @@ extern "C" int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* 
 }
 
 // precision 0: FP64 throughout (the reference's arithmetic); 1: regular pairs
-// of the GLN x GLN rule in FP32 with FP64 near pairs (chosen form)
+// of the GLN x GLN rule in FP32 with FP64 near pairs; 2: regular pairs and
+// singular point sets in double-float; 3 (the chosen form): as 2 with the
+// regular pairs' order adapted to their distance (reg_order)
 extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG,
                                     cplx* dH, double* dF, double* Fs, cudaStream_t st) {
   int Ne = m->sb_Ne[did];
@@ -939,6 +942,7 @@ extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int p
   a.dF = dF;
   a.Fs = Fs;
   a.only = nullptr;
+  a.adapt = precision == 3;
   GB_CUDA(cudaMemsetAsync(G, 0, N * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(H, 0, N * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(dG, 0, 2 * N * N * sizeof(cplx), st));
@@ -948,7 +952,7 @@ extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int p
   size_t npair = N * (size_t)Ne;
   unsigned nb = (unsigned)((npair + 127) / 128);
   uint8_t* redo = nullptr;
-  if (precision == 2 && type == 2) {
+  if (precision >= 2 && type == 2) {
     GB_CUDA(cudaMallocAsync((void**)&redo, npair, st));
     k_asm_regular_df<<<nb, 128, 0, st>>>(a, redo);
     gbi_count_launch();
@@ -965,7 +969,7 @@ extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int p
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   if (redo) GB_CUDA(cudaFreeAsync(redo, st));
-  if (precision == 2) k_asm_singular<true><<<(unsigned)N, 256, 0, st>>>(a);
+  if (precision >= 2) k_asm_singular<true><<<(unsigned)N, 256, 0, st>>>(a);
   else k_asm_singular<false><<<(unsigned)N, 256, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());

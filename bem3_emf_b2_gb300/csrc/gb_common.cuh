@@ -90,9 +90,11 @@ __device__ __forceinline__ void ccossin(cplx z, cplx* cz, cplx* sz) {
 // Gauss-Legendre nodes/weights (computed on the host by the same Newton
 // iteration the reference uses, gauleg.c:3-36) and the small point rules of
 // the reference's init_elem_const (setup2.c:704-745).
+#define GB_NTAB (GB_GLN * (GB_GLN + 1) / 2)  // GL rules of 1..GLN points, rule n at n (n - 1) / 2
 struct GbTables {
   double xli[GB_GLN], wli[GB_GLN];
   double xhi[GB_GHN], whi[GB_GHN];
+  double xn[GB_NTAB], wn[GB_NTAB];
   double zt_44[4], et_44[4], wt_44[4];
   double zt_49[9], et_49[9], wt_49[9];
   double zt_34[4], et_34[4], wt_34[4];

@@ -24,11 +24,12 @@ extern "C" int gbi_upload_tables_field(const void* t) {
 
 // the regular integral of one (point, source element) pair: in double-float
 // when DF and the rule is GLN (falling back to FP64 near the CBD_SDF
-// decision), else FP64 -- the same values to ~1e-14
+// decision), else FP64 -- the same values to ~1e-14; adapt: the double-float
+// rule with the distance-adaptive order (reg_order)
 template <bool DF, int NDIR>
 __device__ __forceinline__ void reg_pair(const Elem& S, int type, const double rt[3], const double (*vt)[3], cplx k,
-                                         bool neg, RegAcc<NDIR>& A) {
-  if (DF && type == 2 && reg_integrate_dn<NDIR>(S, rt, vt, k, neg, A)) return;
+                                         bool neg, RegAcc<NDIR>& A, bool adapt) {
+  if (DF && type == 2 && reg_integrate_dn<NDIR>(S, rt, vt, k, neg, A, adapt)) return;
   reg_integrate<NDIR>(S, type, rt, vt, k, neg, A);
 }
 
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
     if (a.mode == FM_MEMP || a.mode == FM_EH) {
       if (!act) continue;
       RegAcc<0> A;
-      reg_pair<DF, 0>(S, a.type, rt, nullptr, k, neg, A);
+      reg_pair<DF, 0>(S, a.type, rt, nullptr, k, neg, A, o.prec == 3);
       acc[0] += A.F;
       if (a.mode == FM_MEMP) {
         for (int n = 0; n < 4; n++)
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
       RegAcc<1> A;
       bool fb = false;
       if (act) {
-        reg_pair<DF, 1>(S, a.type, rt, vt, k, neg, A);
+        reg_pair<DF, 1>(S, a.type, rt, vt, k, neg, A, o.prec == 3);
         fb = a.type < 3 && fabs(A.dF[0]) > GB_CBD_SDF;
       }
       warp_fallback<1>(fb, S, rt, vt, k, neg, A);
@@ -286,7 +287,7 @@ __global__ void __launch_bounds__(128) k_field_eh_memp(FieldArgs a) {
     RegAcc<3> A;
     bool fb[3] = {false, false, false};
     if (act) {
-      reg_pair<DF, 3>(S, a.type, rt, vt, k, neg, A);
+      reg_pair<DF, 3>(S, a.type, rt, vt, k, neg, A, o.prec == 3);
       if (a.type < 3)
         for (int d = 0; d < 3; d++) fb[d] = fabs(A.dF[d]) > GB_CBD_SDF;
     }
@@ -383,7 +384,7 @@ __global__ void __launch_bounds__(128) k_field_bd(BdArgs a) {
     Elem S;
     load_elem(S, o.cr, o.cw, o.etype, abs(sd));
     RegAcc<0> A;
-    reg_pair<DF, 0>(S, a.type, rt, nullptr, k, sd < 0, A);
+    reg_pair<DF, 0>(S, a.type, rt, nullptr, k, sd < 0, A, o.prec == 3);
     acc[0] += A.F;
     for (int n = 0; n < 4; n++)
       for (int l = 0; l < 3; l++) {
@@ -481,7 +482,7 @@ __global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
     RegAcc<1> A;
     bool fb = false;
     if (todo) {
-      reg_pair<DF, 1>(S, a.type, rt, vt, k, neg, A);
+      reg_pair<DF, 1>(S, a.type, rt, vt, k, neg, A, o.prec == 3);
       fb = a.type < 3 && fabs(A.dF[0]) > GB_CBD_SDF;
     }
     warp_fallback<1>(fb, S, rt, vt, k, neg, A);
@@ -523,7 +524,7 @@ __global__ void __launch_bounds__(128) k_cross_build_df(CrossArgs a, uint8_t* re
   Elem S;
   load_elem(S, o.cr, o.cw, o.etype, abs(sd));
   RegAcc<1> A;
-  if (!reg_integrate_dn<1>(S, rt, vt, k, sd < 0, A)) {
+  if (!reg_integrate_dn<1>(S, rt, vt, k, sd < 0, A, o.prec == 3)) {
     redo[q] = 1;
     return;
   }
@@ -599,7 +600,7 @@ extern "C" int gbi_cross_build(const FieldObj* o, int type, int n, const double*
   a.only = nullptr; a.Fs = nullptr;
   const unsigned nbw = (unsigned)(((size_t)n * 32 + 127) / 128);
   const int Ne = o->sb_Ne[0];
-  if (o->prec == 2 && type == 2 && Ne > 0) {
+  if (o->prec >= 2 && type == 2 && Ne > 0) {
     // double-float pass over all pairs, FP64 pass over the declined ones,
     // then the per-point sums in element order
     const size_t np = (size_t)n * Ne;
@@ -658,7 +659,7 @@ extern "C" int gbi_field(const FieldObj* o, int mode, int type, int n, const dou
   a.out = out;
   a.flag = flag;
   unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
-  const bool dfp = o->prec == 2;
+  const bool dfp = o->prec >= 2;
   if (mode == FM_EH_MEMP) {
     if (dfp) k_field_eh_memp<true><<<nb, 128, 0, st>>>(a);
     else k_field_eh_memp<false><<<nb, 128, 0, st>>>(a);
@@ -683,7 +684,7 @@ extern "C" int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, 
   a.zt = zt;
   a.out = out;
   unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
-  if (o->prec == 2) k_field_bd<true><<<nb, 128, 0, st>>>(a);
+  if (o->prec >= 2) k_field_bd<true><<<nb, 128, 0, st>>>(a);
   else k_field_bd<false><<<nb, 128, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());

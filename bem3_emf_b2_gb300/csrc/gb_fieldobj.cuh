@@ -22,6 +22,7 @@ struct FieldObj {
   const cplx* H[GB_MAXDOM];
   const cplx* dH[GB_MAXDOM];
   double lambda0;
-  int prec;  // 2: regular GLN pairs in double-float (gb_quad_df.cuh), else FP64
+  int prec;  // 2: regular GLN pairs in double-float (gb_quad_df.cuh); 3: the same with the
+             // distance-adaptive order of reg_order; else FP64
 };
 

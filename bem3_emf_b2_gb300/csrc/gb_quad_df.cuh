@@ -14,6 +14,10 @@
 // within 0.05 of CBD_SDF or is not finite, and the caller integrates the pair
 // in FP64.  Each translation unit that includes this header holds its own
 // copy of the tables (c_tabd) and uploads it with gbi_upload_tabd.
+// Adaptive order (precision 3): far pairs take an n x n Gauss-Legendre rule
+// with n < GLN chosen from the pair's distance and the element's phase
+// variation (reg_order); the GLN rule and its tables are unchanged for the
+// pairs that keep it.
 #pragma once
 #include "gb_quad.cuh"
 #include "gb_df64.cuh"
@@ -22,6 +26,7 @@
 struct GbTablesD {  // GL nodes and weights in double-float (hi, lo)
   float2 x[GB_GLN], w[GB_GLN];
   float2 xh[GB_GHN], wh[GB_GHN];
+  float2 xn[GB_NTAB], wn[GB_NTAB];  // the rules of 1..GLN points, rule n at n (n - 1) / 2
 };
 static __constant__ GbTablesD c_tabd;
 
@@ -32,6 +37,12 @@ static int gbi_upload_tabd(const GbTables* d) {
     g.x[i].y = (float)(d->xli[i] - (double)g.x[i].x);
     g.w[i].x = (float)d->wli[i];
     g.w[i].y = (float)(d->wli[i] - (double)g.w[i].x);
+  }
+  for (int i = 0; i < GB_NTAB; i++) {
+    g.xn[i].x = (float)d->xn[i];
+    g.xn[i].y = (float)(d->xn[i] - (double)g.xn[i].x);
+    g.wn[i].x = (float)d->wn[i];
+    g.wn[i].y = (float)(d->wn[i] - (double)g.wn[i].x);
   }
   for (int i = 0; i < GB_GHN; i++) {
     g.xh[i].x = (float)d->xhi[i];
@@ -187,13 +198,41 @@ __device__ __forceinline__ void reg_point_dnq(const PairDN<NDIR>& P, const RowQ&
   reg_kernel_dn<NDIR>(P, R, W, N, w, A);
 }
 
+// Points per direction of the regular rule of a pair in the adaptive form.
+// With a = |c1| + |c2| (+ |c3| for a quadrangle) the size of the source
+// element's parameter map and D = |R0| / a the distance of the observation
+// point from the element's point (0, 0) in those units:
+//   n_D = GLN for D < 2, 9 for D < 3, 6 for D < 5, 5 beyond (the integrand's
+//         nearest complex singularity bounds the Gauss error);
+//   n_k = 5, 7, 8 for |k| a <= 0.75, 2.4, 4.5, else GLN (the phase
+//         e^{ik|R|} varies by up to |k| a over the element);
+// n = max(n_D, n_k).  Calibrated against a 24-point rule on cubed-sphere
+// quadrangles (4 and 8 per face) and cone triangles (the reference's three
+// sub-quadrangle map): every output of a pair (G, H, F and the two
+// derivative sets) is within ~1e-12 of its natural scale (area / R^p with
+// the (1 + |k| R) factors of the kernel).
+__device__ __forceinline__ int reg_order(const Elem& S, double a0, cplx k) {
+  double a = 0.0;
+#pragma unroll
+  for (int j = 1; j < 4; j++) {
+    if (j == 3 && !S.quad) break;
+    a += sqrt(S.cr[0][j] * S.cr[0][j] + S.cr[1][j] * S.cr[1][j] + S.cr[2][j] * S.cr[2][j]);
+  }
+  const double D = a0 / a, ka = sqrt(k.x * k.x + k.y * k.y) * a;
+  const int nD = D < 2.0 ? GB_GLN : (D < 3.0 ? 9 : (D < 5.0 ? 6 : 5));
+  const int nk = ka <= 0.75 ? 5 : (ka <= 2.4 ? 7 : (ka <= 4.5 ? 8 : GB_GLN));
+  const int n = nD > nk ? nD : nk;
+  return n < GB_GLN ? n : GB_GLN;
+}
+
 // GLN x GLN integrals of source element S at the observation point rt (with
 // NDIR directions vt) in double-float, finished (scaled, sub-domain sign) into
 // D as reg_integrate<NDIR>(S, 2, ...) would; false if the pair must be
-// integrated in FP64 (a |dF| within 0.05 of CBD_SDF, or not finite)
+// integrated in FP64 (a |dF| within 0.05 of CBD_SDF, or not finite).
+// adapt: the n x n rule of reg_order instead (n = GLN for near pairs).
 template <int NDIR>
 __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double (*vt)[3], cplx k, bool neg,
-                                 RegAcc<NDIR>& D) {
+                                 RegAcc<NDIR>& D, bool adapt = false) {
   PairDN<NDIR> P;
   double R0[3];
 #pragma unroll
@@ -206,6 +245,8 @@ __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double
     for (int q = 0; q < NDIR; q++) P.vt[q][d] = df_from(vt[q][d]);
   }
   const double a0 = norm3(R0);
+  const int nq = adapt ? reg_order(S, a0, k) : GB_GLN;
+  const int off = nq * (nq - 1) / 2;
   P.a0 = df_from(a0);
   P.kr = df_from(k.x);
   P.ki = df_from(k.y);
@@ -225,22 +266,22 @@ __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double
   double S0;
   if (S.quad) {
     S0 = GB_I_FP;
-    for (int i = 0; i < GB_GLN; i++) {
-      const df x = dfmk(c_tabd.x[i].x, c_tabd.x[i].y), wx = dfmk(c_tabd.w[i].x, c_tabd.w[i].y);
+    for (int i = 0; i < nq; i++) {
+      const df x = dfmk(c_tabd.xn[off + i].x, c_tabd.xn[off + i].y), wx = dfmk(c_tabd.wn[off + i].x, c_tabd.wn[off + i].y);
       RowQ Q;
       reg_rowq_dn<NDIR>(P, x, Q);
-      for (int j = 0; j < GB_GLN; j++) {
-        const df y = dfmk(c_tabd.x[j].x, c_tabd.x[j].y), wy = dfmk(c_tabd.w[j].x, c_tabd.w[j].y);
+      for (int j = 0; j < nq; j++) {
+        const df y = dfmk(c_tabd.xn[off + j].x, c_tabd.xn[off + j].y), wy = dfmk(c_tabd.wn[off + j].x, c_tabd.wn[off + j].y);
         reg_point_dnq<NDIR>(P, Q, y, df_mul(wx, wy), A);
       }
     }
   } else {
     S0 = 0.0625 * GB_SQ3 * GB_I_SPSQ3;
     const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
-    for (int i = 0; i < GB_GLN; i++) {
-      const df x = dfmk(c_tabd.x[i].x, c_tabd.x[i].y), wx = dfmk(c_tabd.w[i].x, c_tabd.w[i].y);
-      for (int j = 0; j < GB_GLN; j++) {
-        const df y = dfmk(c_tabd.x[j].x, c_tabd.x[j].y), wy = dfmk(c_tabd.w[j].x, c_tabd.w[j].y);
+    for (int i = 0; i < nq; i++) {
+      const df x = dfmk(c_tabd.xn[off + i].x, c_tabd.xn[off + i].y), wx = dfmk(c_tabd.wn[off + i].x, c_tabd.wn[off + i].y);
+      for (int j = 0; j < nq; j++) {
+        const df y = dfmk(c_tabd.xn[off + j].x, c_tabd.xn[off + j].y), wy = dfmk(c_tabd.wn[off + j].x, c_tabd.wn[off + j].y);
         // w = wx wy (1 + x/4 + y/4); the three sub-quadrangle maps of the reference
         const df w = df_mul(df_mul(wx, wy), df_add_f(df_mul_f(df_add(x, y), 0.25f), 1.0f));
         const df xy = df_mul(x, y);

@@ -361,7 +361,7 @@ def run_gpu(args):
                "warmup": args.warmup, "ms_per_step": 1000.0 * tmax / args.steps, "higher_is_better": False,
                "scaling": "weak", "vs_baseline": None, "vs_baseline_note": VS_BASELINE_NOTE,
                "dtype": "double-float (f32 pairs) quadrature, c64 block LU + c128 refinement",
-               "data": "synthetic (meshgen %s, seeded)" % ("cones, seed 7" if cones else "cubed sphere"),
+               "data": "synthetic (meshgen %s)" % ("cones, seed 7" if cones else "cubed sphere, seeded by construction"),
                "config": cfg,
                "fp64_form": {"s_per_scene": sum(t64) / len(t64), "steps": len(t64),
                              "force_torque_rel_diff_vs_chosen": force_err,

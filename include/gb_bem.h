@@ -80,6 +80,13 @@ int gb_assemble(gb_obj *o, int did, int type);
  * (gb_field_points, gb_field_bd, gb_add_scattered) then integrate their
  * regular GLN pairs in double-float too; any other precision sets them back
  * to FP64.
+ * precision 3 (the chosen scene form): as precision 2, with the regular
+ * pairs' Gauss order adapted to the pair: n x n points, n = max(n_D, n_k),
+ * n_D = 12, 9, 6, 5 for distances below 2, 3, 5 and beyond (in units of the
+ * element's parameter-map size a), n_k = 5, 7, 8, 12 for |k| a up to 0.75,
+ * 2.4, 4.5 and beyond; pairs that keep n = 12 are integrated exactly as in
+ * precision 2.  Each far pair's integrals stay within ~1e-12 of their
+ * natural scale; the field kernels then use the same rule.
  * precision 1: regular pairs farther than three element radii in FP32
  * relative to the source element's centre (FP64 phase at the centre).
  * Matrix entries then carry ~1e-7 relative error (measured: G 9e-8, dH 2e-7,
@@ -88,12 +95,16 @@ int gb_assemble2(gb_obj *o, int did, int type, int precision);
 /* every domain of the object, as gb_assemble2, the domains at once (one host
  * thread and stream each) */
 int gb_assemble_all(gb_obj *o, int type, int precision);
-/* assembly precision of scene form `form` (1 -> 2, 2 -> 1, 0 and 3 -> 0) */
+/* assembly precision of scene form `form` (1 -> 3, 2 -> 1, 0 and 3 -> 0) */
 int gb_form_precision(int form);
 /* copy the resident matrices of domain did to/from host buffers in the
  * reference's .cmat layout (any pointer may be NULL to skip that matrix) */
 int gb_cmatrix_download(gb_obj *o, int did, void *G, void *H, void *dG, void *dH, double *dF);
 int gb_cmatrix_upload(gb_obj *o, int did, const void *G, const void *H, const void *dG, const void *dH, const double *dF);
+/* selected rows of the resident matrices of domain did (rows[i] in 0..N-1):
+ * row i of G and H (N complex each), rows 2 i, 2 i + 1 of dG and dH, row i
+ * of dF, packed in the order given (any output may be NULL) */
+int gb_cmatrix_rows(gb_obj *o, int did, int nrows, const int *rows, void *G, void *H, void *dG, void *dH, double *dF);
 
 /* Coupled matrix A (na x na, na = 8 NN) from the resident G, H of all domains,
  * LU-factorised with partial pivoting, and its explicit inverse.
@@ -176,8 +187,8 @@ int gb_assemble_domain_noalloc(const double *cr, const double *cw, const int *et
  * gb_ir_info: corrections and final relative residual of the last solve.
  * gb_scene_step: assembly of every domain + factorisation + U, dU + E, H,
  * dE, dH.  form 0: FP64 assembly and FP64 factorisation (gb_factor_fp64);
- * form 1 (chosen): double-float regular pairs (gb_assemble2
- * precision 2) and the mixed factorisation; form 2: FP32 far pairs
+ * form 1 (chosen): double-float regular pairs with the adaptive order
+ * (gb_assemble2 precision 3) and the mixed factorisation; form 2: FP32 far pairs
  * (precision 1) and mixed; form 3: FP64 assembly and mixed. */
 int gb_factor_mixed(gb_obj *o);
 int gb_ir_info(gb_obj *o, int *iters, double *relres);

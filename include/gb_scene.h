@@ -17,9 +17,10 @@ extern "C" {
 DOMD *gbh_scene_open(const char *medium_file, const char *mesh_file, const char *ipw_file);
 /* device step: assembly (quadrature type), factorisation, boundary values,
  * E/H, then the radiation force and torque about rc (type-0 surface rule,
- * mo_force_FN).  form 0: FP64 assembly, FP64 LU + explicit inverse, as the
- * reference; form 1 (chosen): double-float regular-pair assembly, complex
- * FP32 LU + FP64 iterative refinement; form 2: FP32 far-pair assembly (opt-in,
+ * mo_force_FN).  form 0: FP64 assembly and FP64 factorisation (block
+ * elimination for one-interface objects, else LU + explicit inverse as the
+ * reference); form 1 (chosen): double-float regular-pair assembly with the
+ * distance-adaptive order, complex FP32 factors + FP64 iterative refinement; form 2: FP32 far-pair assembly (opt-in,
  * ~1e-7 relative error), mixed LU; form 3: FP64 assembly, mixed LU
  * (gb_scene_step in gb_bem.h) */
 int gbh_scene_step(DOMD *md, int form, int type, const double *rc, double *F, double *N);

@@ -280,3 +280,208 @@ def lapack_inverse(A):
     if info != 0:
         raise np.linalg.LinAlgError("zgetri info=%d" % info)
     return inv
+
+
+# ---- incident plane waves, coupled system and boundary values (numpy) ----
+def ipw_setup(w):
+    """Polarisation and wave vector of one plane wave (restates setup_ipw,
+    reference mfb_src/ipw.c:65-89): dict with ki, E0, (ex, ey, ez), (hx, hy,
+    hz), propagation direction and translation f."""
+    ni, lam, power = float(w.get("ni", 1.0)), float(w.get("lambda0", 1.0)), float(w.get("power", 1.0))
+    e0x, e0y = complex(w.get("e0x", 1.0)), complex(w.get("e0y", 0.0))
+    cs = 1.0 / math.sqrt(abs(e0x) ** 2 + abs(e0y) ** 2)
+    ex, ey = e0x * cs, e0y * cs
+    hx, hy = -ey * ni, ex * ni
+    th, ph = float(w.get("theta", 0.0)), float(w.get("phi", 0.0))
+    st, ct, sp, cp = math.sin(th), math.cos(th), math.sin(ph), math.cos(ph)
+
+    def rot(ax, ay):
+        return np.array([ax * (sp * sp + cp * cp * ct) + ay * (sp * cp * ct - sp * cp),
+                         ax * (sp * cp * ct - sp * cp) + ay * (sp * sp * ct + cp * cp),
+                         -(ax * cp + ay * sp) * st])
+    return dict(ki=2.0 * math.pi * ni / lam, E0=math.sqrt(power * 2.0 / ni), e=rot(ex, ey), h=rot(hx, hy),
+                k=np.array([st * cp, st * sp, ct]), f=np.asarray(w.get("f", (0.0, 0.0, 0.0)), float))
+
+
+def incident(obj, waves):
+    """Incident potential Ui, dUi [(Ne+1)][4][4] at the collocation nodes of
+    the exterior elements (md == 0): E and dE/dn of the summed plane waves,
+    phi = 0 (restates init_boundary_data_u2, reference mo_setup.c:704-758, with
+    calc_ipw_EH_dv, mfb_src/ipw.c:15-33, summed as calc_mfb_EH_dv,
+    multi_fbeam.c:817-833)."""
+    ne = obj.Ne
+    Ui = np.zeros((ne + 1, 4, 4), complex)
+    dUi = np.zeros((ne + 1, 4, 4), complex)
+    ext = np.nonzero(obj.md[1:] == 0)[0] + 1
+    r = obj.ren[ext]                       # (m, 4, 3)
+    v = obj.wen[ext] / np.linalg.norm(obj.wen[ext], axis=2)[..., None]
+    for w in waves:
+        p = ipw_setup(w)
+        te = p["ki"] * ((r - p["f"]) @ p["k"])
+        Ee = (np.cos(te) + 1j * np.sin(te)) * p["E0"]
+        gcf = 1j * p["ki"] * (v @ p["k"])
+        Ui[ext, :, :3] += Ee[..., None] * p["e"]
+        dUi[ext, :, :3] += (Ee * gcf)[..., None] * p["e"]
+    return Ui, dUi
+
+
+def _domain_columns(obj, did):
+    """Per column (s, l) of domain did's matrices: valid mask, node c, main /
+    sub domain of the source element, its node normal (n_bd_node,
+    d3b1_elem.c:38-44), coupling constants delta, beta, sigma
+    (solve_bieq2.c:270-275)."""
+    sid = obj.sids[did][1:]
+    asd = np.abs(sid)
+    N = 4 * len(sid)
+    l = np.tile(np.arange(4), len(sid))
+    e = np.repeat(asd, 4)
+    valid = ~((l == 3) & (obj.etype[e] == 0))
+    c = obj.eni[e, l]
+    mdid, sdid = obj.md[e], obj.sd[e]
+    vn = obj.wen[e, l] / np.linalg.norm(obj.wen[e, l], axis=1)[:, None]
+    k1, k2 = obj.kn[mdid], obj.kn[sdid]
+    delt = k1 * k1 - k2 * k2
+    beps = k1 * k1 / (k2 * k2)
+    return dict(N=N, valid=valid, c=c, e=e, l=l, mdid=mdid, sdid=sdid, vn=vn, delt=delt, beps=beps, sigm=1.0 - beps)
+
+
+def domain_rows(obj, did):
+    """The rows (t - 1) * 4 + tn of domain did's matrices that become rows of
+    A, in order: the fourth node of triangles is skipped
+    (solve_bieq2.c:228-239)"""
+    sid = obj.sids[did][1:]
+    tn = np.tile(np.arange(4), len(sid))
+    e = np.repeat(np.abs(sid), 4)
+    return np.nonzero(~((tn == 3) & (obj.etype[e] == 0)))[0]
+
+
+def build_A_rows(obj, GH, rows_of=None):
+    """Rows of the coupled matrix A (8 NN columns), vectorised restatement of
+    create_Amatrix_csr_dac (reference solve_bieq2.c:209-341).  rows_of None:
+    GH = {did: (G, H)} full domain matrices and every row of A, in A's order;
+    else GH[did] holds only the rows rows_of[did] of domain did's G and H
+    (positions in the domain's N rows, fourth nodes of triangles excluded)
+    and the result has, per domain and component cid = 0..3, those rows."""
+    nn = obj.NN
+    blocks = []
+    for did in range(obj.MN + 1):
+        G, H = GH[did]
+        if rows_of is None:
+            rows = domain_rows(obj, did)
+            Gr, Hr = G[rows], H[rows]
+        else:
+            Gr, Hr = G, H
+        nr = Gr.shape[0]
+        col = _domain_columns(obj, did)
+        m_main = col["valid"] & (col["mdid"] == did)
+        m_sub = col["valid"] & (col["mdid"] != did)
+        cm, cs = np.nonzero(m_main)[0], np.nonzero(m_sub)[0]
+        for cid in range(4):
+            A = np.zeros((nr, 8 * nn), complex)
+            A[:, nn * cid + col["c"][cm]] = Hr[:, cm]
+            A[:, nn * (cid + 4) + col["c"][cm]] = -Gr[:, cm]
+            c = col["c"][cs]
+            g, h = Gr[:, cs], Hr[:, cs]
+            vn = col["vn"][cs]
+            if cid < 3:
+                A[:, nn * cid + c] = h
+                A[:, nn * 3 + c] = g * (col["delt"][cs] * vn[:, cid])
+                A[:, nn * (cid + 4) + c] = g
+            else:
+                for k in range(3):
+                    A[:, nn * k + c] = g * (col["sigm"][cs] * vn[:, k])
+                A[:, nn * 3 + c] = h
+                A[:, nn * 7 + c] = g * col["beps"][cs]
+            blocks.append(A)
+    return np.concatenate(blocks)
+
+
+def build_A_dense(obj, GH):
+    """Coupled matrix A (na x na) from {did: (G, H)} (all rows of build_A_rows;
+    same entries as Obj.build_A)."""
+    return build_A_rows(obj, GH)
+
+
+def build_B(obj, GH, Ui, dUi, rows_of=None):
+    """Right-hand side B from the incident potential, vectorised restatement
+    of create_Bmatrix_dac (reference mo_solve.c:150-244): rows of domain did
+    take, over the source elements whose sub domain is did and whose main
+    domain is 0, -H Ui - G dUi - G Ui_phi delta n_c (c < 3) and
+    -H Ui_phi - sigma G (n . Ui) - beta G dUi_phi (c = 3).  rows_of as in
+    build_A_rows (None: GH full matrices, all of B)."""
+    out = []
+    for did in range(obj.MN + 1):
+        G, H = GH[did]
+        if rows_of is None:
+            rows = domain_rows(obj, did)
+            G, H = G[rows], H[rows]
+        col = _domain_columns(obj, did)
+        m = col["valid"] & (col["mdid"] != did) & (col["mdid"] == 0)
+        cs = np.nonzero(m)[0]
+        e, l = col["e"][cs], col["l"][cs]
+        vn = col["vn"][cs]
+        Gr, Hr = G[:, cs], H[:, cs]
+        u, du = Ui[e, l], dUi[e, l]
+        for cid in range(4):
+            if cid < 3:
+                b = -Hr @ u[:, cid] - Gr @ du[:, cid] - Gr @ (u[:, 3] * col["delt"][cs] * vn[:, cid])
+            else:
+                b = (-Hr @ u[:, 3] - Gr @ (col["sigm"][cs] * (vn * u[:, :3]).sum(1))
+                     - Gr @ (col["beps"][cs] * du[:, 3]))
+            out.append(b)
+    return np.concatenate(out)
+
+
+def store_bv(obj, X, Ui, dUi):
+    """Boundary values U, dU [(Ne_d+1)][4][4] of every domain from the solution
+    X (restates tmatrix_bd_store, reference mo_solve.c:457-545)."""
+    nn = obj.NN
+    res = []
+    for d in range(obj.MN + 1):
+        sid = obj.sids[d]
+        U = np.zeros((len(sid), 4, 4), complex)
+        dU = np.zeros((len(sid), 4, 4), complex)
+        for s in range(1, len(sid)):
+            asd = abs(sid[s])
+            mdid, sdid = obj.md[asd], obj.sd[asd]
+            for l in range(4 if obj.etype[asd] else 3):
+                c = obj.eni[asd, l]
+                if d == mdid:
+                    for i in range(4):
+                        U[s, l, i] = X[nn * i + c]
+                        dU[s, l, i] = X[nn * (i + 4) + c]
+                    continue
+                k1, k2 = obj.kn[mdid], obj.kn[sdid]
+                delt, beps = k1 * k1 - k2 * k2, k1 * k1 / (k2 * k2)
+                sigm = 1.0 - beps
+                n = obj.wen[asd, l] / np.linalg.norm(obj.wen[asd, l])
+                tU = np.array([X[nn * i + c] for i in range(4)])
+                for i in range(3):
+                    U[s, l, i] = tU[i]
+                    dU[s, l, i] = -(X[nn * (i + 4) + c] + delt * tU[3] * n[i])
+                    if mdid == 0:
+                        U[s, l, i] += Ui[asd, l, i]
+                        dU[s, l, i] += -dUi[asd, l, i]
+                U[s, l, 3] = tU[3]
+                dU[s, l, 3] = -(beps * X[nn * 7 + c] + sigm * np.dot(n, tU[:3]))
+                if mdid == 0:
+                    dU[s, l, 3] += -sigm * np.dot(n, Ui[asd, l, :3])
+        res.append(dict(U=U, dU=dU))
+    return res
+
+
+def solve_single(obj, waves, type_=2):
+    """The reference's single-object solve on the CPU: all rows of every
+    domain (C restatement), A and B, X = A^-1 B through LAPACK's LU solve
+    (the reference applies the zgetrf/zgetri inverse, solve_bieq2.c:343-408,
+    mo_solve.c:246-274), boundary values.  Returns (bv, GH, X)."""
+    from scipy.linalg import lu_factor, lu_solve
+    GH = {}
+    for d in range(obj.MN + 1):
+        G, H, _, _, _ = obj.rows(d, type_=type_)
+        GH[d] = (G, H)
+    Ui, dUi = incident(obj, waves)
+    A = build_A_dense(obj, GH)
+    B = build_B(obj, GH, Ui, dUi)
+    X = lu_solve(lu_factor(A, overwrite_a=True, check_finite=False), B, check_finite=False)
+    return store_bv(obj, X, Ui, dUi), GH, X
