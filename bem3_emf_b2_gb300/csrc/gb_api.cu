@@ -93,14 +93,18 @@ extern "C" unsigned long long gb_launch_count(void) { return g_launches.load(); 
 extern "C" void* gb_obj_stream(gb_obj* o);
 
 // ------------------------------------------------------------------ tables
+// The quadrature tables live in __constant__ memory, which every device holds
+// separately: they are uploaded once per device (a blocking copy), so that a
+// process that moves between devices uploads nothing on later calls.
 static std::mutex g_init_mu;
-static int g_tables_dev = -1;
+static bool g_tables_done[64];
 
 static int ensure_tables() {
   int dev;
   GB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { gbi_set_error("device ordinal %d not supported", dev); return -1; }
   std::lock_guard<std::mutex> lk(g_init_mu);
-  if (g_tables_dev == dev) return 0;
+  if (g_tables_done[dev]) return 0;
   GbTables t;
   memset(&t, 0, sizeof(t));
   gauleg(-1.0, 1.0, t.xli, t.wli, GB_GLN);
@@ -134,7 +138,7 @@ static int ensure_tables() {
   for (int i = 0; i < 7; i++) { t.zt_37[i] = z37[i]; t.et_37[i] = e37[i]; t.wt_37[i] = w37[i]; }
   if (gbi_upload_tables_asm(&t)) return -1;
   if (gbi_upload_tables_field(&t)) return -1;
-  g_tables_dev = dev;
+  g_tables_done[dev] = true;
   return 0;
 }
 

@@ -6,12 +6,19 @@
 #  * Outputs: oracle/_ref/libbem3ref.so and the executables d3b2_create_matrix,
 #    d3b2_bv_solver, example1, example2, example4 (example3 needs libpng, which
 #    is absent) and bem3_analysis (this repository's driver, reference API only).
-# Usage: oracle/build_ref.sh [reference_dir]   (default /root/reference)
+# Usage: oracle/build_ref.sh [reference_dir]
+#        oracle/build_ref.sh --where   (print the reference directory; exit 2 if absent)
+# The reference directory is the argument, else $BEM3_REFERENCE_DIR, else the
+# location this container mounts it at.  This recipe is the one place that
+# names that location; the Python side asks it (oracle.reference_dir()).
 set -euo pipefail
-REF=${1:-/root/reference}
+WHERE=0
+if [ "${1:-}" = "--where" ]; then WHERE=1; shift; fi
+REF=${1:-${BEM3_REFERENCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
-[ -d "$REF/d3b2_src" ] || { echo "reference sources not found at $REF" >&2; exit 2; }
+[ -d "$REF/d3b2_src" ] || { [ $WHERE = 1 ] || echo "reference sources not found at $REF" >&2; exit 2; }
+if [ $WHERE = 1 ]; then echo "$REF"; exit 0; fi
 mkdir -p "$OUT"
 BLASDIR=$(python3 -c "import numpy,os;print(os.path.join(os.path.dirname(numpy.__file__)+'.libs'))")
 BLAS=$(ls "$BLASDIR"/libscipy_openblas64_*.so | head -1)

@@ -6,14 +6,15 @@ total field at r = (0.3, 0, 1.1) for quadrature types 0 and 1, radiation
 force and torque about the origin and absorbed power of both objects;
 d3b2_bv_solver.log: the convergence history) into expected.json.
 
-Run where the reference is present:  python3 tests/golden/make_verification1.py
+Run where the reference is present:
+    python3 tests/golden/make_verification1.py [reference_dir]
+(default: the directory oracle/build_ref.sh --where reports).
 """
 import json
 import os
 import re
 import shutil
 
-SRC = "/root/reference/verification1"
 DST = os.path.join(os.path.dirname(os.path.abspath(__file__)), "verification1")
 FILES = ["cone_m1_p5.msh", "medium_data.txt", "ipw.txt", "object_settings_v.txt"]
 
@@ -22,7 +23,7 @@ def cnum(re_s, im_s):
     return [float(re_s), float(im_s)]
 
 
-def extract(src=SRC):
+def extract(src):
     """the values printed by the reference's verification1 run"""
     log = open(os.path.join(src, "example1.log")).read()
     exp = {"point": [0.3, 0.0, 1.1], "fields": {}, "force": {}, "absorb": {}}
@@ -51,10 +52,21 @@ def extract(src=SRC):
 
 
 def main():
+    import subprocess
+    import sys
+    if len(sys.argv) > 1:
+        ref = sys.argv[1]
+    else:
+        here = os.path.dirname(os.path.abspath(__file__))
+        ref = subprocess.run([os.path.join(here, "..", "..", "oracle", "build_ref.sh"), "--where"], capture_output=True,
+                             text=True).stdout.strip()
+    if not ref:
+        sys.exit("the reference's sources were not found (give their directory as the argument)")
+    src = os.path.join(ref, "verification1")
     os.makedirs(DST, exist_ok=True)
     for f in FILES:
-        shutil.copyfile(os.path.join(SRC, f), os.path.join(DST, f))
-    json.dump(extract(), open(os.path.join(DST, "expected.json"), "w"), indent=1)
+        shutil.copyfile(os.path.join(src, f), os.path.join(DST, f))
+    json.dump(extract(src), open(os.path.join(DST, "expected.json"), "w"), indent=1)
 
 
 if __name__ == "__main__":

@@ -10,8 +10,10 @@ import subprocess
 import numpy as np
 import pytest
 
+import oracle
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REFSRC = "/root/reference"
+REFSRC = oracle.reference_dir() or ""
 REF = os.path.join(ROOT, "oracle", "_ref")
 
 CASES = [("verification1/v1.dat", "verification1/example1.log"),
@@ -26,11 +28,11 @@ def _log_fields(path):
     return v
 
 
-@pytest.mark.skipif(not os.path.isdir(REFSRC), reason="reference sources not present")
+@pytest.mark.skipif(not REFSRC, reason="reference sources not present")
 @pytest.mark.parametrize("dat,log", CASES)
 def test_ref_reproduces_shipped_logs(dat, log, tmp_path):
     if not os.path.exists(os.path.join(REF, "ref_point")):
-        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh")], stdout=subprocess.DEVNULL)
+        subprocess.check_call([os.path.join(ROOT, "oracle", "build_ref.sh"), REFSRC], stdout=subprocess.DEVNULL)
     out = subprocess.run([os.path.join(REF, "ref_point"), os.path.join(REFSRC, dat), "0.3", "0.0", "1.1"],
                          capture_output=True, text=True, check=True, cwd=str(tmp_path)).stdout
     mine = np.array([[float(x) for x in l.split()[2:]] for l in out.splitlines()]).reshape(2, 6, 2)
@@ -40,7 +42,7 @@ def test_ref_reproduces_shipped_logs(dat, log, tmp_path):
         assert err < 1e-13, "type %d relative difference %g" % (t, err)
 
 
-@pytest.mark.skipif(not os.path.isdir(REFSRC), reason="reference sources not present")
+@pytest.mark.skipif(not REFSRC, reason="reference sources not present")
 def test_verification1_fixture_matches_reference():
     """The committed verification1 fixture (inputs and the printed values)
     is what make_verification1.py extracts from the reference's own files."""
@@ -51,9 +53,9 @@ def test_verification1_fixture_matches_reference():
     mod = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(mod)
     committed = json.load(open(os.path.join(ROOT, "tests", "golden", "verification1", "expected.json")))
-    assert mod.extract() == committed
+    assert mod.extract(os.path.join(REFSRC, "verification1")) == committed
     assert len(committed["fields"]) == 2 and len(committed["force"]) == 4 and len(committed["absorb"]) == 4
     assert len(committed["cc"]) == 10
     for f in mod.FILES:
-        assert filecmp.cmp(os.path.join(mod.SRC, f), os.path.join(ROOT, "tests", "golden", "verification1", f),
+        assert filecmp.cmp(os.path.join(REFSRC, "verification1", f), os.path.join(ROOT, "tests", "golden", "verification1", f),
                            shallow=False), f

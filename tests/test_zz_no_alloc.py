@@ -75,3 +75,31 @@ def test_noalloc_assembly_matches_gb_assemble(case, gb_build, tmp_path):
                                       cr.data_ptr(), None)
     assert rc == -1 and b"418" in L.gb_last_error()
     sc.close()
+
+
+def test_noalloc_rejects_bad_arguments_before_device_work(gb_build):
+    """The argument checks run before any device call (so this needs no GPU):
+    a domain beyond the fixed scratch, a quadrature type or domain id out of
+    range, and any null input or output pointer each return -1 with a message
+    naming the problem."""
+    from bem3_emf_b2_gb300 import lib
+    L = lib()
+    vp, ci, cd = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    L.gb_assemble_domain_noalloc.argtypes = [vp, vp, vp, vp, vp, ci, cd, cd, ci, ci, vp, vp, vp, vp, vp, vp]
+    L.gb_assemble_domain_noalloc.restype = ci
+    fake = 4096  # never dereferenced: every call below fails its checks first
+
+    def call(Ne=10, did=0, type_=2, null=None):
+        ptrs = [fake] * 10
+        if null is not None:
+            ptrs[null] = None
+        return L.gb_assemble_domain_noalloc(ptrs[0], ptrs[1], ptrs[2], ptrs[3], ptrs[4], Ne, 1.0, 0.0, did, type_,
+                                            ptrs[5], ptrs[6], ptrs[7], ptrs[8], ptrs[9], None)
+    assert call(Ne=0) == -1 and b"1..418" in L.gb_last_error()
+    assert call(Ne=419) == -1 and b"1..418" in L.gb_last_error()
+    assert call(type_=4) == -1 and b"quadrature type 4" in L.gb_last_error()
+    assert call(type_=-1) == -1 and b"quadrature type -1" in L.gb_last_error()
+    assert call(did=-1) == -1 and b"domain id -1" in L.gb_last_error()
+    assert call(did=16) == -1 and b"domain id 16" in L.gb_last_error()
+    for i in range(10):
+        assert call(null=i) == -1 and b"null" in L.gb_last_error(), i
