@@ -74,6 +74,10 @@ int gbi_schur_factor(GbSchur* s, const GbMeshDev* m, const cplx* G0, const cplx*
                      const int* sid0, const int* sid1, const int* rowk0, const int* rowk1, cudaStream_t st);
 int gbi_schur_apply(GbSchur* s, const cplx* r, cplx* x, cudaStream_t st);
 }
+#include <functional>
+typedef std::function<int(const cplx* x, cplx* y, cudaStream_t st)> GbOp;
+extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const GbOp& A, const GbOp& M, int m,
+                         double tol, int maxit, cudaStream_t st, int* iters, double* relres);
 
 // ------------------------------------------------------------------ errors
 static thread_local char g_err[1024];
@@ -210,6 +214,7 @@ struct gb_obj {
   // rounding level) -- the FP64 form of objects whose dense inverse does not fit
   GbSchur* schur64;
   int have_blk64;
+  int refine_mode;  // 0: FP64 GMRES (default), 1: classical refinement (diagnostic)
   // arithmetic of the regular pairs of the field kernels (potentials at
   // points, fields on the boundary, cross operators): 2 double-float after a
   // precision-2 assembly, else FP64
@@ -285,7 +290,7 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   o->LU32 = nullptr; o->ipiv32 = nullptr; o->perm32 = nullptr; o->have_lu32 = 0; o->ir_iters = 0; o->ir_relres = 0.0;
   o->rbt = nullptr; o->lu_rbt = 0; o->lu_mode = 0; o->lu_fallbacks = 0; o->field_prec = 0;
   o->schur = nullptr; o->schur_ok = 0; o->lu_schur = 0;
-  o->schur64 = nullptr; o->have_blk64 = 0;
+  o->schur64 = nullptr; o->have_blk64 = 0; o->refine_mode = 0;
   o->lu_mode = 3;  // block elimination where the object allows it
   {  // GB_LU_MODE: the objects' initial gb_set_lu_pivoting mode (0..3)
     const char* e = getenv("GB_LU_MODE");
@@ -1162,10 +1167,10 @@ static int apply_A(gb_obj* o, const cplx* x, cplx* PQ, cplx* y) {
   return 0;
 }
 
-// FP64 iterative refinement with the FP32 factors: x <- x + LU32^-1 (b - A x)
-// until ||b - A x|| <= 1e-13 ||b|| (at most 30 corrections); b - A x is formed
-// in FP64 from G and H
-static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
+// Classical FP64 iterative refinement with the FP32 factors (refinement mode
+// 1, a diagnostic): x <- x + LU32^-1 (b - A x) until ||b - A x|| <= 1e-13 ||b||
+// (at most 30 corrections); b - A x is formed in FP64 from G and H
+static int ir_classical(gb_obj* o, const cplx* B, cplx* X) {
   size_t na = o->na;
   size_t nmax = 0;
   for (int d = 0; d <= o->m.MN; d++) nmax = std::max(nmax, 4 * (size_t)o->m.sb_Ne[d]);
@@ -1227,6 +1232,78 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
   if (!rc && rel > 1e-10) { gbi_set_error("iterative refinement stalled at relative residual %g", rel); rc = -1; }
   cudaFree(r); cudaFree(y); cudaFree(PQ); cudaFree(d); cudaFree(d2); cudaFree(nrm);
   return rc;
+}
+
+// refactorisation with tournament pivoting after the butterfly or block
+// factors failed to refine
+static int refactor_pivoted(gb_obj* o) {
+  int hinfo = 0;
+  o->lu_fallbacks++;
+  o->lu_schur = 0;
+  if (alloc_lu32(o)) return -1;
+  if (factor32(o, false, &hinfo)) return -1;
+  if (hinfo) { gbi_set_error("ir_solve: FP32 factor singular (info=%d)", hinfo); return -1; }
+  return 0;
+}
+
+// z = M^-1 v with the object's current factors (FP32 dense butterfly or
+// tournament LU, FP32 or FP64 block elimination); d, d2: FP32 work vectors
+static int precond(gb_obj* o, const cplx* v, cplx* z, cplxf* d, cplxf* d2, cudaStream_t st) {
+  const size_t na = o->na;
+  GB_CUDA(cudaMemsetAsync(z, 0, na * sizeof(cplx), st));
+  if (o->have_blk64) return gbi_schur_apply(o->schur64, v, z, st);
+  if (o->lu_schur) return gbi_schur_apply(o->schur, v, z, st);
+  if (o->lu_rbt)
+    return gbi_ir_step_rbt(z, v, d, d2, o->LU32, na, (int)na, o->perm32, o->rbt, o->rbt + 2 * na, st);
+  return gbi_ir_step(z, v, d, d2, o->LU32, na, (int)na, o->perm32, st);
+}
+
+// FP64 GMRES(20) refinement, right-preconditioned by the current factors, to
+// ||b - A x|| <= 1e-13 ||b||; A applied in FP64 from G and H.  A run that
+// does not converge with butterfly or block factors (or, in the diagnostic
+// LU mode 2, after its first iteration) refactorises with tournament
+// pivoting and continues from the current x.
+static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
+  if (o->refine_mode == 1) return ir_classical(o, B, X);
+  const size_t na = o->na;
+  size_t nmax = 0;
+  for (int d = 0; d <= o->m.MN; d++) nmax = std::max(nmax, 4 * (size_t)o->m.sb_Ne[d]);
+  cplx* PQ = nullptr;
+  cplxf *d = nullptr, *d2 = nullptr;
+  if (dalloc((void**)&PQ, 8 * nmax * sizeof(cplx)) || dalloc((void**)&d, na * sizeof(cplxf)) ||
+      dalloc((void**)&d2, na * sizeof(cplxf))) {
+    cudaFree(PQ); cudaFree(d);
+    return -1;
+  }
+  GbOp A = [o, PQ](const cplx* x, cplx* y, cudaStream_t) { return apply_A(o, x, PQ, y); };
+  GbOp M = [o, d, d2](const cplx* v, cplx* z, cudaStream_t st) { return precond(o, v, z, d, d2, st); };
+  int rc = 0;
+  if (cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess) { gbi_set_error("ir_solve: memset"); rc = -1; }
+  int it = 0, tot = 0;
+  double rel = 1.0;
+  const bool forced = o->lu_mode == 2 && o->lu_rbt;  // diagnostic: the fallback after one iteration
+  int r = rc ? -1 : gbi_gmres(na, B, X, true, A, M, 20, 1e-13, forced ? 1 : 60, o->st, &it, &rel);
+  tot += it;
+  if (r == 1 && !o->have_blk64 && (o->lu_rbt || o->lu_schur)) {
+    if (!(rel < 1.0) && cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess) r = -1;
+    if (r == 1 && refactor_pivoted(o)) r = -1;
+    if (r == 1) {
+      r = gbi_gmres(na, B, X, !(rel < 1.0), A, M, 20, 1e-13, 60, o->st, &it, &rel);
+      tot += it;
+    }
+  }
+  o->ir_iters = tot;
+  o->ir_relres = rel;
+  if (r < 0) rc = -1;
+  else if (r == 1 || rel > 1e-10) { gbi_set_error("iterative refinement stalled at relative residual %g", rel); rc = -1; }
+  cudaFree(PQ); cudaFree(d); cudaFree(d2);
+  return rc;
+}
+
+extern "C" int gb_set_refinement(gb_obj* o, int mode) {
+  if (mode < 0 || mode > 1) { gbi_set_error("gb_set_refinement: mode %d not in 0..1", mode); return -1; }
+  o->refine_mode = mode;
+  return 0;
 }
 
 extern "C" int gb_ir_info(gb_obj* o, int* iters, double* relres) {

@@ -1169,6 +1169,7 @@ static int cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, const cplx
 extern "C" size_t gbi_tc_scratch_floats(int M, int N, int K);
 extern "C" int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, const cplxf* B, size_t ldb, cplxf* C,
                                 size_t ldc, int passes, float* scratch, int* err, cudaStream_t st);
+extern "C" int gbi_tc_passes(void);
 
 // Complex-FP32 LU: the trailing updates on the tensor cores (split TF32, three
 // passes: FP32-level products), scratch and the time-out flag shared by all
@@ -1190,7 +1191,7 @@ static int cgetrf_tc(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cuda
   GB_CUDA(cudaMallocAsync((void**)&err, 16, st));
   GB_CUDA(cudaMemsetAsync(err, 0, 4, st));
   auto tc = [scratch, err](int M, int N, int K, const cplxf* a, size_t la, const cplxf* b, size_t lb, cplxf* c, size_t lc,
-                           cudaStream_t s) { return gbi_tc_cgemm_sub(M, N, K, a, la, b, lb, c, lc, 3, scratch, err, s); };
+                           cudaStream_t s) { return gbi_tc_cgemm_sub(M, N, K, a, la, b, lb, c, lc, gbi_tc_passes(), scratch, err, s); };
   int rc = lu_factor<cplxf>(A, lda, n, ipiv, info, st, tc, pivot);
   int h = 0;
   if (!rc && (cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -1986,7 +1987,7 @@ extern "C" int gbi_cinverse_tc(const cplxf* LU, size_t lda, int n, const int* pe
   GB_CUDA(cudaMallocAsync((void**)&err, 16, st));
   GB_CUDA(cudaMemsetAsync(err, 0, 4, st));
   auto tc = [scratch, err](int M, int N, int K, const cplxf* a, size_t la, const cplxf* b, size_t lb, cplxf* c, size_t lc,
-                           cudaStream_t s) { return gbi_tc_cgemm_sub(M, N, K, a, la, b, lb, c, lc, 3, scratch, err, s); };
+                           cudaStream_t s) { return gbi_tc_cgemm_sub(M, N, K, a, la, b, lb, c, lc, gbi_tc_passes(), scratch, err, s); };
   int rc = lu_solve_blocked<cplxf>(LU, lda, n, X, ldx, n, st, tc);
   int h = 0;
   if (!rc && (cudaMemcpyAsync(&h, err, 4, cudaMemcpyDeviceToHost, st) != cudaSuccess ||

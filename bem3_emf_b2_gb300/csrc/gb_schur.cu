@@ -51,6 +51,7 @@ int gbi_perm_identity(int n, int* perm, cudaStream_t st);
 int gbi_cinverse_tc(const cplxf* LU, size_t lda, int n, const int* perm, cplxf* X, size_t ldx, cudaStream_t st);
 int gbi_tc_cgemm_sub(int M, int N, int K, const cplxf* A, size_t lda, const cplxf* B, size_t ldb, cplxf* C, size_t ldc,
                      int passes, float* scratch, int* err, cudaStream_t st);
+int gbi_tc_passes(void);
 void gbi_rbt_params(int n, float* h);
 const char* gb_last_error(void);
 int gbi_rbt_matrix(cplxf* A, size_t lda, int n, const float* pu, const float* pv, cudaStream_t st);
@@ -362,7 +363,8 @@ static int neg_product(GbSchur* s, const void* A, const void* B, void* C, ChainW
   const int n = s->n;
   GB_CUDA(cudaMemsetAsync(C, 0, (size_t)n * n * s->esz, st));
   if (s->fp64) return gbi_zgemm_sub(n, n, n, (const cplx*)A, n, (const cplx*)B, n, (cplx*)C, n, st);
-  return gbi_tc_cgemm_sub(n, n, n, (const cplxf*)A, n, (const cplxf*)B, n, (cplxf*)C, n, 3, nullptr, w.err, st);
+  return gbi_tc_cgemm_sub(n, n, n, (const cplxf*)A, n, (const cplxf*)B, n, (cplxf*)C, n, gbi_tc_passes(), nullptr, w.err,
+                          st);
 }
 
 // one chain: X_inv = P^-1 (P overwritten), then out = -X_inv Q

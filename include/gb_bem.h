@@ -181,9 +181,9 @@ int gb_assemble_domain_noalloc(const double *cr, const double *cw, const int *et
 
 /* ---- mixed-precision form ----
  * gb_factor_mixed: A from the resident G, H, kept in FP64, and its complex
- * FP32 LU factors; later gb_solve_mEMP calls solve A x = b by FP64 iterative
- * refinement with those factors (residual b - A x in FP64, relative residual
- * <= 1e-13) instead of applying an explicit inverse.
+ * FP32 LU factors; later gb_solve_mEMP calls solve A x = b by FP64 GMRES
+ * preconditioned by those factors (gb_set_refinement; residual b - A x in
+ * FP64, relative residual <= 1e-13) instead of applying an explicit inverse.
  * gb_ir_info: corrections and final relative residual of the last solve.
  * gb_scene_step: assembly of every domain + factorisation + U, dU + E, H,
  * dE, dH.  form 0: FP64 assembly and FP64 factorisation (gb_factor_fp64);
@@ -192,6 +192,19 @@ int gb_assemble_domain_noalloc(const double *cr, const double *cw, const int *et
  * (precision 1) and mixed; form 3: FP64 assembly and mixed. */
 int gb_factor_mixed(gb_obj *o);
 int gb_ir_info(gb_obj *o, int *iters, double *relres);
+/* Refinement of the solves that use lower-precision or block factors.
+ * mode 0 (default): FP64 GMRES(20), right-preconditioned by the factors
+ * (residual b - A x in FP64 from G, H; converged at ||b - A x|| <= 1e-13 ||b||;
+ * a run that does not converge with butterfly or block factors refactorises
+ * with tournament pivoting and continues).  mode 1 (diagnostic): classical
+ * refinement x += M^-1 (b - A x) with the same fallback rules.
+ * gb_ir_info reports the preconditioner solves of the last solve. */
+int gb_set_refinement(gb_obj *o, int mode);
+/* tensor-core passes of every complex-FP32 factorisation started afterwards
+ * (process-wide): 3 (default; split TF32, FP32-accurate products) or 1
+ * (plain TF32: a third of the tensor work, ~1e-3 relative error in the
+ * factors, which the GMRES refinement absorbs in more iterations) */
+int gb_set_tc_passes(int passes);
 /* Row interchanges of the FP32 factorisation.  mode 0 (default): A is
  * randomised by two-sided recursive butterfly transforms of depth 2
  * (U^T A V, random diagonal entries e^{rho/10}, fixed seed; Parker 1995,
