@@ -21,6 +21,8 @@ int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* G, cplx* H,
                         double* Fs, cudaStream_t st);
 int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG, cplx* dH,
                          double* dF, double* Fs, cudaStream_t st);
+int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int precision, int row0, int nrow, cplx* G, cplx* H,
+                      cplx* dG, cplx* dH, double* dF, double* Fs, cudaStream_t st);
 int gbi_build_A_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
                        const double* kn_dev, int did, int nrows, size_t base, size_t na, cplx* A, cudaStream_t st);
 int gbi_zgetrf(cplx* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
@@ -460,6 +462,24 @@ extern "C" int gb_assemble_all(gb_obj* o, int type, int precision) {
     if (rcs[d]) { gbi_set_error("%s", msg[d].c_str()); return -1; }
   assembled(o, precision);
   return 0;
+}
+
+extern "C" int gb_assemble_rows(gb_obj* o, int did, int row0, int nrow, int type, int precision, void* G, void* H,
+                                void* dG, void* dH, double* dF) {
+  if (check_did(o, did) || check_asm_args(type, precision)) return -1;
+  if (!G || !H || !dG || !dH || !dF) { gbi_set_error("gb_assemble_rows: null output"); return -1; }
+  const size_t Ne = (size_t)o->m.sb_Ne[did];
+  if (nrow <= 0 || row0 < 0 || (size_t)row0 + (size_t)nrow > 4 * Ne) {
+    gbi_set_error("gb_assemble_rows: rows %d..%d outside 0..%zu", row0, row0 + nrow - 1, 4 * Ne - 1);
+    return -1;
+  }
+  if (ensure_tables()) return -1;
+  double* Fs = nullptr;
+  GB_CUDA(cudaMallocAsync((void**)&Fs, 3 * (size_t)nrow * Ne * sizeof(double), o->st));
+  const int rc = gbi_assemble_rows(&o->m, did, type, precision, row0, nrow, (cplx*)G, (cplx*)H, (cplx*)dG, (cplx*)dH,
+                                   dF, Fs, o->st);
+  cudaFreeAsync(Fs, o->st);
+  return rc;
 }
 
 extern "C" int gb_cmatrix_download(gb_obj* o, int did, void* G, void* H, void* dG, void* dH, double* dF) {

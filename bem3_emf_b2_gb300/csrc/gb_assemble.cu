@@ -69,6 +69,7 @@ struct AsmArgs {
   double* Fs;      // scratch [N][Ne][3]
   const uint8_t* only;  // non-null: k_asm_regular integrates only the pairs flagged here
   int adapt;       // k_asm_regular_df: the distance-adaptive order (precision 3)
+  int row0, nrow;  // the rows row0 .. row0 + nrow - 1 of the domain; outputs hold nrow rows
 };
 
 // unit tangents at collocation node tn of element |td| (reference tz_te_bd_node d3b1_elem.c:122-143)
@@ -88,7 +89,8 @@ __device__ __forceinline__ void node_tangents(const Elem& T, int tn, double vt[2
   }
 }
 
-__device__ __forceinline__ void store_pair(const AsmArgs& a, size_t N, int row, int sidx, const RegAcc<2>& A) {
+__device__ __forceinline__ void store_pair(const AsmArgs& a, size_t N, int grow, int sidx, const RegAcc<2>& A) {
+  const int row = grow - a.row0;  // row of the output block
   size_t col = (size_t)sidx * 4;
   cplx* g = a.G + (size_t)row * N + col;
   cplx* h = a.H + (size_t)row * N + col;
@@ -201,10 +203,10 @@ __device__ __forceinline__ void reg_point_f32(const PairF& P, bool quad, float z
 // FP64 kernel must redo
 __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, uint8_t* redo) {
   const size_t N = (size_t)a.Ne * 4;
-  const size_t npair = N * (size_t)a.Ne;
+  const size_t npair = (size_t)a.nrow * (size_t)a.Ne;
   size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npair) return;
-  const int row = (int)(p / a.Ne), sidx = (int)(p % a.Ne);
+  const int row = a.row0 + (int)(p / a.Ne), sidx = (int)(p % a.Ne);
   const int t = row / 4 + 1, tn = row % 4;
   const int td = __ldg(a.sid + t), sd = __ldg(a.sid + sidx + 1);
   const int atd = abs(td);
@@ -300,10 +302,10 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, uint8_t* red
 // kernel, which decides GLN/GHN exactly as the reference.
 __global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo) {
   const size_t N = (size_t)a.Ne * 4;
-  const size_t npair = N * (size_t)a.Ne;
+  const size_t npair = (size_t)a.nrow * (size_t)a.Ne;
   size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= npair) return;
-  const int row = (int)(p / a.Ne), sidx = (int)(p % a.Ne);
+  const int row = a.row0 + (int)(p / a.Ne), sidx = (int)(p % a.Ne);
   const int t = row / 4 + 1, tn = row % 4;
   const int td = __ldg(a.sid + t), sd = __ldg(a.sid + sidx + 1);
   const int atd = abs(td);
@@ -326,7 +328,7 @@ __global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo
 
 __global__ void __launch_bounds__(128) k_asm_regular(AsmArgs a) {
   const size_t N = (size_t)a.Ne * 4;
-  const size_t npair = N * (size_t)a.Ne;
+  const size_t npair = (size_t)a.nrow * (size_t)a.Ne;
   size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool active = p < npair;
   int row = 0, sidx = 0;
@@ -336,7 +338,7 @@ __global__ void __launch_bounds__(128) k_asm_regular(AsmArgs a) {
   RegAcc<2> A;
   bool neg = false;
   if (active) {
-    row = (int)(p / a.Ne);
+    row = a.row0 + (int)(p / a.Ne);
     sidx = (int)(p % a.Ne);
     int t = row / 4 + 1, tn = row % 4;
     int td = __ldg(a.sid + t);
@@ -841,7 +843,7 @@ static __device__ void sing_item_df(const SingCtx& c, const RowD& R, int q, Sing
 template <bool DF>
 __global__ void __launch_bounds__(256) k_asm_singular(AsmArgs a) {
   __shared__ double red[51 * 8];
-  const int row = blockIdx.x;
+  const int row = a.row0 + blockIdx.x;
   const int t = row / 4 + 1, tn = row % 4;
   const int td = __ldg(a.sid + t);
   const int atd = abs(td);
@@ -885,12 +887,13 @@ __global__ void __launch_bounds__(256) k_asm_singular(AsmArgs a) {
 
 __global__ void k_asm_rows(AsmArgs a) {
   const size_t N = (size_t)a.Ne * 4;
-  int row = blockIdx.x * blockDim.x + threadIdx.x;
-  if (row >= (int)N) return;
+  const int lr = blockIdx.x * blockDim.x + threadIdx.x;  // row of the output block
+  if (lr >= a.nrow) return;
+  const int row = a.row0 + lr;
   int t = row / 4 + 1, tn = row % 4;
   int td = __ldg(a.sid + t);
   if (__ldg(a.etype + abs(td)) == 0 && tn == 3) return;
-  const double* f = a.Fs + (size_t)row * a.Ne * 3;
+  const double* f = a.Fs + (size_t)lr * a.Ne * 3;
   double F = 0.0, Fz = 0.0, Fe = 0.0;
   for (int s = 0; s < a.Ne; s++) {
     F += f[3 * s + 0];
@@ -898,11 +901,11 @@ __global__ void k_asm_rows(AsmArgs a) {
     Fe += f[3 * s + 2];
   }
   double diag = (a.did == 0) ? 1.0 + F : F;
-  cplx* h = a.H + (size_t)row * N + (size_t)(t - 1) * 4 + tn;
+  cplx* h = a.H + (size_t)lr * N + (size_t)(t - 1) * 4 + tn;
   h->x += diag;
-  a.dF[(size_t)row * 3 + 0] = diag;
-  a.dF[(size_t)row * 3 + 1] = Fz;
-  a.dF[(size_t)row * 3 + 2] = Fe;
+  a.dF[(size_t)lr * 3 + 0] = diag;
+  a.dF[(size_t)lr * 3 + 1] = Fz;
+  a.dF[(size_t)lr * 3 + 2] = Fe;
 }
 
 extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG,
@@ -916,15 +919,19 @@ extern "C" int gbi_assemble_domain(const GbMeshDev* m, int did, int type, cplx* 
   return gbi_assemble_domain2(m, did, type, 0, G, H, dG, dH, dF, Fs, st);
 }
 
-// precision 0: FP64 throughout (the reference's arithmetic); 1: regular pairs
-// of the GLN x GLN rule in FP32 with FP64 near pairs; 2: regular pairs and
-// singular point sets in double-float; 3 (the chosen form): as 2 with the
-// regular pairs' order adapted to their distance (reg_order)
-extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG,
-                                    cplx* dH, double* dF, double* Fs, cudaStream_t st) {
+// Rows row0 .. row0 + nrow - 1 of domain did into G, H (nrow x N), dG, dH
+// (2 nrow x N), dF (nrow x 3); Fs: scratch of 3 nrow Ne doubles.  The full
+// domain is row0 = 0, nrow = N.
+extern "C" int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int precision, int row0, int nrow, cplx* G,
+                                 cplx* H, cplx* dG, cplx* dH, double* dF, double* Fs, cudaStream_t st) {
   int Ne = m->sb_Ne[did];
-  if (Ne <= 0) return 0;
+  if (Ne <= 0 || nrow <= 0) return 0;
   size_t N = (size_t)Ne * 4;
+  if (row0 < 0 || (size_t)row0 + (size_t)nrow > N) {
+    gbi_set_error("assembly: rows %d..%d outside 0..%zu", row0, row0 + nrow - 1, N - 1);
+    return -1;
+  }
+  const size_t nr = (size_t)nrow;
   AsmArgs a;
   a.cr = m->cr;
   a.cw = m->cw;
@@ -943,13 +950,15 @@ extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int p
   a.Fs = Fs;
   a.only = nullptr;
   a.adapt = precision == 3;
-  GB_CUDA(cudaMemsetAsync(G, 0, N * N * sizeof(cplx), st));
-  GB_CUDA(cudaMemsetAsync(H, 0, N * N * sizeof(cplx), st));
-  GB_CUDA(cudaMemsetAsync(dG, 0, 2 * N * N * sizeof(cplx), st));
-  GB_CUDA(cudaMemsetAsync(dH, 0, 2 * N * N * sizeof(cplx), st));
-  GB_CUDA(cudaMemsetAsync(dF, 0, 3 * N * sizeof(double), st));
-  GB_CUDA(cudaMemsetAsync(Fs, 0, 3 * N * (size_t)Ne * sizeof(double), st));
-  size_t npair = N * (size_t)Ne;
+  a.row0 = row0;
+  a.nrow = nrow;
+  GB_CUDA(cudaMemsetAsync(G, 0, nr * N * sizeof(cplx), st));
+  GB_CUDA(cudaMemsetAsync(H, 0, nr * N * sizeof(cplx), st));
+  GB_CUDA(cudaMemsetAsync(dG, 0, 2 * nr * N * sizeof(cplx), st));
+  GB_CUDA(cudaMemsetAsync(dH, 0, 2 * nr * N * sizeof(cplx), st));
+  GB_CUDA(cudaMemsetAsync(dF, 0, 3 * nr * sizeof(double), st));
+  GB_CUDA(cudaMemsetAsync(Fs, 0, 3 * nr * (size_t)Ne * sizeof(double), st));
+  size_t npair = nr * (size_t)Ne;
   unsigned nb = (unsigned)((npair + 127) / 128);
   uint8_t* redo = nullptr;
   if (precision >= 2 && type == 2) {
@@ -969,14 +978,23 @@ extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int p
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   if (redo) GB_CUDA(cudaFreeAsync(redo, st));
-  if (precision >= 2) k_asm_singular<true><<<(unsigned)N, 256, 0, st>>>(a);
-  else k_asm_singular<false><<<(unsigned)N, 256, 0, st>>>(a);
+  if (precision >= 2) k_asm_singular<true><<<(unsigned)nr, 256, 0, st>>>(a);
+  else k_asm_singular<false><<<(unsigned)nr, 256, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
-  k_asm_rows<<<(unsigned)((N + 127) / 128), 128, 0, st>>>(a);
+  k_asm_rows<<<(unsigned)((nr + 127) / 128), 128, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
+}
+
+// precision 0: FP64 throughout (the reference's arithmetic); 1: regular pairs
+// of the GLN x GLN rule in FP32 with FP64 near pairs; 2: regular pairs and
+// singular point sets in double-float; 3 (the chosen form): as 2 with the
+// regular pairs' order adapted to their distance (reg_order)
+extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG,
+                                    cplx* dH, double* dF, double* Fs, cudaStream_t st) {
+  return gbi_assemble_rows(m, did, type, precision, 0, 4 * m->sb_Ne[did], G, H, dG, dH, dF, Fs, st);
 }
 
 extern "C" int gbi_upload_tables_asm(const void* t) {

@@ -7,6 +7,7 @@ outside, id 2i with tag 99 (the open region) and the reversed node order.
 
   cubed_sphere   sphere of radius r, n x n bilinear quadrangles per cube face
                  (6 n^2 elements, 6 n^2 + 2 nodes)
+  cube           cube of a given side, n x n planar quadrangles per face
   cone_tri       right circular cone meshed with linear triangles on rings of
                  6k nodes (12 m^2 triangles), seeded tangential node jitter
   cone_mixed     cone with quadrangle rings and triangle fans at apex and base
@@ -67,6 +68,38 @@ def cubed_sphere(n, radius=1.0, center=(0.0, 0.0, 0.0)):
                     for du, dv in ((0, 0), (1, 0), (1, 1), (0, 1)):
                         c = [0, 0, 0]
                         c[axis] = side
+                        c[(axis + 1) % 3] = u + du
+                        c[(axis + 2) % 3] = v + dv
+                        q.append(node(*c))
+                    elems.append(tuple(q))
+    nodes = np.array(nodes)
+    return nodes, _orient(nodes, elems, np.asarray(center, float))
+
+
+def cube(n, side=1.0, center=(0.0, 0.0, 0.0)):
+    """Nodes and planar quadrangles of a cube of the given side, n x n per
+    face (6 n^2 elements, 6 n^2 + 2 nodes), outward orientation."""
+    key = {}
+    nodes = []
+    h = 0.5 * side
+
+    def node(i, j, k):
+        t = (i, j, k)
+        if t not in key:
+            key[t] = len(nodes)
+            nodes.append(np.array([(2.0 * i / n - 1.0) * h, (2.0 * j / n - 1.0) * h, (2.0 * k / n - 1.0) * h])
+                         + np.asarray(center, float))
+        return key[t]
+
+    elems = []
+    for axis in range(3):
+        for s in (0, n):
+            for u in range(n):
+                for v in range(n):
+                    q = []
+                    for du, dv in ((0, 0), (1, 0), (1, 1), (0, 1)):
+                        c = [0, 0, 0]
+                        c[axis] = s
                         c[(axis + 1) % 3] = u + du
                         c[(axis + 2) % 3] = v + dv
                         q.append(node(*c))

@@ -475,6 +475,86 @@ def run_reference(args):
             "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "estimated")}}
 
 
+CUBE = dict(name="cube of side 6 (lambda0 = 1), 80 x 80 planar quadrangles per face (38,400 elements, N = 153,600 "
+                 "rows per domain), n = 1.6 in 1.33; coefficient-matrix assembly of both domains streamed in row "
+                 "blocks (gb_assemble_rows), the 377 GB per-domain matrices never stored",
+            n=80, side=6.0, n_obj=1.6, n_host=1.33, lambda0=1.0)
+
+
+def run_cube(args):
+    """Assembly throughput of the 38,400-element cube (pairs of a collocation
+    node and a source element per second): each step assembles one block of
+    --rows rows of G, H, dG, dH, dF (blocks spread over both domains) in the
+    chosen form's precision; the FP64 form's rate is measured the same way
+    on two blocks."""
+    import torch
+    from bem3_emf_b2_gb300 import Scene, build, lib, meshgen
+    import ctypes
+    build.build()
+    L = lib()
+    vp, ci = ctypes.c_void_p, ctypes.c_int
+    L.gb_assemble_rows.argtypes = [vp, ci, ci, ci, ci, ci, vp, vp, vp, vp, vp]
+    L.gb_assemble_rows.restype = ci
+    L.gb_obj_stream.argtypes = [vp]
+    L.gb_obj_stream.restype = vp
+    wd = tempfile.mkdtemp(prefix="cube_")
+    n = args.cube_n or CUBE["n"]
+    nodes, elems = meshgen.cube(n, CUBE["side"])
+    meshgen.write_mesh(os.path.join(wd, "mesh.msh"), nodes, elems)
+    meshgen.write_medium(os.path.join(wd, "medium.txt"), [CUBE["n_obj"]])
+    meshgen.write_ipw(os.path.join(wd, "ipw.txt"), [dict(lambda0=1.0, ni=CUBE["n_host"], power=1.0, e0x=1.0, e0y=0.0)])
+    sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+    o = sc.obj()
+    ne = len(elems)
+    N = 4 * ne
+    B = min(args.rows, N)
+    G = torch.empty((B, N), dtype=torch.complex128, device="cuda")
+    H = torch.empty_like(G)
+    dG = torch.empty((2 * B, N), dtype=torch.complex128, device="cuda")
+    dH = torch.empty_like(dG)
+    dF = torch.empty((B, 3), dtype=torch.float64, device="cuda")
+    st = torch.cuda.ExternalStream(L.gb_obj_stream(o))
+    nblk = N // B
+
+    def block(i, prec):
+        d = i % 2
+        r0 = ((i // 2) * 7919 % max(nblk, 1)) * B  # blocks spread over the domain
+        if L.gb_assemble_rows(o, d, r0, B, 2, prec, G.data_ptr(), H.data_ptr(), dG.data_ptr(), dH.data_ptr(),
+                              dF.data_ptr()) != 0:
+            raise RuntimeError(L.gb_last_error().decode())
+
+    def timed(prec, steps, warmup):
+        for i in range(warmup):
+            block(i, prec)
+        st.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for i in range(steps):
+            block(warmup + i, prec)
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1000.0
+    l0 = L.gb_launch_count()
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        t = timed(3, args.steps, args.warmup)
+    launches = (L.gb_launch_count() - l0) / (args.steps + args.warmup)
+    t64 = timed(0, 2, 0)
+    pairs = float(B) * ne
+    sc.close()
+    rate = pairs * args.steps / t
+    return {"metric": "assembly pairs/s (collocation node x source element), 38,400-element cube",
+            "value": rate, "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * t / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "vs_baseline_note": VS_BASELINE_NOTE,
+            "dtype": "double-float quadrature, adaptive order (precision 3)", "data": "synthetic (meshgen cube)",
+            "config": {"workload": CUBE["name"] if n == CUBE["n"] else "cube %d x %d per face" % (n, n),
+                       "elements": ne, "rows_per_step": B, "pairs_per_step": pairs,
+                       "full_assembly_s_estimate": 2.0 * N * ne / rate},
+            "fp64_form": {"pairs_per_s": pairs * 2 / t64},
+            "gpu_launches": int(round(launches)), "clocks": clk.summary()}
+
+
 def profile_step(args):
     """Warm-up steps then exactly one chosen-form step (for ncu launch lists)."""
     import torch
@@ -500,15 +580,21 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--profile-step", action="store_true",
                     help="profiling run: one chosen-form scene step after --warmup steps, nothing else, no JSON line")
-    ap.add_argument("--workload", choices=["cones", "sphere"], default="cones",
-                    help="cones: the two-cone scene (default); sphere: the 384-element sphere")
+    ap.add_argument("--workload", choices=["cones", "sphere", "cube"], default="cones",
+                    help="cones: the two-cone scene (default); sphere: the 384-element sphere; cube: assembly "
+                         "throughput of the 38,400-element cube")
+    ap.add_argument("--cube-n", type=int, default=None, help="quadrangles per cube edge (cube workload)")
+    ap.add_argument("--rows", type=int, default=1024, help="rows per step of the cube workload")
     ap.add_argument("--faces", type=int, default=8, help="quadrangles per cube face of the sphere workload")
     ap.add_argument("--cone-m", type=int, default=None, help="rings per cone surface (12 m^2 triangles per cone)")
     args = ap.parse_args()
     if args.profile_step:
         profile_step(args)
         return
-    out = run_reference(args) if args.impl == "reference" else run_gpu(args)
+    if args.workload == "cube" and args.impl != "reference":
+        out = run_cube(args)
+    else:
+        out = run_reference(args) if args.impl == "reference" else run_gpu(args)
     if out is not None:
         print(json.dumps(out))
 

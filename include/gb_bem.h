@@ -92,6 +92,16 @@ int gb_assemble(gb_obj *o, int did, int type);
  * Matrix entries then carry ~1e-7 relative error (measured: G 9e-8, dH 2e-7,
  * radiation force up to 8e-7 on the 384-element sphere): an opt-in only. */
 int gb_assemble2(gb_obj *o, int did, int type, int precision);
+/* Rows row0 .. row0 + nrow - 1 of domain did's G, H, dG, dH, dF (the rows
+ * that create_cmatrix_domain writes, solve_bieq2.c:98-184, free term on the
+ * diagonal included) into caller DEVICE buffers: G, H nrow x N, dG, dH
+ * 2 nrow x N, dF nrow x 3 (N = 4 sb_Ne[did]); precision as gb_assemble2.
+ * The object's own matrices are neither allocated nor touched, so a domain
+ * too large to store (the 38,400-element cube: 377 GB per matrix) can be
+ * assembled block by block and streamed to a consumer.  Asynchronous on the
+ * object's stream (gb_obj_stream); its small scratch is stream-ordered. */
+int gb_assemble_rows(gb_obj *o, int did, int row0, int nrow, int type, int precision, void *G, void *H, void *dG,
+                     void *dH, double *dF);
 /* every domain of the object, as gb_assemble2, the domains at once (one host
  * thread and stream each) */
 int gb_assemble_all(gb_obj *o, int type, int precision);
