@@ -237,6 +237,7 @@ struct gb_obj {
   double* ext_v;
   int* ext_idx;
   std::vector<int> h_etype, h_sid;
+  std::mutex bv_mu;  // first allocation of the boundary-value buffers
 };
 
 static int dalloc(void** p, size_t bytes) {
@@ -662,7 +663,14 @@ extern "C" int gb_zgesv(int n, int nrhs, void* Ah, void* Bh) {
 }
 
 // ------------------------------------------------------------------ boundary values
+static int ensure_bv_locked(gb_obj* o);
+// allocates the boundary-value buffers on first use; safe against concurrent
+// first calls from several host threads
 static int ensure_bv(gb_obj* o) {
+  std::lock_guard<std::mutex> lk(o->bv_mu);
+  return ensure_bv_locked(o);
+}
+static int ensure_bv_locked(gb_obj* o) {
   for (int d = 0; d <= o->m.MN; d++) {
     if (o->bU[d]) continue;
     size_t n1 = (size_t)o->m.sb_Ne[d] + 1;
@@ -987,24 +995,43 @@ extern "C" int gb_solve_EH(gb_obj* o) {
 }
 
 // ------------------------------------------------------------------ points
+// The point entry points are synchronous and may be called from several host
+// threads at once (the reference's examples call the per-point field functions
+// from OpenMP loops): each calling thread runs them on its own stream, with
+// stream-ordered temporaries (no cudaFree and its device-wide synchronisation),
+// after the object's own stream has drained.
+static thread_local cudaStream_t t_point_stream[64];
+static int point_stream(gb_obj* o, cudaStream_t* st) {
+  int dev = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) { gbi_set_error("device ordinal %d not supported", dev); return -1; }
+  if (!t_point_stream[dev]) GB_CUDA(cudaStreamCreateWithFlags(&t_point_stream[dev], cudaStreamNonBlocking));
+  GB_CUDA(cudaStreamSynchronize(o->st));
+  *st = t_point_stream[dev];
+  return 0;
+}
+
 extern "C" int gb_domain_id(gb_obj* o, int n, const double* rt, int* did) {
   if (n <= 0) return 0;
+  cudaStream_t st;
+  if (point_stream(o, &st)) return -1;
   double* drt = nullptr;
   int* dd = nullptr;
-  if (dalloc((void**)&drt, (size_t)n * 3 * sizeof(double)) || dalloc((void**)&dd, (size_t)n * sizeof(int))) {
-    cudaFree(drt);
+  if (cudaMallocAsync((void**)&drt, (size_t)n * 3 * sizeof(double), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&dd, (size_t)n * sizeof(int), st) != cudaSuccess) {
+    gbi_set_error("gb_domain_id: out of device memory");
+    if (drt) cudaFreeAsync(drt, st);
     return -1;
   }
   FieldObj f = field_view(o);
   int rc = 0;
-  if (cudaMemcpyAsync(drt, rt, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, o->st) != cudaSuccess) rc = -1;
-  if (!rc) rc = gbi_domain_id(&f, n, drt, dd, o->st);
-  if (!rc && (cudaMemcpyAsync(did, dd, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
-              cudaStreamSynchronize(o->st) != cudaSuccess)) {
-    gbi_set_error("gb_domain_id failed");
-    rc = -1;
-  }
-  cudaFree(drt); cudaFree(dd);
+  if (cudaMemcpyAsync(drt, rt, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess) rc = -1;
+  if (!rc) rc = gbi_domain_id(&f, n, drt, dd, st);
+  if (!rc && cudaMemcpyAsync(did, dd, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = -1;
+  cudaFreeAsync(drt, st);
+  cudaFreeAsync(dd, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
+  if (rc) gbi_set_error("gb_domain_id failed");
   return rc;
 }
 
@@ -1013,59 +1040,74 @@ extern "C" int gb_field_points(gb_obj* o, int mode, int type, int n, const doubl
   if (n <= 0) return 0;
   if (mode < 0 || mode > 3 || type < 0 || type > 3) { gbi_set_error("gb_field_points: mode %d type %d", mode, type); return -1; }
   if (ensure_bv(o)) return -1;
+  cudaStream_t st;
+  if (point_stream(o, &st)) return -1;
   int nout = (mode == 0) ? 4 : (mode == 3 ? 8 : 6);
   double *drt = nullptr, *dv = nullptr;
   int *dd = nullptr, *df = nullptr;
   cplx* dout = nullptr;
   int rc = 0;
-  if (dalloc((void**)&drt, (size_t)n * 3 * sizeof(double)) || dalloc((void**)&dv, (size_t)n * 3 * sizeof(double)) ||
-      dalloc((void**)&dd, (size_t)n * sizeof(int)) || dalloc((void**)&df, (size_t)n * sizeof(int)) ||
-      dalloc((void**)&dout, (size_t)n * nout * sizeof(cplx)))
+  if (cudaMallocAsync((void**)&drt, (size_t)n * 3 * sizeof(double), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&dv, (size_t)n * 3 * sizeof(double), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&dd, (size_t)n * sizeof(int), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&df, (size_t)n * sizeof(int), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&dout, (size_t)n * nout * sizeof(cplx), st) != cudaSuccess) {
+    gbi_set_error("gb_field_points: out of device memory");
     rc = -1;
+  }
   FieldObj f = field_view(o);
-  if (!rc && (cudaMemcpyAsync(drt, rt, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, o->st) != cudaSuccess ||
-              (v && cudaMemcpyAsync(dv, v, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, o->st) != cudaSuccess) ||
-              cudaMemcpyAsync(dd, did, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, o->st) != cudaSuccess ||
-              cudaMemsetAsync(dout, 0, (size_t)n * nout * sizeof(cplx), o->st) != cudaSuccess)) {
+  if (!rc && (cudaMemcpyAsync(drt, rt, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+              (v && cudaMemcpyAsync(dv, v, (size_t)n * 3 * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess) ||
+              cudaMemcpyAsync(dd, did, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+              cudaMemsetAsync(dout, 0, (size_t)n * nout * sizeof(cplx), st) != cudaSuccess)) {
     gbi_set_error("gb_field_points: upload failed");
     rc = -1;
   }
-  if (!rc) rc = gbi_field(&f, mode, type, n, drt, dv, dd, dout, df, o->st);
-  if (!rc && cudaMemcpyAsync(out, dout, (size_t)n * nout * sizeof(cplx), cudaMemcpyDeviceToHost, o->st) != cudaSuccess) rc = -1;
-  if (!rc && flag && mode == 2 && cudaMemcpyAsync(flag, df, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, o->st) != cudaSuccess) rc = -1;
-  if (!rc && cudaStreamSynchronize(o->st) != cudaSuccess) rc = -1;
+  if (!rc) rc = gbi_field(&f, mode, type, n, drt, dv, dd, dout, df, st);
+  if (!rc && cudaMemcpyAsync(out, dout, (size_t)n * nout * sizeof(cplx), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = -1;
+  if (!rc && flag && mode == 2 && cudaMemcpyAsync(flag, df, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = -1;
+  void* tmp[5] = {drt, dv, dd, df, dout};
+  for (void* t : tmp)
+    if (t) cudaFreeAsync(t, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
   if (rc && !gb_last_error()[0]) gbi_set_error("gb_field_points failed");
-  cudaFree(drt); cudaFree(dv); cudaFree(dd); cudaFree(df); cudaFree(dout);
   return rc;
 }
 
 extern "C" int gb_field_bd(gb_obj* o, int type, int n, const int* did, const int* t, const double* zt, void* out) {
   if (n <= 0) return 0;
   if (ensure_bv(o)) return -1;
+  for (int i = 0; i < n; i++) {
+    if (did[i] < 0 || did[i] > o->m.MN || t[i] < 1 || t[i] > o->m.sb_Ne[did[i]]) {
+      gbi_set_error("gb_field_bd: point %d: domain %d element %d out of range", i, did[i], t[i]);
+      return -1;
+    }
+  }
+  cudaStream_t st;
+  if (point_stream(o, &st)) return -1;
   int *dd = nullptr, *dt = nullptr;
   double* dz = nullptr;
   cplx* dout = nullptr;
   int rc = 0;
-  if (dalloc((void**)&dd, (size_t)n * sizeof(int)) || dalloc((void**)&dt, (size_t)n * sizeof(int)) ||
-      dalloc((void**)&dz, (size_t)n * 2 * sizeof(double)) || dalloc((void**)&dout, (size_t)n * 6 * sizeof(cplx)))
+  if (cudaMallocAsync((void**)&dd, (size_t)n * sizeof(int), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&dt, (size_t)n * sizeof(int), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&dz, (size_t)n * 2 * sizeof(double), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&dout, (size_t)n * 6 * sizeof(cplx), st) != cudaSuccess) {
+    gbi_set_error("gb_field_bd: out of device memory");
     rc = -1;
-  for (int i = 0; i < n && !rc; i++) {
-    if (did[i] < 0 || did[i] > o->m.MN || t[i] < 1 || t[i] > o->m.sb_Ne[did[i]]) {
-      gbi_set_error("gb_field_bd: point %d: domain %d element %d out of range", i, did[i], t[i]);
-      rc = -1;
-    }
   }
   FieldObj f = field_view(o);
-  if (!rc && (cudaMemcpyAsync(dd, did, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, o->st) != cudaSuccess ||
-              cudaMemcpyAsync(dt, t, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, o->st) != cudaSuccess ||
-              cudaMemcpyAsync(dz, zt, (size_t)n * 2 * sizeof(double), cudaMemcpyHostToDevice, o->st) != cudaSuccess))
+  if (!rc && (cudaMemcpyAsync(dd, did, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+              cudaMemcpyAsync(dt, t, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+              cudaMemcpyAsync(dz, zt, (size_t)n * 2 * sizeof(double), cudaMemcpyHostToDevice, st) != cudaSuccess))
     rc = -1;
-  if (!rc) rc = gbi_field_bd(&f, type, n, dd, dt, dz, dout, o->st);
-  if (!rc && (cudaMemcpyAsync(out, dout, (size_t)n * 6 * sizeof(cplx), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
-              cudaStreamSynchronize(o->st) != cudaSuccess))
-    rc = -1;
+  if (!rc) rc = gbi_field_bd(&f, type, n, dd, dt, dz, dout, st);
+  if (!rc && cudaMemcpyAsync(out, dout, (size_t)n * 6 * sizeof(cplx), cudaMemcpyDeviceToHost, st) != cudaSuccess) rc = -1;
+  void* tmp[4] = {dd, dt, dz, dout};
+  for (void* p : tmp)
+    if (p) cudaFreeAsync(p, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) rc = -1;
   if (rc && !gb_last_error()[0]) gbi_set_error("gb_field_bd failed");
-  cudaFree(dd); cudaFree(dt); cudaFree(dz); cudaFree(dout);
   return rc;
 }
 

@@ -1,25 +1,37 @@
 /*
  * field.c -- potentials and fields at points (reference d3b1_field.c,
  * mo_field.c, setup2.c:944-978).  Every call evaluates on the GPU; the
- * per-point entry points keep the reference's signatures and are safe to call
- * from several host threads (the calls are serialised).  gb_mo_EH_points()
- * evaluates many points in one launch.
+ * per-point entry points keep the reference's signatures and may be called
+ * from several host threads at once, as the reference's examples do from
+ * OpenMP loops (example2.c:45, example4.c:53): only the one-time setup of an
+ * object's device copy is serialised; the evaluations run concurrently, each
+ * thread on its own stream (gb_field_points).  gb_mo_EH_points() evaluates
+ * many points in one launch per object.
  */
 #include "gb_host.h"
 
+/* the object's device copy with its boundary values uploaded (once) */
 static gb_obj *gb_ready(DOMD *md)
 {
+  gb_call_lock();
   gb_obj *o=gb_dev(md);
   gb_bv_to_device(md);
+  gb_call_unlock();
+  return o;
+}
+
+static gb_obj *gb_dev_locked(DOMD *md)
+{
+  gb_call_lock();
+  gb_obj *o=gb_dev(md);
+  gb_call_unlock();
   return o;
 }
 
 int domain_id(double *rt,DOMD *md)
 {
   int did;
-  gb_call_lock();
-  if(gb_domain_id(gb_dev(md),1,rt,&did)) gb_die("field.c, domain_id()");
-  gb_call_unlock();
+  if(gb_domain_id(gb_dev_locked(md),1,rt,&did)) gb_die("field.c, domain_id()");
   return did;
 }
 
@@ -28,17 +40,14 @@ int domain_id(double *rt,DOMD *md)
 static int gb_obj_field(double complex *out,double *rt,int type,DOMD *md,int mode)
 {
   int did,flag=0;
-  gb_call_lock();
   gb_obj *o=gb_ready(md);
   if(gb_domain_id(o,1,rt,&did)) gb_die("field.c, domain_id()");
   if(did<0){
     int n=(mode==0)?4:6;
     for(int i=0;i<n;i++) out[i]=0.0;
-    gb_call_unlock();
     return did;
   }
   if(gb_field_points(o,mode,type,1,rt,NULL,&did,out,&flag)) gb_die("field.c, gb_field_points()");
-  gb_call_unlock();
   if(mode==2) return flag;
   return did;
 }
@@ -145,10 +154,8 @@ void gb_EH_s_bd(double complex *E,double complex *H,int did,int t,double zt,doub
 {
   double z[2]={zt,et};
   double complex o[6];
-  gb_call_lock();
   gb_obj *ob=gb_ready(md);
   if(gb_field_bd(ob,type,1,&did,&t,z,o)) gb_die("field.c, EH_s_bd()");
-  gb_call_unlock();
   for(int i=0;i<3;i++){ E[i]=o[i]; H[i]=o[3+i]; }
 }
 
@@ -213,7 +220,6 @@ int gb_mo_EH_points(MOBJ *mo,int n,const double *rt,int type,int which,int memp,
   int *did=(int *)m_alloc2((size_t)n*mo->N,sizeof(int),"field.c did");
   double complex *buf=(double complex *)m_alloc2((size_t)n*6,sizeof(double complex),"field.c buf");
   int *flag=(int *)m_alloc2(n,sizeof(int),"field.c flag");
-  gb_call_lock();
   for(int m=0;m<mo->N;m++){
     gb_obj *o=gb_ready(&mo->md[m]);
     if(gb_domain_id(o,n,rt,did+(size_t)m*n)) gb_die("field.c, gb_mo_EH_points()");
@@ -250,7 +256,6 @@ int gb_mo_EH_points(MOBJ *mo,int n,const double *rt,int type,int which,int memp,
     }
     free(pr); free(pd); free(pi);
   }
-  gb_call_unlock();
   if(oid) for(int p=0;p<n;p++) oid[p]=own[p];
   free(own); free(did); free(buf); free(flag);
   return 0;

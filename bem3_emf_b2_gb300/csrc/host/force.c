@@ -98,8 +98,8 @@ static void gb_point_fields(gb_pts *p,int oid,MOBJ *mo)
   gb_call_lock();
   gb_obj *o=gb_dev(md);
   gb_bv_to_device(md);
-  if(nb>0 && gb_field_bd(o,PREC_DEF,nb,bdid,bt,bz,bo)) gb_die("force.c, EH_s_bd()");
   gb_call_unlock();
+  if(nb>0 && gb_field_bd(o,PREC_DEF,nb,bdid,bt,bz,bo)) gb_die("force.c, EH_s_bd()");
   q=0;
   for(int k=0;k<n;k++){
     if(p->node[k]>=0){
@@ -118,9 +118,9 @@ static void gb_point_fields(gb_pts *p,int oid,MOBJ *mo)
     gb_call_lock();
     gb_obj *om=gb_dev(&mo->md[m]);
     gb_bv_to_device(&mo->md[m]);
+    gb_call_unlock();
     if(gb_domain_id(om,n,fr,did)) gb_die("force.c, domain_id()");
     if(gb_field_points(om,1,PREC_DEF,n,fr,NULL,did,buf,NULL)) gb_die("force.c, EH_s()");
-    gb_call_unlock();
     for(int k=0;k<n;k++) for(int j=0;j<3;j++){ p->E[3*k+j]+=buf[6*k+j]; p->H[3*k+j]+=buf[6*k+3+j]; }
   }
   /* incident wave */

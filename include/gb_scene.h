@@ -52,6 +52,19 @@ void gbh_mscene_drop_device(MOBJ *mo);
 size_t gbh_mscene_h2d_bytes(MOBJ *mo);
 size_t gbh_mscene_d2h_bytes(MOBJ *mo);
 void gbh_mscene_close(MOBJ *mo);
+/* Batched field map of a solved multi-object scene (the examples' per-point
+ * loops, reference example2.c:43-50, example4.c:53-66, in one call): the
+ * total (which = 1), scattered (0) or incident (2) field E[3 n], H[3 n] at the
+ * points rt[3 n], through the boundary-value formula (memp = 0, as mo_EH_t /
+ * mo_EH_s) or the potential-derivative formula (memp = 1, as mo_EH_mEMP_t /
+ * mo_EH_mEMP_s, the far-field form of example4.c); quadrature type as the
+ * reference's.  One domain-id and one field launch per object instead of one
+ * per point; each point's value equals the per-point function's.  oid[n]
+ * (may be NULL): the object containing the point, -1 outside all.  Returns 0.
+ * The per-point functions (mo_EH_*, mo_mEMP_*, domain_id) may also be called
+ * from several host threads at once: each thread evaluates on its own stream. */
+int gb_mo_EH_points(MOBJ *mo, int n, const double *rt, int type, int which, int memp, double complex *E,
+                    double complex *H, int *oid);
 /* suppress (1) or restore (0) the progress messages of mo_solve_bv */
 void gbh_set_quiet(int q);
 /* iteration count and convergence measure cc of the last mo_solve_bv */
