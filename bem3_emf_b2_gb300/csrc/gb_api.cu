@@ -75,6 +75,8 @@ void gbi_schur_destroy(GbSchur* s);
 int gbi_schur_factor(GbSchur* s, const GbMeshDev* m, const cplx* G0, const cplx* H0, const cplx* G1, const cplx* H1,
                      const int* sid0, const int* sid1, const int* rowk0, const int* rowk1, cudaStream_t st);
 int gbi_schur_apply(GbSchur* s, const cplx* r, cplx* x, cudaStream_t st);
+void gbi_schur_mats(GbSchur* s, void** out);
+int gbi_schur_prepare(GbSchur* s, const GbMeshDev* m, cudaStream_t st);
 }
 #include <functional>
 typedef std::function<int(const cplx* x, cplx* y, cudaStream_t st)> GbOp;
@@ -149,6 +151,11 @@ static int ensure_tables() {
 }
 
 extern "C" int gbi_ensure_tables(void) { return ensure_tables(); }
+
+extern "C" int gb_device_memory(size_t* free_bytes, size_t* total_bytes) {
+  GB_CUDA(cudaMemGetInfo(free_bytes, total_bytes));
+  return 0;
+}
 
 extern "C" int gb_device_count(void) {
   int n = 0;
@@ -1403,6 +1410,35 @@ extern "C" int gb_factor_fp64(gb_obj* o) {
     return 0;
   }
   return gb_invA_compute(o);
+}
+
+extern "C" int gb_obj_one_interface(gb_obj* o) { return o->schur_ok; }
+
+extern "C" int gb_block_factors_download(gb_obj* o, void* G0i, void* G1i, void* nX0, void* Minv, void* Si) {
+  if (!o->have_blk64) { gbi_set_error("gb_block_factors_download: no FP64 block factors"); return -1; }
+  void* d[5];
+  gbi_schur_mats(o->schur64, d);
+  void* h[5] = {G0i, G1i, nX0, Minv, Si};
+  const size_t bytes = (size_t)o->m.NN * o->m.NN * sizeof(cplx);
+  for (int i = 0; i < 5; i++)
+    if (h[i]) GB_CUDA(cudaMemcpy(h[i], d[i], bytes, cudaMemcpyDeviceToHost));
+  return 0;
+}
+
+extern "C" int gb_block_factors_upload(gb_obj* o, const void* G0i, const void* G1i, const void* nX0, const void* Minv,
+                                       const void* Si) {
+  if (!o->schur_ok) { gbi_set_error("gb_block_factors_upload: the object does not have one interface"); return -1; }
+  if (!o->schur64 && gbi_schur_create(o->m.NN, 1, &o->schur64)) return -1;
+  void* d[5];
+  gbi_schur_mats(o->schur64, d);
+  const void* h[5] = {G0i, G1i, nX0, Minv, Si};
+  const size_t bytes = (size_t)o->m.NN * o->m.NN * sizeof(cplx);
+  for (int i = 0; i < 5; i++) GB_CUDA(cudaMemcpy(d[i], h[i], bytes, cudaMemcpyHostToDevice));
+  if (gbi_schur_prepare(o->schur64, &o->m, o->st)) return -1;
+  o->have_blk64 = 1;
+  o->have_invA = 0;
+  o->have_lu32 = 0;
+  return 0;
 }
 
 extern "C" int gb_scene_step(gb_obj* o, int form, int type) {

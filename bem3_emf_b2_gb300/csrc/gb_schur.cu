@@ -555,3 +555,27 @@ extern "C" int gbi_schur_apply(GbSchur* s, const cplx* r, cplx* x, cudaStream_t 
 }
 
 extern "C" int gbi_schur_is_fp64(const GbSchur* s) { return s ? s->fp64 : -1; }
+
+// device addresses of the five factors (G0^-1, G1^-1, -X0, M^-1, S^-1)
+extern "C" void gbi_schur_mats(GbSchur* s, void** out) {
+  out[0] = s->G0i; out[1] = s->G1i; out[2] = s->nX0; out[3] = s->Minv; out[4] = s->Si;
+}
+
+// after the five factors were loaded from a file: the node normals and the
+// interface constants, as gbi_schur_factor sets them
+extern "C" int gbi_schur_prepare(GbSchur* s, const GbMeshDev* m, cudaStream_t st) {
+  const std::complex<double> k0(m->kn[0], m->kn[1]), k1(m->kn[2], m->kn[3]);
+  const std::complex<double> delt = k0 * k0 - k1 * k1, beps = (k0 * k0) / (k1 * k1), sigm = 1.0 - beps;
+  const std::complex<double> sd = sigm * delt;
+  s->beta = cmk(beps.real(), beps.imag());
+  s->sigma = cmk(sigm.real(), sigm.imag());
+  s->delta = cmk(delt.real(), delt.imag());
+  s->sigdel = cmk(sd.real(), sd.imag());
+  const unsigned g = (unsigned)((4 * m->Ne + 255) / 256);
+  if (s->fp64) k_schur_normals<double><<<g, 256, 0, st>>>(m->wen, m->eni, m->etype, m->Ne, (double*)s->vn);
+  else k_schur_normals<float><<<g, 256, 0, st>>>(m->wen, m->eni, m->etype, m->Ne, (float*)s->vn);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
+  return 0;
+}

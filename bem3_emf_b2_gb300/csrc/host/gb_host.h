@@ -40,6 +40,17 @@ void gb_call_unlock(void);
 void gb_bv_to_device(DOMD *md);    /* host SUBD boundary values -> device (once) */
 void gb_bv_to_host(DOMD *md);      /* device boundary values -> host SUBD */
 
+/* Versioned .cmat of the FP64 block factors, written in place of the dense
+ * inverse for objects with one interface (GB_CMAT_FORMAT=block, or when the
+ * dense inverse would take more than half the device memory): a 64-byte
+ * header -- the 8 bytes "GBBLKF64", int32 version 1, int32 NN, int32 number
+ * of matrices 5, int32 bytes per element 16, zeros -- then G0^-1, G1^-1,
+ * -G0^-1 H0, M^-1, S^-1, each NN x NN complex128 row-major.  The dense
+ * inverse stays the reference's headerless file. */
+#define GB_BLK_MAGIC "GBBLKF64"
+#define GB_BLK_HEADER 64
+#define GB_BLK_VERSION 1
+
 /* matrix.c */
 void gb_initalize_cmd2(CMD *cm);
 void gb_finalize_cmd2(CMD *cm);

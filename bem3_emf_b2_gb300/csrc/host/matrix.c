@@ -79,9 +79,48 @@ static void gb_create_cmatrix(CMD *cm,DOMD *md)
   }
 }
 
+/* block factors in place of the dense inverse? (GB_CMAT_FORMAT = block or
+ * dense; by default dense, as the reference, unless the inverse would take
+ * more than half the device memory) */
+static int gb_use_block(DOMD *md,gb_obj *o)
+{
+  if(!gb_obj_one_interface(o)) return 0;
+  const char *e=getenv("GB_CMAT_FORMAT");
+  if(e && strcmp(e,"block")==0) return 1;
+  if(e && strcmp(e,"dense")==0) return 0;
+  size_t fr=0,tot=0;
+  if(gb_device_memory(&fr,&tot)) return 0;
+  size_t na=8*(size_t)md->bd.NN;
+  return na*na*sizeof(double complex)>tot/2;
+}
+
+static void gb_write_block(CMD *cm,DOMD *md,gb_obj *o)
+{
+  if(gb_factor_fp64(o)) gb_die("matrix.c, block factors");
+  size_t nn=(size_t)md->bd.NN;
+  snprintf(cm->lupfn,128,"tmpblk.cmat");
+  FILE *fp=gb_fopen_w(cm->lupfn);
+  unsigned char hdr[GB_BLK_HEADER];
+  memset(hdr,0,sizeof(hdr));
+  memcpy(hdr,GB_BLK_MAGIC,8);
+  int meta[4]={GB_BLK_VERSION,(int)nn,5,(int)sizeof(double complex)};
+  memcpy(hdr+8,meta,sizeof(meta));
+  gb_fwrite(hdr,1,GB_BLK_HEADER,fp,cm->lupfn);
+  double complex *buf=(double complex *)m_alloc2(nn*nn,sizeof(double complex),"matrix.c blk");
+  for(int i=0;i<5;i++){
+    void *p[5]={NULL,NULL,NULL,NULL,NULL};
+    p[i]=buf;
+    if(gb_block_factors_download(o,p[0],p[1],p[2],p[3],p[4])) gb_die("matrix.c, block factors");
+    gb_fwrite(buf,sizeof(double complex),nn*nn,fp,cm->lupfn);
+  }
+  free(buf);
+  fclose(fp);
+}
+
 static void gb_lu_dec_A(CMD *cm,DOMD *md)
 {
   gb_obj *o=gb_dev(md);
+  if(gb_use_block(md,o)){ gb_write_block(cm,md,o); return; }
   if(gb_invA_compute(o)) gb_die("matrix.c, lu_dec_A()");
   double complex *buf=(double complex *)m_alloc2(cm->na*cm->na,sizeof(double complex),"matrix.c invA");
   if(gb_invA_download(o,buf)) gb_die("matrix.c, lu_dec_A()");

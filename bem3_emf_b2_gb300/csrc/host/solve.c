@@ -31,6 +31,31 @@ static double complex *gb_read_cmat_file(const char *fn,size_t n)
   return b;
 }
 
+/* the object's factors from a block-factor file (GB_BLK_MAGIC); 0 if the
+ * file is the reference's dense inverse instead, 1 when loaded */
+static int gb_read_block_file(DOMD *md,gb_obj *o)
+{
+  FILE *fp=fopen(md->cm.lupfn,"rb");
+  if(fp==NULL){ printf("solve.c, failed to open %s. exit...\n",md->cm.lupfn); exit(1); }
+  unsigned char hdr[GB_BLK_HEADER];
+  size_t got=fread(hdr,1,GB_BLK_HEADER,fp);
+  if(got!=GB_BLK_HEADER || memcmp(hdr,GB_BLK_MAGIC,8)!=0){ fclose(fp); return 0; }
+  int meta[4];
+  memcpy(meta,hdr+8,sizeof(meta));
+  size_t nn=(size_t)md->bd.NN;
+  if(meta[0]!=GB_BLK_VERSION || meta[1]!=(int)nn || meta[2]!=5 || meta[3]!=(int)sizeof(double complex)){
+    printf("solve.c, %s: block factors version %d for %d nodes, expected version %d for %zu nodes. exit...\n",
+           md->cm.lupfn,meta[0],meta[1],GB_BLK_VERSION,nn);
+    exit(1);
+  }
+  double complex *m=(double complex *)m_alloc2(5*nn*nn,sizeof(double complex),"solve.c blk");
+  if(fread(m,sizeof(double complex),5*nn*nn,fp)!=5*nn*nn){ printf("solve.c, failed to read %s. exit...\n",md->cm.lupfn); exit(1); }
+  fclose(fp);
+  if(gb_block_factors_upload(o,m,m+nn*nn,m+2*nn*nn,m+3*nn*nn,m+4*nn*nn)) gb_die("solve.c, gb_block_factors_upload()");
+  free(m);
+  return 1;
+}
+
 void gb_cmat_read(DOMD *md,int with_inverse)
 {
   gb_obj *o=gb_dev(md);
@@ -54,10 +79,12 @@ void gb_cmat_read(DOMD *md,int with_inverse)
     gb_dev_set_flags(md,GB_F_CMAT,0);
   }
   if(with_inverse && !(gb_dev_flags(md)&GB_F_INV)){
-    size_t na=8*(size_t)md->bd.NN;
-    double complex *A=gb_read_cmat_file(md->cm.lupfn,na*na);
-    if(gb_invA_upload(o,A)) gb_die("solve.c, gb_invA_upload()");
-    free(A);
+    if(gb_read_block_file(md,o)==0){
+      size_t na=8*(size_t)md->bd.NN;
+      double complex *A=gb_read_cmat_file(md->cm.lupfn,na*na);
+      if(gb_invA_upload(o,A)) gb_die("solve.c, gb_invA_upload()");
+      free(A);
+    }
     gb_dev_set_flags(md,GB_F_INV,0);
   }
 }

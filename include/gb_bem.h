@@ -46,6 +46,8 @@ typedef struct gb_mesh_desc {
 
 const char *gb_last_error(void);
 int gb_device_count(void);
+/* free and total memory of the current device, bytes */
+int gb_device_memory(size_t *free_bytes, size_t *total_bytes);
 /* kernel launches made by this library so far (all threads) */
 unsigned long long gb_launch_count(void);
 /* the CUDA stream (cudaStream_t) the object's work runs on */
@@ -247,6 +249,17 @@ int gb_set_tc_passes(int passes);
 int gb_set_lu_pivoting(gb_obj *o, int mode);
 int gb_lu_info(gb_obj *o, int *rbt, int *fallbacks);
 int gb_factor_fp64(gb_obj *o);
+/* 1 if every element of the object separates domain 0 (outside) from domain
+ * 1 (inside): the block elimination applies */
+int gb_obj_one_interface(gb_obj *o);
+/* the FP64 block factors of gb_factor_fp64 (each NN x NN complex, row-major):
+ * G0^-1, G1^-1, -G0^-1 H0, M^-1, S^-1 -- to and from host memory (upload
+ * makes them the object's factors for later gb_solve_mEMP calls).  The
+ * tools keep them in the versioned <prefix>_blk.cmat file in place of the
+ * dense inverse. */
+int gb_block_factors_download(gb_obj *o, void *G0i, void *G1i, void *nX0, void *Minv, void *Si);
+int gb_block_factors_upload(gb_obj *o, const void *G0i, const void *G1i, const void *nX0, const void *Minv,
+                            const void *Si);
 int gb_scene_step(gb_obj *o, int form, int type);
 
 /* Dense complex FP64 LU solve of a host system: A (n x n, row-major) X = B

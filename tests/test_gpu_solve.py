@@ -61,3 +61,32 @@ def test_bv_solver_parity(case, gb_build, tmp_path):
     wd = str(tmp_path)
     out, ana = _solve(meta, gb_build, wd)
     _check(meta, gold, wd, out, ana)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["cube1", "sphere2", "cone_mix", "cone_tri", "pair"])
+def test_tools_with_block_factor_files(case, gb_build, tmp_path):
+    """d3b2_create_matrix with GB_CMAT_FORMAT=block writes the versioned
+    <prefix>_blk.cmat (header + the five FP64 node-sized factors) in place of
+    the dense <prefix>_invA.cmat, records it in the .obj, and d3b2_bv_solver
+    solves from it: the same boundary values, convergence history, fields,
+    forces and absorbed powers as the reference's golden outputs."""
+    import struct
+    meta, gold = load_case(case)
+    wd = str(tmp_path)
+    write_inputs(meta, wd)
+    env = {"GB_CMAT_FORMAT": "block"}
+    run([os.path.join(gb_build, "d3b2_create_matrix"), "medium.txt", "mesh.msh", "obj.obj"], wd, env)
+    obj = formats.read_obj(os.path.join(wd, "obj.obj"))
+    assert obj["invA"] == "obj_blk.cmat", obj["invA"]
+    assert not os.path.exists(os.path.join(wd, "obj_invA.cmat"))
+    with open(os.path.join(wd, "obj_blk.cmat"), "rb") as f:
+        hdr = f.read(64)
+    assert hdr[:8] == b"GBBLKF64"
+    ver, nn, nmat, esz = struct.unpack("<4i", hdr[8:24])
+    assert (ver, nn, nmat, esz) == (1, meta["NN"], 5, 16)
+    assert os.path.getsize(os.path.join(wd, "obj_blk.cmat")) == 64 + 5 * nn * nn * 16
+    meshgen.write_object_settings(os.path.join(wd, "objs.txt"), [(o[0], o[1]) for o in meta["objects"]])
+    out = run([os.path.join(gb_build, "d3b2_bv_solver"), "objs.txt", "res.dat"], wd)
+    ana = run([os.path.join(gb_build, "bem3_analysis"), "res.dat"], wd)
+    _check(meta, gold, wd, out, ana)
