@@ -204,6 +204,25 @@ class MultiScene:
     def drop_device(self):
         lib().gbh_mscene_drop_device(self.h)
 
+    def field_map(self, pts, type_=2, which=0, memp=1):
+        """E, H (n x 3 complex) and containing object at points pts (n x 3) of the
+        solved scene (gb_mo_EH_points): scattered (which 0), total (1) or
+        incident (2) field; memp 1 the potential-derivative (far-field) form"""
+        import numpy as np
+        L = lib()
+        vp, ci = ctypes.c_void_p, ctypes.c_int
+        L.gb_mo_EH_points.argtypes = [vp, ci, vp, ci, ci, ci, vp, vp, vp]
+        L.gb_mo_EH_points.restype = ci
+        p = np.ascontiguousarray(pts, float).reshape(-1, 3)
+        n = len(p)
+        E = np.zeros((n, 3), complex)
+        H = np.zeros((n, 3), complex)
+        oid = np.zeros(n, np.int32)
+        if L.gb_mo_EH_points(self.h, n, p.ctypes.data, type_, which, memp, E.ctypes.data, H.ctypes.data,
+                             oid.ctypes.data) != 0:
+            raise RuntimeError("gb_mo_EH_points failed: %s" % last_error())
+        return E, H, oid
+
     def h2d_bytes(self):
         return int(lib().gbh_mscene_h2d_bytes(self.h))
 

@@ -224,6 +224,12 @@ struct gb_obj {
   GbSchur* schur64;
   int have_blk64;
   int refine_mode;  // 0: FP64 GMRES (default), 1: classical refinement (diagnostic)
+  // right-hand side and solution of the last gb_solve_mEMP, kept between
+  // calls: the next solve with the same factors starts from that solution
+  // (the multiple-scattering iteration changes the right-hand side less and
+  // less); invalidated by an assembly or a factorisation
+  cplx *Bw, *Xw;
+  int have_xw;
   // arithmetic of the regular pairs of the field kernels (potentials at
   // points, fields on the boundary, cross operators): 2 double-float after a
   // precision-2 assembly, else FP64
@@ -274,6 +280,7 @@ extern "C" void gb_obj_destroy(gb_obj* o) {
   cudaFree(o->LU32); cudaFree(o->ipiv32); cudaFree(o->perm32); cudaFree(o->rbt);
   gbi_schur_destroy(o->schur);
   gbi_schur_destroy(o->schur64);
+  cudaFree(o->Bw); cudaFree(o->Xw);
   for (int d = 0; d < GB_MAXDOM; d++) {
     cudaFree(o->bU[d]); cudaFree(o->bdU[d]); cudaFree(o->bE[d]); cudaFree(o->bdE[d]); cudaFree(o->bH[d]); cudaFree(o->bdH[d]);
   }
@@ -301,6 +308,7 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   o->rbt = nullptr; o->lu_rbt = 0; o->lu_mode = 0; o->lu_fallbacks = 0; o->field_prec = 0;
   o->schur = nullptr; o->schur_ok = 0; o->lu_schur = 0;
   o->schur64 = nullptr; o->have_blk64 = 0; o->refine_mode = 0;
+  o->Bw = o->Xw = nullptr; o->have_xw = 0;
   o->lu_mode = 3;  // block elimination where the object allows it
   {  // GB_LU_MODE: the objects' initial gb_set_lu_pivoting mode (0..3)
     const char* e = getenv("GB_LU_MODE");
@@ -428,6 +436,7 @@ static void assembled(gb_obj* o, int precision) {
   o->have_invA = 0;
   o->have_lu32 = 0;
   o->have_blk64 = 0;
+  o->have_xw = 0;
   o->field_prec = precision >= 2 ? precision : 0;
 }
 
@@ -535,6 +544,7 @@ extern "C" int gb_cmatrix_upload(gb_obj* o, int did, const void* G, const void* 
   if (dH) GB_CUDA(cudaMemcpy(o->dH[did], dH, 2 * N * N * sizeof(cplx), cudaMemcpyHostToDevice));
   if (dF) GB_CUDA(cudaMemcpy(o->dF[did], dF, 3 * N * sizeof(double), cudaMemcpyHostToDevice));
   o->have_invA = 0;
+  o->have_xw = 0;
   return 0;
 }
 
@@ -754,7 +764,7 @@ static int sync_obj(gb_obj* o, const char* what) {
   return 0;
 }
 
-static int ir_solve(gb_obj* o, const cplx* B, cplx* X);
+static int ir_solve(gb_obj* o, const cplx* B, cplx* X, bool warm);
 
 extern "C" int gb_solve_mEMP(gb_obj* o) {
   if (!o->have_invA && !o->have_lu32 && !o->have_blk64) {
@@ -763,8 +773,12 @@ extern "C" int gb_solve_mEMP(gb_obj* o) {
   }
   if (ensure_bv(o)) return -1;
   size_t na = o->na;
-  cplx *B = nullptr, *X = nullptr;
-  if (dalloc((void**)&B, na * sizeof(cplx)) || dalloc((void**)&X, na * sizeof(cplx))) { cudaFree(B); return -1; }
+  if (!o->Bw && (dalloc((void**)&o->Bw, na * sizeof(cplx)) || dalloc((void**)&o->Xw, na * sizeof(cplx)))) {
+    cudaFree(o->Bw);
+    o->Bw = nullptr;
+    return -1;
+  }
+  cplx *B = o->Bw, *X = o->Xw;
   int rc = 0;
   size_t base = 0;
   for (int d = 0; d <= o->m.MN && !rc; d++) {
@@ -773,11 +787,12 @@ extern "C" int gb_solve_mEMP(gb_obj* o) {
                      o->nrows[d], base, B, o->st);
     base += 4 * (size_t)o->nrows[d];
   }
-  if (!rc) rc = o->have_invA ? gbi_zgemv(o->invA, na, (int)na, (int)na, B, X, o->st) : ir_solve(o, B, X);
+  const bool warm = o->have_xw != 0;
+  o->have_xw = 0;
+  if (!rc) rc = o->have_invA ? gbi_zgemv(o->invA, na, (int)na, (int)na, B, X, o->st) : ir_solve(o, B, X, warm);
   for (int d = 0; d <= o->m.MN && !rc; d++) rc = gbi_store_bv(X, &o->m, o->kn_dev, o->Ui, o->dUi, d, o->bU[d], o->bdU[d], o->st);
   if (!rc) rc = sync_obj(o, "gb_solve_mEMP");
-  cudaFree(B);
-  cudaFree(X);
+  if (!rc) o->have_xw = 1;
   return rc;
 }
 
@@ -1185,6 +1200,7 @@ static int factor_schur(gb_obj* o) {
 extern "C" int gb_factor_mixed(gb_obj* o) {
   size_t na = o->na;
   o->have_lu32 = 0;
+  o->have_xw = 0;
   o->have_blk64 = 0;
   if (o->lu_mode == 3 && o->schur_ok) {
     const int r = factor_schur(o);
@@ -1327,12 +1343,12 @@ static int precond(gb_obj* o, const cplx* v, cplx* z, cplxf* d, cplxf* d2, cudaS
   return gbi_ir_step(z, v, d, d2, o->LU32, na, (int)na, o->perm32, st);
 }
 
-// FP64 GMRES(20) refinement, right-preconditioned by the current factors, to
+// FP64 flexible GMRES(20) refinement, right-preconditioned by the current factors, to
 // ||b - A x|| <= 1e-13 ||b||; A applied in FP64 from G and H.  A run that
 // does not converge with butterfly or block factors (or, in the diagnostic
 // LU mode 2, after its first iteration) refactorises with tournament
 // pivoting and continues from the current x.
-static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
+static int ir_solve(gb_obj* o, const cplx* B, cplx* X, bool warm) {
   if (o->refine_mode == 1) return ir_classical(o, B, X);
   const size_t na = o->na;
   size_t nmax = 0;
@@ -1347,11 +1363,12 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X) {
   GbOp A = [o, PQ](const cplx* x, cplx* y, cudaStream_t) { return apply_A(o, x, PQ, y); };
   GbOp M = [o, d, d2](const cplx* v, cplx* z, cudaStream_t st) { return precond(o, v, z, d, d2, st); };
   int rc = 0;
-  if (cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess) { gbi_set_error("ir_solve: memset"); rc = -1; }
+  // from the previous solution with the same factors (warm), else from zero
+  if (!warm && cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess) { gbi_set_error("ir_solve: memset"); rc = -1; }
   int it = 0, tot = 0;
   double rel = 1.0;
   const bool forced = o->lu_mode == 2 && o->lu_rbt;  // diagnostic: the fallback after one iteration
-  int r = rc ? -1 : gbi_gmres(na, B, X, true, A, M, 20, 1e-13, forced ? 1 : 60, o->st, &it, &rel);
+  int r = rc ? -1 : gbi_gmres(na, B, X, !warm, A, M, 20, 1e-13, forced ? 1 : 60, o->st, &it, &rel);
   tot += it;
   if (r == 1 && !o->have_blk64 && (o->lu_rbt || o->lu_schur)) {
     if (!(rel < 1.0) && cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess) r = -1;
@@ -1397,6 +1414,7 @@ extern "C" int gb_form_precision(int form) { return form == 1 ? 3 : (form == 2 ?
 // inverse of A as the reference (gb_invA_compute).
 extern "C" int gb_factor_fp64(gb_obj* o) {
   o->have_lu32 = 0;
+  o->have_xw = 0;
   o->have_blk64 = 0;
   if (o->lu_mode == 3 && o->schur_ok) {
     if (!o->G[0] || !o->G[1]) { gbi_set_error("coupled matrix: a domain has no coefficient matrices"); return -1; }
@@ -1435,6 +1453,7 @@ extern "C" int gb_block_factors_upload(gb_obj* o, const void* G0i, const void* G
   const size_t bytes = (size_t)o->m.NN * o->m.NN * sizeof(cplx);
   for (int i = 0; i < 5; i++) GB_CUDA(cudaMemcpy(d[i], h[i], bytes, cudaMemcpyHostToDevice));
   if (gbi_schur_prepare(o->schur64, &o->m, o->st)) return -1;
+  o->have_xw = 0;
   o->have_blk64 = 1;
   o->have_invA = 0;
   o->have_lu32 = 0;

@@ -5,13 +5,16 @@
 // tournament LU or the block elimination's node inverses -- or with the FP64
 // block factors).
 //
-// GMRES(m) (Saad and Schultz 1986) on A M^-1 u = b, x = M^-1 u: per
-// iteration one preconditioner solve z = M^-1 v_j, one FP64 product w = A z,
+// Flexible GMRES(m) (Saad 1993) on A M^-1 u = b: per iteration one
+// preconditioner solve z_j = M^-1 v_j, kept, and one FP64 product w = A z_j,
 // classical Gram-Schmidt against v_0..v_j done twice (Giraud, Langou and
 // Rozloznik 2005: "twice is enough"), complex Givens rotations on the host
-// for the (m+1) x m Hessenberg least-squares problem.  The recurrence's
-// residual estimate ends a cycle; the true residual b - A x is formed in FP64
-// at the start of every cycle and decides convergence.  Against classical
+// for the (m+1) x m Hessenberg least-squares problem; the update is
+// x += Z y with the stored z_j (the lower-precision solve is not exactly
+// linear, so x = M^-1 (V y) would reintroduce its rounding: a second cycle
+// per solve).  The recurrence's residual estimate ends a cycle; the true
+// residual b - A x is formed in FP64 at the start of every cycle and decides
+// convergence.  Against classical
 // refinement (x += M^-1 (b - A x)) it costs the same per step but converges
 // whenever the preconditioned operator's spectrum stays away from zero,
 // which tolerates much less accurate factors (Carson and Higham 2017).
@@ -124,7 +127,7 @@ struct Work {
 };
 }  // namespace
 
-// Solves A x = b to ||b - A x|| <= tol ||b|| by GMRES(m) right-preconditioned
+// Solves A x = b to ||b - A x|| <= tol ||b|| by flexible GMRES(m) right-preconditioned
 // by M (z = M^-1 v), from the initial guess in x (x_zero: x is zero, so the
 // first residual is b without a product).  At most maxit iterations.
 // Returns 0 when converged, 1 when not (maxit reached, or a cycle that did not
@@ -141,11 +144,12 @@ extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const Gb
   W.n = n;
   W.nchunk = (int)((n + GS_CHUNK - 1) / GS_CHUNK);
   W.st = st;
-  cplx *V = nullptr, *w = nullptr, *z = nullptr, *r = nullptr, *yd = nullptr, *h2 = nullptr;
+  cplx *V = nullptr, *Z = nullptr, *w = nullptr, *z = nullptr, *r = nullptr, *yd = nullptr, *h2 = nullptr;
   W.partial = nullptr;
   W.h = nullptr;
   int rc = 0;
   if (cudaMallocAsync((void**)&V, (size_t)(m + 1) * n * sizeof(cplx), st) != cudaSuccess ||
+      cudaMallocAsync((void**)&Z, (size_t)m * n * sizeof(cplx), st) != cudaSuccess ||
       cudaMallocAsync((void**)&w, n * sizeof(cplx), st) != cudaSuccess ||
       cudaMallocAsync((void**)&z, n * sizeof(cplx), st) != cudaSuccess ||
       cudaMallocAsync((void**)&r, n * sizeof(cplx), st) != cudaSuccess ||
@@ -200,8 +204,9 @@ extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const Gb
     int jend = 0;
     for (int j = 0; j < m && it < maxit; j++) {
       cplx* vj = V + (size_t)j * n;
-      if (M(vj, z, st)) { rc = -1; break; }
-      if (A(z, w, st)) { rc = -1; break; }
+      cplx* zj = Z + (size_t)j * n;
+      if (M(vj, zj, st)) { rc = -1; break; }
+      if (A(zj, w, st)) { rc = -1; break; }
       it++;
       // classical Gram-Schmidt, twice
       if (W.dots(V, n, j + 1, w, h2)) { rc = -1; break; }
@@ -240,7 +245,7 @@ extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const Gb
       if (!(std::abs(g[j + 1]) > 0.5 * tol * bnorm) || hn == 0.0) break;
     }
     if (rc || jend == 0) break;
-    // y = H^-1 g (upper triangular), x += M^-1 (V y)
+    // y = H^-1 g (upper triangular), x += Z y
     for (int i = jend - 1; i >= 0; i--) {
       C s = g[i];
       for (int k = i + 1; k < jend; k++) s -= H[(size_t)i * m + k] * y[k];
@@ -253,9 +258,8 @@ extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const Gb
       rc = -1;
       break;
     }
-    k_gs_combine<<<W.grid(), 256, 0, st>>>(V, n, jend, n, yd, w);
+    k_gs_combine<<<W.grid(), 256, 0, st>>>(Z, n, jend, n, yd, z);
     gbi_count_launch();
-    if (M(w, z, st)) { rc = -1; break; }
     k_gs_add<<<W.grid(), 256, 0, st>>>(x, z, n);
     gbi_count_launch();
     if (cudaStreamSynchronize(st) != cudaSuccess) { rc = -1; break; }  // yh is host memory
@@ -264,7 +268,7 @@ extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const Gb
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) gbi_set_error("gmres: %s", cudaGetErrorString(e));
   }
-  void* tmp[7] = {V, w, z, r, yd, h2, W.partial};
+  void* tmp[8] = {V, Z, w, z, r, yd, h2, W.partial};
   for (void* t : tmp)
     if (t) cudaFreeAsync(t, st);
   cudaStreamSynchronize(st);

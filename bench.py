@@ -335,6 +335,21 @@ def run_gpu(args):
         torch.cuda.synchronize()
         te.append(time.perf_counter() - t0)
     e2e = dist_max(dist, sum(te)) / (len(te) * ws)
+    # far field of the solved scene on the 91 x 180 angular grid at r = 2000
+    # lambda0 (reference example4.c:32-66) through the batched field map
+    far = None
+    if cones:
+        th = np.linspace(0.0, np.pi, 91)
+        ph = np.arange(180) * (2.0 * np.pi / 180)
+        T, P = np.meshgrid(th, ph, indexing="ij")
+        pts = 2000.0 * np.stack([np.sin(T) * np.cos(P), np.sin(T) * np.sin(P), np.cos(T)], -1).reshape(-1, 3)
+        sc.field_map(pts[:64])
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        Ef, Hf, _ = sc.field_map(pts)
+        far = {"points": len(pts), "s": time.perf_counter() - t0, "r": 2000.0,
+               "form": "mo_EH_mEMP_s (scattered, potential-derivative formula), quadrature type 2",
+               "max_abs_E": float(np.abs(Ef).max())}
     # instrumented step for the roofline (per-launch events), outside the timed steps
     L.gb_ktime_enable(1)
     torch.cuda.synchronize()
@@ -371,6 +386,8 @@ def run_gpu(args):
                "gpu_launches": int(round(launches)), "clocks": clk.summary()}
         if phases:
             out["phases_s_last_step"] = phases
+        if far:
+            out["far_field_91x180"] = far
         if iters:
             out["iterations"] = {"count": iters[0], "cc": iters[1]}
         if roof:

@@ -205,7 +205,7 @@ int gb_assemble_domain_noalloc(const double *cr, const double *cw, const int *et
 int gb_factor_mixed(gb_obj *o);
 int gb_ir_info(gb_obj *o, int *iters, double *relres);
 /* Refinement of the solves that use lower-precision or block factors.
- * mode 0 (default): FP64 GMRES(20), right-preconditioned by the factors
+ * mode 0 (default): FP64 flexible GMRES(20), right-preconditioned by the factors
  * (residual b - A x in FP64 from G, H; converged at ||b - A x|| <= 1e-13 ||b||;
  * a run that does not converge with butterfly or block factors refactorises
  * with tournament pivoting and continues).  mode 1 (diagnostic): classical
