@@ -23,6 +23,7 @@ int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, c
                          double* dF, double* Fs, cudaStream_t st);
 int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int precision, int row0, int nrow, cplx* G, cplx* H,
                       cplx* dG, cplx* dH, double* dF, double* Fs, cudaStream_t st);
+int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precision, cudaStream_t st);
 int gbi_build_A_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
                        const double* kn_dev, int did, int nrows, size_t base, size_t na, cplx* A, cudaStream_t st);
 int gbi_zgetrf(cplx* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
@@ -497,6 +498,27 @@ extern "C" int gb_assemble_rows(gb_obj* o, int did, int row0, int nrow, int type
                                    dF, Fs, o->st);
   cudaFreeAsync(Fs, o->st);
   return rc;
+}
+
+extern "C" int gb_assemble_objects(gb_obj** objs, int n, int type, int precision) {
+  if (n <= 0) return 0;
+  if (check_asm_args(type, precision)) return -1;
+  std::vector<GbAsmItem> items;
+  for (int i = 0; i < n; i++) {
+    gb_obj* o = objs[i];
+    for (int d = 0; d <= o->m.MN; d++) {
+      if (ensure_cmatrix(o, d)) return -1;
+      if (o->m.sb_Ne[d] == 0) continue;
+      GbAsmItem it;
+      it.m = &o->m; it.did = d; it.row0 = 0; it.nrow = 4 * o->m.sb_Ne[d];
+      it.G = o->G[d]; it.H = o->H[d]; it.dG = o->dG[d]; it.dH = o->dH[d]; it.dF = o->dF[d];
+      items.push_back(it);
+    }
+    GB_CUDA(cudaStreamSynchronize(o->st));  // earlier work on these matrices
+  }
+  if (gbi_assemble_list(items.data(), (int)items.size(), type, precision, objs[0]->st)) return -1;
+  for (int i = 0; i < n; i++) assembled(objs[i], precision);
+  return 0;
 }
 
 extern "C" int gb_cmatrix_download(gb_obj* o, int did, void* G, void* H, void* dG, void* dH, double* dF) {
@@ -1462,7 +1484,7 @@ extern "C" int gb_block_factors_upload(gb_obj* o, const void* G0i, const void* G
 
 extern "C" int gb_scene_step(gb_obj* o, int form, int type) {
   if (form < 0 || form > 3) { gbi_set_error("gb_scene_step: form %d not in 0..3", form); return -1; }
-  if (gb_assemble_all(o, type, gb_form_precision(form))) return -1;
+  if (gb_assemble_objects(&o, 1, type, gb_form_precision(form))) return -1;
   if (form == 0) { if (gb_factor_fp64(o)) return -1; }
   else if (gb_factor_mixed(o)) return -1;
   if (gb_solve_mEMP(o)) return -1;

@@ -48,6 +48,7 @@
 #include "gb_internal.h"
 #include "gb_quad_df.cuh"
 #include <mutex>
+#include <vector>
 
 
 
@@ -70,6 +71,7 @@ struct AsmArgs {
   const uint8_t* only;  // non-null: k_asm_regular integrates only the pairs flagged here
   int adapt;       // k_asm_regular_df: the distance-adaptive order (precision 3)
   int row0, nrow;  // the rows row0 .. row0 + nrow - 1 of the domain; outputs hold nrow rows
+  uint8_t* redo;   // work-list launches: the item's flags of pairs for the FP64 pass
 };
 
 // unit tangents at collocation node tn of element |td| (reference tz_te_bd_node d3b1_elem.c:122-143)
@@ -300,10 +302,10 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, uint8_t* red
 // (reg_integrate_dn, gb_quad_df.cuh); pairs whose |Re dF/dt| is within 0.05
 // of the CBD_SDF decision (or not finite) are flagged and redone by the FP64
 // kernel, which decides GLN/GHN exactly as the reference.
-__global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo) {
+__device__ __forceinline__ void asm_regular_df_body(const AsmArgs& a, uint8_t* redo, unsigned bx) {
   const size_t N = (size_t)a.Ne * 4;
   const size_t npair = (size_t)a.nrow * (size_t)a.Ne;
-  size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t p = (size_t)bx * blockDim.x + threadIdx.x;
   if (p >= npair) return;
   const int row = a.row0 + (int)(p / a.Ne), sidx = (int)(p % a.Ne);
   const int t = row / 4 + 1, tn = row % 4;
@@ -325,11 +327,16 @@ __global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo
   }
   store_pair(a, N, row, sidx, D);
 }
+__global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo) {
+  asm_regular_df_body(a, redo, blockIdx.x);
+}
 
-__global__ void __launch_bounds__(128) k_asm_regular(AsmArgs a) {
+// FP64 regular pairs (all, or those flagged in only); the whole warp
+// integrates each pair that needs the GHN fallback
+__device__ __forceinline__ void asm_regular_body(const AsmArgs& a, const uint8_t* only, unsigned bx) {
   const size_t N = (size_t)a.Ne * 4;
   const size_t npair = (size_t)a.nrow * (size_t)a.Ne;
-  size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  size_t p = (size_t)bx * blockDim.x + threadIdx.x;
   bool active = p < npair;
   int row = 0, sidx = 0;
   bool work = false, fb = false;
@@ -348,7 +355,7 @@ __global__ void __launch_bounds__(128) k_asm_regular(AsmArgs a) {
     Elem T;
     load_elem(T, a.cr, a.cw, a.etype, atd);
     bool rowok = T.quad || tn < 3;
-    if (rowok && sd != td && (a.only == nullptr || a.only[p] != 0)) {
+    if (rowok && sd != td && (only == nullptr || only[p] != 0)) {
       work = true;
       for (int d = 0; d < 3; d++) rt[d] = __ldg(a.ren + (size_t)atd * 12 + tn * 3 + d);
       node_tangents(T, tn, vt);
@@ -381,6 +388,7 @@ __global__ void __launch_bounds__(128) k_asm_regular(AsmArgs a) {
   }
   if (work) store_pair(a, N, row, sidx, A);
 }
+__global__ void __launch_bounds__(128) k_asm_regular(AsmArgs a) { asm_regular_body(a, a.only, blockIdx.x); }
 
 // ---- double-float set B of the singular pairs (precision 2)
 // The derivative integrals on [DEPS, rm] with the GHN rule (sing_bil_setB /
@@ -841,9 +849,9 @@ static __device__ void sing_item_df(const SingCtx& c, const RowD& R, int q, Sing
 }
 
 template <bool DF>
-__global__ void __launch_bounds__(256) k_asm_singular(AsmArgs a) {
+__device__ __forceinline__ void asm_singular_body(const AsmArgs& a, unsigned bx) {
   __shared__ double red[51 * 8];
-  const int row = a.row0 + blockIdx.x;
+  const int row = a.row0 + (int)bx;
   const int t = row / 4 + 1, tn = row % 4;
   const int td = __ldg(a.sid + t);
   const int atd = abs(td);
@@ -884,10 +892,12 @@ __global__ void __launch_bounds__(256) k_asm_singular(AsmArgs a) {
     store_pair(a, (size_t)a.Ne * 4, row, t - 1, R);
   }
 }
+template <bool DF>
+__global__ void __launch_bounds__(256) k_asm_singular(AsmArgs a) { asm_singular_body<DF>(a, blockIdx.x); }
 
-__global__ void k_asm_rows(AsmArgs a) {
+__device__ __forceinline__ void asm_rows_body(const AsmArgs& a, unsigned bx) {
   const size_t N = (size_t)a.Ne * 4;
-  const int lr = blockIdx.x * blockDim.x + threadIdx.x;  // row of the output block
+  const int lr = (int)bx * blockDim.x + threadIdx.x;  // row of the output block
   if (lr >= a.nrow) return;
   const int row = a.row0 + lr;
   int t = row / 4 + 1, tn = row % 4;
@@ -906,6 +916,41 @@ __global__ void k_asm_rows(AsmArgs a) {
   a.dF[(size_t)lr * 3 + 0] = diag;
   a.dF[(size_t)lr * 3 + 1] = Fz;
   a.dF[(size_t)lr * 3 + 2] = Fe;
+}
+__global__ void k_asm_rows(AsmArgs a) { asm_rows_body(a, blockIdx.x); }
+
+// ---- work-list launches: one launch per phase over items of uneven size
+// (every domain of every object of a scene).  Item i owns the blocks
+// blk0[i] .. blk0[i + 1] - 1 of the launch; a block finds its item by binary
+// search and runs the single-domain body with its local block index.
+__device__ __forceinline__ int find_item(const unsigned* __restrict__ blk0, int nitems, unsigned b) {
+  int lo = 0, hi = nitems - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (blk0[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+__global__ void __launch_bounds__(128) k_asm_regular_df_list(const AsmArgs* __restrict__ items,
+                                                             const unsigned* __restrict__ blk0, int nitems) {
+  const int i = find_item(blk0, nitems, blockIdx.x);
+  asm_regular_df_body(items[i], items[i].redo, blockIdx.x - blk0[i]);
+}
+__global__ void __launch_bounds__(128) k_asm_regular_list(const AsmArgs* __restrict__ items,
+                                                          const unsigned* __restrict__ blk0, int nitems, int flagged) {
+  const int i = find_item(blk0, nitems, blockIdx.x);
+  asm_regular_body(items[i], flagged ? items[i].redo : nullptr, blockIdx.x - blk0[i]);
+}
+template <bool DF>
+__global__ void __launch_bounds__(256) k_asm_singular_list(const AsmArgs* __restrict__ items,
+                                                           const unsigned* __restrict__ blk0, int nitems) {
+  const int i = find_item(blk0, nitems, blockIdx.x);
+  asm_singular_body<DF>(items[i], blockIdx.x - blk0[i]);
+}
+__global__ void k_asm_rows_list(const AsmArgs* __restrict__ items, const unsigned* __restrict__ blk0, int nitems) {
+  const int i = find_item(blk0, nitems, blockIdx.x);
+  asm_rows_body(items[i], blockIdx.x - blk0[i]);
 }
 
 extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG,
@@ -952,6 +997,7 @@ extern "C" int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int prec
   a.adapt = precision == 3;
   a.row0 = row0;
   a.nrow = nrow;
+  a.redo = nullptr;
   GB_CUDA(cudaMemsetAsync(G, 0, nr * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(H, 0, nr * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(dG, 0, 2 * nr * N * sizeof(cplx), st));
@@ -986,6 +1032,88 @@ extern "C" int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int prec
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
+}
+
+// Work-list assembly: every item (rows of one domain of one object) with one
+// launch per phase -- double-float regular pairs (precision >= 2), FP64
+// regular pairs (the flagged ones after a double-float pass), singular
+// pairs, row sums -- instead of a launch sequence per domain.  Items of
+// uneven size share the GPU without tails of their own.  Synchronises st.
+extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precision, cudaStream_t st) {
+  if (n <= 0) return 0;
+  std::vector<AsmArgs> it((size_t)n);
+  std::vector<unsigned> breg((size_t)n + 1, 0), bsing((size_t)n + 1, 0), brows((size_t)n + 1, 0);
+  std::vector<void*> tmp;
+  int rc = 0;
+  for (int i = 0; i < n && !rc; i++) {
+    const GbMeshDev* m = d[i].m;
+    const int did = d[i].did, Ne = m->sb_Ne[did];
+    const size_t N = (size_t)Ne * 4, nr = (size_t)d[i].nrow;
+    AsmArgs& a = it[i];
+    memset(&a, 0, sizeof(a));
+    a.cr = m->cr; a.cw = m->cw; a.etype = m->etype; a.ren = m->ren;
+    a.sid = m->sid + m->sb_off[did];
+    a.Ne = Ne;
+    a.k = cmk(m->kn[2 * did], m->kn[2 * did + 1]);
+    a.type = type; a.did = did;
+    a.G = d[i].G; a.H = d[i].H; a.dG = d[i].dG; a.dH = d[i].dH; a.dF = d[i].dF;
+    a.adapt = precision == 3;
+    a.row0 = d[i].row0; a.nrow = d[i].nrow;
+    const size_t npair = nr * (size_t)Ne;
+    if (cudaMallocAsync((void**)&a.Fs, 3 * nr * (size_t)Ne * sizeof(double), st) != cudaSuccess ||
+        cudaMallocAsync((void**)&a.redo, npair + 16, st) != cudaSuccess) {
+      gbi_set_error("work-list assembly: out of device memory");
+      rc = -1;
+      break;
+    }
+    tmp.push_back(a.Fs);
+    tmp.push_back(a.redo);
+    if (cudaMemsetAsync(a.G, 0, nr * N * sizeof(cplx), st) != cudaSuccess ||
+        cudaMemsetAsync(a.H, 0, nr * N * sizeof(cplx), st) != cudaSuccess ||
+        cudaMemsetAsync(a.dG, 0, 2 * nr * N * sizeof(cplx), st) != cudaSuccess ||
+        cudaMemsetAsync(a.dH, 0, 2 * nr * N * sizeof(cplx), st) != cudaSuccess ||
+        cudaMemsetAsync(a.dF, 0, 3 * nr * sizeof(double), st) != cudaSuccess ||
+        cudaMemsetAsync(a.Fs, 0, 3 * nr * (size_t)Ne * sizeof(double), st) != cudaSuccess) {
+      gbi_set_error("work-list assembly: memset");
+      rc = -1;
+    }
+    breg[i + 1] = breg[i] + (unsigned)((npair + 127) / 128);
+    bsing[i + 1] = bsing[i] + (unsigned)nr;
+    brows[i + 1] = brows[i] + (unsigned)((nr + 127) / 128);
+  }
+  AsmArgs* dit = nullptr;
+  unsigned* db = nullptr;
+  if (!rc && (cudaMallocAsync((void**)&dit, (size_t)n * sizeof(AsmArgs), st) != cudaSuccess ||
+              cudaMallocAsync((void**)&db, 3 * ((size_t)n + 1) * sizeof(unsigned), st) != cudaSuccess ||
+              cudaMemcpyAsync(dit, it.data(), (size_t)n * sizeof(AsmArgs), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+              cudaMemcpyAsync(db, breg.data(), ((size_t)n + 1) * sizeof(unsigned), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+              cudaMemcpyAsync(db + n + 1, bsing.data(), ((size_t)n + 1) * sizeof(unsigned), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+              cudaMemcpyAsync(db + 2 * (n + 1), brows.data(), ((size_t)n + 1) * sizeof(unsigned), cudaMemcpyHostToDevice, st) != cudaSuccess)) {
+    gbi_set_error("work-list assembly: upload");
+    rc = -1;
+  }
+  if (!rc) {
+    const bool df = precision >= 2 && type == 2;
+    if (df) {
+      k_asm_regular_df_list<<<breg[n], 128, 0, st>>>(dit, db, n);
+      gbi_count_launch();
+    }
+    k_asm_regular_list<<<breg[n], 128, 0, st>>>(dit, db, n, df ? 1 : 0);
+    gbi_count_launch();
+    if (precision >= 2) k_asm_singular_list<true><<<bsing[n], 256, 0, st>>>(dit, db + n + 1, n);
+    else k_asm_singular_list<false><<<bsing[n], 256, 0, st>>>(dit, db + n + 1, n);
+    gbi_count_launch();
+    k_asm_rows_list<<<brows[n], 128, 0, st>>>(dit, db + 2 * (n + 1), n);
+    gbi_count_launch();
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) { gbi_set_error("work-list assembly launch: %s", cudaGetErrorString(e)); rc = -1; }
+  }
+  if (dit) cudaFreeAsync(dit, st);
+  if (db) cudaFreeAsync(db, st);
+  for (void* t : tmp) cudaFreeAsync(t, st);
+  const cudaError_t e = cudaStreamSynchronize(st);  // the host arrays above are read by the copies
+  if (!rc && e != cudaSuccess) { gbi_set_error("work-list assembly: %s", cudaGetErrorString(e)); rc = -1; }
+  return rc;
 }
 
 // precision 0: FP64 throughout (the reference's arithmetic); 1: regular pairs

@@ -25,6 +25,16 @@ typedef struct GbMeshDev {
   double kn[2 * GB_MAXDOM];
 } GbMeshDev;
 
+// one item of a work-list assembly: rows row0 .. row0 + nrow - 1 of domain did
+// of the object with mesh m, into the given outputs (nrow rows each)
+struct cplx;
+typedef struct GbAsmItem {
+  const GbMeshDev* m;
+  int did, row0, nrow;
+  struct cplx *G, *H, *dG, *dH;
+  double* dF;
+} GbAsmItem;
+
 #ifdef __cplusplus
 extern "C" {
 #endif

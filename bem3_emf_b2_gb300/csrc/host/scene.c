@@ -126,22 +126,20 @@ MOBJ *gbh_mscene_open(int n,const char *const *medium_files,const char *const *m
 static double g_phase[4];
 static double gbh_now(void){ struct timespec t; clock_gettime(CLOCK_MONOTONIC,&t); return t.tv_sec+1e-9*t.tv_nsec; }
 
-/* assembly and factorisation of one object (its own gb_obj and stream), run
- * for all objects at once from one host thread each: the objects are
- * independent until the multiple-scattering iteration, and one object's
- * quadrature fills the SMs that another's LU panel chain leaves idle */
-struct mscene_job { gb_obj *o; int MN,form,type,dev,rc; double ta,tf; char err[256]; };
+/* factorisation of one object (its own gb_obj and streams), run for all
+ * objects at once from one host thread each: the objects are independent
+ * until the multiple-scattering iteration, and their LU panel chains leave
+ * most SMs idle one by one */
+struct mscene_job { gb_obj *o; int MN,form,type,dev,rc; double tf; char err[256]; };
 
 static void *mscene_worker(void *p)
 {
   struct mscene_job *j=(struct mscene_job *)p;
   if(gb_use_device(j->dev)){ j->rc=-1; snprintf(j->err,sizeof(j->err),"%s",gb_last_error()); return NULL; }
-  double t1=gbh_now();
-  if(gb_assemble_all(j->o,j->type,gb_form_precision(j->form))) j->rc=-1;
   double t2=gbh_now();
-  if(!j->rc && (j->form==0 ? gb_factor_fp64(j->o) : gb_factor_mixed(j->o))) j->rc=-1;
+  if(j->form==0 ? gb_factor_fp64(j->o) : gb_factor_mixed(j->o)) j->rc=-1;
   if(j->rc) snprintf(j->err,sizeof(j->err),"%s",gb_last_error());
-  j->ta=t2-t1; j->tf=gbh_now()-t2;
+  j->tf=gbh_now()-t2;
   return NULL;
 }
 
@@ -150,11 +148,19 @@ int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double
   double t0=gbh_now(),ta=0.0,tf=0.0;
   struct mscene_job *jobs=(struct mscene_job *)calloc(mo->N,sizeof(struct mscene_job));
   pthread_t *th=(pthread_t *)calloc(mo->N,sizeof(pthread_t));
+  gb_obj **objs=(gb_obj **)calloc(mo->N,sizeof(gb_obj *));
   int dev=gb_current_device();
   for(int m=0;m<mo->N;m++){  /* device copies first (host tables, sequential) */
-    jobs[m].o=gb_dev(&mo->md[m]);
+    jobs[m].o=objs[m]=gb_dev(&mo->md[m]);
     jobs[m].MN=mo->md[m].MN; jobs[m].form=form; jobs[m].type=type; jobs[m].dev=dev;
   }
+  /* every domain of every object: one launch per assembly phase */
+  double ta0=gbh_now();
+  if(gb_assemble_objects(objs,mo->N,type,gb_form_precision(form))){
+    printf("gbh_mscene_step: %s\n",gb_last_error()); free(jobs); free(th); free(objs); return -1;
+  }
+  ta=gbh_now()-ta0;
+  free(objs);
   double tw=gbh_now();
   for(int m=0;m<mo->N;m++)
     if(pthread_create(&th[m],NULL,mscene_worker,&jobs[m])){ jobs[m].rc=-2; }
@@ -163,13 +169,11 @@ int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double
     if(jobs[m].rc!=-2) pthread_join(th[m],NULL);
     else { jobs[m].rc=0; mscene_worker(&jobs[m]); }  /* no thread available: run here */
     if(jobs[m].rc && bad<0) bad=m;
-    ta+=jobs[m].ta; tf+=jobs[m].tf;
   }
   double tw2=gbh_now();
   if(bad>=0){ printf("gbh_mscene_step: %s\n",jobs[bad].err); free(jobs); free(th); return -1; }
   free(jobs); free(th);
-  /* the two phases overlap across objects: report their shares of the wall time */
-  if(ta+tf>0.0){ double w=tw2-tw; double sa=ta/(ta+tf); ta=w*sa; tf=w-ta; }
+  tf=tw2-tw;
   /* matrices and the factors are resident: the iteration reads no .cmat file */
   for(int m=0;m<mo->N;m++) gb_dev_set_flags(&mo->md[m],GB_F_CMAT|GB_F_INV,GB_F_BV);
   double t3=gbh_now();

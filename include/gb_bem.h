@@ -104,6 +104,10 @@ int gb_assemble2(gb_obj *o, int did, int type, int precision);
  * object's stream (gb_obj_stream); its small scratch is stream-ordered. */
 int gb_assemble_rows(gb_obj *o, int did, int row0, int nrow, int type, int precision, void *G, void *H, void *dG,
                      void *dH, double *dF);
+/* every domain of every object of a scene (objects of uneven sizes, on the
+ * current device), as gb_assemble2, with one launch per phase over a work
+ * list of (object, domain) items instead of a launch sequence per domain */
+int gb_assemble_objects(gb_obj **objs, int n, int type, int precision);
 /* every domain of the object, as gb_assemble2, the domains at once (one host
  * thread and stream each) */
 int gb_assemble_all(gb_obj *o, int type, int precision);

@@ -103,3 +103,49 @@ def test_cube_rows_match_oracle(gb_build, tmp_path):
                 err = formats.rel_fro(a, b)
                 assert err <= 1e-10, "precision %d domain %d %s: %g" % (prec, d, name, err)
     sc.close()
+
+
+@pytest.mark.gpu
+def test_work_list_assembly_matches_per_domain(gb_build, tmp_path):
+    """gb_assemble_objects (every domain of several objects of uneven size in
+    one launch per phase) gives bit for bit the matrices of gb_assemble2 per
+    domain, FP64 and the chosen form's precision."""
+    from bem3_emf_b2_gb300 import Scene
+    L = _lib()
+    vp, ci = ctypes.c_void_p, ctypes.c_int
+    L.gb_assemble_objects.argtypes = [vp, ci, ci, ci]
+    L.gb_assemble_objects.restype = ci
+    L.gb_cmatrix_download.argtypes = [vp, ci, vp, vp, vp, vp, vp]
+    scenes, metas = [], []
+    for case in ("sphere2", "cone_mix", "cone_tri"):
+        meta, _ = load_case(case)
+        wd = os.path.join(str(tmp_path), case)
+        os.makedirs(wd)
+        write_inputs(meta, wd)
+        scenes.append(Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt")))
+        metas.append(meta)
+    objs = (ctypes.c_void_p * len(scenes))(*[s.obj() for s in scenes])
+
+    def download(o, meta):
+        out = []
+        for d, ne in enumerate(meta["sb_Ne"]):
+            N = 4 * ne
+            m = [np.zeros((N, N), complex), np.zeros((N, N), complex), np.zeros((2 * N, N), complex),
+                 np.zeros((2 * N, N), complex), np.zeros((N, 3))]
+            assert L.gb_cmatrix_download(o, d, *[x.ctypes.data for x in m]) == 0
+            out.append(m)
+        return out
+    for prec in (0, 3):
+        ref = []
+        for sc, meta in zip(scenes, metas):
+            for d in range(len(meta["sb_Ne"])):
+                assert L.gb_assemble2(sc.obj(), d, 2, prec) == 0, L.gb_last_error()
+            ref.append(download(sc.obj(), meta))
+        assert L.gb_assemble_objects(ctypes.cast(objs, vp), len(scenes), 2, prec) == 0, L.gb_last_error()
+        for sc, meta, r in zip(scenes, metas, ref):
+            got = download(sc.obj(), meta)
+            for d in range(len(r)):
+                for a, b in zip(got[d], r[d]):
+                    assert np.array_equal(a, b), (meta["case"], prec, d)
+    for sc in scenes:
+        sc.close()
