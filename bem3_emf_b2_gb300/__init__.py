@@ -189,6 +189,28 @@ class MultiScene:
             raise RuntimeError("gbh_mscene_step failed: %s" % last_error())
         return F.reshape(self.n, 3), N.reshape(self.n, 3)
 
+    def beams(self, beams_file, form=1, type_=2, rc=None):
+        """every plane wave of beams_file as its own incident field
+        (gbh_mscene_beams): force, torque [nbeam][n][3]"""
+        import numpy as np
+        L = lib()
+        vp, ci = ctypes.c_void_p, ctypes.c_int
+        L.gbh_mscene_beams.argtypes = [vp, ci, ci, ctypes.c_char_p, vp, vp, vp, vp]
+        L.gbh_mscene_beams.restype = ci
+        with open(beams_file) as f:
+            nmax = int([l for l in f.read().splitlines() if l.strip() and not l.startswith("#")][0].split()[0])
+        F = np.zeros((nmax, self.n, 3))
+        N = np.zeros((nmax, self.n, 3))
+        nb = ctypes.c_int(0)
+        rcp = None
+        if rc is not None:
+            rca = np.ascontiguousarray(rc, float).reshape(-1)
+            rcp = rca.ctypes.data
+        if L.gbh_mscene_beams(self.h, form, type_, beams_file.encode(), rcp, F.ctypes.data, N.ctypes.data,
+                              ctypes.byref(nb)) != 0:
+            raise RuntimeError("gbh_mscene_beams failed: %s" % last_error())
+        return F[:nb.value], N[:nb.value]
+
     def phase_times(self):
         """(assembly, factorisation, iteration + E/H, force) seconds of the last step"""
         import numpy as np

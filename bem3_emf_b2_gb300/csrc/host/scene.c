@@ -143,9 +143,11 @@ static void *mscene_worker(void *p)
   return NULL;
 }
 
-int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double *N)
+/* assembly of every object (one work list) and the objects' factorisations
+ * (concurrently); *ta, *tf: their wall times */
+static int mscene_factor(MOBJ *mo,int form,int type,double *ta_out,double *tf_out)
 {
-  double t0=gbh_now(),ta=0.0,tf=0.0;
+  double ta=0.0,tf=0.0;
   struct mscene_job *jobs=(struct mscene_job *)calloc(mo->N,sizeof(struct mscene_job));
   pthread_t *th=(pthread_t *)calloc(mo->N,sizeof(pthread_t));
   gb_obj **objs=(gb_obj **)calloc(mo->N,sizeof(gb_obj *));
@@ -176,6 +178,14 @@ int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double
   tf=tw2-tw;
   /* matrices and the factors are resident: the iteration reads no .cmat file */
   for(int m=0;m<mo->N;m++) gb_dev_set_flags(&mo->md[m],GB_F_CMAT|GB_F_INV,GB_F_BV);
+  *ta_out=ta; *tf_out=tf;
+  return 0;
+}
+
+int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double *N)
+{
+  double ta=0.0,tf=0.0;
+  if(mscene_factor(mo,form,type,&ta,&tf)) return -1;
   double t3=gbh_now();
   mo_solve_bv(mo);
   double t4=gbh_now();
@@ -185,8 +195,64 @@ int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double
     if(mo_force_FN(F+3*m,N+3*m,c,m,0,mo)<0) return -1;
   }
   g_phase[0]=ta; g_phase[1]=tf; g_phase[2]=t4-t3; g_phase[3]=gbh_now()-t4;
-  (void)t0;
   return 0;
+}
+
+/* Many incident beams as right-hand sides of one scene (the reference sums
+ * every wave of ipw.txt into one field, multi_fbeam.c:817-833, so beam b
+ * alone is what a reference run with an ipw.txt holding only wave b
+ * computes).  The coefficient matrices, the factors and the
+ * multiple-scattering operators do not depend on the beam: they are built
+ * once -- assembly (one work list over every domain of every object),
+ * factorisations, and the cross operators (by the first beam's iteration,
+ * then kept) -- and each beam costs its incident potential, the iteration,
+ * E/H and the force.  Beam b is wave b of beams_file (ipw.txt layout); its
+ * force and torque on object m about rc[3m..] (NULL: the object's
+ * translation point) go to F, N [b][m][3]; *nbeam the number of waves read.
+ * The phases' wall times are those of gbh_mscene_phase_times, the iteration
+ * and force summed over the beams. */
+int gbh_mscene_beams(MOBJ *mo,int form,int type,const char *beams_file,const double *rc,double *F,double *N,
+                     int *nbeam)
+{
+  Bobj all;
+  memset(&all,0,sizeof(all));
+  init_mfb(&all);
+  int nb=read_data_mfb_ipw((char *)beams_file,&all);
+  if(nb<=0){ printf("gbh_mscene_beams: no plane wave in %s\n",beams_file); return -1; }
+  setup_mfb(&all);
+  *nbeam=nb;
+  double ta=0.0,tf=0.0;
+  if(mscene_factor(mo,form,type,&ta,&tf)){ free_mfb(&all); return -1; }
+  double tit=0.0,tfo=0.0;
+  Ipw **keep=(Ipw **)calloc(mo->N,sizeof(Ipw *));
+  int *keepn=(int *)calloc(mo->N,sizeof(int));
+  for(int m=0;m<mo->N;m++){ keep[m]=mo->md[m].mw.bd.ipw; keepn[m]=mo->md[m].mw.n_ipw; }
+  int rcode=0;
+  for(int b=0;b<nb && !rcode;b++){
+    for(int m=0;m<mo->N;m++){  /* this beam alone, as the objects' incident field */
+      DOMD *md=&mo->md[m];
+      md->mw.n_ipw=1;
+      md->mw.bd.ipw=all.bd.ipw+b;
+      gb_init_boundary_data_u2(md);
+      gb_dev_set_flags(md,0,GB_F_INC|GB_F_BV);
+    }
+    double t3=gbh_now();
+    mo_solve_bv(mo);
+    double t4=gbh_now();
+    for(int m=0;m<mo->N && !rcode;m++){
+      double c[3];
+      for(int i=0;i<3;i++) c[i]=rc?rc[3*m+i]:mo->md[m].tv[i];
+      if(mo_force_FN(F+3*((size_t)b*mo->N+m),N+3*((size_t)b*mo->N+m),c,m,0,mo)<0) rcode=-1;
+    }
+    tit+=t4-t3; tfo+=gbh_now()-t4;
+  }
+  for(int m=0;m<mo->N;m++){ mo->md[m].mw.bd.ipw=keep[m]; mo->md[m].mw.n_ipw=keepn[m]; }
+  /* the objects' own incident field again (their beams were replaced above) */
+  for(int m=0;m<mo->N;m++){ gb_init_boundary_data_u2(&mo->md[m]); gb_dev_set_flags(&mo->md[m],0,GB_F_INC|GB_F_BV); }
+  free(keep); free(keepn);
+  free_mfb(&all);
+  g_phase[0]=ta; g_phase[1]=tf; g_phase[2]=tit; g_phase[3]=tfo;
+  return rcode;
 }
 
 void gbh_mscene_phase_times(double *t){ for(int i=0;i<4;i++) t[i]=g_phase[i]; }

@@ -216,6 +216,59 @@ def cone_mixed(nth, nr, radius=0.5, height=1.0):
     return nodes, _orient(nodes, elems, np.array([0.0, 0.0, height / 4.0]))
 
 
+def batch_scene(seed, n_obj, box=20.0, size=(0.3, 1.5), elems=(200, 6000), n_range=(1.33, 2.0)):
+    """Seeded multi-object scene: n_obj non-overlapping spheres, cubes and
+    cones in a cube of side box centred at the origin, characteristic size
+    uniform in size, element count uniform in elems (the nearest the
+    generators allow), real refractive index uniform in n_range, random
+    orientation.  Returns a list of dicts: kind, nodes (already rotated and
+    placed), elems, n, centre, radius (bounding)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    kinds = ("sphere", "cube", "cone")
+    tries = 0
+    while len(out) < n_obj:
+        tries += 1
+        if tries > 10000:
+            raise RuntimeError("batch_scene: the objects do not fit in the box")
+        kind = kinds[rng.integers(3)]
+        s = rng.uniform(*size)
+        ne = rng.uniform(*elems)
+        if kind == "sphere":
+            k = max(2, int(round(math.sqrt(ne / 6.0))))
+            nodes, el = cubed_sphere(k, 0.5 * s)
+            rad = 0.5 * s
+        elif kind == "cube":
+            k = max(2, int(round(math.sqrt(ne / 6.0))))
+            nodes, el = cube(k, s)
+            rad = 0.5 * math.sqrt(3.0) * s
+        else:
+            k = max(2, int(round(math.sqrt(ne / 12.0))))
+            nodes, el = cone_tri(k, 0.5 * s, s, jitter=0.05, seed=int(rng.integers(1 << 30)))
+            nodes = nodes - np.array([0.0, 0.0, 0.25 * s])
+            rad = math.sqrt((0.5 * s) ** 2 + (0.75 * s) ** 2)
+        axis = rng.normal(size=3)
+        nodes = transform(nodes, axis / np.linalg.norm(axis), rng.uniform(0.0, 2.0 * math.pi))
+        c = rng.uniform(-0.5 * box + rad, 0.5 * box - rad, 3)
+        if any(np.linalg.norm(c - o["centre"]) < 1.05 * (rad + o["radius"]) for o in out):
+            continue
+        out.append(dict(kind=kind, nodes=nodes + c, elems=el, n=float(rng.uniform(*n_range)), centre=c, radius=rad))
+    return out
+
+
+def random_waves(seed, n, lambda0=1.0, ni=1.33, power=1.0):
+    """n plane waves with directions uniform on the sphere and uniformly
+    random linear polarisation angles (ipw.txt parameters)"""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        th = math.acos(1.0 - 2.0 * rng.uniform())
+        ph = rng.uniform(0.0, 2.0 * math.pi)
+        psi = rng.uniform(0.0, math.pi)
+        out.append(dict(lambda0=lambda0, ni=ni, power=power, e0x=math.cos(psi), e0y=math.sin(psi), theta=th, phi=ph))
+    return out
+
+
 def transform(nodes, axis=(1.0, 0.0, 0.0), angle=0.0, shift=(0.0, 0.0, 0.0)):
     """Rodrigues rotation then translation (the reference's convention)."""
     a = np.asarray(axis, float)

@@ -91,7 +91,21 @@ CONE_TV = np.array([[0.0, 0.0, 0.0], [1.5, 0.0, 0.0]])
 
 def open_workload(args, wd):
     """(scene, description dict) of the chosen workload, set up from its input files"""
-    from bem3_emf_b2_gb300 import MultiScene, Scene
+    from bem3_emf_b2_gb300 import MultiScene, Scene, meshgen
+    if args.workload == "beams":
+        objs = meshgen.batch_scene(BATCH["seed"], BATCH["n_obj"], box=BATCH["box"], elems=BATCH["elems"])
+        med, msh = [], []
+        for i, o in enumerate(objs):
+            meshgen.write_mesh(os.path.join(wd, "o%d.msh" % i), o["nodes"], o["elems"])
+            meshgen.write_medium(os.path.join(wd, "m%d.txt" % i), [o["n"]])
+            med.append(os.path.join(wd, "m%d.txt" % i))
+            msh.append(os.path.join(wd, "o%d.msh" % i))
+        meshgen.write_ipw(os.path.join(wd, "beams.txt"), meshgen.random_waves(BATCH["seed"], BATCH["n_beam"]))
+        sc = MultiScene(med, msh, os.path.join(wd, "beams.txt"))
+        ne = [len(o["elems"]) for o in objs]
+        return _Beams(sc, os.path.join(wd, "beams.txt")), dict(
+            workload=BATCH["name"], objects=len(objs), elements_per_object=ne, beams=BATCH["n_beam"],
+            na_per_object=[8 * (3 if o["kind"] == "cone" else 4) * len(o["elems"]) for o in objs])
     if args.workload == "cones":
         ne = write_cones(wd, args.cone_m)
         med = [os.path.join(wd, "medium.txt")] * 2
@@ -105,6 +119,25 @@ def open_workload(args, wd):
     name = SPHERE["name"] if args.faces == 8 else "sphere r=1, cubed %dx%d quads/face (%d elements)" % (
         args.faces, args.faces, ne)
     return sc, dict(workload=name, objects=1, elements_per_object=ne, na_per_object=8 * 4 * ne)
+
+
+BATCH = dict(name="seeded multi-object scene (seed 11): 8 spheres, cubes and cones in a 20^3 box, characteristic size "
+                  "U[0.3, 1.5], element counts U[200, 600], n U[1.33, 2.0] in 1.33, random orientation; 32 plane "
+                  "waves of random direction and linear polarisation, each its own right-hand side",
+             seed=11, n_obj=8, n_beam=32, box=20.0, elems=(200, 600))
+
+
+class _Beams:
+    """a multi-object scene whose step solves every beam (gbh_mscene_beams)"""
+
+    def __init__(self, sc, beams_file):
+        self.sc, self.beams_file = sc, beams_file
+
+    def step(self, form=1):
+        return self.sc.beams(self.beams_file, form=form)
+
+    def __getattr__(self, k):
+        return getattr(self.sc, k)
 
 
 def force_vec(F, N):
@@ -307,7 +340,7 @@ def run_gpu(args):
     L = lib()
     wd = tempfile.mkdtemp(prefix="bench_")
     sc, desc = open_workload(args, wd)
-    cones = args.workload == "cones"
+    cones = args.workload in ("cones", "beams")
 
     # chosen form: warm-up, then exactly K timed steps (launch count over them)
     for _ in range(args.warmup):
@@ -338,7 +371,7 @@ def run_gpu(args):
     # far field of the solved scene on the 91 x 180 angular grid at r = 2000
     # lambda0 (reference example4.c:32-66) through the batched field map
     far = None
-    if cones:
+    if args.workload == "cones":
         th = np.linspace(0.0, np.pi, 91)
         ph = np.arange(180) * (2.0 * np.pi / 180)
         T, P = np.meshgrid(th, ph, indexing="ij")
@@ -364,19 +397,21 @@ def run_gpu(args):
     out = None
     if rank == 0:
         roof = roofline_live(kt, t_instr, 1)
-        cpu = cpu_baseline(args, wd, iters[0] if iters else 11) if (ws == 1 and not args.no_cpu) else None
+        cpu = cpu_baseline(args, wd, iters[0] if iters else 11) if (ws == 1 and not args.no_cpu and
+                                                                    args.workload != "beams") else None
         cfg = {"workload": desc["workload"], "objects": desc["objects"],
                "elements_per_object": desc["elements_per_object"], "na_per_object": desc["na_per_object"],
                "form": "chosen (double-float quadrature, FP32 block elimination + FP64 refinement)",
                "parallelism": "replicas x%d" % ws,
                "l2": "working set larger than L2 (coefficient matrices %s) and a 256 MB L2 flush before each step" % (
-                   "2 x 29 GB" if cones else "0.45 GB"),
+                   {"cones": "2 x 29 GB", "beams": "8 x 0.1-0.4 GB"}.get(args.workload, "0.45 GB")),
                "timing": "CUDA events on the current stream with a device-wide synchronise on both sides of each step"}
         out = {"metric": METRIC, "value": value, "unit": "s/scene", "n_gpus": ws, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": 1000.0 * tmax / args.steps, "higher_is_better": False,
                "scaling": "weak", "vs_baseline": None, "vs_baseline_note": VS_BASELINE_NOTE,
                "dtype": "double-float (f32 pairs) quadrature, c64 block LU + c128 refinement",
-               "data": "synthetic (meshgen %s)" % ("cones, seed 7" if cones else "cubed sphere, seeded by construction"),
+               "data": "synthetic (meshgen %s)" % {"cones": "cones, seed 7", "beams": "batch_scene seed 11, random_waves seed 11"}.get(
+                   args.workload, "cubed sphere, seeded by construction"),
                "config": cfg,
                "fp64_form": {"s_per_scene": sum(t64) / len(t64), "steps": len(t64),
                              "force_torque_rel_diff_vs_chosen": force_err,
@@ -476,6 +511,9 @@ def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return None
+    if args.workload in ("beams", "cube"):
+        return {"impl": "reference", "unavailable": "the CPU restatement of the path has no multi-object iteration "
+                "or row-block assembly timing for this workload"}
     wd = tempfile.mkdtemp(prefix="bench_ref_")
     if args.workload == "cones":
         write_cones(wd, args.cone_m)
@@ -597,7 +635,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--profile-step", action="store_true",
                     help="profiling run: one chosen-form scene step after --warmup steps, nothing else, no JSON line")
-    ap.add_argument("--workload", choices=["cones", "sphere", "cube"], default="cones",
+    ap.add_argument("--workload", choices=["cones", "sphere", "cube", "beams"], default="cones",
                     help="cones: the two-cone scene (default); sphere: the 384-element sphere; cube: assembly "
                          "throughput of the 38,400-element cube")
     ap.add_argument("--cube-n", type=int, default=None, help="quadrangles per cube edge (cube workload)")

@@ -48,6 +48,15 @@ MOBJ *gbh_mscene_open(int n, const char *const *medium_files, const char *const 
  * force and torque of each object (type-0 surface rule) about rc[3m..3m+2]
  * (rc NULL: the object's translation point); F, N: 3 n */
 int gbh_mscene_step(MOBJ *mo, int form, int type, const double *rc, double *F, double *N);
+/* Many incident beams as right-hand sides: beam b is wave b of beams_file
+ * (ipw.txt layout) on its own -- what a reference run with an ipw.txt that
+ * holds only that wave computes (the reference sums all waves of ipw.txt
+ * into one field, multi_fbeam.c:817-833).  Assembly, factorisations and the
+ * multiple-scattering operators are built once for all beams; each beam
+ * then takes the iteration, E/H and force and torque of every object,
+ * F, N [nbeam][n][3] (rc as in gbh_mscene_step).  *nbeam: waves read. */
+int gbh_mscene_beams(MOBJ *mo, int form, int type, const char *beams_file, const double *rc, double *F, double *N,
+                     int *nbeam);
 void gbh_mscene_drop_device(MOBJ *mo);
 size_t gbh_mscene_h2d_bytes(MOBJ *mo);
 size_t gbh_mscene_d2h_bytes(MOBJ *mo);
