@@ -127,77 +127,6 @@ __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[
 }
 
 
-template <int NDIR>
-__device__ __forceinline__ void reg_point_dn(const PairDN<NDIR>& P, bool quad, df z, df e, df w, AccDN<NDIR>& A) {
-  df d[3], R[3], W[3];
-  const df ze = df_mul(z, e);
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    d[i] = df_fma(df_fma(df_mul(P.c1[i], z), P.c2[i], e), P.c3[i], ze);
-    R[i] = df_add(P.R0[i], d[i]);
-    W[i] = df_fma(df_fma(P.w0[i], P.w1[i], z), P.w2[i], e);
-  }
-  df N[4];
-  if (quad) {
-    const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // 1 / GB_P44_N = sqrt(3)
-    const df za = df_mul(z, ia), ea = df_mul(e, ia);
-    const df zm = df_add_f(df_neg(za), 1.0f), zp = df_add_f(za, 1.0f);
-    const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
-    N[0] = df_mul_f(df_mul(zm, em), 0.25f);
-    N[1] = df_mul_f(df_mul(zp, em), 0.25f);
-    N[2] = df_mul_f(df_mul(zp, ep), 0.25f);
-    N[3] = df_mul_f(df_mul(zm, ep), 0.25f);
-  } else {  // 3 x the shape functions (0.5 / GB_P34_N0 = 2.5 exactly); the 1/3 is applied in FP64
-    const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
-    const df se = df_mul(s3, e);
-    N[0] = df_add_f(df_mul_f(df_add(z, se), -2.5f), 1.0f);
-    N[1] = df_add_f(df_mul_f(z, 5.0f), 1.0f);
-    N[2] = df_add_f(df_mul_f(df_sub(z, se), -2.5f), 1.0f);
-    N[3] = dfmk(0.0f, 0.0f);
-  }
-  reg_kernel_dn<NDIR>(P, R, W, N, w, A);
-}
-
-// quadrangle, one row z of the tensor rule: the point's geometry is affine in
-// e with row constants R = aR + bR e (aR = R0 + c1 z, bR = c2 + c3 z),
-// W = aW + w2 e (aW = w0 + w1 z), and the shape functions factor into row
-// factors zm/4, zp/4 and (1 -+ sqrt(3) e)
-struct RowQ {
-  df aR[3], bR[3], aW[3];
-  df zm4, zp4;
-};
-template <int NDIR>
-__device__ __forceinline__ void reg_rowq_dn(const PairDN<NDIR>& P, df z, RowQ& Q) {
-  const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // 1 / GB_P44_N = sqrt(3)
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    Q.aR[i] = df_fma(P.R0[i], P.c1[i], z);
-    Q.bR[i] = df_fma(P.c2[i], P.c3[i], z);
-    Q.aW[i] = df_fma(P.w0[i], P.w1[i], z);
-  }
-  const df za = df_mul(z, ia);
-  Q.zm4 = df_mul_f(df_add_f(df_neg(za), 1.0f), 0.25f);
-  Q.zp4 = df_mul_f(df_add_f(za, 1.0f), 0.25f);
-}
-template <int NDIR>
-__device__ __forceinline__ void reg_point_dnq(const PairDN<NDIR>& P, const RowQ& Q, df e, df w, AccDN<NDIR>& A) {
-  df R[3], W[3];
-#pragma unroll
-  for (int i = 0; i < 3; i++) {
-    R[i] = df_fma(Q.aR[i], Q.bR[i], e);
-    W[i] = df_fma(Q.aW[i], P.w2[i], e);
-  }
-  const df ia = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
-  const df ea = df_mul(e, ia);
-  const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
-  df N[4];
-  N[0] = df_mul(Q.zm4, em);
-  N[1] = df_mul(Q.zp4, em);
-  N[2] = df_mul(Q.zp4, ep);
-  N[3] = df_mul(Q.zm4, ep);
-  reg_kernel_dn<NDIR>(P, R, W, N, w, A);
-}
-
 // Points per direction of the regular rule of a pair in the adaptive form.
 // With a = |c1| + |c2| (+ |c3| for a quadrangle) the size of the source
 // element's parameter map and D = |R0| / a the distance of the observation
@@ -263,39 +192,61 @@ __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double
   A.F = zero;
 #pragma unroll
   for (int q = 0; q < GB_ND(NDIR); q++) A.dF[q] = zero;
-  double S0;
-  if (S.quad) {
-    S0 = GB_I_FP;
-    for (int i = 0; i < nq; i++) {
-      const df x = dfmk(c_tabd.xn[off + i].x, c_tabd.xn[off + i].y), wx = dfmk(c_tabd.wn[off + i].x, c_tabd.wn[off + i].y);
-      RowQ Q;
-      reg_rowq_dn<NDIR>(P, x, Q);
-      for (int j = 0; j < nq; j++) {
-        const df y = dfmk(c_tabd.xn[off + j].x, c_tabd.xn[off + j].y), wy = dfmk(c_tabd.wn[off + j].x, c_tabd.wn[off + j].y);
-        reg_point_dnq<NDIR>(P, Q, y, df_mul(wx, wy), A);
+  const double S0 = S.quad ? GB_I_FP : 0.0625 * GB_SQ3 * GB_I_SPSQ3;
+  // one loop over every point of the rule -- an n x n tensor rule on a
+  // quadrangle, the same on each of the three sub-quadrangles of a triangle
+  // (the reference's maps) -- so that the integrand is inlined at one site
+  // (the kernel is instruction-fetch bound otherwise)
+  const int npts = (S.quad ? 1 : 3) * nq * nq;
+  const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // sqrt(3)
+#pragma unroll 1
+  for (int q = 0; q < npts; q++) {
+    int sub = 0, ij = q;
+    if (!S.quad) { sub = q % 3; ij = q / 3; }
+    const int i = ij / nq, j = ij - i * nq;
+    const df x = dfmk(c_tabd.xn[off + i].x, c_tabd.xn[off + i].y), wx = dfmk(c_tabd.wn[off + i].x, c_tabd.wn[off + i].y);
+    const df y = dfmk(c_tabd.xn[off + j].x, c_tabd.xn[off + j].y), wy = dfmk(c_tabd.wn[off + j].x, c_tabd.wn[off + j].y);
+    df z, e, w, N[4];
+    if (S.quad) {
+      z = x;
+      e = y;
+      w = df_mul(wx, wy);
+      const df za = df_mul(z, s3), ea = df_mul(e, s3);  // 1 / GB_P44_N = sqrt(3)
+      const df zm = df_add_f(df_neg(za), 1.0f), zp = df_add_f(za, 1.0f);
+      const df em = df_add_f(df_neg(ea), 1.0f), ep = df_add_f(ea, 1.0f);
+      N[0] = df_mul_f(df_mul(zm, em), 0.25f);
+      N[1] = df_mul_f(df_mul(zp, em), 0.25f);
+      N[2] = df_mul_f(df_mul(zp, ep), 0.25f);
+      N[3] = df_mul_f(df_mul(zm, ep), 0.25f);
+    } else {
+      // w = wx wy (1 + x/4 + y/4); the three sub-quadrangle maps of the reference
+      w = df_mul(df_mul(wx, wy), df_add_f(df_mul_f(df_add(x, y), 0.25f), 1.0f));
+      const df xy = df_mul(x, y);
+      if (sub == 0) {
+        z = df_mul_f(df_add(df_add_f(df_mul_f(df_add(x, y), 2.0f), 3.0f), xy), 0.125f);
+        e = df_mul_f(df_mul(s3, df_sub(y, x)), 0.125f);
+      } else if (sub == 1) {
+        z = df_mul_f(df_sub(df_add_f(df_sub(x, df_mul_f(y, 5.0f)), -3.0f), xy), 0.0625f);
+        e = df_mul_f(df_mul(s3, df_add(df_add_f(df_add(df_mul_f(x, 3.0f), y), 3.0f), xy)), 0.0625f);
+      } else {
+        z = df_mul_f(df_sub(df_add_f(df_sub(y, df_mul_f(x, 5.0f)), -3.0f), xy), 0.0625f);
+        e = df_mul_f(df_mul(s3, df_sub(df_add_f(df_neg(df_add(x, df_mul_f(y, 3.0f))), -3.0f), xy)), 0.0625f);
       }
+      // 3 x the shape functions (0.5 / GB_P34_N0 = 2.5 exactly); the 1/3 is applied in FP64
+      const df se = df_mul(s3, e);
+      N[0] = df_add_f(df_mul_f(df_add(z, se), -2.5f), 1.0f);
+      N[1] = df_add_f(df_mul_f(z, 5.0f), 1.0f);
+      N[2] = df_add_f(df_mul_f(df_sub(z, se), -2.5f), 1.0f);
+      N[3] = dfmk(0.0f, 0.0f);
     }
-  } else {
-    S0 = 0.0625 * GB_SQ3 * GB_I_SPSQ3;
-    const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);
-    for (int i = 0; i < nq; i++) {
-      const df x = dfmk(c_tabd.xn[off + i].x, c_tabd.xn[off + i].y), wx = dfmk(c_tabd.wn[off + i].x, c_tabd.wn[off + i].y);
-      for (int j = 0; j < nq; j++) {
-        const df y = dfmk(c_tabd.xn[off + j].x, c_tabd.xn[off + j].y), wy = dfmk(c_tabd.wn[off + j].x, c_tabd.wn[off + j].y);
-        // w = wx wy (1 + x/4 + y/4); the three sub-quadrangle maps of the reference
-        const df w = df_mul(df_mul(wx, wy), df_add_f(df_mul_f(df_add(x, y), 0.25f), 1.0f));
-        const df xy = df_mul(x, y);
-        const df z1 = df_mul_f(df_add(df_add_f(df_mul_f(df_add(x, y), 2.0f), 3.0f), xy), 0.125f);
-        const df e1 = df_mul_f(df_mul(s3, df_sub(y, x)), 0.125f);
-        const df z2 = df_mul_f(df_sub(df_add_f(df_sub(x, df_mul_f(y, 5.0f)), -3.0f), xy), 0.0625f);
-        const df e2 = df_mul_f(df_mul(s3, df_add(df_add_f(df_add(df_mul_f(x, 3.0f), y), 3.0f), xy)), 0.0625f);
-        const df z3 = df_mul_f(df_sub(df_add_f(df_sub(y, df_mul_f(x, 5.0f)), -3.0f), xy), 0.0625f);
-        const df e3 = df_mul_f(df_mul(s3, df_sub(df_add_f(df_neg(df_add(x, df_mul_f(y, 3.0f))), -3.0f), xy)), 0.0625f);
-        reg_point_dn<NDIR>(P, false, z1, e1, w, A);
-        reg_point_dn<NDIR>(P, false, z2, e2, w, A);
-        reg_point_dn<NDIR>(P, false, z3, e3, w, A);
-      }
+    df R[3], W[3];
+    const df ze = df_mul(z, e);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      R[d] = df_add(P.R0[d], df_fma(df_fma(df_mul(P.c1[d], z), P.c2[d], e), P.c3[d], ze));
+      W[d] = df_fma(df_fma(P.w0[d], P.w1[d], z), P.w2[d], e);
     }
+    reg_kernel_dn<NDIR>(P, R, W, N, w, A);
   }
   const double sh = neg ? -S0 : S0;
   const double s3n = S.quad ? 1.0 : 1.0 / 3.0;
