@@ -556,13 +556,17 @@ static int trsm_rows(int upper, const T* L, size_t ldl, T* X, size_t ldx, int nb
   if (c1 <= c0) return 0;
   const size_t tri = upper ? (size_t)nb * (nb + 1) : (size_t)LU_NB * (LU_NB + 1);
   size_t sm = (tri + LU_NB + (size_t)LU_NB * (TRSM_COLS + 1)) * sizeof(T);
+  // the function attribute is process-wide and host threads factorise
+  // objects at once: it is always set to the largest request (nb = LU_NB),
+  // never to this call's, so that no thread lowers it under another's launch
+  const int sm_max = (int)(((size_t)LU_NB * (LU_NB + 1) + LU_NB + (size_t)LU_NB * (TRSM_COLS + 1)) * sizeof(T));
   unsigned nblk = (unsigned)((c1 - c0 + TRSM_COLS - 1) / TRSM_COLS);
   if (upper) {
-    GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_max));
     k_trsm_rows<T, 1><<<nblk, 256, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
     gbi_count_launch();
   } else {
-    GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+    GB_CUDA(cudaFuncSetAttribute(k_trsm_rows<T, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm_max));
     k_trsm_rows<T, 0><<<nblk, 256, sm, st>>>(L, ldl, X, ldx, nb, c0, c1);
     gbi_count_launch();
   }
