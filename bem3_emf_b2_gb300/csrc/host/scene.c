@@ -7,6 +7,8 @@
 #include "gb_host.h"
 #include "gb_scene.h"
 
+void gbi_set_error(const char *fmt, ...);
+
 /* host setup of one object in md (rotation th about rv, then translation tv,
  * as d3b2_create_matrix's optional arguments); 0 on success */
 static int gbh_setup_object(DOMD *md,const char *medium_file,const char *mesh_file,const char *ipw_file,
@@ -173,7 +175,11 @@ static int mscene_factor(MOBJ *mo,int form,int type,double *ta_out,double *tf_ou
     if(jobs[m].rc && bad<0) bad=m;
   }
   double tw2=gbh_now();
-  if(bad>=0){ printf("gbh_mscene_step: %s\n",jobs[bad].err); free(jobs); free(th); return -1; }
+  if(bad>=0){
+    printf("gbh_mscene_step: %s\n",jobs[bad].err);
+    gbi_set_error("%s",jobs[bad].err);  /* the worker's message, for this thread's gb_last_error() */
+    free(jobs); free(th); return -1;
+  }
   free(jobs); free(th);
   tf=tw2-tw;
   /* matrices and the factors are resident: the iteration reads no .cmat file */
