@@ -20,7 +20,7 @@ INCLUDE = os.path.join(ROOT, "include")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SRCS = ["gb_api.cu", "gb_assemble.cu", "gb_linalg.cu", "gb_tc.cu", "gb_field.cu", "gb_solve.cu", "gb_schur.cu", "gb_mlp.cu",
-           "gb_gmres.cu"]
+           "gb_gmres.cu", "gb_beam.cu"]
 LIB = os.path.join(BUILD, "libbem3gb.so")
 APPS = ["d3b2_create_matrix", "d3b2_bv_solver", "bem3_analysis"]
 

@@ -224,16 +224,26 @@ int gb_mo_EH_points(MOBJ *mo,int n,const double *rt,int type,int which,int memp,
     gb_obj *o=gb_ready(&mo->md[m]);
     if(gb_domain_id(o,n,rt,did+(size_t)m*n)) gb_die("field.c, gb_mo_EH_points()");
   }
+  /* the incident field where it is wanted, all such points in one call */
+  double *ip=(double *)m_alloc2((size_t)n*3,sizeof(double),"field.c ip");
+  int *ix=(int *)m_alloc2(n,sizeof(int),"field.c ix");
+  int ni=0;
   for(int p=0;p<n;p++){
     own[p]=-1;
     for(int m=0;m<mo->N;m++) if(did[(size_t)m*n+p]!=0){ own[p]=m; break; }
     for(int i=0;i<3;i++){ E[3*p+i]=0.0; H[3*p+i]=0.0; }
     if(which==2 || (which==1 && own[p]<0)){
-      double complex te[3],th[3];
-      calc_mfb_EH(te,th,(double *)rt+3*p,&mo->md[0].mw);
-      for(int i=0;i<3;i++){ E[3*p+i]=te[i]; H[3*p+i]=th[i]; }
+      for(int i=0;i<3;i++) ip[3*ni+i]=rt[3*p+i];
+      ix[ni++]=p;
     }
   }
+  if(ni>0){
+    double complex *ti=(double complex *)m_alloc2((size_t)6*ni,sizeof(double complex),"field.c ti");
+    calc_mfb_EH_points(&mo->md[0].mw,ni,ip,ti,ti+(size_t)3*ni);
+    for(int k=0;k<ni;k++) for(int i=0;i<3;i++){ E[3*ix[k]+i]=ti[3*k+i]; H[3*ix[k]+i]=ti[(size_t)3*ni+3*k+i]; }
+    free(ti);
+  }
+  free(ip); free(ix);
   if(which!=2){
     double *pr=(double *)m_alloc2((size_t)n*3,sizeof(double),"field.c pr");
     int *pd=(int *)m_alloc2(n,sizeof(int),"field.c pd");

@@ -123,11 +123,12 @@ static void gb_point_fields(gb_pts *p,int oid,MOBJ *mo)
     if(gb_field_points(om,1,PREC_DEF,n,fr,NULL,did,buf,NULL)) gb_die("force.c, EH_s()");
     for(int k=0;k<n;k++) for(int j=0;j<3;j++){ p->E[3*k+j]+=buf[6*k+j]; p->H[3*k+j]+=buf[6*k+3+j]; }
   }
-  /* incident wave */
-  for(int k=0;k<n;k++){
-    double complex te[3],th[3];
-    calc_mfb_EH(te,th,fr+3*k,&mo->md[0].mw);
-    for(int j=0;j<3;j++){ p->E[3*k+j]+=te[j]; p->H[3*k+j]+=th[j]; }
+  /* incident field, all points in one call */
+  {
+    double complex *ti=(double complex *)m_alloc2((size_t)6*n+6,sizeof(double complex),"force.c");
+    calc_mfb_EH_points(&mo->md[0].mw,n,fr,ti,ti+(size_t)3*n);
+    for(int k=0;k<n;k++) for(int j=0;j<3;j++){ p->E[3*k+j]+=ti[3*k+j]; p->H[3*k+j]+=ti[(size_t)3*n+3*k+j]; }
+    free(ti);
   }
   free(buf); free(did); free(bt); free(bdid); free(bz); free(bo); free(fr);
 }

@@ -147,8 +147,7 @@ static void gb_dat_write2(char *fname,DOMD *md)
   gb_fwrite(&md->MN,sizeof(int),1,fp,fname);
   gb_fwrite(md->n,sizeof(double complex),md->MN+1,fp,fname);
   gb_fwrite(md->kn,sizeof(double complex),md->MN+1,fp,fname);
-  gb_fwrite(&md->mw,sizeof(Bobj),1,fp,fname);
-  gb_fwrite(md->mw.bd.ipw,sizeof(Ipw),md->mw.n_ipw,fp,fname);
+  gb_mfb_write(fp,&md->mw);
   gb_fwrite(&bd->Nn,sizeof(int),1,fp,fname);
   gb_fwrite(&bd->Ne,sizeof(int),1,fp,fname);
   for(i=0;i<=bd->Nn;i++) gb_fwrite(bd->rn[i],sizeof(double),3,fp,fname);

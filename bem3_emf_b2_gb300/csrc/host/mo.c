@@ -30,18 +30,10 @@ void gb_mo_malloc(MOBJ *mo)
   }
 }
 
-/* raw Bobj plus its plane waves; the stored pointers are replaced */
+/* raw Bobj plus its beam arrays; the stored pointers are replaced */
 static void gb_read_beam(FILE *fp,Bobj *mw)
 {
-  gb_fread(mw,sizeof(Bobj),1,fp,"multi_fbeam");
-  if(mw->n_fpw||mw->n_lgb||mw->n_bsb||mw->n_blg||mw->n_rab){
-    printf("mo.c: the stored incident field holds beam types other than plane waves, which this library does not support. Exit...\n");
-    exit(1);
-  }
-  memset(&mw->bd,0,sizeof(Bdata));
-  mw->bd.ipw=(Ipw *)m_alloc2(mw->n_ipw>0?mw->n_ipw:1,sizeof(Ipw),"mo.c ipw");
-  gb_fread(mw->bd.ipw,sizeof(Ipw),mw->n_ipw,fp,"ipw");
-  setup_mfb(mw);
+  gb_mfb_read(fp,mw);
 }
 
 /* mesh part common to .obj and .dat (reference dat_read2 / mo_dat_read) */
@@ -124,9 +116,14 @@ static void gb_renew_beam_data(DOMD *md)
 void gb_init_boundary_data_u2(DOMD *md)
 {
   BOUD *bd=&md->bd;
+  /* collocation points and normals; the exterior ones are gathered for one
+   * batched evaluation of the incident field */
+  double *xr=(double *)m_alloc2((size_t)4*bd->Ne+1,3*sizeof(double),"mo.c xr");
+  double *xw=(double *)m_alloc2((size_t)4*bd->Ne+1,3*sizeof(double),"mo.c xw");
+  int *xi=(int *)m_alloc2((size_t)4*bd->Ne+1,sizeof(int),"mo.c xi");
+  int nx=0;
   for(int i=1;i<=bd->Ne;i++){
     double cr[3][4],cw[3][3],r[3],w[3];
-    double complex h[3],dh[3];
     for(int l=0;l<3;l++){ for(int m=0;m<4;m++) cr[l][m]=bd->cr[i][l][m]; for(int m=0;m<3;m++) cw[l][m]=bd->cw[i][l][m]; }
     for(int j=0;j<4;j++){
       if(bd->ed[i][3]==0) lit_rw_zeta_eta(r,w,bd->zt_34[j],bd->et_34[j],cr,cw);
@@ -134,17 +131,29 @@ void gb_init_boundary_data_u2(DOMD *md)
       for(int l=0;l<3;l++){ bd->ren[i][j][l]=r[l]; bd->wen[i][j][l]=w[l]; }
       if(bd->md[i]==0){
         vuni_d(w);
-        calc_mfb_EH_dv(bd->Ui[i][j],h,bd->dUi[i][j],dh,r,w,&md->mw);
-        bd->Ui[i][j][3]=0.0;
-        bd->dUi[i][j][3]=0.0;
-        for(int l=0;l<4;l++){
-          bd->Ui0[i][j][l]=bd->Ui[i][j][l];
-          bd->dUi0[i][j][l]=bd->dUi[i][j][l];
-          bd->Uip[i][j][l]=bd->Ui[i][j][l];
-        }
+        for(int l=0;l<3;l++){ xr[3*nx+l]=r[l]; xw[3*nx+l]=w[l]; }
+        xi[nx++]=4*i+j;
       }
     }
   }
+  if(nx>0){
+    double complex *f=(double complex *)m_alloc2((size_t)12*nx,sizeof(double complex),"mo.c f");
+    double complex *e=f,*h=f+(size_t)3*nx,*de=f+(size_t)6*nx,*dh=f+(size_t)9*nx;
+    calc_mfb_EH_dv_points(&md->mw,nx,xr,xw,e,h,de,dh);
+    for(int k=0;k<nx;k++){
+      int i=xi[k]/4,j=xi[k]%4;
+      for(int l=0;l<3;l++){ bd->Ui[i][j][l]=e[3*k+l]; bd->dUi[i][j][l]=de[3*k+l]; }
+      bd->Ui[i][j][3]=0.0;
+      bd->dUi[i][j][3]=0.0;
+      for(int l=0;l<4;l++){
+        bd->Ui0[i][j][l]=bd->Ui[i][j][l];
+        bd->dUi0[i][j][l]=bd->dUi[i][j][l];
+        bd->Uip[i][j][l]=bd->Ui[i][j][l];
+      }
+    }
+    free(f);
+  }
+  free(xr); free(xw); free(xi);
 }
 
 void mo_initialize(int argc,char **argv,MOBJ *mo)
@@ -237,8 +246,7 @@ void mo_dat_write(char *fname,MOBJ *mo)
     gb_fwr(&md->MN,sizeof(int),1,fp);
     gb_fwr(md->n,sizeof(double complex),md->MN+1,fp);
     gb_fwr(md->kn,sizeof(double complex),md->MN+1,fp);
-    gb_fwr(&md->mw,sizeof(Bobj),1,fp);
-    gb_fwr(md->mw.bd.ipw,sizeof(Ipw),md->mw.n_ipw,fp);
+    gb_mfb_write(fp,&md->mw);
     gb_fwr(&bd->Nn,sizeof(int),1,fp);
     gb_fwr(&bd->Ne,sizeof(int),1,fp);
     for(int i=0;i<=bd->Nn;i++) gb_fwr(bd->rn[i],sizeof(double),3,fp);

@@ -90,3 +90,4 @@ double OSUtoMKSA_Power_per_unit_area(double p){ return p*GB_UP/(GB_UL*GB_UL); }
 double OSUtoMKSA_Force(double f){ return f*GB_UP/GB_C0; }
 double OSUtoMKSA_Torque(double n){ return n*GB_UL*GB_UP/GB_C0; }
 double OSUtoMKSA_Power(double p){ return p*GB_UP; }
+double OSUtoMKSA_power(double p){ return p*GB_UP; }

@@ -1,17 +1,19 @@
 /*
- * multi_fbeam.h -- incident-field container of the reference (mfb_src/multi_fbeam.h).
- *
- * The BEM hot path supports the plane-wave member (ipw).  The other five beam
- * families of the reference (focused, Laguerre-Gaussian, Bessel, Bessel-LG,
- * radial/azimuthal) are outside this library's scope; their struct types are
- * left incomplete so that Bobj keeps the reference's exact layout (it is
- * stored as raw bytes in .obj/.dat files), and a file that defines such a
- * beam is rejected with a message.
+ * multi_fbeam.h -- incident-field container of the reference
+ * (mfb_src/multi_fbeam.h): plane waves and the five angular-spectrum beam
+ * families, read from ipw.txt, fpw.txt, lgb.txt, bsb.txt, blg.txt and
+ * rab.txt and summed in that order.  Bobj keeps the reference's exact layout
+ * (it is stored as raw bytes in .obj/.dat files).
  */
 #if !defined MULTI_FBEAM_H
 #define MULTI_FBEAM_H
 
 #include "ipw.h"
+#include "fpw.h"
+#include "lgb.h"
+#include "bsb.h"
+#include "bslgb.h"
+#include "rab.h"
 
 #define fn_ipw "ipw.txt"
 #define fn_fpw "fpw.txt"
@@ -19,12 +21,6 @@
 #define fn_bsb "bsb.txt"
 #define fn_blg "blg.txt"
 #define fn_rab "rab.txt"
-
-typedef struct focused_planewave Fpw;
-typedef struct lg_beam LGb;
-typedef struct bessel_beam Bsb;
-typedef struct bessel_lg_beam BsLGb;
-typedef struct ra_beam RAb;
 
 typedef struct beam_data{
   Ipw *ipw;
@@ -57,5 +53,20 @@ void free_mfb(Bobj *obj);
 void calc_mfb_EH(double complex *e,double complex *h,double *x,Bobj *obj);
 void calc_mfb_EH_dv(double complex *e,double complex *h,double complex *dedv,double complex *dhdv,double *x,double *v,Bobj *obj);
 int read_data_mfb_ipw(char *fname,Bobj *obj);
+int read_data_mfb_fpw(char *fname,Bobj *obj);
+int read_data_mfb_lgb(char *fname,Bobj *obj);
+int read_data_mfb_bsb(char *fname,Bobj *obj);
+int read_data_mfb_blg(char *fname,Bobj *obj);
+int read_data_mfb_rab(char *fname,Bobj *obj);
+
+/* Batched forms of calc_mfb_EH / calc_mfb_EH_dv: n points x[n][3] (and
+ * directions v[n][3]) at once, outputs [n][3].  The angular-spectrum beams
+ * are evaluated on the GPU in one launch set per call. */
+void calc_mfb_EH_points(Bobj *obj,int n,const double *x,double complex *e,double complex *h);
+void calc_mfb_EH_dv_points(Bobj *obj,int n,const double *x,const double *v,double complex *e,double complex *h,
+                           double complex *dedv,double complex *dhdv);
+/* the beam part of .obj/.dat files: raw Bobj, then the six beam arrays */
+void gb_mfb_write(FILE *fp,Bobj *obj);
+void gb_mfb_read(FILE *fp,Bobj *obj);
 
 #endif

@@ -9,4 +9,5 @@ double OSUtoMKSA_Power_per_unit_area(double p);
 double OSUtoMKSA_Force(double f);
 double OSUtoMKSA_Torque(double n);
 double OSUtoMKSA_Power(double p);
+double OSUtoMKSA_power(double p);
 #endif

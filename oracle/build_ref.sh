@@ -5,7 +5,8 @@
 #    headers in oracle/ref_shim/.
 #  * Outputs: oracle/_ref/libbem3ref.so and the executables d3b2_create_matrix,
 #    d3b2_bv_solver, example1, example2, example4 (example3 needs libpng, which
-#    is absent) and bem3_analysis (this repository's driver, reference API only).
+#    is absent), bem3_analysis (this repository's driver, reference API only) and
+#    the two probes ref_point and ref_beam.
 # Usage: oracle/build_ref.sh [reference_dir]
 #        oracle/build_ref.sh --where   (print the reference directory; exit 2 if absent)
 # The reference directory is the argument, else $BEM3_REFERENCE_DIR, else the
@@ -40,5 +41,6 @@ done
 APPS="$HERE/../bem3_emf_b2_gb300/apps"
 gcc $CFLAGS -o "$OUT/bem3_analysis" "$APPS/bem3_analysis.c" -L"$OUT" -lbem3ref -Wl,-rpath,"$OUT" "$BLAS" -Wl,-rpath,"$BLASDIR" -lm
 gcc $CFLAGS -o "$OUT/ref_point" "$HERE/ref_point.c" -L"$OUT" -lbem3ref -Wl,-rpath,"$OUT" "$BLAS" -Wl,-rpath,"$BLASDIR" -lm
+gcc $CFLAGS -o "$OUT/ref_beam" "$HERE/ref_beam.c" -L"$OUT" -lbem3ref -Wl,-rpath,"$OUT" "$BLAS" -Wl,-rpath,"$BLASDIR" -lm
 rm -f "$OUT"/*.o
 echo "built $OUT"

@@ -41,6 +41,21 @@ def test_struct_layouts_match_the_reference_lp64_sizes(tmp_path):
     assert out == ["264", "240", "2648", "1936", "112", "64", "216"]
 
 
+def test_beam_struct_layouts_match_the_reference(tmp_path):
+    """The five angular-spectrum beam structs are stored as raw bytes after
+    Bobj in .obj/.dat files (reference mo_setup.c:170-176): sizes and member
+    offsets of the reference's mfb_src headers (LP64)."""
+    src = tmp_path / "sz.c"
+    src.write_text('#include "multi_fbeam.h"\n#include <stddef.h>\nint main(){printf("' + "%zu " * 16 + '\\n",'
+                   'sizeof(Fpw),sizeof(LGb),sizeof(Bsb),sizeof(BsLGb),sizeof(RAb),offsetof(Fpw,nn),offsetof(Fpw,data),'
+                   'offsetof(FpwD,nt),offsetof(LGb,lg_m),offsetof(LGbD,ph_p),offsetof(Bsb,data),offsetof(BsbD,ct),'
+                   'offsetof(BsLGb,lg_m),offsetof(BsLGbD,ph_p),offsetof(RAb,nn),offsetof(RAbD,sp));return 0;}\n')
+    exe = tmp_path / "sz"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    out = subprocess.check_output([str(exe)], text=True).split()
+    assert out == "272 280 248 264 272 104 112 112 104 160 104 112 104 144 104 152".split()
+
+
 def _declared(header):
     txt = open(os.path.join(ROOT, "include", header)).read()
     txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
