@@ -48,9 +48,9 @@ int gbi_field(const FieldObj* o, int mode, int type, int n, const double* rt, co
 int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, const int* t, const double* zt, cplx* out,
                  cudaStream_t st);
 int gbi_cross_build(const FieldObj* o, int type, int n, const double* rt, const double* v, int C, cplx* Gm, cplx* Hm,
-                    cplx* dGm, cplx* dHm, double* Fp, cudaStream_t st);
+                    cplx* dGm, cplx* dHm, double* Fp, int dfout, cudaStream_t st);
 int gbi_cross_apply(int n, int C, const cplx* Gm, const cplx* Hm, const cplx* dGm, const cplx* dHm, const double* Fp,
-                    const cplx* U, const cplx* dU, cplx* out, cudaStream_t st);
+                    const cplx* U, const cplx* dU, cplx* out, int dfin, cudaStream_t st);
 int gbi_cgetrf(cplxf* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_t st);
 int gbi_build_A32_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
                          const double* kn_dev, int did, int nrows, size_t base, size_t na, cplxf* A32, cudaStream_t st);
@@ -178,6 +178,7 @@ struct CrossCache {
   int n, C;
   int* did;
   int bad;  // first invalid domain id (+1000), 0 if all nodes are outside the source
+  int df;   // coefficients in double-float (the source's fields are): applied on the FP32 pipes
   cplx *Gm, *Hm, *dGm, *dHm;
   double* Fp;
 };
@@ -859,6 +860,7 @@ static CrossCache* cross_entry(gb_obj* dst, gb_obj* src, int type) {
   e.prec = src->field_prec;
   e.n = dst->next;
   e.C = 4 * src->m.sb_Ne[0];
+  e.df = (src->field_prec >= 2 && type == 2) ? 1 : 0;
   if (dalloc((void**)&e.did, (size_t)e.n * sizeof(int))) return nullptr;
   FieldObj f = field_view(src);
   int* bad = nullptr;
@@ -885,7 +887,7 @@ static CrossCache* cross_entry(gb_obj* dst, gb_obj* src, int type) {
         cudaMalloc((void**)&e.dGm, nc * sizeof(cplx)) == cudaSuccess &&
         cudaMalloc((void**)&e.dHm, nc * sizeof(cplx)) == cudaSuccess &&
         cudaMalloc((void**)&e.Fp, (size_t)e.n * 2 * sizeof(double)) == cudaSuccess &&
-        gbi_cross_build(&f, type, e.n, dst->ext_r, dst->ext_v, e.C, e.Gm, e.Hm, e.dGm, e.dHm, e.Fp, dst->st) == 0 &&
+        gbi_cross_build(&f, type, e.n, dst->ext_r, dst->ext_v, e.C, e.Gm, e.Hm, e.dGm, e.dHm, e.Fp, e.df, dst->st) == 0 &&
         cudaStreamSynchronize(dst->st) == cudaSuccess) {
       // kept
     } else {
@@ -913,7 +915,7 @@ extern "C" int gb_add_scattered(gb_obj* dst, gb_obj* src, int type) {
   if (dalloc((void**)&out, (size_t)n * 8 * sizeof(cplx))) return -1;
   int rc = 0;
   if (e->Gm) {
-    rc = gbi_cross_apply(n, e->C, e->Gm, e->Hm, e->dGm, e->dHm, e->Fp, src->bU[0], src->bdU[0], out, dst->st);
+    rc = gbi_cross_apply(n, e->C, e->Gm, e->Hm, e->dGm, e->dHm, e->Fp, src->bU[0], src->bdU[0], out, e->df, dst->st);
   } else {
     FieldObj f = field_view(src);
     rc = gbi_field(&f, 3, type, n, dst->ext_r, dst->ext_v, e->did, out, nullptr, dst->st);

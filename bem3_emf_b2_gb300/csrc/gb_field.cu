@@ -455,7 +455,17 @@ struct CrossArgs {
   // of the per-point sums
   const uint8_t* only;
   double* Fs;
+  // coefficients stored in double-float (float4: re.hi, re.lo, im.hi, im.lo
+  // in the 16 bytes of a complex FP64 entry), for k_cross_apply_df
+  int dfout;
 };
+
+// one coefficient into a cross-operator matrix, complex FP64 or double-float
+__device__ __forceinline__ void store_coef(cplx* M, size_t i, cplx v, int dfout) {
+  if (!dfout) { M[i] = v; return; }
+  const float rh = (float)v.x, ih = (float)v.y;
+  ((float4*)M)[i] = make_float4(rh, (float)(v.x - (double)rh), ih, (float)(v.y - (double)ih));
+}
 
 template <bool DF>
 __global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
@@ -495,10 +505,10 @@ __global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
     dF += A.dF[0];
     const size_t c = row + (size_t)(s - 1) * 4;
     for (int nn = 0; nn < 4; nn++) {
-      a.Gm[c + nn] = A.G[nn];
-      a.Hm[c + nn] = A.H[nn];
-      a.dGm[c + nn] = A.dG[0][nn];
-      a.dHm[c + nn] = A.dH[0][nn];
+      store_coef(a.Gm, c + nn, A.G[nn], a.dfout);
+      store_coef(a.Hm, c + nn, A.H[nn], a.dfout);
+      store_coef(a.dGm, c + nn, A.dG[0][nn], a.dfout);
+      store_coef(a.dHm, c + nn, A.dH[0][nn], a.dfout);
     }
   }
   for (int o2 = 16; o2 > 0; o2 >>= 1) {
@@ -532,10 +542,10 @@ __global__ void __launch_bounds__(128) k_cross_build_df(CrossArgs a, uint8_t* re
   const size_t c = (size_t)p * a.C + (size_t)(s - 1) * 4;
 #pragma unroll
   for (int nn = 0; nn < 4; nn++) {
-    a.Gm[c + nn] = A.G[nn];
-    a.Hm[c + nn] = A.H[nn];
-    a.dGm[c + nn] = A.dG[0][nn];
-    a.dHm[c + nn] = A.dH[0][nn];
+    store_coef(a.Gm, c + nn, A.G[nn], a.dfout);
+    store_coef(a.Hm, c + nn, A.H[nn], a.dfout);
+    store_coef(a.dGm, c + nn, A.dG[0][nn], a.dfout);
+    store_coef(a.dHm, c + nn, A.dH[0][nn], a.dfout);
   }
   a.Fs[2 * q] = A.F;
   a.Fs[2 * q + 1] = A.dF[0];
@@ -592,14 +602,18 @@ __global__ void __launch_bounds__(128) k_cross_apply(int n, int C, const cplx* _
 }
 
 extern "C" int gbi_cross_build(const FieldObj* o, int type, int n, const double* rt, const double* v, int C, cplx* Gm,
-                               cplx* Hm, cplx* dGm, cplx* dHm, double* Fp, cudaStream_t st) {
+                               cplx* Hm, cplx* dGm, cplx* dHm, double* Fp, int dfout, cudaStream_t st) {
   if (n <= 0) return 0;
   CrossArgs a;
   a.o = *o; a.type = type; a.n = n; a.C = C; a.rt = rt; a.v = v;
   a.Gm = Gm; a.Hm = Hm; a.dGm = dGm; a.dHm = dHm; a.Fp = Fp;
-  a.only = nullptr; a.Fs = nullptr;
+  a.only = nullptr; a.Fs = nullptr; a.dfout = dfout;
   const unsigned nbw = (unsigned)(((size_t)n * 32 + 127) / 128);
   const int Ne = o->sb_Ne[0];
+  if (o->prec >= 2 && type == 2 && Ne > 0 && !dfout) {
+    gbi_set_error("gbi_cross_build: the double-float build stores double-float coefficients");
+    return -1;
+  }
   if (o->prec >= 2 && type == 2 && Ne > 0) {
     // double-float pass over all pairs, FP64 pass over the declined ones,
     // then the per-point sums in element order
@@ -627,11 +641,91 @@ extern "C" int gbi_cross_build(const FieldObj* o, int type, int n, const double*
   return 0;
 }
 
+// the source's boundary values U, dU (elements 1..C/4, nodes, components)
+// in double-float, for k_cross_apply_df
+__global__ void k_bv_to_df(int C, const cplx* __restrict__ U, const cplx* __restrict__ dU, float4* Ud, float4* dUd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 4 * C) return;
+  const cplx u = U[16 + i], du = dU[16 + i];  // skip element 0
+  const float a = (float)u.x, b = (float)u.y, c = (float)du.x, d = (float)du.y;
+  Ud[i] = make_float4(a, (float)(u.x - (double)a), b, (float)(u.y - (double)b));
+  dUd[i] = make_float4(c, (float)(du.x - (double)c), d, (float)(du.y - (double)d));
+}
+
+__device__ __forceinline__ dfc dfc_ld(const float4& f) { return dfcmk(dfmk(f.x, f.y), dfmk(f.z, f.w)); }
+// acc + a b (complex double-float)
+__device__ __forceinline__ dfc dfc_fma(dfc acc, dfc a, dfc b) {
+  dfc r;
+  r.re = df_fma(df_fma(acc.re, a.re, b.re), df_neg(a.im), b.im);
+  r.im = df_fma(df_fma(acc.im, a.re, b.im), a.im, b.re);
+  return r;
+}
+
+// k_cross_apply with double-float coefficients and boundary values: the
+// same sums on the FP32 pipes (the FP64 version is bound by the DFMA rate);
+// the division by 1 + F in FP64
+__global__ void __launch_bounds__(128) k_cross_apply_df(int n, int C, const float4* __restrict__ Gm,
+                                                        const float4* __restrict__ Hm, const float4* __restrict__ dGm,
+                                                        const float4* __restrict__ dHm, const double* __restrict__ Fp,
+                                                        const float4* __restrict__ Ud, const float4* __restrict__ dUd,
+                                                        cplx* out) {
+  const int lane = threadIdx.x & 31;
+  const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (p >= n) return;
+  const df z = dfmk(0.0f, 0.0f);
+  dfc u[4], du[4];
+#pragma unroll
+  for (int l = 0; l < 4; l++) { u[l] = dfcmk(z, z); du[l] = dfcmk(z, z); }
+  const size_t row = (size_t)p * C;
+  for (int c = lane; c < C; c += 32) {
+    const dfc g = dfc_ld(Gm[row + c]), h = dfc_ld(Hm[row + c]), dg = dfc_ld(dGm[row + c]), dh = dfc_ld(dHm[row + c]);
+    const dfc mh = dfcmk(df_neg(h.re), df_neg(h.im)), mdh = dfcmk(df_neg(dh.re), df_neg(dh.im));
+#pragma unroll
+    for (int l = 0; l < 4; l++) {
+      const dfc a = dfc_ld(dUd[(size_t)c * 4 + l]), b = dfc_ld(Ud[(size_t)c * 4 + l]);
+      u[l] = dfc_fma(dfc_fma(u[l], g, a), mh, b);
+      du[l] = dfc_fma(dfc_fma(du[l], dg, a), mdh, b);
+    }
+  }
+  double acc[16];
+#pragma unroll
+  for (int l = 0; l < 4; l++) {
+    acc[2 * l] = df_to(u[l].re);
+    acc[2 * l + 1] = df_to(u[l].im);
+    acc[8 + 2 * l] = df_to(du[l].re);
+    acc[9 + 2 * l] = df_to(du[l].im);
+  }
+  warp_allreduce<16>(acc);
+  if (lane != 0) return;
+  const double den = 1.0 + Fp[2 * p], dF = Fp[2 * p + 1];
+  for (int l = 0; l < 4; l++) {
+    const cplx uu = cdivr(cmk(acc[2 * l], acc[2 * l + 1]), den);
+    const cplx dd = cdivr(cmk(acc[8 + 2 * l], acc[9 + 2 * l]) - uu * dF, den);
+    out[(size_t)p * 8 + l] = uu;
+    out[(size_t)p * 8 + 4 + l] = dd;
+  }
+}
+
+// dfin: the coefficients are in double-float (gbi_cross_build with dfout)
 extern "C" int gbi_cross_apply(int n, int C, const cplx* Gm, const cplx* Hm, const cplx* dGm, const cplx* dHm,
-                               const double* Fp, const cplx* U, const cplx* dU, cplx* out, cudaStream_t st) {
+                               const double* Fp, const cplx* U, const cplx* dU, cplx* out, int dfin, cudaStream_t st) {
   if (n <= 0) return 0;
-  k_cross_apply<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(n, C, Gm, Hm, dGm, dHm, Fp, U, dU, out);
+  if (!dfin) {
+    k_cross_apply<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(n, C, Gm, Hm, dGm, dHm, Fp, U, dU, out);
+    gbi_count_launch();
+    GB_CUDA(cudaGetLastError());
+    return 0;
+  }
+  float4 *Ud = nullptr, *dUd = nullptr;
+  GB_CUDA(cudaMallocAsync((void**)&Ud, (size_t)4 * C * sizeof(float4), st));
+  GB_CUDA(cudaMallocAsync((void**)&dUd, (size_t)4 * C * sizeof(float4), st));
+  k_bv_to_df<<<(unsigned)((4 * (size_t)C + 255) / 256), 256, 0, st>>>(C, U, dU, Ud, dUd);
+  k_cross_apply_df<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(
+      n, C, (const float4*)Gm, (const float4*)Hm, (const float4*)dGm, (const float4*)dHm, Fp, Ud, dUd, out);
   gbi_count_launch();
+  gbi_count_launch();
+  cudaFreeAsync(Ud, st);
+  cudaFreeAsync(dUd, st);
   GB_CUDA(cudaGetLastError());
   return 0;
 }
