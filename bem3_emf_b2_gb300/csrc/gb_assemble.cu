@@ -47,8 +47,11 @@
 #include "gb_reduce.cuh"
 #include "gb_internal.h"
 #include "gb_quad_df.cuh"
+#include <algorithm>
 #include <mutex>
 #include <vector>
+
+#include "gb_mlp.h"
 
 
 
@@ -72,6 +75,7 @@ struct AsmArgs {
   int adapt;       // k_asm_regular_df: the distance-adaptive order (precision 3)
   int row0, nrow;  // the rows row0 .. row0 + nrow - 1 of the domain; outputs hold nrow rows
   uint8_t* redo;   // work-list launches: the item's flags of pairs for the FP64 pass
+  GbLqList lq;     // learned quadrature: quadrangle fallback pairs listed instead of integrated
 };
 
 // unit tangents at collocation node tn of element |td| (reference tz_te_bd_node d3b1_elem.c:122-143)
@@ -371,6 +375,32 @@ __device__ __forceinline__ void asm_regular_body(const AsmArgs& a, const uint8_t
   while (mask) {
     int src = __ffs(mask) - 1;
     mask &= mask - 1;
+    // learned quadrature: a quadrangle pair keeps its GLN x GLN values and is
+    // listed for the network's correction (when the list has room)
+    int listed = 0;
+    if (lane == src && a.lq.p != nullptr && S.quad) {
+      const unsigned slot = atomicAdd(a.lq.count, 1u);
+      if (slot < a.lq.cap) {
+        GbLqPair& q = a.lq.p[slot];
+        for (int i = 0; i < 12; i++) q.cr[i] = (&S.cr[0][0])[i];
+        for (int i = 0; i < 9; i++) q.cw[i] = (&S.cw[0][0])[i];
+        for (int i = 0; i < 3; i++) q.rt[i] = rt[i];
+        for (int i = 0; i < 6; i++) q.vt[i] = (&vt[0][0])[i];
+        q.k[0] = a.k.x;
+        q.k[1] = a.k.y;
+        const size_t lr = (size_t)(row - a.row0), col = (size_t)sidx * 4;
+        q.out[0] = (struct cplx*)(a.G + lr * N + col);
+        q.out[1] = (struct cplx*)(a.H + lr * N + col);
+        q.out[2] = (struct cplx*)(a.dG + (lr * 2 + 0) * N + col);
+        q.out[3] = (struct cplx*)(a.dG + (lr * 2 + 1) * N + col);
+        q.out[4] = (struct cplx*)(a.dH + (lr * 2 + 0) * N + col);
+        q.out[5] = (struct cplx*)(a.dH + (lr * 2 + 1) * N + col);
+        q.f = a.Fs + (lr * a.Ne + sidx) * 3;
+        q.neg = neg ? 1 : 0;
+        listed = 1;
+      }
+    }
+    if (__shfl_sync(0xffffffffu, listed, src)) continue;
     // broadcast the flagged pair's geometry
     Elem Sb;
     double rtb[3], vtb[2][3];
@@ -953,6 +983,507 @@ __global__ void k_asm_rows_list(const AsmArgs* __restrict__ items, const unsigne
   asm_rows_body(items[i], blockIdx.x - blk0[i]);
 }
 
+// ------------------------------------------------------------------ learned quadrature
+// A near-singular quadrangle pair that needs the reference's fallback rule
+// (|Re dF| > CBD_SDF: the 64 x 64 rule, d3b1_elem.c:503-504,
+// bil_dcoef_v2.c:235-326) keeps its 12 x 12 values and is listed; a network
+// then predicts the difference between the two rules.  Inputs (20, invariant
+// under rigid motions and scaling): the element's corners in a frame at the
+// observation node (z along the normal at the element's centre, x along the
+// first edge) divided by the element size h = 2 sqrt|W(0,0)|, the node's two
+// tangents in that frame, and k h.  Outputs (51): the 64 x 64 minus 12 x 12
+// difference of G/h, H, dG, dH h, F and dF h (G, H, dG, dH complex, four
+// shape functions, two tangents) for the element's own orientation; the
+// sub-domain sign flips H, F, dH, dF as reg_finish does.  Every assembly
+// checks the corrected values of a sample of its listed pairs against the
+// 64 x 64 rule and integrates all listed pairs by that rule if the sample's
+// RMS error exceeds the tolerance.
+#define GB_LQ_NIN 20
+#define GB_LQ_NOUT 51
+
+__device__ __forceinline__ void lq_elem(const GbLqPair& q, Elem& S, double& h) {
+  for (int i = 0; i < 12; i++) (&S.cr[0][0])[i] = q.cr[i];
+  for (int i = 0; i < 9; i++) (&S.cw[0][0])[i] = q.cw[i];
+  S.quad = 1;
+  h = 2.0 * sqrt(sqrt(q.cw[0] * q.cw[0] + q.cw[3] * q.cw[3] + q.cw[6] * q.cw[6]));
+}
+
+// the 27 values of a pair as 51 reals in the network's units
+__device__ __forceinline__ void lq_scaled(const RegAcc<2>& A, double h, double* o) {
+  for (int n = 0; n < 4; n++) {
+    o[2 * n] = A.G[n].x / h;
+    o[2 * n + 1] = A.G[n].y / h;
+    o[8 + 2 * n] = A.H[n].x;
+    o[9 + 2 * n] = A.H[n].y;
+    for (int d = 0; d < 2; d++) {
+      o[16 + 8 * d + 2 * n] = A.dG[d][n].x;
+      o[17 + 8 * d + 2 * n] = A.dG[d][n].y;
+      o[32 + 8 * d + 2 * n] = A.dH[d][n].x * h;
+      o[33 + 8 * d + 2 * n] = A.dH[d][n].y * h;
+    }
+  }
+  o[48] = A.F;
+  o[49] = A.dF[0] * h;
+  o[50] = A.dF[1] * h;
+}
+
+// the pair's GLN x GLN (GL) and GHN x GHN (GH) integrals by the whole warp,
+// finished with the given sign
+__device__ void lq_rules(const GbLqPair& q, int lane, bool neg, bool want_gl, RegAcc<2>& GL, RegAcc<2>& GH) {
+  Elem S;
+  double h;
+  lq_elem(q, S, h);
+  const double vt[2][3] = {{q.vt[0], q.vt[1], q.vt[2]}, {q.vt[3], q.vt[4], q.vt[5]}};
+  const cplx k = cmk(q.k[0], q.k[1]);
+  reg_integrate_gh_part<2>(S, lane, 32, q.rt, vt, k, GH);
+  warp_allreduce<sizeof(RegAcc<2>) / sizeof(double)>((double*)&GH);
+  reg_finish<2>(GH, GB_I_FP, neg);
+  if (want_gl) {
+    regacc_zero(GL);
+    for (int p = lane; p < GB_GLN * GB_GLN; p += 32) {
+      const int i = p / GB_GLN, j = p % GB_GLN;
+      reg_point<2>(S, c_tab.xli[i], c_tab.xli[j], c_tab.wli[i] * c_tab.wli[j], q.rt, vt, k, GL);
+    }
+    warp_allreduce<sizeof(RegAcc<2>) / sizeof(double)>((double*)&GL);
+    reg_finish<2>(GL, GB_I_FP, neg);
+  }
+}
+
+// network inputs, standardised by (mu, sd)
+__global__ void k_lq_features(int n, const GbLqPair* __restrict__ P, const float* __restrict__ mu,
+                              const float* __restrict__ sd, float* X) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const GbLqPair& q = P[i];
+  Elem S;
+  double h;
+  lq_elem(q, S, h);
+  double z[3] = {q.cw[0], q.cw[3], q.cw[6]};
+  const double zn = norm3(z);
+  for (int d = 0; d < 3; d++) z[d] /= zn;
+  double c[4][3];
+  const double sz[4] = {-1.0, 1.0, 1.0, -1.0}, se[4] = {-1.0, -1.0, 1.0, 1.0};
+  for (int j = 0; j < 4; j++)
+    for (int d = 0; d < 3; d++)
+      c[j][d] = S.cr[d][0] + S.cr[d][1] * sz[j] + S.cr[d][2] * se[j] + S.cr[d][3] * sz[j] * se[j];
+  double x[3] = {c[1][0] - c[0][0], c[1][1] - c[0][1], c[1][2] - c[0][2]};
+  const double xz = x[0] * z[0] + x[1] * z[1] + x[2] * z[2];
+  for (int d = 0; d < 3; d++) x[d] -= xz * z[d];
+  const double xn = norm3(x);
+  for (int d = 0; d < 3; d++) x[d] /= xn;
+  const double y[3] = {z[1] * x[2] - z[2] * x[1], z[2] * x[0] - z[0] * x[2], z[0] * x[1] - z[1] * x[0]};
+  double f[GB_LQ_NIN];
+  for (int j = 0; j < 4; j++) {
+    const double r[3] = {c[j][0] - q.rt[0], c[j][1] - q.rt[1], c[j][2] - q.rt[2]};
+    f[3 * j] = (r[0] * x[0] + r[1] * x[1] + r[2] * x[2]) / h;
+    f[3 * j + 1] = (r[0] * y[0] + r[1] * y[1] + r[2] * y[2]) / h;
+    f[3 * j + 2] = (r[0] * z[0] + r[1] * z[1] + r[2] * z[2]) / h;
+  }
+  for (int t = 0; t < 2; t++) {
+    const double* v = q.vt + 3 * t;
+    f[12 + 3 * t] = v[0] * x[0] + v[1] * x[1] + v[2] * x[2];
+    f[13 + 3 * t] = v[0] * y[0] + v[1] * y[1] + v[2] * y[2];
+    f[14 + 3 * t] = v[0] * z[0] + v[1] * z[1] + v[2] * z[2];
+  }
+  f[18] = q.k[0] * h;
+  f[19] = q.k[1] * h;
+  for (int j = 0; j < GB_LQ_NIN; j++) X[(size_t)i * GB_LQ_NIN + j] = (float)((f[j] - mu[j]) / sd[j]);
+}
+
+// training targets: GH minus GL in the network's units (element's own orientation)
+__global__ void __launch_bounds__(128) k_lq_label(int n, const GbLqPair* __restrict__ P, float* T) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= n) return;
+  RegAcc<2> GL, GH;
+  lq_rules(P[w], lane, false, true, GL, GH);
+  if (lane != 0) return;
+  double h, a[GB_LQ_NOUT], b[GB_LQ_NOUT];
+  Elem S;
+  lq_elem(P[w], S, h);
+  lq_scaled(GH, h, a);
+  lq_scaled(GL, h, b);
+  for (int j = 0; j < GB_LQ_NOUT; j++) T[(size_t)w * GB_LQ_NOUT + j] = (float)(a[j] - b[j]);
+}
+
+// the network's corrections (standardised outputs Y, scales mu, sd) added to
+// the listed pairs' matrix entries and solid-angle terms
+__global__ void k_lq_apply(int n, const GbLqPair* __restrict__ P, const float* __restrict__ Y,
+                           const float* __restrict__ mu, const float* __restrict__ sd) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const GbLqPair& q = P[i];
+  Elem S;
+  double h;
+  lq_elem(q, S, h);
+  double d[GB_LQ_NOUT];
+  for (int j = 0; j < GB_LQ_NOUT; j++) d[j] = (double)Y[(size_t)i * GB_LQ_NOUT + j] * sd[j] + mu[j];
+  const double sh = q.neg ? -1.0 : 1.0;
+  cplx* g = q.out[0];
+  cplx* hh = q.out[1];
+  for (int nn = 0; nn < 4; nn++) {
+    g[nn] = g[nn] + cmk(d[2 * nn] * h, d[2 * nn + 1] * h);
+    hh[nn] = hh[nn] + cmk(d[8 + 2 * nn] * sh, d[9 + 2 * nn] * sh);
+    for (int t = 0; t < 2; t++) {
+      cplx* dg = q.out[2 + t];
+      cplx* dh = q.out[4 + t];
+      dg[nn] = dg[nn] + cmk(d[16 + 8 * t + 2 * nn], d[17 + 8 * t + 2 * nn]);
+      dh[nn] = dh[nn] + cmk(d[32 + 8 * t + 2 * nn] * sh / h, d[33 + 8 * t + 2 * nn] * sh / h);
+    }
+  }
+  q.f[0] += d[48] * sh;
+  q.f[1] += d[49] * sh / h;
+  q.f[2] += d[50] * sh / h;
+}
+
+// the current (corrected) values of sampled pairs against the GH rule: per
+// pair the largest error over the 51 outputs in the network's units, over the
+// largest GH output; also the plain GL rule's error
+__global__ void __launch_bounds__(128) k_lq_judge(int m, const int* __restrict__ idx, const GbLqPair* __restrict__ P,
+                                                  double* err) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= m) return;
+  const GbLqPair& q = P[idx[w]];
+  RegAcc<2> GL, GH, C;
+  lq_rules(q, lane, q.neg != 0, true, GL, GH);
+  if (lane != 0) return;
+  for (int nn = 0; nn < 4; nn++) {
+    C.G[nn] = q.out[0][nn];
+    C.H[nn] = q.out[1][nn];
+    for (int t = 0; t < 2; t++) {
+      C.dG[t][nn] = q.out[2 + t][nn];
+      C.dH[t][nn] = q.out[4 + t][nn];
+    }
+  }
+  C.F = q.f[0];
+  C.dF[0] = q.f[1];
+  C.dF[1] = q.f[2];
+  Elem S;
+  double h, a[GB_LQ_NOUT], b[GB_LQ_NOUT], c[GB_LQ_NOUT];
+  lq_elem(q, S, h);
+  lq_scaled(GH, h, a);
+  lq_scaled(GL, h, b);
+  lq_scaled(C, h, c);
+  double sc = 0.0, ec = 0.0, eg = 0.0;
+  for (int j = 0; j < GB_LQ_NOUT; j++) {
+    sc = fmax(sc, fabs(a[j]));
+    ec = fmax(ec, fabs(c[j] - a[j]));
+    eg = fmax(eg, fabs(b[j] - a[j]));
+  }
+  err[2 * w] = ec / sc;
+  err[2 * w + 1] = eg / sc;
+}
+
+// the GH rule written for every listed pair (the judge's fallback)
+__global__ void __launch_bounds__(128) k_lq_exact(int n, const GbLqPair* __restrict__ P) {
+  const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const GbLqPair& q = P[w];
+  RegAcc<2> GL, GH;
+  lq_rules(q, lane, q.neg != 0, false, GL, GH);
+  if (lane != 0) return;
+  for (int nn = 0; nn < 4; nn++) {
+    q.out[0][nn] = GH.G[nn];
+    q.out[1][nn] = GH.H[nn];
+    for (int t = 0; t < 2; t++) {
+      q.out[2 + t][nn] = GH.dG[t][nn];
+      q.out[4 + t][nn] = GH.dH[t][nn];
+    }
+  }
+  q.f[0] = GH.F;
+  q.f[1] = GH.dF[0];
+  q.f[2] = GH.dF[1];
+}
+
+__global__ void k_lq_gather(size_t n, int w, const int* __restrict__ perm, const float* __restrict__ src, float* dst) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n * w) return;
+  const size_t r = i / w, c = i % w;
+  dst[i] = src[(size_t)perm[r] * w + c];
+}
+
+// ---- model state (process-wide)
+struct LqState {
+  gb_mlp* net = nullptr;
+  float xmu[GB_LQ_NIN], xsd[GB_LQ_NIN], ymu[GB_LQ_NOUT], ysd[GB_LQ_NOUT];
+  int enabled = 0;
+  int collect = 0;
+  double tol = 1e-7;
+  double stats[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  std::vector<float*> cx, ct;      // collected raw features / targets, per assembly
+  std::vector<size_t> cn;
+};
+static LqState g_lq;
+static std::mutex g_lq_mu;
+
+static bool lq_active(int precision, int type) {
+  std::lock_guard<std::mutex> lk(g_lq_mu);
+  return precision >= 2 && type == 2 && (g_lq.collect || (g_lq.enabled && g_lq.net));
+}
+
+static int lq_alloc(GbLqList& L, size_t npair, cudaStream_t st) {
+  L.cap = (unsigned)std::min<size_t>(npair / 32 + 4096, (size_t)4 << 20);
+  GB_CUDA(cudaMallocAsync((void**)&L.p, (size_t)L.cap * sizeof(GbLqPair), st));
+  GB_CUDA(cudaMallocAsync((void**)&L.count, sizeof(unsigned), st));
+  GB_CUDA(cudaMemsetAsync(L.count, 0, sizeof(unsigned), st));
+  return 0;
+}
+
+static void lq_free(GbLqList& L, cudaStream_t st) {
+  if (L.p) cudaFreeAsync(L.p, st);
+  if (L.count) cudaFreeAsync(L.count, st);
+  L.p = nullptr;
+  L.count = nullptr;
+}
+
+// After the regular passes: correct the listed pairs (or, collecting, keep
+// their features and targets); synchronises st.
+static int lq_stage(GbLqList& L, cudaStream_t st) {
+  unsigned cnt = 0;
+  GB_CUDA(cudaMemcpyAsync(&cnt, L.count, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  const int n = (int)std::min(cnt, L.cap);
+  std::lock_guard<std::mutex> lk(g_lq_mu);
+  if (n == 0) {
+    for (int i = 0; i < 8; i++) g_lq.stats[i] = 0.0;
+    return 0;
+  }
+  if (g_lq.collect) {
+    float *X = nullptr, *T = nullptr, *mu = nullptr, *sd = nullptr;
+    GB_CUDA(cudaMalloc((void**)&X, (size_t)n * GB_LQ_NIN * sizeof(float)));
+    GB_CUDA(cudaMalloc((void**)&T, (size_t)n * GB_LQ_NOUT * sizeof(float)));
+    GB_CUDA(cudaMallocAsync((void**)&mu, 2 * GB_LQ_NIN * sizeof(float), st));
+    sd = mu + GB_LQ_NIN;
+    std::vector<float> id(2 * GB_LQ_NIN, 0.0f);
+    for (int j = 0; j < GB_LQ_NIN; j++) id[GB_LQ_NIN + j] = 1.0f;
+    GB_CUDA(cudaMemcpyAsync(mu, id.data(), id.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+    k_lq_features<<<(n + 127) / 128, 128, 0, st>>>(n, L.p, mu, sd, X);
+    k_lq_label<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(n, L.p, T);
+    gbi_count_launch();
+    gbi_count_launch();
+    GB_CUDA(cudaGetLastError());
+    cudaFreeAsync(mu, st);
+    GB_CUDA(cudaStreamSynchronize(st));
+    g_lq.cx.push_back(X);
+    g_lq.ct.push_back(T);
+    g_lq.cn.push_back((size_t)n);
+    g_lq.stats[0] = n;
+    return 0;
+  }
+  cudaEvent_t e0, e1;
+  GB_CUDA(cudaEventCreate(&e0));
+  GB_CUDA(cudaEventCreate(&e1));
+  GB_CUDA(cudaEventRecord(e0, st));
+  float *X = nullptr, *Y = nullptr, *nrm = nullptr;
+  int* idx = nullptr;
+  double* err = nullptr;
+  const int m = std::min(n, 2048);
+  GB_CUDA(cudaMallocAsync((void**)&X, (size_t)n * GB_LQ_NIN * sizeof(float), st));
+  GB_CUDA(cudaMallocAsync((void**)&Y, (size_t)n * GB_LQ_NOUT * sizeof(float), st));
+  GB_CUDA(cudaMallocAsync((void**)&nrm, 2 * (GB_LQ_NIN + GB_LQ_NOUT) * sizeof(float), st));
+  GB_CUDA(cudaMallocAsync((void**)&idx, (size_t)m * sizeof(int), st));
+  GB_CUDA(cudaMallocAsync((void**)&err, (size_t)m * 2 * sizeof(double), st));
+  std::vector<float> h(2 * (GB_LQ_NIN + GB_LQ_NOUT));
+  memcpy(h.data(), g_lq.xmu, sizeof(g_lq.xmu));
+  memcpy(h.data() + GB_LQ_NIN, g_lq.xsd, sizeof(g_lq.xsd));
+  memcpy(h.data() + 2 * GB_LQ_NIN, g_lq.ymu, sizeof(g_lq.ymu));
+  memcpy(h.data() + 2 * GB_LQ_NIN + GB_LQ_NOUT, g_lq.ysd, sizeof(g_lq.ysd));
+  std::vector<int> hi(m);
+  for (int i = 0; i < m; i++) hi[i] = (int)(((long long)i * n) / m);
+  GB_CUDA(cudaMemcpyAsync(nrm, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, st));
+  GB_CUDA(cudaMemcpyAsync(idx, hi.data(), (size_t)m * sizeof(int), cudaMemcpyHostToDevice, st));
+  k_lq_features<<<(n + 127) / 128, 128, 0, st>>>(n, L.p, nrm, nrm + GB_LQ_NIN, X);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  GB_CUDA(cudaStreamSynchronize(st));
+  for (int r0 = 0; r0 < n; r0 += 65536) {
+    const int b = std::min(65536, n - r0);
+    if (gb_mlp_forward(g_lq.net, b, X + (size_t)r0 * GB_LQ_NIN, Y + (size_t)r0 * GB_LQ_NOUT)) return -1;
+  }
+  k_lq_apply<<<(n + 127) / 128, 128, 0, st>>>(n, L.p, Y, nrm + 2 * GB_LQ_NIN, nrm + 2 * GB_LQ_NIN + GB_LQ_NOUT);
+  k_lq_judge<<<(unsigned)(((size_t)m * 32 + 127) / 128), 128, 0, st>>>(m, idx, L.p, err);
+  gbi_count_launch();
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  std::vector<double> he((size_t)m * 2);
+  GB_CUDA(cudaMemcpyAsync(he.data(), err, he.size() * sizeof(double), cudaMemcpyDeviceToHost, st));
+  GB_CUDA(cudaStreamSynchronize(st));
+  double sc = 0.0, sg = 0.0, mc = 0.0;
+  for (int i = 0; i < m; i++) {
+    sc += he[2 * i] * he[2 * i];
+    sg += he[2 * i + 1] * he[2 * i + 1];
+    mc = std::max(mc, he[2 * i]);
+  }
+  const double rc = sqrt(sc / m), rg = sqrt(sg / m);
+  const bool revert = !(rc <= g_lq.tol);
+  if (revert) {
+    k_lq_exact<<<(unsigned)(((size_t)n * 32 + 127) / 128), 128, 0, st>>>(n, L.p);
+    gbi_count_launch();
+    GB_CUDA(cudaGetLastError());
+  }
+  GB_CUDA(cudaEventRecord(e1, st));
+  GB_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  for (void* p : {(void*)X, (void*)Y, (void*)nrm, (void*)idx, (void*)err}) cudaFreeAsync(p, st);
+  const double s[8] = {(double)n, (double)(cnt - (unsigned)n), (double)m, rc, rg, mc, revert ? 1.0 : 0.0, ms};
+  for (int i = 0; i < 8; i++) g_lq.stats[i] = s[i];
+  return 0;
+}
+
+extern "C" int gb_lq_collect(int on) {
+  std::lock_guard<std::mutex> lk(g_lq_mu);
+  g_lq.collect = on ? 1 : 0;
+  if (on) {
+    for (float* p : g_lq.cx) cudaFree(p);
+    for (float* p : g_lq.ct) cudaFree(p);
+    g_lq.cx.clear();
+    g_lq.ct.clear();
+    g_lq.cn.clear();
+  }
+  return 0;
+}
+
+extern "C" int gb_lq_enable(int on, double tol) {
+  std::lock_guard<std::mutex> lk(g_lq_mu);
+  if (on && !g_lq.net) {
+    gbi_set_error("gb_lq_enable: no trained network (gb_lq_train)");
+    return -1;
+  }
+  if (!(tol > 0.0)) {
+    gbi_set_error("gb_lq_enable: tolerance %g must be positive", tol);
+    return -1;
+  }
+  g_lq.enabled = on ? 1 : 0;
+  g_lq.tol = tol;
+  return 0;
+}
+
+extern "C" int gb_lq_stats(double* out) {
+  std::lock_guard<std::mutex> lk(g_lq_mu);
+  for (int i = 0; i < 8; i++) out[i] = g_lq.stats[i];
+  return 0;
+}
+
+// Training on the collected pairs: a seeded shuffle, 1/20 held out, inputs
+// and targets standardised per component, Adam with a cosine learning rate.
+// info: samples trained on, held out, last 100 steps' mean training loss,
+// held-out loss (standardised units), the held-out loss of predicting zero.
+extern "C" int gb_lq_train(int epochs, int batch, float lr, unsigned seed, double* info) {
+  std::lock_guard<std::mutex> lk(g_lq_mu);
+  size_t n = 0;
+  for (size_t c : g_lq.cn) n += c;
+  if (n < (size_t)4 * batch || batch < 1 || epochs < 1) {
+    gbi_set_error("gb_lq_train: %zu collected pairs for batches of %d (collect with gb_lq_collect(1) and a "
+                  "precision >= 2 assembly of quadrangle meshes first)", n, batch);
+    return -1;
+  }
+  // host copies: raw features and targets, concatenated
+  std::vector<float> X(n * GB_LQ_NIN), T(n * GB_LQ_NOUT);
+  size_t off = 0;
+  for (size_t i = 0; i < g_lq.cn.size(); i++) {
+    GB_CUDA(cudaMemcpy(X.data() + off * GB_LQ_NIN, g_lq.cx[i], g_lq.cn[i] * GB_LQ_NIN * sizeof(float),
+                       cudaMemcpyDeviceToHost));
+    GB_CUDA(cudaMemcpy(T.data() + off * GB_LQ_NOUT, g_lq.ct[i], g_lq.cn[i] * GB_LQ_NOUT * sizeof(float),
+                       cudaMemcpyDeviceToHost));
+    off += g_lq.cn[i];
+  }
+  // seeded shuffle (64-bit LCG, Fisher-Yates)
+  std::vector<int> perm(n);
+  for (size_t i = 0; i < n; i++) perm[i] = (int)i;
+  unsigned long long s = 0x9E3779B97F4A7C15ull ^ seed;
+  for (size_t i = n - 1; i > 0; i--) {
+    s = s * 6364136223846793005ull + 1442695040888963407ull;
+    const size_t j = (size_t)((s >> 33) % (i + 1));
+    std::swap(perm[i], perm[j]);
+  }
+  const size_t nval = std::max<size_t>(n / 20, 1), ntr = n - nval;
+  // standardisation from the training part
+  double mx[GB_LQ_NIN] = {0}, sx[GB_LQ_NIN] = {0}, my[GB_LQ_NOUT] = {0}, sy[GB_LQ_NOUT] = {0};
+  for (size_t r = 0; r < ntr; r++) {
+    const size_t p = perm[r];
+    for (int j = 0; j < GB_LQ_NIN; j++) { const double v = X[p * GB_LQ_NIN + j]; mx[j] += v; sx[j] += v * v; }
+    for (int j = 0; j < GB_LQ_NOUT; j++) { const double v = T[p * GB_LQ_NOUT + j]; my[j] += v; sy[j] += v * v; }
+  }
+  for (int j = 0; j < GB_LQ_NIN; j++) {
+    mx[j] /= ntr;
+    const double v = sx[j] / ntr - mx[j] * mx[j];
+    g_lq.xmu[j] = (float)mx[j];
+    g_lq.xsd[j] = (float)(v > 1e-24 ? sqrt(v) : 1.0);
+  }
+  for (int j = 0; j < GB_LQ_NOUT; j++) {
+    my[j] /= ntr;
+    const double v = sy[j] / ntr - my[j] * my[j];
+    g_lq.ymu[j] = (float)my[j];
+    g_lq.ysd[j] = (float)(v > 1e-36 ? sqrt(v) : 1.0);
+  }
+  std::vector<float> Xs(n * GB_LQ_NIN), Ts(n * GB_LQ_NOUT);
+  for (size_t r = 0; r < n; r++) {
+    const size_t p = perm[r];
+    for (int j = 0; j < GB_LQ_NIN; j++) Xs[r * GB_LQ_NIN + j] = (X[p * GB_LQ_NIN + j] - g_lq.xmu[j]) / g_lq.xsd[j];
+    for (int j = 0; j < GB_LQ_NOUT; j++) Ts[r * GB_LQ_NOUT + j] = (T[p * GB_LQ_NOUT + j] - g_lq.ymu[j]) / g_lq.ysd[j];
+  }
+  float *dX = nullptr, *dT = nullptr, *dY = nullptr;
+  GB_CUDA(cudaMalloc((void**)&dX, Xs.size() * sizeof(float)));
+  GB_CUDA(cudaMalloc((void**)&dT, Ts.size() * sizeof(float)));
+  GB_CUDA(cudaMalloc((void**)&dY, nval * GB_LQ_NOUT * sizeof(float)));
+  GB_CUDA(cudaMemcpy(dX, Xs.data(), Xs.size() * sizeof(float), cudaMemcpyHostToDevice));
+  GB_CUDA(cudaMemcpy(dT, Ts.data(), Ts.size() * sizeof(float), cudaMemcpyHostToDevice));
+  // network 20 -> 256 -> 256 -> 256 -> 51, He-scaled seeded initialisation
+  if (g_lq.net) { gb_mlp_destroy(g_lq.net); g_lq.net = nullptr; }
+  const int widths[5] = {GB_LQ_NIN, 256, 256, 256, GB_LQ_NOUT};
+  if (gb_mlp_create(4, widths, &g_lq.net)) return -1;
+  std::vector<float> par(gb_mlp_param_count(g_lq.net));
+  size_t o = 0;
+  for (int l = 0; l < 4; l++) {
+    const double sc = sqrt(2.0 / widths[l]);
+    for (int i = 0; i < widths[l] * widths[l + 1]; i++) {
+      s = s * 6364136223846793005ull + 1442695040888963407ull;
+      const double u1 = ((s >> 11) + 0.5) / 9007199254740992.0;
+      s = s * 6364136223846793005ull + 1442695040888963407ull;
+      const double u2 = ((s >> 11) + 0.5) / 9007199254740992.0;
+      par[o++] = (float)(sc * sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2));
+    }
+    for (int i = 0; i < widths[l + 1]; i++) par[o++] = 0.0f;
+  }
+  int rc = gb_mlp_set_params(g_lq.net, par.data());
+  const long steps = (long)epochs * (long)(ntr / batch);
+  double tail = 0.0;
+  int ntail = 0;
+  for (long st = 0; st < steps && !rc; st++) {
+    const size_t r0 = (size_t)(st % (long)(ntr / batch)) * batch;
+    const float a = (float)(lr * 0.5 * (1.0 + cos(3.141592653589793 * (double)st / (double)steps)));
+    double loss = 0.0;
+    rc = gb_mlp_train_step(g_lq.net, batch, dX + r0 * GB_LQ_NIN, dT + r0 * GB_LQ_NOUT, a, &loss);
+    if (st >= steps - 100) { tail += loss; ntail++; }
+  }
+  double val = 0.0, zero = 0.0;
+  if (!rc) rc = gb_mlp_forward(g_lq.net, (int)nval, dX + ntr * GB_LQ_NIN, dY);
+  if (!rc) {
+    std::vector<float> hy(nval * GB_LQ_NOUT);
+    cudaMemcpy(hy.data(), dY, hy.size() * sizeof(float), cudaMemcpyDeviceToHost);
+    for (size_t r = 0; r < nval; r++)
+      for (int j = 0; j < GB_LQ_NOUT; j++) {
+        const double t = Ts[(ntr + r) * GB_LQ_NOUT + j], d = hy[r * GB_LQ_NOUT + j] - t;
+        val += d * d;
+        zero += t * t;
+      }
+    val /= nval;
+    zero /= nval;
+  }
+  cudaFree(dX);
+  cudaFree(dT);
+  cudaFree(dY);
+  if (rc) return -1;
+  info[0] = (double)ntr;
+  info[1] = (double)nval;
+  info[2] = ntail ? tail / ntail : 0.0;
+  info[3] = val;
+  info[4] = zero;
+  return 0;
+}
+
 extern "C" int gbi_assemble_domain2(const GbMeshDev* m, int did, int type, int precision, cplx* G, cplx* H, cplx* dG,
                                     cplx* dH, double* dF, double* Fs, cudaStream_t st);
 
@@ -998,6 +1529,7 @@ extern "C" int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int prec
   a.row0 = row0;
   a.nrow = nrow;
   a.redo = nullptr;
+  memset(&a.lq, 0, sizeof(a.lq));
   GB_CUDA(cudaMemsetAsync(G, 0, nr * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(H, 0, nr * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(dG, 0, 2 * nr * N * sizeof(cplx), st));
@@ -1007,6 +1539,8 @@ extern "C" int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int prec
   size_t npair = nr * (size_t)Ne;
   unsigned nb = (unsigned)((npair + 127) / 128);
   uint8_t* redo = nullptr;
+  const bool lq = lq_active(precision, type);
+  if (lq && lq_alloc(a.lq, npair, st)) return -1;
   if (precision >= 2 && type == 2) {
     GB_CUDA(cudaMallocAsync((void**)&redo, npair, st));
     k_asm_regular_df<<<nb, 128, 0, st>>>(a, redo);
@@ -1024,6 +1558,12 @@ extern "C" int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int prec
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   if (redo) GB_CUDA(cudaFreeAsync(redo, st));
+  if (lq) {
+    const int r = lq_stage(a.lq, st);
+    lq_free(a.lq, st);
+    memset(&a.lq, 0, sizeof(a.lq));
+    if (r) return -1;
+  }
   if (precision >= 2) k_asm_singular<true><<<(unsigned)nr, 256, 0, st>>>(a);
   else k_asm_singular<false><<<(unsigned)nr, 256, 0, st>>>(a);
   gbi_count_launch();
@@ -1045,6 +1585,14 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
   std::vector<unsigned> breg((size_t)n + 1, 0), bsing((size_t)n + 1, 0), brows((size_t)n + 1, 0);
   std::vector<void*> tmp;
   int rc = 0;
+  GbLqList lql;
+  memset(&lql, 0, sizeof(lql));
+  const bool lq = lq_active(precision, type);
+  if (lq) {
+    size_t tot = 0;
+    for (int i = 0; i < n; i++) tot += (size_t)d[i].nrow * (size_t)d[i].m->sb_Ne[d[i].did];
+    if (lq_alloc(lql, tot, st)) return -1;
+  }
   for (int i = 0; i < n && !rc; i++) {
     const GbMeshDev* m = d[i].m;
     const int did = d[i].did, Ne = m->sb_Ne[did];
@@ -1059,6 +1607,7 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
     a.G = d[i].G; a.H = d[i].H; a.dG = d[i].dG; a.dH = d[i].dH; a.dF = d[i].dF;
     a.adapt = precision == 3;
     a.row0 = d[i].row0; a.nrow = d[i].nrow;
+    a.lq = lql;
     const size_t npair = nr * (size_t)Ne;
     if (cudaMallocAsync((void**)&a.Fs, 3 * nr * (size_t)Ne * sizeof(double), st) != cudaSuccess ||
         cudaMallocAsync((void**)&a.redo, npair + 16, st) != cudaSuccess) {
@@ -1100,6 +1649,9 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
     }
     k_asm_regular_list<<<breg[n], 128, 0, st>>>(dit, db, n, df ? 1 : 0);
     gbi_count_launch();
+    if (lq && lq_stage(lql, st)) rc = -1;
+  }
+  if (!rc) {
     if (precision >= 2) k_asm_singular_list<true><<<bsing[n], 256, 0, st>>>(dit, db + n + 1, n);
     else k_asm_singular_list<false><<<bsing[n], 256, 0, st>>>(dit, db + n + 1, n);
     gbi_count_launch();
@@ -1111,6 +1663,7 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
   if (dit) cudaFreeAsync(dit, st);
   if (db) cudaFreeAsync(db, st);
   for (void* t : tmp) cudaFreeAsync(t, st);
+  lq_free(lql, st);
   const cudaError_t e = cudaStreamSynchronize(st);  // the host arrays above are read by the copies
   if (!rc && e != cudaSuccess) { gbi_set_error("work-list assembly: %s", cudaGetErrorString(e)); rc = -1; }
   return rc;

@@ -35,6 +35,25 @@ typedef struct GbAsmItem {
   double* dF;
 } GbAsmItem;
 
+// one near-singular quadrangle pair handed to the learned quadrature: the
+// source element, the observation node with its two tangents, the wave
+// number, the sub-domain sign, and where its matrix entries and solid-angle
+// terms live (G, H, dG0, dG1, dH0, dH1 rows of 4 entries; F, dF0, dF1)
+typedef struct GbLqPair {
+  double cr[12], cw[9];
+  double rt[3], vt[6];
+  double k[2];
+  struct cplx* out[6];
+  double* f;
+  int neg, pad;
+} GbLqPair;
+typedef struct GbLqList {
+  GbLqPair* p;       // null: the assembly integrates every fallback pair by the 64 x 64 rule
+  unsigned* count;   // pairs offered (may exceed cap: the surplus took the 64 x 64 rule)
+  unsigned cap;
+  int pad;
+} GbLqList;
+
 #ifdef __cplusplus
 extern "C" {
 #endif

@@ -266,6 +266,35 @@ int gb_block_factors_upload(gb_obj *o, const void *G0i, const void *G1i, const v
                             const void *Si);
 int gb_scene_step(gb_obj *o, int form, int type);
 
+/* ---- learned near-singular quadrature (quadrangles) ----
+ * The reference integrates a (node, element) pair with |Re dF| > CBD_SDF by
+ * its 64 x 64 fallback rule (d3b1_elem.c:503-504, bil_dcoef_v2.c:235-326).
+ * With a trained network enabled, a precision >= 2 assembly keeps such a
+ * quadrangle pair's 12 x 12 values and adds the network's prediction of the
+ * difference between the two rules (G, H, dG, dH, F, dF); every assembly
+ * then checks a sample of up to 2,048 of its corrected pairs against the
+ * 64 x 64 rule and, if the sample's RMS error (largest output error over
+ * the pair's largest output, in size-scaled units) exceeds tol, integrates
+ * all of them by that rule.  FP64 (precision 0) assemblies never use it.
+ * gb_lq_collect(1): later precision >= 2 assemblies list their fallback
+ * quadrangle pairs and keep features and targets for training (their
+ * matrices then hold the 12 x 12 values of those pairs); (0) stops.
+ * gb_lq_train: trains the process-wide network (20 -> 256 x 3 -> 51, GELU)
+ * on everything collected: seeded shuffle, 1/20 held out, standardised
+ * inputs and targets, Adam with a cosine schedule from lr; info[5]: pairs
+ * trained on, held out, final training loss, held-out loss, held-out loss of
+ * a zero prediction (standardised units).
+ * gb_lq_enable(on, tol): use it in later assemblies (default off).
+ * gb_lq_stats(out[8]) of the last assembly that listed pairs: pairs
+ * corrected, pairs beyond the list's capacity (64 x 64 rule), pairs judged,
+ * RMS error of the corrected sample, RMS error of the 12 x 12 rule alone on
+ * the same sample, largest corrected error, 1 if the assembly reverted to
+ * the 64 x 64 rule, milliseconds of the stage. */
+int gb_lq_collect(int on);
+int gb_lq_train(int epochs, int batch, float lr, unsigned seed, double *info);
+int gb_lq_enable(int on, double tol);
+int gb_lq_stats(double *out);
+
 /* Dense complex FP64 LU solve of a host system: A (n x n, row-major) X = B
  * (n x nrhs, row-major), B overwritten by X.  The kernel behind the dE/dn,
  * dH/dn solve (LAPACKE_zgesv, mo_solve.c:751). */
