@@ -89,6 +89,16 @@ CONE_TH = np.array([0.0, np.pi])
 CONE_TV = np.array([[0.0, 0.0, 0.0], [1.5, 0.0, 0.0]])
 
 
+def write_sphere3(wd, nf):
+    from bem3_emf_b2_gb300 import meshgen
+    nodes, elems = meshgen.cubed_sphere(nf, SPHERE3["radius"])
+    meshgen.write_mesh(os.path.join(wd, "mesh.msh"), nodes, elems)
+    meshgen.write_medium(os.path.join(wd, "medium.txt"), [SPHERE3["n_obj"]])
+    meshgen.write_ipw(os.path.join(wd, "ipw.txt"), [dict(lambda0=SPHERE3["lambda0"], ni=SPHERE3["n_host"], power=1.0,
+                                                          e0x=1.0, e0y=0.0)])
+    return len(elems)
+
+
 def open_workload(args, wd):
     """(scene, description dict) of the chosen workload, set up from its input files"""
     from bem3_emf_b2_gb300 import MultiScene, Scene, meshgen
@@ -114,12 +124,22 @@ def open_workload(args, wd):
         m = args.cone_m or CONES["m"]
         name = CONES["name"] if m == CONES["m"] else CONES["name"].replace("m = 16: 3,072", "m = %d: %d" % (m, ne))
         return sc, dict(workload=name, objects=2, elements_per_object=ne, na_per_object=8 * 3 * ne)
+    if args.workload == "sphere3":
+        nf = args.faces3
+        ne = write_sphere3(wd, nf)
+        sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
+        return sc, dict(workload=SPHERE3["name"] % (nf, nf, ne), objects=1, elements_per_object=ne,
+                        na_per_object=8 * 4 * ne)
     ne = write_sphere(wd, args.faces)
     sc = Scene(os.path.join(wd, "medium.txt"), os.path.join(wd, "mesh.msh"), os.path.join(wd, "ipw.txt"))
     name = SPHERE["name"] if args.faces == 8 else "sphere r=1, cubed %dx%d quads/face (%d elements)" % (
         args.faces, args.faces, ne)
     return sc, dict(workload=name, objects=1, elements_per_object=ne, na_per_object=8 * 4 * ne)
 
+
+SPHERE3 = dict(name="sphere r=3, cubed %dx%d quads/face (%d elements), n = 1.5+0.01i in 1.33, lambda0 = 1, x-pol "
+                    "plane wave +z: the 64x64-per-face sphere's geometry and media at a size whose FP64 form fits "
+                    "one GPU", radius=3.0, n_obj=complex(1.5, 0.01), n_host=1.33, lambda0=1.0)
 
 BATCH = dict(name="seeded multi-object scene (seed 11): 8 spheres, cubes and cones in a 20^3 box, characteristic size "
                   "U[0.3, 1.5], element counts U[200, 600], n U[1.33, 2.0] in 1.33, random orientation; 32 plane "
@@ -256,7 +276,8 @@ def cpu_baseline(args, wd, iterations=11):
         objs = [port.Obj(os.path.join(wd, "cone.msh"), [CONES["n_obj"]], CONES["lambda0"], CONES["n_host"])]
         nobj = 2
     else:
-        objs = [port.Obj(os.path.join(wd, "mesh.msh"), [SPHERE["n_obj"]], SPHERE["lambda0"], SPHERE["n_host"])]
+        S = SPHERE3 if args.workload == "sphere3" else SPHERE
+        objs = [port.Obj(os.path.join(wd, "mesh.msh"), [S["n_obj"]], S["lambda0"], S["n_host"])]
         nobj = 1
     o = objs[0]
     t_asm = 0.0
@@ -517,6 +538,8 @@ def run_reference(args):
     wd = tempfile.mkdtemp(prefix="bench_ref_")
     if args.workload == "cones":
         write_cones(wd, args.cone_m)
+    elif args.workload == "sphere3":
+        write_sphere3(wd, args.faces3)
     else:
         write_sphere(wd, args.faces)
     cpu = cpu_baseline(args, wd)
@@ -524,7 +547,8 @@ def run_reference(args):
               "solve_bieq2.c:343-408); for this workload that is %s and cannot finish a scene inside this run; "
               "sampled estimate %.0f s/scene on %d cores" % (
                   "2 x order 73,728 (87 GB c128 each, ~3.2e15 flop each)" if args.workload == "cones"
-                  else "order 12,288 plus the E/H stage and force that the CPU restatement does not cover",
+                  else "order %d plus the E/H stage and force that the CPU restatement does not cover" % (
+                      8 * 4 * 6 * (args.faces3 if args.workload == "sphere3" else args.faces) ** 2),
                   cpu["value"], cpu["cores"]))
     return {"impl": "reference", "unavailable": reason,
             "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "estimated")}}
@@ -635,7 +659,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--profile-step", action="store_true",
                     help="profiling run: one chosen-form scene step after --warmup steps, nothing else, no JSON line")
-    ap.add_argument("--workload", choices=["cones", "sphere", "cube", "beams"], default="cones",
+    ap.add_argument("--faces3", type=int, default=24, help="quadrangles per cube face of the sphere3 workload")
+    ap.add_argument("--workload", choices=["cones", "sphere", "sphere3", "cube", "beams"], default="cones",
                     help="cones: the two-cone scene (default); sphere: the 384-element sphere; cube: assembly "
                          "throughput of the 38,400-element cube")
     ap.add_argument("--cube-n", type=int, default=None, help="quadrangles per cube edge (cube workload)")
