@@ -81,8 +81,13 @@ int gbi_schur_prepare(GbSchur* s, const GbMeshDev* m, cudaStream_t st);
 }
 #include <functional>
 typedef std::function<int(const cplx* x, cplx* y, cudaStream_t st)> GbOp;
-extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const GbOp& A, const GbOp& M, int m,
-                         double tol, int maxit, cudaStream_t st, int* iters, double* relres);
+extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const GbOp& A, const GbOp* Af, const GbOp& M,
+                         int m, double tol, int maxit, cudaStream_t st, const cplx* Ax0, cplx* Ax_out, int* ax_ok,
+                         int* iters, double* relres);
+extern "C" int gbi_to_df(size_t n, const cplx* src, void* dst, cudaStream_t st);
+extern "C" int gbi_apply_A_domain_df(const void* Gd, const void* Hd, const int* sid, const int* rowk, const GbMeshDev* m,
+                          const double* kn_dev, int did, int nrows, size_t base, const cplx* x, cplx* PQ, void* PQd,
+                          cplx* y, cudaStream_t st);
 
 // ------------------------------------------------------------------ errors
 static thread_local char g_err[1024];
@@ -232,6 +237,14 @@ struct gb_obj {
   // less); invalidated by an assembly or a factorisation
   cplx *Bw, *Xw;
   int have_xw;
+  // A Xw from the last solve's final FP64 residual (valid with have_xw):
+  // the next warm-started solve's first residual needs no product
+  cplx* Axw;
+  int have_axw;
+  // double-float copies of G, H for the GMRES iterations' products (chosen
+  // form), rebuilt after an assembly or upload
+  void* GHdf[GB_MAXDOM][2];
+  int have_ghdf;
   // arithmetic of the regular pairs of the field kernels (potentials at
   // points, fields on the boundary, cross operators): 2 double-float after a
   // precision-2 assembly, else FP64
@@ -282,7 +295,8 @@ extern "C" void gb_obj_destroy(gb_obj* o) {
   cudaFree(o->LU32); cudaFree(o->ipiv32); cudaFree(o->perm32); cudaFree(o->rbt);
   gbi_schur_destroy(o->schur);
   gbi_schur_destroy(o->schur64);
-  cudaFree(o->Bw); cudaFree(o->Xw);
+  cudaFree(o->Bw); cudaFree(o->Xw); cudaFree(o->Axw);
+  for (int d = 0; d < GB_MAXDOM; d++) { cudaFree(o->GHdf[d][0]); cudaFree(o->GHdf[d][1]); }
   for (int d = 0; d < GB_MAXDOM; d++) {
     cudaFree(o->bU[d]); cudaFree(o->bdU[d]); cudaFree(o->bE[d]); cudaFree(o->bdE[d]); cudaFree(o->bH[d]); cudaFree(o->bdH[d]);
   }
@@ -311,6 +325,9 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   o->schur = nullptr; o->schur_ok = 0; o->lu_schur = 0;
   o->schur64 = nullptr; o->have_blk64 = 0; o->refine_mode = 0;
   o->Bw = o->Xw = nullptr; o->have_xw = 0;
+  o->Axw = nullptr; o->have_axw = 0;
+  for (int d = 0; d < GB_MAXDOM; d++) o->GHdf[d][0] = o->GHdf[d][1] = nullptr;
+  o->have_ghdf = 0;
   o->lu_mode = 3;  // block elimination where the object allows it
   {  // GB_LU_MODE: the objects' initial gb_set_lu_pivoting mode (0..3)
     const char* e = getenv("GB_LU_MODE");
@@ -439,6 +456,7 @@ static void assembled(gb_obj* o, int precision) {
   o->have_lu32 = 0;
   o->have_blk64 = 0;
   o->have_xw = 0;
+  o->have_ghdf = 0;
   o->field_prec = precision >= 2 ? precision : 0;
 }
 
@@ -568,6 +586,7 @@ extern "C" int gb_cmatrix_upload(gb_obj* o, int did, const void* G, const void* 
   if (dF) GB_CUDA(cudaMemcpy(o->dF[did], dF, 3 * N * sizeof(double), cudaMemcpyHostToDevice));
   o->have_invA = 0;
   o->have_xw = 0;
+  o->have_ghdf = 0;
   return 0;
 }
 
@@ -812,6 +831,7 @@ extern "C" int gb_solve_mEMP(gb_obj* o) {
   }
   const bool warm = o->have_xw != 0;
   o->have_xw = 0;
+  if (!o->have_invA && !o->Axw && dalloc((void**)&o->Axw, na * sizeof(cplx))) return -1;
   if (!rc) rc = o->have_invA ? gbi_zgemv(o->invA, na, (int)na, (int)na, B, X, o->st) : ir_solve(o, B, X, warm);
   for (int d = 0; d <= o->m.MN && !rc; d++) rc = gbi_store_bv(X, &o->m, o->kn_dev, o->Ui, o->dUi, d, o->bU[d], o->bdU[d], o->st);
   if (!rc) rc = sync_obj(o, "gb_solve_mEMP");
@@ -1264,6 +1284,37 @@ extern "C" int gb_lu_info(gb_obj* o, int* rbt, int* fallbacks) {
   return 0;
 }
 
+// double-float copies of G and H (for the GMRES products); 0 when present
+static int ensure_ghdf(gb_obj* o) {
+  if (o->have_ghdf) return 0;
+  for (int d = 0; d <= o->m.MN; d++) {
+    const size_t N = 4 * (size_t)o->m.sb_Ne[d];
+    if (N == 0) continue;
+    for (int i = 0; i < 2; i++) {
+      if (!o->GHdf[d][i] && cudaMalloc(&o->GHdf[d][i], N * N * 16) != cudaSuccess) {
+        cudaGetLastError();
+        o->GHdf[d][i] = nullptr;
+        return 1;  // no room: the products stay in FP64
+      }
+      if (gbi_to_df(N * N, i ? o->H[d] : o->G[d], o->GHdf[d][i], o->st)) return -1;
+    }
+  }
+  o->have_ghdf = 1;
+  return 0;
+}
+
+// y = A x with G and H in double-float (PQ, PQd: scratch of 8 N_max entries)
+static int apply_A_df(gb_obj* o, const cplx* x, cplx* PQ, void* PQd, cplx* y) {
+  size_t base = 0;
+  for (int d = 0; d <= o->m.MN; d++) {
+    if (gbi_apply_A_domain_df(o->GHdf[d][0], o->GHdf[d][1], o->m.sid + o->m.sb_off[d], o->rowk[d], &o->m, o->kn_dev,
+                              d, o->nrows[d], base, x, PQ, PQd, y, o->st))
+      return -1;
+    base += 4 * (size_t)o->nrows[d];
+  }
+  return 0;
+}
+
 // y = A x in FP64 from G and H (PQ: scratch of 8 N_max complex)
 static int apply_A(gb_obj* o, const cplx* x, cplx* PQ, cplx* y) {
   size_t base = 0;
@@ -1373,40 +1424,59 @@ static int precond(gb_obj* o, const cplx* v, cplx* z, cplxf* d, cplxf* d2, cudaS
 // LU mode 2, after its first iteration) refactorises with tournament
 // pivoting and continues from the current x.
 static int ir_solve(gb_obj* o, const cplx* B, cplx* X, bool warm) {
-  if (o->refine_mode == 1) return ir_classical(o, B, X);
+  if (o->refine_mode == 1) {
+    o->have_axw = 0;
+    return ir_classical(o, B, X);
+  }
   const size_t na = o->na;
   size_t nmax = 0;
   for (int d = 0; d <= o->m.MN; d++) nmax = std::max(nmax, 4 * (size_t)o->m.sb_Ne[d]);
   cplx* PQ = nullptr;
+  void* PQd = nullptr;
   cplxf *d = nullptr, *d2 = nullptr;
-  if (dalloc((void**)&PQ, 8 * nmax * sizeof(cplx)) || dalloc((void**)&d, na * sizeof(cplxf)) ||
-      dalloc((void**)&d2, na * sizeof(cplxf))) {
-    cudaFree(PQ); cudaFree(d);
+  if (dalloc((void**)&PQ, 8 * nmax * sizeof(cplx)) || dalloc(&PQd, 8 * nmax * 16) ||
+      dalloc((void**)&d, na * sizeof(cplxf)) || dalloc((void**)&d2, na * sizeof(cplxf))) {
+    cudaFree(PQ); cudaFree(PQd); cudaFree(d);
     return -1;
   }
   GbOp A = [o, PQ](const cplx* x, cplx* y, cudaStream_t) { return apply_A(o, x, PQ, y); };
+  GbOp Adf = [o, PQ, PQd](const cplx* x, cplx* y, cudaStream_t) { return apply_A_df(o, x, PQ, PQd, y); };
   GbOp M = [o, d, d2](const cplx* v, cplx* z, cudaStream_t st) { return precond(o, v, z, d, d2, st); };
   int rc = 0;
-  // from the previous solution with the same factors (warm), else from zero
+  // lower-precision factors: the iterations' products in double-float
+  // (every true residual, the convergence test, stays FP64); the FP64 block
+  // factors of the plain FP64 form keep FP64 products
+  const GbOp* Af = nullptr;
+  if (!o->have_blk64) {
+    const int e = ensure_ghdf(o);
+    if (e < 0) rc = -1;
+    else if (e == 0) Af = &Adf;
+  }
+  // from the previous solution with the same factors (warm), else from zero;
+  // warm, the previous solve's last FP64 product A x gives the first residual
   if (!warm && cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess) { gbi_set_error("ir_solve: memset"); rc = -1; }
-  int it = 0, tot = 0;
+  const cplx* ax0 = (warm && o->have_axw) ? o->Axw : nullptr;
+  o->have_axw = 0;
+  int it = 0, tot = 0, axok = 0;
   double rel = 1.0;
   const bool forced = o->lu_mode == 2 && o->lu_rbt;  // diagnostic: the fallback after one iteration
-  int r = rc ? -1 : gbi_gmres(na, B, X, !warm, A, M, 20, 1e-13, forced ? 1 : 60, o->st, &it, &rel);
+  int r = rc ? -1
+             : gbi_gmres(na, B, X, !warm, A, Af, M, 20, 1e-13, forced ? 1 : 60, o->st, ax0, o->Axw, &axok, &it, &rel);
   tot += it;
   if (r == 1 && !o->have_blk64 && (o->lu_rbt || o->lu_schur)) {
     if (!(rel < 1.0) && cudaMemsetAsync(X, 0, na * sizeof(cplx), o->st) != cudaSuccess) r = -1;
     if (r == 1 && refactor_pivoted(o)) r = -1;
     if (r == 1) {
-      r = gbi_gmres(na, B, X, !(rel < 1.0), A, M, 20, 1e-13, 60, o->st, &it, &rel);
+      r = gbi_gmres(na, B, X, !(rel < 1.0), A, Af, M, 20, 1e-13, 60, o->st, nullptr, o->Axw, &axok, &it, &rel);
       tot += it;
     }
   }
+  o->have_axw = (r == 0 && axok) ? 1 : 0;
   o->ir_iters = tot;
   o->ir_relres = rel;
   if (r < 0) rc = -1;
   else if (r == 1 || rel > 1e-10) { gbi_set_error("iterative refinement stalled at relative residual %g", rel); rc = -1; }
-  cudaFree(PQ); cudaFree(d); cudaFree(d2);
+  cudaFree(PQ); cudaFree(PQd); cudaFree(d); cudaFree(d2);
   return rc;
 }
 

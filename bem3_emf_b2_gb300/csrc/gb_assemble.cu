@@ -1276,7 +1276,8 @@ static int lq_stage(GbLqList& L, cudaStream_t st) {
   float *X = nullptr, *Y = nullptr, *nrm = nullptr;
   int* idx = nullptr;
   double* err = nullptr;
-  const int m = std::min(n, 2048);
+  // the judged sample: every 16th pair (at least 64, at most 2,048)
+  const int m = std::min(n, std::min(2048, std::max(64, n / 16)));
   GB_CUDA(cudaMallocAsync((void**)&X, (size_t)n * GB_LQ_NIN * sizeof(float), st));
   GB_CUDA(cudaMallocAsync((void**)&Y, (size_t)n * GB_LQ_NOUT * sizeof(float), st));
   GB_CUDA(cudaMallocAsync((void**)&nrm, 2 * (GB_LQ_NIN + GB_LQ_NOUT) * sizeof(float), st));

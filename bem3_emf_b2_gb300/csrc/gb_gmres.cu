@@ -134,10 +134,17 @@ struct Work {
 // reduce the true residual 10x while far from the target), -1 on error.
 // *iters: iterations (preconditioner solves) done, *relres: the last true
 // relative residual.  Synchronises st.
-extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const GbOp& A, const GbOp& M, int m,
-                         double tol, int maxit, cudaStream_t st, int* iters, double* relres) {
+// Af (may be null): the operator of the Arnoldi products (a lower-precision
+// application of A); every true residual still uses A.  Ax0 (may be null,
+// only with !x_zero): A x for the initial x, so the first residual takes no
+// product.  Ax_out (may be null): on convergence, A x of the returned x;
+// *ax_ok (with Ax_out) 1 when it was written.
+extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const GbOp& A, const GbOp* Af, const GbOp& M,
+                         int m, double tol, int maxit, cudaStream_t st, const cplx* Ax0, cplx* Ax_out, int* ax_ok,
+                         int* iters, double* relres) {
   *iters = 0;
   *relres = 1.0;
+  if (ax_ok) *ax_ok = 0;
   if (n == 0) return 0;
   if (m < 1) m = 1;
   Work W;
@@ -174,14 +181,21 @@ extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const Gb
   int it = 0, status = 1;
   double prev_cycle = -1.0;
   bool first = true;
+  const cplx* ax = nullptr;  // where A x of the current x is, if known
   while (!rc) {
     // true residual r = b - A x
     if (first && x_zero) {
       if (cudaMemcpyAsync(r, b, n * sizeof(cplx), cudaMemcpyDeviceToDevice, st) != cudaSuccess) { rc = -1; break; }
+      ax = nullptr;
+    } else if (first && Ax0) {
+      k_gs_sub<<<W.grid(), 256, 0, st>>>(b, Ax0, n, r);
+      gbi_count_launch();
+      ax = Ax0;
     } else {
       if (A(x, w, st)) { rc = -1; break; }
       k_gs_sub<<<W.grid(), 256, 0, st>>>(b, w, n, r);
       gbi_count_launch();
+      ax = w;
     }
     first = false;
     if (W.dots(r, n, 1, r, yd)) { rc = -1; break; }
@@ -191,7 +205,15 @@ extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const Gb
     const double beta = sqrt(hr.x);
     const double rel = bnorm > 0.0 ? beta / bnorm : 0.0;
     *relres = rel;
-    if (!(rel > tol)) { status = (rel == rel) ? 0 : 1; break; }
+    if (!(rel > tol)) {
+      status = (rel == rel) ? 0 : 1;
+      if (status == 0 && Ax_out && ax) {
+        if (ax != Ax_out &&
+            cudaMemcpyAsync(Ax_out, ax, n * sizeof(cplx), cudaMemcpyDeviceToDevice, st) != cudaSuccess) { rc = -1; break; }
+        if (ax_ok) *ax_ok = 1;
+      }
+      break;
+    }
     if (it >= maxit) break;
     // a cycle that did not reduce the residual 10x (far from the target) stalls
     if (prev_cycle > 0.0 && rel > 0.1 * prev_cycle && rel > 1e3 * tol) break;
@@ -206,7 +228,7 @@ extern "C" int gbi_gmres(size_t n, const cplx* b, cplx* x, bool x_zero, const Gb
       cplx* vj = V + (size_t)j * n;
       cplx* zj = Z + (size_t)j * n;
       if (M(vj, zj, st)) { rc = -1; break; }
-      if (A(zj, w, st)) { rc = -1; break; }
+      if ((Af ? (*Af)(zj, w, st) : A(zj, w, st))) { rc = -1; break; }
       it++;
       // classical Gram-Schmidt, twice
       if (W.dots(V, n, j + 1, w, h2)) { rc = -1; break; }

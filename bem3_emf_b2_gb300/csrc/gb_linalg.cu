@@ -39,6 +39,7 @@
 // 256-column outer block, the trailing matrix is updated once per outer
 // block with K = 256.
 #include "gb_common.cuh"
+#include "gb_df64.cuh"
 #include "gb_internal.h"
 #include <vector>
 
@@ -295,6 +296,86 @@ __global__ void k_apply_rows(const cplx* __restrict__ G, const cplx* __restrict_
     for (int o = 16; o > 0; o >>= 1) acc[i] += __shfl_down_sync(0xffffffffu, acc[i], o);
   if (lane == 0)
     for (int q = 0; q < 4; q++) y[base + (size_t)q * nrows + k] = cmk(acc[2 * q], acc[2 * q + 1]);
+}
+
+// complex FP64 to double-float (float4: re.hi, re.lo, im.hi, im.lo)
+__global__ void k_to_df(size_t n, const cplx* __restrict__ src, float4* dst) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const cplx v = src[i];
+  const float a = (float)v.x, b = (float)v.y;
+  dst[i] = make_float4(a, (float)(v.x - (double)a), b, (float)(v.y - (double)b));
+}
+
+extern "C" int gbi_to_df(size_t n, const cplx* src, void* dst, cudaStream_t st) {
+  if (n == 0) return 0;
+  k_to_df<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, src, (float4*)dst);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
+__device__ __forceinline__ dfc dfc_ld4(const float4 f) { return dfcmk(dfmk(f.x, f.y), dfmk(f.z, f.w)); }
+// acc + a b, complex double-float
+__device__ __forceinline__ dfc dfc_mac(dfc acc, dfc a, dfc b) {
+  dfc r;
+  r.re = df_fma(df_fma(acc.re, a.re, b.re), df_neg(a.im), b.im);
+  r.im = df_fma(df_fma(acc.im, a.re, b.im), a.im, b.re);
+  return r;
+}
+
+// k_apply_rows with the matrices and node vectors in double-float: the
+// products of the GMRES iterations on the FP32 pipes (the FP64 version is
+// bound by the DFMA rate); sums finished in FP64
+__global__ void k_apply_rows_df(const float4* __restrict__ G, const float4* __restrict__ H, const int* rowk, int Ne,
+                                int nrows, size_t base, const float4* __restrict__ PQ, cplx* y) {
+  const int lane = threadIdx.x & 31;
+  const size_t N = (size_t)Ne * 4;
+  size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (row >= N) return;
+  int k = rowk[row];
+  if (k < 0) return;
+  const float4* g = G + row * N;
+  const float4* h = H + row * N;
+  const df z = dfmk(0.0f, 0.0f);
+  dfc acc[4];
+#pragma unroll
+  for (int q = 0; q < 4; q++) acc[q] = dfcmk(z, z);
+  for (size_t c = lane; c < N; c += 32) {
+    const dfc gv = dfc_ld4(g[c]), hv = dfc_ld4(h[c]);
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const dfc p = dfc_ld4(PQ[(size_t)q * N + c]), qq = dfc_ld4(PQ[(size_t)(4 + q) * N + c]);
+      acc[q] = dfc_mac(dfc_mac(acc[q], hv, p), gv, qq);
+    }
+  }
+  double s[8];
+#pragma unroll
+  for (int q = 0; q < 4; q++) { s[2 * q] = df_to(acc[q].re); s[2 * q + 1] = df_to(acc[q].im); }
+  for (int i = 0; i < 8; i++)
+    for (int o = 16; o > 0; o >>= 1) s[i] += __shfl_down_sync(0xffffffffu, s[i], o);
+  if (lane == 0)
+    for (int q = 0; q < 4; q++) y[base + (size_t)q * nrows + k] = cmk(s[2 * q], s[2 * q + 1]);
+}
+
+extern "C" int gbi_apply_A_domain_df(const void* Gd, const void* Hd, const int* sid, const int* rowk,
+                                     const GbMeshDev* m, const double* kn_dev, int did, int nrows, size_t base,
+                                     const cplx* x, cplx* PQ, void* PQd, cplx* y, cudaStream_t st) {
+  const int Ne = m->sb_Ne[did];
+  const size_t N = (size_t)Ne * 4;
+  if (N == 0) return 0;
+  PQArgs a;
+  a.sid = sid; a.eni = m->eni; a.md = m->md; a.sd = m->sd; a.etype = m->etype; a.wen = m->wen; a.kn = kn_dev;
+  a.Ne = Ne; a.did = did; a.nn = (size_t)m->NN; a.x = x; a.PQ = PQ;
+  k_pq_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(a);
+  gbi_count_launch();
+  k_to_df<<<(unsigned)((8 * N + 255) / 256), 256, 0, st>>>(8 * N, PQ, (float4*)PQd);
+  gbi_count_launch();
+  k_apply_rows_df<<<(unsigned)((N * 32 + 255) / 256), 256, 0, st>>>((const float4*)Gd, (const float4*)Hd, rowk, Ne,
+                                                                     nrows, base, (const float4*)PQd, y);
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
 }
 
 extern "C" int gbi_apply_A_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,

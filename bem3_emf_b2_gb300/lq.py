@@ -10,7 +10,7 @@ against the 64 x 64 rule, keeping the correction only if the sample's RMS
 error is within the tolerance.
 
 train() collects such pairs from a seeded family of quadrangle meshes --
-cubed spheres and cubes of random size, resolution and refractive index,
+coarse cubed spheres, cubes and cuboids of random size, resolution and index,
 both domains of each -- labels them on the GPU (both rules in FP64) and
 trains the network there.
 """
@@ -51,20 +51,25 @@ def enable(on=True, tol=1e-7):
 
 
 def training_meshes(seed):
-    """An endless seeded sequence of (nodes, elems, n_inside, lambda0)."""
+    """An endless seeded sequence of (nodes, elems, n_inside, lambda0):
+    coarse cubed spheres, cubes and cuboids (edges and curvature are where
+    the fallback rule is needed), random size and refractive index."""
     rng = np.random.default_rng(seed)
     while True:
-        if rng.random() < 0.8:
-            nf = int(rng.integers(6, 21))
-            nodes, elems = meshgen.cubed_sphere(nf, float(np.exp(rng.uniform(np.log(0.3), np.log(3.0)))))
-        else:
-            nf = int(rng.integers(6, 17))
-            nodes, elems = meshgen.cube(nf, float(np.exp(rng.uniform(np.log(0.5), np.log(6.0)))))
+        u = rng.random()
+        size = float(np.exp(rng.uniform(np.log(0.3), np.log(4.0))))
+        if u < 0.4:
+            nodes, elems = meshgen.cubed_sphere(int(rng.integers(2, 9)), size)
+        elif u < 0.7:
+            nodes, elems = meshgen.cube(int(rng.integers(3, 17)), size)
+        else:  # cuboid: a cube stretched along its axes (elements of aspect ratio up to 3)
+            nodes, elems = meshgen.cube(int(rng.integers(3, 13)), size)
+            nodes = nodes * rng.uniform(0.5, 1.5, 3)
         n_in = complex(rng.uniform(1.1, 2.6), rng.uniform(0.0, 0.05))
         yield nodes, elems, n_in, 1.0
 
 
-def collect(target, seed=1, max_meshes=400, log=None):
+def collect(target, seed=1, max_meshes=4000, log=None):
     """List fallback quadrangle pairs from training meshes until `target`
     pairs are held; returns the count."""
     L = _api()

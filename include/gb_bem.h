@@ -272,8 +272,9 @@ int gb_scene_step(gb_obj *o, int form, int type);
  * With a trained network enabled, a precision >= 2 assembly keeps such a
  * quadrangle pair's 12 x 12 values and adds the network's prediction of the
  * difference between the two rules (G, H, dG, dH, F, dF); every assembly
- * then checks a sample of up to 2,048 of its corrected pairs against the
- * 64 x 64 rule and, if the sample's RMS error (largest output error over
+ * then checks a sample of its corrected pairs (every 16th, at least 64, at
+ * most 2,048) against the 64 x 64 rule and, if the sample's RMS error
+ * (largest output error over
  * the pair's largest output, in size-scaled units) exceeds tol, integrates
  * all of them by that rule.  FP64 (precision 0) assemblies never use it.
  * gb_lq_collect(1): later precision >= 2 assemblies list their fallback
