@@ -30,8 +30,9 @@ int gbi_zgetrf(cplx* A, size_t lda, int n, int64_t* ipiv, int* info, cudaStream_
 int gbi_zgetrs(const cplx* LU, size_t lda, int n, const int64_t* ipiv, cplx* X, size_t ldx, int nrhs, cudaStream_t st);
 int gbi_zinverse(const cplx* LU, size_t lda, int n, const int64_t* ipiv, cplx* X, size_t ldx, cudaStream_t st);
 int gbi_zgemv(const cplx* M, size_t ldm, int n, int ncol, const cplx* x, cplx* y, cudaStream_t st);
-int gbi_build_B(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m, const double* kn_dev,
-                const cplx* Ui, const cplx* dUi, int did, int nrows, size_t base, cplx* B, cudaStream_t st);
+int gbi_build_B(const cplx* G, const cplx* H, const void* Gd, const void* Hd, const int* sid, const int* rowk,
+                const GbMeshDev* m, const double* kn_dev, const cplx* Ui, const cplx* dUi, int did, int nrows, size_t base,
+                cplx* B, cudaStream_t st);
 int gbi_store_bv(const cplx* X, const GbMeshDev* m, const double* kn_dev, const cplx* Ui, const cplx* dUi, int did,
                  cplx* U, cplx* dU, cudaStream_t st);
 int gbi_eh_bv(const cplx* dG, const cplx* dH, const double* dF, const GbMeshDev* m, int did, double lambda0,
@@ -807,6 +808,7 @@ static int sync_obj(gb_obj* o, const char* what) {
 }
 
 static int ir_solve(gb_obj* o, const cplx* B, cplx* X, bool warm);
+static int ensure_ghdf(gb_obj* o);
 
 extern "C" int gb_solve_mEMP(gb_obj* o) {
   if (!o->have_invA && !o->have_lu32 && !o->have_blk64) {
@@ -823,10 +825,18 @@ extern "C" int gb_solve_mEMP(gb_obj* o) {
   cplx *B = o->Bw, *X = o->Xw;
   int rc = 0;
   size_t base = 0;
+  // lower-precision factors (the chosen form): B's products in double-float
+  bool df = false;
+  if (!o->have_invA && !o->have_blk64) {
+    const int e = ensure_ghdf(o);
+    if (e < 0) return -1;
+    df = e == 0;
+  }
   for (int d = 0; d <= o->m.MN && !rc; d++) {
     if (!o->G[d]) { gbi_set_error("gb_solve_mEMP: domain %d has no coefficient matrices", d); rc = -1; break; }
-    rc = gbi_build_B(o->G[d], o->H[d], o->m.sid + o->m.sb_off[d], o->rowk[d], &o->m, o->kn_dev, o->Ui, o->dUi, d,
-                     o->nrows[d], base, B, o->st);
+    rc = gbi_build_B(o->G[d], o->H[d], df ? o->GHdf[d][0] : nullptr, df ? o->GHdf[d][1] : nullptr,
+                     o->m.sid + o->m.sb_off[d], o->rowk[d], &o->m, o->kn_dev, o->Ui, o->dUi, d, o->nrows[d], base, B,
+                     o->st);
     base += 4 * (size_t)o->nrows[d];
   }
   const bool warm = o->have_xw != 0;

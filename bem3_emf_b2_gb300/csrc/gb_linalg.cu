@@ -378,6 +378,25 @@ extern "C" int gbi_apply_A_domain_df(const void* Gd, const void* Hd, const int* 
   return 0;
 }
 
+// y rows of H P + G Q for a gathered PQ [8][N]: FP64, or with Gd, Hd
+// (double-float copies of G, H) on the FP32 pipes (PQd: scratch of 8 N float4)
+extern "C" int gbi_rows_apply(const cplx* G, const cplx* H, const void* Gd, const void* Hd, const int* rowk, int Ne,
+                              int nrows, size_t base, cplx* PQ, void* PQd, cplx* y, cudaStream_t st) {
+  const size_t N = (size_t)Ne * 4;
+  if (N == 0) return 0;
+  if (Gd && Hd) {
+    k_to_df<<<(unsigned)((8 * N + 255) / 256), 256, 0, st>>>(8 * N, PQ, (float4*)PQd);
+    gbi_count_launch();
+    k_apply_rows_df<<<(unsigned)((N * 32 + 255) / 256), 256, 0, st>>>((const float4*)Gd, (const float4*)Hd, rowk, Ne,
+                                                                       nrows, base, (const float4*)PQd, y);
+  } else {
+    k_apply_rows<<<(unsigned)((N * 32 + 255) / 256), 256, 0, st>>>(G, H, rowk, Ne, nrows, base, PQ, y);
+  }
+  gbi_count_launch();
+  GB_CUDA(cudaGetLastError());
+  return 0;
+}
+
 extern "C" int gbi_apply_A_domain(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
                                   const double* kn_dev, int did, int nrows, size_t base, const cplx* x, cplx* PQ, cplx* y,
                                   cudaStream_t st) {

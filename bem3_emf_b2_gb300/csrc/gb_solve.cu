@@ -1,7 +1,9 @@
 // gb_solve.cu -- kernels of the multi-object iteration (reference mo_solve.c).
 //
-//   k_build_B   right-hand side B of the coupled system from the incident
-//               potential at the exterior nodes (create_Bmatrix_dac, mo_solve.c:150-244)
+//   k_build_B_prep + k_b_gather  right-hand side B of the coupled system
+//               from the incident potential at the exterior nodes
+//               (create_Bmatrix_dac, mo_solve.c:150-244) as rows of H P + G Q
+//               (the row product of gb_linalg.cu)
 //   k_store_bv  unpack X = invA B into U, dU of every domain (tmatrix_bd_store :457-545)
 //   k_eh_bv     E, H at the nodes from U, dU and the tangential derivative
 //               matrices dG, dH, dF (solve_eh_bv :547-661)
@@ -35,7 +37,7 @@ struct BArgs {
   cplx* B;
 };
 
-// per source element of the domain, the constants k_build_B needs: the
+// per source element of the domain, the constants of the right-hand side: the
 // interface factors of its (main, sub) media and the unit normals at its
 // nodes (the same operations as before, done once per element instead of
 // once per row and component)
@@ -66,62 +68,63 @@ __global__ void k_build_B_prep(BArgs a, BElem* E) {
   E[s - 1] = e;
 }
 
-__global__ void k_build_B(BArgs a, const BElem* __restrict__ E) {
-  const int lane = threadIdx.x & 31;
-  size_t w = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  size_t N = (size_t)a.Ne * 4;
-  if (w >= 4 * N) return;
-  int row = (int)(w % N), cid = (int)(w / N);
-  int k = a.rowk[row];
-  if (k < 0) return;
-  const cplx* g = a.G + (size_t)row * N;
-  const cplx* h = a.H + (size_t)row * N;
-  double br = 0.0, bi = 0.0;
-  for (int s = 1 + lane; s <= a.Ne; s += 32) {
-    const BElem& e = E[s - 1];
-    if (!e.active) continue;
-    const int asd = e.asd, nl = e.nl;
-    const cplx delt = e.delt, beps = e.beps, sigm = e.sigm;
-    for (int l = 0; l < nl; l++) {
-      const double vn[3] = {e.vn[l][0], e.vn[l][1], e.vn[l][2]};
-      cplx tg = g[(size_t)(s - 1) * 4 + l], th = h[(size_t)(s - 1) * 4 + l];
-      const cplx* ui = a.Ui + ((size_t)asd * 4 + l) * 4;
-      const cplx* dui = a.dUi + ((size_t)asd * 4 + l) * 4;
-      cplx t;
-      if (cid < 3) {
-        t = -(th * ui[cid]) - tg * dui[cid] - (tg * ui[3]) * (delt * vn[cid]);
-      } else {
-        cplx un = ui[0] * vn[0] + ui[1] * vn[1] + ui[2] * vn[2];
-        t = -(th * ui[3]) - sigm * (tg * un) - beps * (tg * dui[3]);
-      }
-      br += t.x;
-      bi += t.y;
+
+// The same right-hand side as the rows of H P + G Q: per column (source
+// element s, node l) the four components of P = -Ui and of Q = -(dUi + the
+// interface terms) -- the column form of the reference's row sum, so that B is
+// one product of G and H with four vectors (k_apply_rows / _df)
+__global__ void k_b_gather(BArgs a, const BElem* __restrict__ E, cplx* PQ) {
+  const size_t N = (size_t)a.Ne * 4;
+  const size_t col = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= N) return;
+  const int s = (int)(col / 4) + 1, l = (int)(col % 4);
+  const BElem& e = E[s - 1];
+  cplx P[4], Q[4];
+  for (int q = 0; q < 4; q++) { P[q] = cmk(0.0, 0.0); Q[q] = cmk(0.0, 0.0); }
+  if (e.active && l < e.nl) {
+    const cplx* ui = a.Ui + ((size_t)e.asd * 4 + l) * 4;
+    const cplx* dui = a.dUi + ((size_t)e.asd * 4 + l) * 4;
+    const double* vn = e.vn[l];
+    for (int c = 0; c < 3; c++) {
+      P[c] = -ui[c];
+      Q[c] = -(dui[c] + ui[3] * (e.delt * vn[c]));
     }
+    const cplx un = ui[0] * vn[0] + ui[1] * vn[1] + ui[2] * vn[2];
+    P[3] = -ui[3];
+    Q[3] = -(e.sigm * un + e.beps * dui[3]);
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    br += __shfl_down_sync(0xffffffffu, br, o);
-    bi += __shfl_down_sync(0xffffffffu, bi, o);
-  }
-  if (lane == 0) a.B[a.base + (size_t)cid * a.nrows + k] = cmk(br, bi);
+  for (int q = 0; q < 4; q++) { PQ[(size_t)q * N + col] = P[q]; PQ[(size_t)(4 + q) * N + col] = Q[q]; }
 }
 
-extern "C" int gbi_build_B(const cplx* G, const cplx* H, const int* sid, const int* rowk, const GbMeshDev* m,
-                           const double* kn_dev, const cplx* Ui, const cplx* dUi, int did, int nrows, size_t base, cplx* B,
-                           cudaStream_t st) {
+extern "C" int gbi_rows_apply(const cplx* G, const cplx* H, const void* Gd, const void* Hd, const int* rowk, int Ne,
+                              int nrows, size_t base, cplx* PQ, void* PQd, cplx* y, cudaStream_t st);
+
+// B of one domain; Gd, Hd (may be null): double-float copies of G, H, which
+// take the products onto the FP32 pipes (the chosen form)
+extern "C" int gbi_build_B(const cplx* G, const cplx* H, const void* Gd, const void* Hd, const int* sid,
+                           const int* rowk, const GbMeshDev* m, const double* kn_dev, const cplx* Ui, const cplx* dUi,
+                           int did, int nrows, size_t base, cplx* B, cudaStream_t st) {
   BArgs a;
   a.G = G; a.H = H; a.sid = sid; a.rowk = rowk; a.md = m->md; a.sd = m->sd; a.etype = m->etype; a.wen = m->wen;
   a.kn = kn_dev; a.Ui = Ui; a.dUi = dUi; a.Ne = m->sb_Ne[did]; a.did = did; a.nrows = nrows; a.base = base; a.B = B;
-  size_t warps = 4 * 4 * (size_t)a.Ne;
-  if (warps == 0) return 0;
+  const size_t N = 4 * (size_t)a.Ne;
+  if (N == 0) return 0;
   BElem* E = nullptr;
+  cplx* PQ = nullptr;
+  void* PQd = nullptr;
   GB_CUDA(cudaMallocAsync((void**)&E, (size_t)a.Ne * sizeof(BElem), st));
+  GB_CUDA(cudaMallocAsync((void**)&PQ, 8 * N * sizeof(cplx), st));
+  if (Gd) GB_CUDA(cudaMallocAsync(&PQd, 8 * N * 16, st));
   k_build_B_prep<<<(unsigned)((a.Ne + 127) / 128), 128, 0, st>>>(a, E);
   gbi_count_launch();
-  k_build_B<<<(unsigned)((warps * 32 + 255) / 256), 256, 0, st>>>(a, E);
+  k_b_gather<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(a, E, PQ);
   gbi_count_launch();
-  cudaFreeAsync(E, st);
   GB_CUDA(cudaGetLastError());
-  return 0;
+  const int rc = gbi_rows_apply(G, H, Gd, Hd, rowk, a.Ne, nrows, base, PQ, PQd, B, st);
+  cudaFreeAsync(E, st);
+  cudaFreeAsync(PQ, st);
+  if (PQd) cudaFreeAsync(PQd, st);
+  return rc;
 }
 
 struct StoreArgs {
