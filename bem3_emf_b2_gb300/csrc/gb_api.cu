@@ -941,8 +941,12 @@ extern "C" int gb_add_scattered(gb_obj* dst, gb_obj* src, int type) {
     gbi_set_error("scattered field domain id error!(overlapped). domain id=%d", e->bad - 1000);
     return -1;
   }
+  // stream-ordered scratch: no device-wide synchronisation (objects of a
+  // multiple-scattering sweep run concurrently)
   cplx* out = nullptr;
-  if (dalloc((void**)&out, (size_t)n * 8 * sizeof(cplx))) return -1;
+  int* bad = nullptr;
+  GB_CUDA(cudaMallocAsync((void**)&out, (size_t)n * 8 * sizeof(cplx), dst->st));
+  GB_CUDA(cudaMallocAsync((void**)&bad, sizeof(int), dst->st));
   int rc = 0;
   if (e->Gm) {
     rc = gbi_cross_apply(n, e->C, e->Gm, e->Hm, e->dGm, e->dHm, e->Fp, src->bU[0], src->bdU[0], out, e->df, dst->st);
@@ -950,30 +954,26 @@ extern "C" int gb_add_scattered(gb_obj* dst, gb_obj* src, int type) {
     FieldObj f = field_view(src);
     rc = gbi_field(&f, 3, type, n, dst->ext_r, dst->ext_v, e->did, out, nullptr, dst->st);
   }
-  int* bad = nullptr;
-  if (!rc && dalloc((void**)&bad, sizeof(int))) rc = -1;
   if (!rc && cudaMemsetAsync(bad, 0, sizeof(int), dst->st) != cudaSuccess) rc = -1;
   if (!rc) rc = gbi_add_incident(n, dst->ext_idx, out, dst->Ui, dst->dUi, e->did, bad, dst->st);
+  cudaFreeAsync(out, dst->st);
+  cudaFreeAsync(bad, dst->st);
   if (!rc && cudaStreamSynchronize(dst->st) != cudaSuccess) {
     gbi_set_error("gb_add_scattered: %s", cudaGetErrorString(cudaGetLastError()));
     rc = -1;
   }
-  cudaFree(out);
-  cudaFree(bad);
   return rc;
 }
 
 extern "C" int gb_ccd_sums(gb_obj* o, double* hout) {
   if (ensure_bv(o)) return -1;
   double* out = nullptr;
-  if (dalloc((void**)&out, 3 * sizeof(double))) return -1;
+  GB_CUDA(cudaMallocAsync((void**)&out, 3 * sizeof(double), o->st));
   int rc = gbi_ccd(o->m.Ne, o->m.md, o->Ui, o->Uip, out, o->st);
-  if (!rc && (cudaMemcpyAsync(hout, out, 3 * sizeof(double), cudaMemcpyDeviceToHost, o->st) != cudaSuccess ||
-              cudaStreamSynchronize(o->st) != cudaSuccess)) {
-    gbi_set_error("gb_ccd_sums failed");
-    rc = -1;
-  }
-  cudaFree(out);
+  if (!rc && cudaMemcpyAsync(hout, out, 3 * sizeof(double), cudaMemcpyDeviceToHost, o->st) != cudaSuccess) rc = -1;
+  cudaFreeAsync(out, o->st);
+  if (!rc && cudaStreamSynchronize(o->st) != cudaSuccess) rc = -1;
+  if (rc) gbi_set_error("gb_ccd_sums failed");
   return rc;
 }
 
@@ -1444,11 +1444,11 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X, bool warm) {
   cplx* PQ = nullptr;
   void* PQd = nullptr;
   cplxf *d = nullptr, *d2 = nullptr;
-  if (dalloc((void**)&PQ, 8 * nmax * sizeof(cplx)) || dalloc(&PQd, 8 * nmax * 16) ||
-      dalloc((void**)&d, na * sizeof(cplxf)) || dalloc((void**)&d2, na * sizeof(cplxf))) {
-    cudaFree(PQ); cudaFree(PQd); cudaFree(d);
-    return -1;
-  }
+  // stream-ordered scratch (no device-wide synchronisation)
+  GB_CUDA(cudaMallocAsync((void**)&PQ, 8 * nmax * sizeof(cplx), o->st));
+  GB_CUDA(cudaMallocAsync(&PQd, 8 * nmax * 16, o->st));
+  GB_CUDA(cudaMallocAsync((void**)&d, na * sizeof(cplxf), o->st));
+  GB_CUDA(cudaMallocAsync((void**)&d2, na * sizeof(cplxf), o->st));
   GbOp A = [o, PQ](const cplx* x, cplx* y, cudaStream_t) { return apply_A(o, x, PQ, y); };
   GbOp Adf = [o, PQ, PQd](const cplx* x, cplx* y, cudaStream_t) { return apply_A_df(o, x, PQ, PQd, y); };
   GbOp M = [o, d, d2](const cplx* v, cplx* z, cudaStream_t st) { return precond(o, v, z, d, d2, st); };
@@ -1486,7 +1486,7 @@ static int ir_solve(gb_obj* o, const cplx* B, cplx* X, bool warm) {
   o->ir_relres = rel;
   if (r < 0) rc = -1;
   else if (r == 1 || rel > 1e-10) { gbi_set_error("iterative refinement stalled at relative residual %g", rel); rc = -1; }
-  cudaFree(PQ); cudaFree(PQd); cudaFree(d); cudaFree(d2);
+  cudaFreeAsync(PQ, o->st); cudaFreeAsync(PQd, o->st); cudaFreeAsync(d, o->st); cudaFreeAsync(d2, o->st);
   return rc;
 }
 

@@ -10,6 +10,7 @@
  * ITER_MAX) are the reference's.
  */
 #include "gb_host.h"
+#include <pthread.h>
 
 /* progress messages of mo_solve_bv (the reference's); off with gbh_set_quiet(1) */
 static int g_quiet=0;
@@ -192,6 +193,58 @@ static void gb_solve_coefficient_EH(int flg,DOMD *md)
   if(flg==1) MSG("finished. Elapsed time : %5g (sec)\n",difftime(me,ms));
 }
 
+/* One phase of an iteration for every object at once, one host thread per
+ * object (at most 16 at a time).  The iteration is a Jacobi sweep: every
+ * object's incident field takes the other objects' boundary values of the
+ * previous sweep (add_scattered_mEMP, mo_solve.c:296-349, reads them before
+ * any object solves again), so within a phase the objects are independent;
+ * each object's kernels run on its own stream, and the results are those of
+ * the sequential order bit for bit.  phase 0: the incident field plus the
+ * other objects' scattered potentials; 1: the boundary values; 2: E, H. */
+typedef struct { MOBJ *mo; int phase,dev; int *next; pthread_mutex_t *mu; } gb_phase_pool;
+
+static void gb_phase_object(MOBJ *mo,int m,int phase)
+{
+  if(phase==0){
+    if(gb_reset_incident(gb_dev(&mo->md[m]))) gb_die("mo_solve.c, reset_incident_bd()");
+    for(int d=0;d<mo->N;d++){
+      if(d==m) continue;
+      if(gb_add_scattered(gb_dev(&mo->md[d]),gb_dev(&mo->md[m]),PREC_DEF)) gb_die("mo_solve.c, add_scattered_mEMP()");
+    }
+  }
+  else if(phase==1){ if(gb_solve_mEMP(gb_dev(&mo->md[m]))) gb_die("mo_solve.c, solve_coefficient_mEMP()"); }
+  else { if(gb_solve_EH(gb_dev(&mo->md[m]))) gb_die("mo_solve.c, solve_coefficient_EH()"); }
+}
+
+static void *gb_phase_worker(void *p)
+{
+  gb_phase_pool *q=(gb_phase_pool *)p;
+  if(gb_use_device(q->dev)) gb_die("mo_solve.c, worker device");
+  for(;;){
+    pthread_mutex_lock(q->mu);
+    int m=(*q->next)++;
+    pthread_mutex_unlock(q->mu);
+    if(m>=q->mo->N) break;
+    gb_phase_object(q->mo,m,q->phase);
+  }
+  return NULL;
+}
+
+static void gb_phase_all(MOBJ *mo,int phase)
+{
+  int nt=mo->N<16?mo->N:16,next=0;
+  pthread_mutex_t mu=PTHREAD_MUTEX_INITIALIZER;
+  gb_phase_pool q={mo,phase,gb_current_device(),&next,&mu};
+  pthread_t th[16];
+  int started=0;
+  for(int i=0;i<nt;i++){
+    if(pthread_create(&th[i],NULL,gb_phase_worker,&q)) break;
+    started++;
+  }
+  if(started==0) gb_phase_worker(&q);  /* no thread available: here */
+  for(int i=0;i<started;i++) pthread_join(th[i],NULL);
+}
+
 static double gb_ccd_f(MOBJ *mo)
 {
   double us=0.0,ps=0.0,sc=0.0,out[3];
@@ -247,13 +300,8 @@ void mo_solve_bv(MOBJ *mo)
     time(&start);
     for(iter=2;iter<itermax;iter++){
       MSG("count =% 3d",iter);
-      for(int m=0;m<mo->N;m++) if(gb_reset_incident(gb_dev(&mo->md[m]))) gb_die("mo_solve.c, reset_incident_bd()");
-      for(int m=0;m<mo->N;m++)
-        for(int d=0;d<mo->N;d++){
-          if(d==m) continue;
-          if(gb_add_scattered(gb_dev(&mo->md[d]),gb_dev(&mo->md[m]),PREC_DEF)) gb_die("mo_solve.c, add_scattered_mEMP()");
-        }
-      for(int m=0;m<mo->N;m++) gb_solve_coefficient_mEMP(0,&mo->md[m]);
+      gb_phase_all(mo,0);
+      gb_phase_all(mo,1);
       double cc=gb_ccd_f(mo);
       g_last_iter=iter;
       g_last_cc=cc;
@@ -262,7 +310,7 @@ void mo_solve_bv(MOBJ *mo)
       if(cc<CCD && iter>ITER_MIN) break;
     }
     if(iter==itermax) MSG("The maximum number of iterations has been reached (The result has not converged).\n");
-    for(int m=0;m<mo->N;m++) gb_solve_coefficient_EH(0,&mo->md[m]);
+    gb_phase_all(mo,2);
     time(&end);
     MSG("finished. Elapsed time : %5g (sec)\n",difftime(end,start));
   }
