@@ -38,6 +38,7 @@ the path has no exchange step): value = max-over-ranks time / scenes.
 when it can finish a scene inside the run, else prints its `unavailable` line.
 """
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -359,6 +360,9 @@ def run_gpu(args):
     from bem3_emf_b2_gb300 import build, ktime_list, ktime_read, lib
     build.build()
     L = lib()
+    L.gb_set_tc_passes.argtypes = [ctypes.c_int]
+    if L.gb_set_tc_passes(args.tc_passes) != 0:
+        raise RuntimeError("gb_set_tc_passes(%d) refused" % args.tc_passes)
     wd = tempfile.mkdtemp(prefix="bench_")
     sc, desc = open_workload(args, wd)
     cones = args.workload in ("cones", "beams")
@@ -422,7 +426,8 @@ def run_gpu(args):
                                                                     args.workload != "beams") else None
         cfg = {"workload": desc["workload"], "objects": desc["objects"],
                "elements_per_object": desc["elements_per_object"], "na_per_object": desc["na_per_object"],
-               "form": "chosen (double-float quadrature, FP32 block elimination + FP64 refinement)",
+               "form": "chosen (double-float quadrature, FP32 block elimination (tensor-core passes: %d) + FP64 "
+                       "GMRES refinement)" % args.tc_passes,
                "parallelism": "replicas x%d" % ws,
                "l2": "working set larger than L2 (coefficient matrices %s) and a 256 MB L2 flush before each step" % (
                    {"cones": "2 x 29 GB", "beams": "8 x 0.1-0.4 GB"}.get(args.workload, "0.45 GB")),
@@ -660,6 +665,8 @@ def main():
     ap.add_argument("--profile-step", action="store_true",
                     help="profiling run: one chosen-form scene step after --warmup steps, nothing else, no JSON line")
     ap.add_argument("--faces3", type=int, default=24, help="quadrangles per cube face of the sphere3 workload")
+    ap.add_argument("--tc-passes", type=int, default=3, choices=[1, 3],
+                    help="tensor-core passes of the FP32 factorisations (gb_set_tc_passes)")
     ap.add_argument("--workload", choices=["cones", "sphere", "sphere3", "cube", "beams"], default="cones",
                     help="cones: the two-cone scene (default); sphere: the 384-element sphere; cube: assembly "
                          "throughput of the 38,400-element cube")
