@@ -381,7 +381,10 @@ def run_gpu(args):
     iters = sc.iteration() if cones else None
     # plain FP64 form (after the chosen form: its allocations are not in the line's steps)
     n64 = 1 if cones else max(1, min(args.steps, 2))
-    t64, F64, N64 = timed_steps(sc, 0, n64, 0, dist)
+    if args.no_fp64:  # a comparison run of the chosen form alone
+        t64, F64, N64 = [float("nan")], F32, N32
+    else:
+        t64, F64, N64 = timed_steps(sc, 0, n64, 0, dist)
     # e2e: device copies rebuilt from host memory every step (H2D), results read back (D2H)
     h2d, d2h = sc.h2d_bytes(), sc.d2h_bytes()
     te = []
@@ -439,9 +442,10 @@ def run_gpu(args):
                "data": "synthetic (meshgen %s)" % {"cones": "cones, seed 7", "beams": "batch_scene seed 11, random_waves seed 11"}.get(
                    args.workload, "cubed sphere, seeded by construction"),
                "config": cfg,
-               "fp64_form": {"s_per_scene": sum(t64) / len(t64), "steps": len(t64),
-                             "force_torque_rel_diff_vs_chosen": force_err,
-                             "form": "FP64 quadrature, FP64 block elimination (node LUs + inverses), FP64 E/H"},
+               "fp64_form": None if args.no_fp64 else {
+                   "s_per_scene": sum(t64) / len(t64), "steps": len(t64),
+                   "force_torque_rel_diff_vs_chosen": force_err,
+                   "form": "FP64 quadrature, FP64 block elimination (node LUs + inverses), FP64 E/H"},
                "force": np.asarray(F32).tolist(), "torque": np.asarray(N32).tolist(),
                "e2e": {"value": e2e, "unit": "s/scene", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                "gpu_launches": int(round(launches)), "clocks": clk.summary()}
@@ -665,6 +669,7 @@ def main():
     ap.add_argument("--profile-step", action="store_true",
                     help="profiling run: one chosen-form scene step after --warmup steps, nothing else, no JSON line")
     ap.add_argument("--faces3", type=int, default=24, help="quadrangles per cube face of the sphere3 workload")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 form (comparison runs of the chosen form)")
     ap.add_argument("--tc-passes", type=int, default=3, choices=[1, 3],
                     help="tensor-core passes of the FP32 factorisations (gb_set_tc_passes)")
     ap.add_argument("--workload", choices=["cones", "sphere", "sphere3", "cube", "beams"], default="cones",
