@@ -1076,14 +1076,23 @@ extern "C" int gb_solve_EH(gb_obj* o) {
 // from OpenMP loops): each calling thread runs them on its own stream, with
 // stream-ordered temporaries (no cudaFree and its device-wide synchronisation),
 // after the object's own stream has drained.
-static thread_local cudaStream_t t_point_stream[64];
+// the calling thread's stream per device for point evaluations, destroyed
+// when the thread ends (worker threads come and go)
+struct ThreadStreams {
+  cudaStream_t s[64] = {};
+  ~ThreadStreams() {
+    for (int d = 0; d < 64; d++)
+      if (s[d] && cudaSetDevice(d) == cudaSuccess) cudaStreamDestroy(s[d]);
+  }
+};
+static thread_local ThreadStreams t_point_stream;
 static int point_stream(gb_obj* o, cudaStream_t* st) {
   int dev = 0;
   GB_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) { gbi_set_error("device ordinal %d not supported", dev); return -1; }
-  if (!t_point_stream[dev]) GB_CUDA(cudaStreamCreateWithFlags(&t_point_stream[dev], cudaStreamNonBlocking));
+  if (!t_point_stream.s[dev]) GB_CUDA(cudaStreamCreateWithFlags(&t_point_stream.s[dev], cudaStreamNonBlocking));
   GB_CUDA(cudaStreamSynchronize(o->st));
-  *st = t_point_stream[dev];
+  *st = t_point_stream.s[dev];
   return 0;
 }
 

@@ -207,7 +207,15 @@ __global__ void k_beam_sum(int n, int T, int nb, const GbBeamDesc* beams, const 
       for (int i = 0; i < 6; i++) outs[g][(size_t)p * 6 + i] = acc[6 * g + i];
 }
 
-thread_local cudaStream_t t_beam_stream[64];
+// the calling thread's stream per device, destroyed when the thread ends
+struct BeamStreams {
+  cudaStream_t s[64] = {};
+  ~BeamStreams() {
+    for (int d = 0; d < 64; d++)
+      if (s[d] && cudaSetDevice(d) == cudaSuccess) cudaStreamDestroy(s[d]);
+  }
+};
+thread_local BeamStreams t_beam_stream;
 
 }  // namespace
 
@@ -226,8 +234,8 @@ extern "C" int gbi_beam_points(int nb, const GbBeamDesc* beams, int T, const int
     gbi_set_error("gbi_beam_points: device %d", dev);
     return -1;
   }
-  if (!t_beam_stream[dev]) GB_CUDA(cudaStreamCreateWithFlags(&t_beam_stream[dev], cudaStreamNonBlocking));
-  cudaStream_t st = t_beam_stream[dev];
+  if (!t_beam_stream.s[dev]) GB_CUDA(cudaStreamCreateWithFlags(&t_beam_stream.s[dev], cudaStreamNonBlocking));
+  cudaStream_t st = t_beam_stream.s[dev];
   // points in chunks: at most 256 MiB of node partial sums at a time
   const size_t per_point = (size_t)T * 24 * sizeof(double);
   int chunk = (int)(((size_t)256 << 20) / per_point);

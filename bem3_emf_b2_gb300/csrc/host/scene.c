@@ -188,6 +188,41 @@ static int mscene_factor(MOBJ *mo,int form,int type,double *ta_out,double *tf_ou
   return 0;
 }
 
+/* force and torque of every object at once (mo_force_FN per object, one
+ * host thread each, at most 16): the objects' sums are independent, their
+ * field evaluations run on each thread's own stream */
+struct force_pool { MOBJ *mo; const double *rc; double *F,*N; int dev,next,bad; pthread_mutex_t mu; };
+
+static void *force_worker(void *p)
+{
+  struct force_pool *q=(struct force_pool *)p;
+  if(gb_use_device(q->dev)){ q->bad=1; return NULL; }
+  for(;;){
+    pthread_mutex_lock(&q->mu);
+    int m=q->next++;
+    pthread_mutex_unlock(&q->mu);
+    if(m>=q->mo->N) break;
+    double c[3];
+    for(int i=0;i<3;i++) c[i]=q->rc?q->rc[3*m+i]:q->mo->md[m].tv[i];
+    if(mo_force_FN(q->F+3*m,q->N+3*m,c,m,0,q->mo)<0){ pthread_mutex_lock(&q->mu); q->bad=1; pthread_mutex_unlock(&q->mu); }
+  }
+  return NULL;
+}
+
+static int mscene_forces(MOBJ *mo,const double *rc,double *F,double *N)
+{
+  struct force_pool q;
+  q.mo=mo; q.rc=rc; q.F=F; q.N=N; q.dev=gb_current_device(); q.next=0; q.bad=0;
+  pthread_mutex_init(&q.mu,NULL);
+  int nt=mo->N<16?mo->N:16,started=0;
+  pthread_t th[16];
+  for(int i=0;i<nt;i++){ if(pthread_create(&th[i],NULL,force_worker,&q)) break; started++; }
+  if(started==0) force_worker(&q);
+  for(int i=0;i<started;i++) pthread_join(th[i],NULL);
+  pthread_mutex_destroy(&q.mu);
+  return q.bad?-1:0;
+}
+
 int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double *N)
 {
   double ta=0.0,tf=0.0;
@@ -195,11 +230,7 @@ int gbh_mscene_step(MOBJ *mo,int form,int type,const double *rc,double *F,double
   double t3=gbh_now();
   mo_solve_bv(mo);
   double t4=gbh_now();
-  for(int m=0;m<mo->N;m++){
-    double c[3];
-    for(int i=0;i<3;i++) c[i]=rc?rc[3*m+i]:mo->md[m].tv[i];
-    if(mo_force_FN(F+3*m,N+3*m,c,m,0,mo)<0) return -1;
-  }
+  if(mscene_forces(mo,rc,F,N)) return -1;
   g_phase[0]=ta; g_phase[1]=tf; g_phase[2]=t4-t3; g_phase[3]=gbh_now()-t4;
   return 0;
 }
@@ -245,11 +276,7 @@ int gbh_mscene_beams(MOBJ *mo,int form,int type,const char *beams_file,const dou
     double t3=gbh_now();
     mo_solve_bv(mo);
     double t4=gbh_now();
-    for(int m=0;m<mo->N && !rcode;m++){
-      double c[3];
-      for(int i=0;i<3;i++) c[i]=rc?rc[3*m+i]:mo->md[m].tv[i];
-      if(mo_force_FN(F+3*((size_t)b*mo->N+m),N+3*((size_t)b*mo->N+m),c,m,0,mo)<0) rcode=-1;
-    }
+    if(mscene_forces(mo,rc,F+3*(size_t)b*mo->N,N+3*(size_t)b*mo->N)) rcode=-1;
     tit+=t4-t3; tfo+=gbh_now()-t4;
   }
   for(int m=0;m<mo->N;m++){ mo->md[m].mw.bd.ipw=keep[m]; mo->md[m].mw.n_ipw=keepn[m]; }
