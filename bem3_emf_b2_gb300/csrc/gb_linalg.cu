@@ -41,10 +41,13 @@
 #include "gb_common.cuh"
 #include "gb_df64.cuh"
 #include "gb_internal.h"
+#include <atomic>
 #include <vector>
 
 #define LU_NB 64
-#define LU_NBO 256  // outer block: the trailing update's K
+// outer block: the trailing update's K (256 unless set or tuned: gb_set_lu_outer_block, gb_tune_lu_outer_block)
+static std::atomic<int> g_lu_nbo{256};
+#define LU_NBO (g_lu_nbo.load(std::memory_order_relaxed))
 
 // ------------------------------------------------------------------ A build
 struct ABuildArgs {
@@ -2105,5 +2108,81 @@ extern "C" int gbi_cinverse_tc(const cplxf* LU, size_t lda, int n, const int* pe
     gbi_set_error("FP32 inverse: a tensor-core pipeline wait timed out");
     rc = -1;
   }
+  return rc;
+}
+
+// ---- outer block size of the blocked LU / inverse, and its tuner
+extern "C" int gb_set_lu_outer_block(int nbo) {
+  if (nbo < LU_NB || nbo > 2048 || nbo % LU_NB) {
+    gbi_set_error("gb_set_lu_outer_block: %d is not a multiple of %d in %d..2048", nbo, LU_NB, LU_NB);
+    return -1;
+  }
+  g_lu_nbo.store(nbo);
+  return 0;
+}
+extern "C" int gb_lu_outer_block(void) { return g_lu_nbo.load(); }
+
+// seeded diagonally dominant complex test matrix (an integer hash per entry)
+__global__ void k_tune_matrix(cplxf* A, int n) {
+  const size_t p = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (size_t)n * n) return;
+  unsigned h = (unsigned)p * 2654435761u + 12345u;
+  h ^= h >> 15; h *= 2246822519u; h ^= h >> 13;
+  const float a = (float)(h & 0xffff) / 65536.0f - 0.5f, b = (float)(h >> 16) / 65536.0f - 0.5f;
+  const int i = (int)(p / n), j = (int)(p % n);
+  A[p] = cmkf(a + (i == j ? (float)n * 0.05f : 0.0f), b);
+}
+
+// Times the FP32 LU (without interchanges) and inverse of an n x n test
+// matrix with outer blocks of 128, 256, 512 and 1024 columns (second of two
+// runs each, CUDA events), sets the fastest (gb_set_lu_outer_block) and
+// returns it in *best, the four times (ms) in ms[4].
+extern "C" int gb_tune_lu_outer_block(int n, int* best, double* ms) {
+  if (n < 2 * LU_NB) { gbi_set_error("gb_tune_lu_outer_block: order %d below %d", n, 2 * LU_NB); return -1; }
+  const int cand[4] = {128, 256, 512, 1024};
+  const size_t nn = (size_t)n * n;
+  cudaStream_t st = nullptr;
+  GB_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cplxf *A = nullptr, *LU = nullptr, *X = nullptr;
+  int64_t* ipiv = nullptr;
+  int *perm = nullptr, *info = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  int rc = 0;
+  if (cudaMalloc((void**)&A, nn * sizeof(cplxf)) != cudaSuccess || cudaMalloc((void**)&LU, nn * sizeof(cplxf)) != cudaSuccess ||
+      cudaMalloc((void**)&X, nn * sizeof(cplxf)) != cudaSuccess || cudaMalloc((void**)&ipiv, (size_t)n * sizeof(int64_t)) != cudaSuccess ||
+      cudaMalloc((void**)&perm, (size_t)n * sizeof(int)) != cudaSuccess || cudaMalloc((void**)&info, sizeof(int)) != cudaSuccess ||
+      cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    gbi_set_error("gb_tune_lu_outer_block: %s", cudaGetErrorString(cudaGetLastError()));
+    rc = -1;
+  }
+  const int keep = g_lu_nbo.load();
+  double bestms = 1e300;
+  int bestc = keep;
+  if (!rc) {
+    k_tune_matrix<<<(unsigned)((nn + 255) / 256), 256, 0, st>>>(A, n);
+    gbi_count_launch();
+  }
+  for (int c = 0; c < 4 && !rc; c++) {
+    g_lu_nbo.store(cand[c]);
+    float t = 0.0f;
+    for (int rep = 0; rep < 2 && !rc; rep++) {
+      if (cudaMemcpyAsync(LU, A, nn * sizeof(cplxf), cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+          cudaEventRecord(e0, st) != cudaSuccess) { rc = -1; break; }
+      rc = gbi_cgetrf_nopiv(LU, (size_t)n, n, ipiv, info, st);
+      if (!rc) rc = gbi_make_perm(ipiv, n, perm, st);
+      if (!rc) rc = gbi_cinverse_tc(LU, (size_t)n, n, perm, X, (size_t)n, st);
+      if (!rc && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                  cudaEventElapsedTime(&t, e0, e1) != cudaSuccess)) rc = -1;
+    }
+    ms[c] = t;
+    if (!rc && t < bestms) { bestms = t; bestc = cand[c]; }
+  }
+  g_lu_nbo.store(rc ? keep : bestc);
+  *best = g_lu_nbo.load();
+  if (st) cudaStreamSynchronize(st);
+  cudaFree(A); cudaFree(LU); cudaFree(X); cudaFree(ipiv); cudaFree(perm); cudaFree(info);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (st) cudaStreamDestroy(st);
   return rc;
 }

@@ -366,6 +366,18 @@ def run_gpu(args):
     wd = tempfile.mkdtemp(prefix="bench_")
     sc, desc = open_workload(args, wd)
     cones = args.workload in ("cones", "beams")
+    # outer block of the node-matrix LUs and inverses, tuned on the
+    # workload's node count before any timed step
+    tune = None
+    if args.workload in ("cones", "sphere", "sphere3") and not args.no_tune:
+        nn = desc["na_per_object"] // 8
+        best = ctypes.c_int(0)
+        ms = (ctypes.c_double * 4)()
+        L.gb_tune_lu_outer_block.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p]
+        if L.gb_tune_lu_outer_block(nn, ctypes.byref(best), ms) != 0:
+            raise RuntimeError("gb_tune_lu_outer_block failed")
+        tune = {"lu_outer_block": best.value, "order": nn,
+                "lu_plus_inverse_ms": dict(zip(("128", "256", "512", "1024"), [round(v, 3) for v in ms]))}
 
     # chosen form: warm-up, then exactly K timed steps (launch count over them)
     for _ in range(args.warmup):
@@ -449,6 +461,8 @@ def run_gpu(args):
                "force": np.asarray(F32).tolist(), "torque": np.asarray(N32).tolist(),
                "e2e": {"value": e2e, "unit": "s/scene", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                "gpu_launches": int(round(launches)), "clocks": clk.summary()}
+        if tune:
+            out["autotune"] = tune
         if phases:
             out["phases_s_last_step"] = phases
         if far:
@@ -670,6 +684,7 @@ def main():
                     help="profiling run: one chosen-form scene step after --warmup steps, nothing else, no JSON line")
     ap.add_argument("--faces3", type=int, default=24, help="quadrangles per cube face of the sphere3 workload")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 form (comparison runs of the chosen form)")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default LU outer block (no tuning run)")
     ap.add_argument("--tc-passes", type=int, default=3, choices=[1, 3],
                     help="tensor-core passes of the FP32 factorisations (gb_set_tc_passes)")
     ap.add_argument("--workload", choices=["cones", "sphere", "sphere3", "cube", "beams"], default="cones",

@@ -251,6 +251,15 @@ int gb_set_tc_passes(int passes);
  * the dense LU and explicit inverse of A as the reference's lu_dec_A
  * (gb_invA_compute). */
 int gb_set_lu_pivoting(gb_obj *o, int mode);
+/* Outer block of the blocked LUs and inverses (process-wide; the K of the
+ * trailing tensor-core updates, inner 64-column panels update only inside
+ * it): 256 by default, a multiple of 64 up to 2048.  gb_tune_lu_outer_block
+ * times the complex-FP32 LU and inverse of an n x n test matrix with 128,
+ * 256, 512 and 1024 (ms[4], CUDA events, second of two runs), keeps the
+ * fastest and returns it in *best. */
+int gb_set_lu_outer_block(int nbo);
+int gb_lu_outer_block(void);
+int gb_tune_lu_outer_block(int n, int *best, double *ms);
 int gb_lu_info(gb_obj *o, int *rbt, int *fallbacks);
 int gb_factor_fp64(gb_obj *o);
 /* 1 if every element of the object separates domain 0 (outside) from domain
