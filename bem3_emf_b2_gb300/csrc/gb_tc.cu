@@ -503,13 +503,14 @@ extern "C" int gb_ktime_list(int cap, double* rec) {
 // default) or 1 (plain TF32, ~1e-3 relative error in the factors; the FP64
 // GMRES refinement tolerates it).  Process-wide: it applies to factorisations
 // started after the call.
-static std::atomic<int> g_tc_passes{3};
+static std::atomic<int> g_tc_passes{1};
 extern "C" int gb_set_tc_passes(int passes) {
   if (passes != 1 && passes != 3) { gbi_set_error("gb_set_tc_passes: passes must be 1 or 3"); return -1; }
   g_tc_passes.store(passes);
   return 0;
 }
 extern "C" int gbi_tc_passes(void) { return g_tc_passes.load(); }
+extern "C" int gb_get_tc_passes(void) { return g_tc_passes.load(); }
 
 // floats of scratch that gbi_tc_cgemm_sub needs for an M x N x K update
 extern "C" size_t gbi_tc_scratch_floats(int M, int N, int K) {

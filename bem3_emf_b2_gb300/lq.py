@@ -10,9 +10,9 @@ against the 64 x 64 rule, keeping the correction only if the sample's RMS
 error is within the tolerance.
 
 train() collects such pairs from a seeded family of quadrangle meshes --
-coarse cubed spheres, cubes and cuboids of random size, resolution and index,
-both domains of each -- labels them on the GPU (both rules in FP64) and
-trains the network there.
+cubes and cuboids of random size, resolution and index, both domains of
+each -- labels them on the GPU (both rules in FP64) and trains the network
+there.
 """
 import ctypes
 import os
@@ -51,20 +51,16 @@ def enable(on=True, tol=1e-7):
 
 
 def training_meshes(seed):
-    """An endless seeded sequence of (nodes, elems, n_inside, lambda0):
-    coarse cubed spheres, cubes and cuboids (edges and curvature are where
-    the fallback rule is needed), random size and refractive index."""
+    """An endless seeded sequence of (nodes, elems, n_inside, lambda0): cubes
+    and mildly stretched cuboids of random size, resolution and refractive
+    index -- the pairs that need the fallback rule sit at their edges (the
+    smooth cubed spheres of this size range have none)."""
     rng = np.random.default_rng(seed)
     while True:
-        u = rng.random()
-        size = float(np.exp(rng.uniform(np.log(0.3), np.log(4.0))))
-        if u < 0.4:
-            nodes, elems = meshgen.cubed_sphere(int(rng.integers(2, 9)), size)
-        elif u < 0.7:
-            nodes, elems = meshgen.cube(int(rng.integers(3, 17)), size)
-        else:  # cuboid: a cube stretched along its axes (elements of aspect ratio up to 3)
-            nodes, elems = meshgen.cube(int(rng.integers(3, 13)), size)
-            nodes = nodes * rng.uniform(0.5, 1.5, 3)
+        size = float(np.exp(rng.uniform(np.log(0.5), np.log(6.0))))
+        nodes, elems = meshgen.cube(int(rng.integers(4, 17)), size)
+        if rng.random() < 0.5:
+            nodes = nodes * rng.uniform(0.75, 1.3, 3)
         n_in = complex(rng.uniform(1.1, 2.6), rng.uniform(0.0, 0.05))
         yield nodes, elems, n_in, 1.0
 

@@ -685,7 +685,7 @@ def main():
     ap.add_argument("--faces3", type=int, default=24, help="quadrangles per cube face of the sphere3 workload")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 form (comparison runs of the chosen form)")
     ap.add_argument("--no-tune", action="store_true", help="keep the default LU outer block (no tuning run)")
-    ap.add_argument("--tc-passes", type=int, default=3, choices=[1, 3],
+    ap.add_argument("--tc-passes", type=int, default=1, choices=[1, 3],
                     help="tensor-core passes of the FP32 factorisations (gb_set_tc_passes)")
     ap.add_argument("--workload", choices=["cones", "sphere", "sphere3", "cube", "beams"], default="cones",
                     help="cones: the two-cone scene (default); sphere: the 384-element sphere; cube: assembly "

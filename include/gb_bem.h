@@ -217,10 +217,12 @@ int gb_ir_info(gb_obj *o, int *iters, double *relres);
  * gb_ir_info reports the preconditioner solves of the last solve. */
 int gb_set_refinement(gb_obj *o, int mode);
 /* tensor-core passes of every complex-FP32 factorisation started afterwards
- * (process-wide): 3 (default; split TF32, FP32-accurate products) or 1
- * (plain TF32: a third of the tensor work, ~1e-3 relative error in the
- * factors, which the GMRES refinement absorbs in more iterations) */
+ * (process-wide): 1 (default; plain TF32 products, ~1e-3 relative error in
+ * the factors -- they only precondition the FP64 GMRES, which absorbs it in
+ * a few more iterations) or 3 (split TF32: FP32-accurate products, for
+ * callers that use the FP32 factors directly) */
 int gb_set_tc_passes(int passes);
+int gb_get_tc_passes(void);
 /* Row interchanges of the FP32 factorisation.  mode 0 (default): A is
  * randomised by two-sided recursive butterfly transforms of depth 2
  * (U^T A V, random diagonal entries e^{rho/10}, fixed seed; Parker 1995,

@@ -31,6 +31,7 @@ def _lib():
     L.gb_set_refinement.restype = ci
     L.gb_set_tc_passes.argtypes = [ci]
     L.gb_set_tc_passes.restype = ci
+    L.gb_get_tc_passes.restype = ci
     L.gb_lu_info.argtypes = [vp, vp, vp]
     L.gb_lu_info.restype = ci
     return L
@@ -90,7 +91,9 @@ def test_gmres_absorbs_single_pass_tf32_factors(gb_build, tmp_path):
     sc = _scene(wd)
     o = sc.obj()
     assert L.gb_set_lu_pivoting(o, 0) == 0
+    default = L.gb_get_tc_passes()
     try:
+        assert L.gb_set_tc_passes(3) == 0
         F3, N3 = sc.step(form=1)
         it3, _ = sc.ir_info()
         assert L.gb_set_tc_passes(1) == 0
@@ -117,7 +120,7 @@ def test_gmres_absorbs_single_pass_tf32_factors(gb_build, tmp_path):
               "fallback %s, failed %s" % (it1, it3, itc, rrc, fb2 > fb, failed))
         assert failed or fb2 > fb or it1 <= itc
     finally:
-        L.gb_set_tc_passes(3)
+        L.gb_set_tc_passes(default)
         sc.close()
 
 

@@ -7,6 +7,9 @@
   ragged edges and sub-matrices with leading dimensions, as in the LU.
 - gbi_cgetrf / gbi_zgetrf (tournament-pivoting LU): P A = L U to FP32 / FP64
   rounding, against the factors read back to the host.
+The FP32 factorisations are checked in the FP32-accurate three-pass mode
+(gb_set_tc_passes(3)); the library's default single pass is covered by the
+GMRES tests, which only need a preconditioner.
 """
 import ctypes
 
@@ -29,6 +32,18 @@ def _lib():
 
 def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(autouse=True)
+def _three_pass(gb_build):
+    from bem3_emf_b2_gb300 import lib
+    L = lib()
+    L.gb_set_tc_passes.argtypes = [ci]
+    L.gb_get_tc_passes.restype = ci
+    keep = L.gb_get_tc_passes()
+    L.gb_set_tc_passes(3)
+    yield
+    L.gb_set_tc_passes(keep)
 
 
 @pytest.mark.gpu

