@@ -125,7 +125,8 @@ __device__ __forceinline__ dfc dfc_scale(dfc a, df s) { return dfcmk(df_mul(a.re
 
 // cos and sin of x in double-float, |x| < 1000: x = j pi/8 + t with
 // |t| <= pi/16 (pi/8 carried to about 70 bits in three floats), Taylor
-// polynomials of t to t^15 (truncation below 1e-20 for |t| <= pi/16), then the
+// polynomials of t to t^11 / t^10 (truncation below 1e-17 for |t| <= pi/16,
+// under the double-float rounding of ~4e-15), then the
 // rotation by j pi/8 with cos, sin (j pi/8) from a double-float table.
 // Coefficients: 1/n! in double-float (hi, lo).
 static __device__ const float2 g_df_sin_c[8] = {
@@ -158,9 +159,9 @@ __device__ __forceinline__ void df_sincos(df x, df* s, df* c) {
   t = df_sub(t, two_prod(jf, P2));
   t = df_add_f(t, -jf * P3);
   const df mu = df_neg(df_sqr(t));  // -t^2
-  df sp = df_ld(g_df_sin_c, 7), cp = df_ld(g_df_cos_c, 7);
+  df sp = df_ld(g_df_sin_c, 5), cp = df_ld(g_df_cos_c, 5);
 #pragma unroll
-  for (int m = 6; m >= 0; m--) {
+  for (int m = 4; m >= 0; m--) {
     sp = df_fma(df_ld(g_df_sin_c, m), sp, mu);
     cp = df_fma(df_ld(g_df_cos_c, m), cp, mu);
   }
