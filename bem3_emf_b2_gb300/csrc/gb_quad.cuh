@@ -60,8 +60,11 @@ __device__ __forceinline__ void reg_point(const Elem& E, double z, double e, dou
   shape_fn(E, z, e, N);
   cplx g = ce * (iR * aW * w);
   cplx h = (cb * ce) * (tD * w);
+  // a triangle's fourth shape function is zero: its sums are skipped
+  const int ns = E.quad ? 4 : 3;
 #pragma unroll
-  for (int n = 0; n < 4; n++) { A.G[n] += g * N[n]; A.H[n] += h * N[n]; }
+  for (int n = 0; n < 4; n++)
+    if (n < ns) { A.G[n] += g * N[n]; A.H[n] += h * N[n]; }
   A.F += w * tD;
   if (NDIR > 0) {
     cplx kR = k * aR;
@@ -74,7 +77,8 @@ __device__ __forceinline__ void reg_point(const Elem& E, double z, double e, dou
       cplx dg = (cb * ce) * (iR * iR * rdv * aW * w);
       cplx dh = (ce * (t1 * (rdv * rdW) - cb * Wdv)) * (iR3 * w);
 #pragma unroll
-      for (int n = 0; n < 4; n++) { A.dG[d][n] += dg * N[n]; A.dH[d][n] += dh * N[n]; }
+      for (int n = 0; n < 4; n++)
+        if (n < ns) { A.dG[d][n] += dg * N[n]; A.dH[d][n] += dh * N[n]; }
       A.dF[d] += w * iR3 * (3.0 * rdv * rdW - Wdv);
     }
   }

@@ -83,7 +83,7 @@ struct PairDN {
 // functions N, weight w) added to the sums
 template <int NDIR>
 __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[3], const df W[3], const df N[4], df w,
-                                              AccDN<NDIR>& A) {
+                                              AccDN<NDIR>& A, int ns = 4) {
   const df aR = df_sqrt(dot3d(R, R));
   const df iR = df_rcp(aR);
   const df aW = df_sqrt(dot3d(W, W));
@@ -100,10 +100,13 @@ __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[
   const dfc g = dfc_scale(ph, df_mul(df_mul(iR, aW), w));
   const dfc cbe = dfc_mul(cb, ph);
   const dfc h = dfc_scale(cbe, df_mul(tD, w));
+  // ns = 3 for a triangle, whose fourth shape function is zero: skipped
 #pragma unroll
   for (int n = 0; n < 4; n++) {
-    A.G[n] = dfc_fma_re(A.G[n], g, N[n]);
-    A.H[n] = dfc_fma_re(A.H[n], h, N[n]);
+    if (n < ns) {
+      A.G[n] = dfc_fma_re(A.G[n], g, N[n]);
+      A.H[n] = dfc_fma_re(A.H[n], h, N[n]);
+    }
   }
   A.F = df_fma(A.F, w, tD);
   if (NDIR > 0) {
@@ -118,8 +121,10 @@ __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[
       const dfc dh = dfc_scale(dfc_mul(ph, u), iR3w);
 #pragma unroll
       for (int n = 0; n < 4; n++) {
-        A.dG[q][n] = dfc_fma_re(A.dG[q][n], dg, N[n]);
-        A.dH[q][n] = dfc_fma_re(A.dH[q][n], dh, N[n]);
+        if (n < ns) {
+          A.dG[q][n] = dfc_fma_re(A.dG[q][n], dg, N[n]);
+          A.dH[q][n] = dfc_fma_re(A.dH[q][n], dh, N[n]);
+        }
       }
       A.dF[q] = df_fma(A.dF[q], iR3w, df_sub(df_mul_f(df_mul(rdv, rdW), 3.0f), Wdv));
     }
@@ -246,7 +251,7 @@ __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double
       R[d] = df_add(P.R0[d], df_fma(df_fma(df_mul(P.c1[d], z), P.c2[d], e), P.c3[d], ze));
       W[d] = df_fma(df_fma(P.w0[d], P.w1[d], z), P.w2[d], e);
     }
-    reg_kernel_dn<NDIR>(P, R, W, N, w, A);
+    reg_kernel_dn<NDIR>(P, R, W, N, w, A, S.quad ? 4 : 3);
   }
   const double sh = neg ? -S0 : S0;
   const double s3n = S.quad ? 1.0 : 1.0 / 3.0;
