@@ -139,7 +139,10 @@ __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[
 //   n_D = GLN for D < 2, 9 for D < 3, 6 for D < 5, 5 beyond (the integrand's
 //         nearest complex singularity bounds the Gauss error);
 //   n_k = 5, 7, 8 for |k| a <= 0.75, 2.4, 4.5, else GLN (the phase
-//         e^{ik|R|} varies by up to |k| a over the element);
+//         e^{ik|R|} varies by up to |k| a over the element); a triangle,
+//         whose three sub-quadrangles each span about half of a, takes
+//         5, 6 for |k| a <= 1.2, 2.4 (largest error over random triangles
+//         at D >= 3 against a 40-point rule: 5e-13 of the natural scale);
 // n = max(n_D, n_k).  Calibrated against a 24-point rule on cubed-sphere
 // quadrangles (4 and 8 per face) and cone triangles (the reference's three
 // sub-quadrangle map): every output of a pair (G, H, F and the two
@@ -154,7 +157,8 @@ __device__ __forceinline__ int reg_order(const Elem& S, double a0, cplx k) {
   }
   const double D = a0 / a, ka = sqrt(k.x * k.x + k.y * k.y) * a;
   const int nD = D < 2.0 ? GB_GLN : (D < 3.0 ? 9 : (D < 5.0 ? 6 : 5));
-  const int nk = ka <= 0.75 ? 5 : (ka <= 2.4 ? 7 : (ka <= 4.5 ? 8 : GB_GLN));
+  const int nk = S.quad ? (ka <= 0.75 ? 5 : (ka <= 2.4 ? 7 : (ka <= 4.5 ? 8 : GB_GLN)))
+                        : (ka <= 1.2 ? 5 : (ka <= 2.4 ? 6 : (ka <= 4.5 ? 8 : GB_GLN)));
   const int n = nD > nk ? nD : nk;
   return n < GB_GLN ? n : GB_GLN;
 }
