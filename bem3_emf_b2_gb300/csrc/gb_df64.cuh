@@ -6,6 +6,12 @@
 // Bailey, "Library for double-double and quad-double arithmetic", 2000).
 // GB300's FP32 pipes are 64 times wider than its FP64 pipe, so quadrature that
 // needs FP64-level accuracy runs faster in double-float than in FP64.
+//
+// The compiler may fuse a multiply and a following add into one fused
+// multiply-add, which is exact where the algorithms rely on the rounded
+// product: inside the error-free transformations every sum and every product
+// that feeds a sum goes through __fadd_rn / __fsub_rn / __fmul_rn, which are
+// never fused, so the results do not depend on the surrounding code's shape.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -22,34 +28,34 @@ __device__ __forceinline__ double df_to(df a) { return (double)a.hi + (double)a.
 
 // s + e = a + b exactly
 __device__ __forceinline__ df two_sum(float a, float b) {
-  const float s = a + b;
-  const float bb = s - a;
-  const float e = (a - (s - bb)) + (b - bb);
+  const float s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
   return dfmk(s, e);
 }
 // |a| >= |b|
 __device__ __forceinline__ df quick_two_sum(float a, float b) {
-  const float s = a + b;
-  return dfmk(s, b - (s - a));
+  const float s = __fadd_rn(a, b);
+  return dfmk(s, __fsub_rn(b, __fsub_rn(s, a)));
 }
 __device__ __forceinline__ df two_prod(float a, float b) {
-  const float p = a * b;
+  const float p = __fmul_rn(a, b);
   return dfmk(p, fmaf(a, b, -p));
 }
 
 __device__ __forceinline__ df df_add(df a, df b) {
   df s = two_sum(a.hi, b.hi);
   const df t = two_sum(a.lo, b.lo);
-  s.lo += t.hi;
+  s.lo = __fadd_rn(s.lo, t.hi);
   s = quick_two_sum(s.hi, s.lo);
-  s.lo += t.lo;
+  s.lo = __fadd_rn(s.lo, t.lo);
   return quick_two_sum(s.hi, s.lo);
 }
 __device__ __forceinline__ df df_neg(df a) { return dfmk(-a.hi, -a.lo); }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
 __device__ __forceinline__ df df_add_f(df a, float b) {
   df s = two_sum(a.hi, b);
-  s.lo += a.lo;
+  s.lo = __fadd_rn(s.lo, a.lo);
   return quick_two_sum(s.hi, s.lo);
 }
 __device__ __forceinline__ df df_mul(df a, df b) {
@@ -66,13 +72,13 @@ __device__ __forceinline__ df df_mul_f(df a, float b) {
 // error terms folded into the sum's (two_sum of the high parts, then one
 // renormalisation); about half the instructions of df_add(c, df_mul(a, b))
 __device__ __forceinline__ df df_fma(df c, df a, df b) {
-  const float p = a.hi * b.hi;
+  const float p = __fmul_rn(a.hi, b.hi);
   float pe = fmaf(a.hi, b.hi, -p);
   pe = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, pe));
-  const float s = c.hi + p;
-  const float bb = s - c.hi;
-  const float e = (c.hi - (s - bb)) + (p - bb);
-  return quick_two_sum(s, e + (c.lo + pe));
+  const float s = __fadd_rn(c.hi, p);
+  const float bb = __fsub_rn(s, c.hi);
+  const float e = __fadd_rn(__fsub_rn(c.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  return quick_two_sum(s, __fadd_rn(e, __fadd_rn(c.lo, pe)));
 }
 __device__ __forceinline__ df df_sqr(df a) {
   df p = two_prod(a.hi, a.hi);
@@ -96,20 +102,20 @@ __device__ __forceinline__ df df_rcp(df b) {
   const float q1 = rcp_approx(b.hi);
   float r = fmaf(-b.hi, q1, 1.0f);
   r = fmaf(-b.lo, q1, r);
-  return quick_two_sum(q1, r * q1);
+  return quick_two_sum(q1, __fmul_rn(r, q1));
 }
 // a / b: a first quotient, its remainder, a correction
 __device__ __forceinline__ df df_div(df a, df b) {
   const float ib = rcp_approx(b.hi);
-  const float q1 = a.hi * ib;
+  const float q1 = __fmul_rn(a.hi, ib);
   const df r = df_sub(a, df_mul_f(b, q1));
-  return quick_two_sum(q1, r.hi * ib);
+  return quick_two_sum(q1, __fmul_rn(r.hi, ib));
 }
 // sqrt(a), a > 0: the FP32 root corrected by one Newton step in double-float
 __device__ __forceinline__ df df_sqrt(df a) {
   const float s = sqrtf(a.hi);
   const df e = df_sub(a, two_prod(s, s));
-  return quick_two_sum(s, e.hi * (0.5f * rsqrt_approx(a.hi)));
+  return quick_two_sum(s, __fmul_rn(e.hi, 0.5f * rsqrt_approx(a.hi)));
 }
 
 // complex double-float
@@ -157,7 +163,7 @@ __device__ __forceinline__ void df_sincos(df x, df* s, df* c) {
   const float jf = rintf(x.hi * 2.5464789867401123f);                                                  // x 8/pi
   df t = df_sub(x, two_prod(jf, P1));
   t = df_sub(t, two_prod(jf, P2));
-  t = df_add_f(t, -jf * P3);
+  t = df_add_f(t, __fmul_rn(-jf, P3));
   const df mu = df_neg(df_sqr(t));  // -t^2
   df sp = df_ld(g_df_sin_c, 5), cp = df_ld(g_df_cos_c, 5);
 #pragma unroll
@@ -189,7 +195,7 @@ __device__ __forceinline__ df df_exp(df y) {
   const float nf = rintf(y.hi * 1.4426950216293335f);
   df r = df_sub(y, two_prod(nf, L1));
   r = df_sub(r, two_prod(nf, L2));
-  r = df_add_f(r, -nf * L3);
+  r = df_add_f(r, __fmul_rn(-nf, L3));
   df e = df_ld(g_df_exp_c, 15);
 #pragma unroll
   for (int k = 14; k >= 0; k--) e = df_fma(df_ld(g_df_exp_c, k), e, r);
