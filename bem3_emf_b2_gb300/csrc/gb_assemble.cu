@@ -76,6 +76,17 @@ struct AsmArgs {
   int row0, nrow;  // the rows row0 .. row0 + nrow - 1 of the domain; outputs hold nrow rows
   uint8_t* redo;   // work-list launches: the item's flags of pairs for the FP64 pass
   GbLqList lq;     // learned quadrature: quadrangle fallback pairs listed instead of integrated
+  // pairs that certainly take the GHN fallback rule, listed by the
+  // double-float pass for k_asm_gh_df (null: they go to the FP64 pass)
+  struct GbGhPair* gh;
+  unsigned* ghn;
+  unsigned ghcap;
+  int item;        // this item's index in the launch's item array
+};
+
+// one pair of the GHN list: item, row (in the domain), source element index, sign
+struct GbGhPair {
+  int item, row, sidx, neg;
 };
 
 // unit tangents at collocation node tn of element |td| (reference tz_te_bd_node d3b1_elem.c:122-143)
@@ -325,11 +336,54 @@ __device__ __forceinline__ void asm_regular_df_body(const AsmArgs& a, uint8_t* r
   for (int d = 0; d < 3; d++) rt[d] = __ldg(a.ren + (size_t)atd * 12 + tn * 3 + d);
   node_tangents(T, tn, vt);
   RegAcc<2> D;
-  if (!reg_integrate_dn<2>(S, rt, vt, a.k, sd < 0, D, a.adapt != 0)) {
+  int why = 0;
+  if (!reg_integrate_dn<2>(S, rt, vt, a.k, sd < 0, D, a.adapt != 0, &why)) {
     redo[p] = 1;
+    // certainly the GHN rule (the FP64 decision cannot differ): listed for
+    // the double-float GHN kernel instead of the FP64 pass (the learned
+    // quadrature, when on, takes these pairs in the FP64 pass)
+    if (why == 2 && a.gh != nullptr && a.lq.p == nullptr) {
+      const unsigned slot = atomicAdd(a.ghn, 1u);
+      if (slot < a.ghcap) {
+        GbGhPair e;
+        e.item = a.item; e.row = row; e.sidx = sidx; e.neg = sd < 0 ? 1 : 0;
+        a.gh[slot] = e;
+        redo[p] = 0;
+      }
+    }
     return;
   }
   store_pair(a, N, row, sidx, D);
+}
+
+// The listed GHN pairs in double-float: one warp per pair, the GHN x GHN
+// points shared by the lanes, the sums reduced across the warp in FP64 and
+// finished as reg_finish does (the FP64 pass integrates the same pairs with
+// the same rule in FP64)
+__global__ void __launch_bounds__(128) k_asm_gh_df(const AsmArgs* __restrict__ items, const GbGhPair* __restrict__ L,
+                                                   unsigned n) {
+  const unsigned w = (unsigned)(((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const GbGhPair e = L[w];
+  const AsmArgs& a = items[e.item];
+  const int t = e.row / 4 + 1, tn = e.row % 4;
+  const int td = __ldg(a.sid + t), sd = __ldg(a.sid + e.sidx + 1);
+  const int atd = abs(td);
+  Elem T, S;
+  load_elem(T, a.cr, a.cw, a.etype, atd);
+  load_elem(S, a.cr, a.cw, a.etype, abs(sd));
+  double rt[3], vt[2][3];
+  for (int d = 0; d < 3; d++) rt[d] = __ldg(a.ren + (size_t)atd * 12 + tn * 3 + d);
+  node_tangents(T, tn, vt);
+  RegAcc<2> R;
+  cplx E0;
+  reg_gh_part_dn<2>(S, rt, vt, a.k, lane, 32, R, E0);
+  warp_allreduce<sizeof(RegAcc<2>) / sizeof(double)>((double*)&R);
+  if (lane != 0) return;
+  RegAcc<2> D;
+  finish_dn<2>(R, S, e.neg != 0, E0, D);
+  store_pair(a, (size_t)a.Ne * 4, e.row, e.sidx, D);
 }
 __global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo) {
   asm_regular_df_body(a, redo, blockIdx.x);
@@ -1531,6 +1585,7 @@ extern "C" int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int prec
   a.nrow = nrow;
   a.redo = nullptr;
   memset(&a.lq, 0, sizeof(a.lq));
+  a.gh = nullptr; a.ghn = nullptr; a.ghcap = 0; a.item = 0;
   GB_CUDA(cudaMemsetAsync(G, 0, nr * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(H, 0, nr * N * sizeof(cplx), st));
   GB_CUDA(cudaMemsetAsync(dG, 0, 2 * nr * N * sizeof(cplx), st));
@@ -1544,9 +1599,30 @@ extern "C" int gbi_assemble_rows(const GbMeshDev* m, int did, int type, int prec
   if (lq && lq_alloc(a.lq, npair, st)) return -1;
   if (precision >= 2 && type == 2) {
     GB_CUDA(cudaMallocAsync((void**)&redo, npair, st));
+    a.ghcap = (unsigned)std::min<size_t>(npair / 16 + 4096, (size_t)1 << 26);
+    GB_CUDA(cudaMallocAsync((void**)&a.gh, (size_t)a.ghcap * sizeof(GbGhPair), st));
+    GB_CUDA(cudaMallocAsync((void**)&a.ghn, sizeof(unsigned), st));
+    GB_CUDA(cudaMemsetAsync(a.ghn, 0, sizeof(unsigned), st));
     k_asm_regular_df<<<nb, 128, 0, st>>>(a, redo);
     gbi_count_launch();
     GB_CUDA(cudaGetLastError());
+    unsigned ng = 0;
+    GB_CUDA(cudaMemcpyAsync(&ng, a.ghn, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    ng = std::min(ng, a.ghcap);
+    if (ng > 0) {
+      AsmArgs* da = nullptr;
+      GB_CUDA(cudaMallocAsync((void**)&da, sizeof(AsmArgs), st));
+      GB_CUDA(cudaMemcpyAsync(da, &a, sizeof(AsmArgs), cudaMemcpyHostToDevice, st));
+      k_asm_gh_df<<<(unsigned)(((size_t)ng * 32 + 127) / 128), 128, 0, st>>>(da, a.gh, ng);
+      gbi_count_launch();
+      GB_CUDA(cudaGetLastError());
+      cudaFreeAsync(da, st);
+      GB_CUDA(cudaStreamSynchronize(st));  // a (host) was the copy's source
+    }
+    cudaFreeAsync(a.gh, st);
+    cudaFreeAsync(a.ghn, st);
+    a.gh = nullptr; a.ghn = nullptr; a.ghcap = 0;
     a.only = redo;
   } else if (precision == 1 && type == 2) {
     GB_CUDA(cudaMallocAsync((void**)&redo, npair, st));
@@ -1589,10 +1665,21 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
   GbLqList lql;
   memset(&lql, 0, sizeof(lql));
   const bool lq = lq_active(precision, type);
-  if (lq) {
-    size_t tot = 0;
-    for (int i = 0; i < n; i++) tot += (size_t)d[i].nrow * (size_t)d[i].m->sb_Ne[d[i].did];
-    if (lq_alloc(lql, tot, st)) return -1;
+  size_t tot = 0;
+  for (int i = 0; i < n; i++) tot += (size_t)d[i].nrow * (size_t)d[i].m->sb_Ne[d[i].did];
+  if (lq && lq_alloc(lql, tot, st)) return -1;
+  // the certain-GHN pairs of the double-float pass (k_asm_gh_df)
+  GbGhPair* ghl = nullptr;
+  unsigned* ghn = nullptr;
+  unsigned ghcap = 0;
+  if (precision >= 2 && type == 2) {
+    ghcap = (unsigned)std::min<size_t>(tot / 16 + 4096, (size_t)1 << 26);
+    if (cudaMallocAsync((void**)&ghl, (size_t)ghcap * sizeof(GbGhPair), st) != cudaSuccess ||
+        cudaMallocAsync((void**)&ghn, sizeof(unsigned), st) != cudaSuccess ||
+        cudaMemsetAsync(ghn, 0, sizeof(unsigned), st) != cudaSuccess) {
+      gbi_set_error("work-list assembly: out of device memory");
+      return -1;
+    }
   }
   for (int i = 0; i < n && !rc; i++) {
     const GbMeshDev* m = d[i].m;
@@ -1609,6 +1696,7 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
     a.adapt = precision == 3;
     a.row0 = d[i].row0; a.nrow = d[i].nrow;
     a.lq = lql;
+    a.gh = ghl; a.ghn = ghn; a.ghcap = ghcap; a.item = i;
     const size_t npair = nr * (size_t)Ne;
     if (cudaMallocAsync((void**)&a.Fs, 3 * nr * (size_t)Ne * sizeof(double), st) != cudaSuccess ||
         cudaMallocAsync((void**)&a.redo, npair + 16, st) != cudaSuccess) {
@@ -1647,6 +1735,17 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
     if (df) {
       k_asm_regular_df_list<<<breg[n], 128, 0, st>>>(dit, db, n);
       gbi_count_launch();
+      unsigned ng = 0;
+      if (cudaMemcpyAsync(&ng, ghn, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+          cudaStreamSynchronize(st) != cudaSuccess) {
+        gbi_set_error("work-list assembly: %s", cudaGetErrorString(cudaGetLastError()));
+        rc = -1;
+      }
+      ng = std::min(ng, ghcap);
+      if (!rc && ng > 0) {
+        k_asm_gh_df<<<(unsigned)(((size_t)ng * 32 + 127) / 128), 128, 0, st>>>(dit, ghl, ng);
+        gbi_count_launch();
+      }
     }
     k_asm_regular_list<<<breg[n], 128, 0, st>>>(dit, db, n, df ? 1 : 0);
     gbi_count_launch();
@@ -1665,6 +1764,8 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
   if (db) cudaFreeAsync(db, st);
   for (void* t : tmp) cudaFreeAsync(t, st);
   lq_free(lql, st);
+  if (ghl) cudaFreeAsync(ghl, st);
+  if (ghn) cudaFreeAsync(ghn, st);
   const cudaError_t e = cudaStreamSynchronize(st);  // the host arrays above are read by the copies
   if (!rc && e != cudaSuccess) { gbi_set_error("work-list assembly: %s", cudaGetErrorString(e)); rc = -1; }
   return rc;

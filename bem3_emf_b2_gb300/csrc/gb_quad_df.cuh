@@ -163,58 +163,24 @@ __device__ __forceinline__ int reg_order(const Elem& S, double a0, cplx k) {
   return n < GB_GLN ? n : GB_GLN;
 }
 
-// GLN x GLN integrals of source element S at the observation point rt (with
-// NDIR directions vt) in double-float, finished (scaled, sub-domain sign) into
-// D as reg_integrate<NDIR>(S, 2, ...) would; false if the pair must be
-// integrated in FP64 (a |dF| within 0.05 of CBD_SDF, or not finite).
-// adapt: the n x n rule of reg_order instead (n = GLN for near pairs).
-template <int NDIR>
-__device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double (*vt)[3], cplx k, bool neg,
-                                 RegAcc<NDIR>& D, bool adapt = false) {
-  PairDN<NDIR> P;
-  double R0[3];
-#pragma unroll
-  for (int d = 0; d < 3; d++) {
-    R0[d] = S.cr[d][0] - rt[d];
-    P.R0[d] = df_from(R0[d]);
-    P.c1[d] = df_from(S.cr[d][1]); P.c2[d] = df_from(S.cr[d][2]); P.c3[d] = df_from(S.cr[d][3]);
-    P.w0[d] = df_from(S.cw[d][0]); P.w1[d] = df_from(S.cw[d][1]); P.w2[d] = df_from(S.cw[d][2]);
-#pragma unroll
-    for (int q = 0; q < NDIR; q++) P.vt[q][d] = df_from(vt[q][d]);
-  }
-  const double a0 = norm3(R0);
-  const int nq = adapt ? reg_order(S, a0, k) : GB_GLN;
-  const int off = nq * (nq - 1) / 2;
-  P.a0 = df_from(a0);
-  P.kr = df_from(k.x);
-  P.ki = df_from(k.y);
-  const cplx E0 = cexpik(k, a0);
-  AccDN<NDIR> A;
-  const df zero = dfmk(0.0f, 0.0f);
-#pragma unroll
-  for (int n = 0; n < 4; n++) {
-    A.G[n] = dfcmk(zero, zero);
-    A.H[n] = dfcmk(zero, zero);
-#pragma unroll
-    for (int q = 0; q < GB_ND(NDIR); q++) { A.dG[q][n] = dfcmk(zero, zero); A.dH[q][n] = dfcmk(zero, zero); }
-  }
-  A.F = zero;
-#pragma unroll
-  for (int q = 0; q < GB_ND(NDIR); q++) A.dF[q] = zero;
-  const double S0 = S.quad ? GB_I_FP : 0.0625 * GB_SQ3 * GB_I_SPSQ3;
-  // one loop over every point of the rule -- an n x n tensor rule on a
-  // quadrangle, the same on each of the three sub-quadrangles of a triangle
-  // (the reference's maps) -- so that the integrand is inlined at one site
-  // (the kernel is instruction-fetch bound otherwise)
+// Points q0, q0 + qstep, ... of the n x n Gauss-Legendre rule over source
+// element S -- the tensor rule on a quadrangle, the same on each of the
+// three sub-quadrangles of a triangle (the reference's maps) -- added to A.
+// GH: the GHN rule (n = GHN), else the rule of nq points (tables at off).
+template <int NDIR, bool GH>
+__device__ __forceinline__ void reg_points_dn(const Elem& S, const PairDN<NDIR>& P, int nq, int off, int q0, int qstep,
+                                              AccDN<NDIR>& A) {
   const int npts = (S.quad ? 1 : 3) * nq * nq;
   const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // sqrt(3)
 #pragma unroll 1
-  for (int q = 0; q < npts; q++) {
+  for (int q = q0; q < npts; q += qstep) {
     int sub = 0, ij = q;
     if (!S.quad) { sub = q % 3; ij = q / 3; }
     const int i = ij / nq, j = ij - i * nq;
-    const df x = dfmk(c_tabd.xn[off + i].x, c_tabd.xn[off + i].y), wx = dfmk(c_tabd.wn[off + i].x, c_tabd.wn[off + i].y);
-    const df y = dfmk(c_tabd.xn[off + j].x, c_tabd.xn[off + j].y), wy = dfmk(c_tabd.wn[off + j].x, c_tabd.wn[off + j].y);
+    const float2 xi = GH ? c_tabd.xh[i] : c_tabd.xn[off + i], wi = GH ? c_tabd.wh[i] : c_tabd.wn[off + i];
+    const float2 xj = GH ? c_tabd.xh[j] : c_tabd.xn[off + j], wj = GH ? c_tabd.wh[j] : c_tabd.wn[off + j];
+    const df x = dfmk(xi.x, xi.y), wx = dfmk(wi.x, wi.y);
+    const df y = dfmk(xj.x, xj.y), wy = dfmk(wj.x, wj.y);
     df z, e, w, N[4];
     if (S.quad) {
       z = x;
@@ -257,24 +223,136 @@ __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double
     }
     reg_kernel_dn<NDIR>(P, R, W, N, w, A, S.quad ? 4 : 3);
   }
+}
+
+// the pair's constants in double-float (source element S, observation point
+// rt, directions vt, wave number k); returns |R0|, the distance to the
+// element's point (0, 0)
+template <int NDIR>
+__device__ __forceinline__ double pair_setup_dn(const Elem& S, const double rt[3], const double (*vt)[3], cplx k,
+                                                PairDN<NDIR>& P) {
+  double R0[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    R0[d] = S.cr[d][0] - rt[d];
+    P.R0[d] = df_from(R0[d]);
+    P.c1[d] = df_from(S.cr[d][1]); P.c2[d] = df_from(S.cr[d][2]); P.c3[d] = df_from(S.cr[d][3]);
+    P.w0[d] = df_from(S.cw[d][0]); P.w1[d] = df_from(S.cw[d][1]); P.w2[d] = df_from(S.cw[d][2]);
+#pragma unroll
+    for (int q = 0; q < NDIR; q++) P.vt[q][d] = df_from(vt[q][d]);
+  }
+  const double a0 = norm3(R0);
+  P.a0 = df_from(a0);
+  P.kr = df_from(k.x);
+  P.ki = df_from(k.y);
+  return a0;
+}
+
+template <int NDIR>
+__device__ __forceinline__ void acc_zero_dn(AccDN<NDIR>& A) {
+  const df zero = dfmk(0.0f, 0.0f);
+#pragma unroll
+  for (int n = 0; n < 4; n++) {
+    A.G[n] = dfcmk(zero, zero);
+    A.H[n] = dfcmk(zero, zero);
+#pragma unroll
+    for (int q = 0; q < GB_ND(NDIR); q++) { A.dG[q][n] = dfcmk(zero, zero); A.dH[q][n] = dfcmk(zero, zero); }
+  }
+  A.F = zero;
+#pragma unroll
+  for (int q = 0; q < GB_ND(NDIR); q++) A.dF[q] = zero;
+}
+
+// the sums of A as doubles (unscaled), for reductions across threads
+template <int NDIR>
+__device__ __forceinline__ void acc_to_double(const AccDN<NDIR>& A, RegAcc<NDIR>& R) {
+#pragma unroll
+  for (int n = 0; n < 4; n++) {
+    R.G[n] = cmk(df_to(A.G[n].re), df_to(A.G[n].im));
+    R.H[n] = cmk(df_to(A.H[n].re), df_to(A.H[n].im));
+#pragma unroll
+    for (int q = 0; q < NDIR; q++) {
+      R.dG[q][n] = cmk(df_to(A.dG[q][n].re), df_to(A.dG[q][n].im));
+      R.dH[q][n] = cmk(df_to(A.dH[q][n].re), df_to(A.dH[q][n].im));
+    }
+  }
+  R.F = df_to(A.F);
+#pragma unroll
+  for (int q = 0; q < NDIR; q++) R.dF[q] = df_to(A.dF[q]);
+}
+
+// raw sums R (as acc_to_double gives them) finished into D: the phase
+// e^{ik|R0|}, the rule's scale (1/3 of the triangle's tripled shape
+// functions) and the sub-domain sign, as reg_finish does in FP64
+template <int NDIR>
+__device__ __forceinline__ void finish_dn(const RegAcc<NDIR>& R, const Elem& S, bool neg, cplx E0, RegAcc<NDIR>& D) {
+  const double S0 = S.quad ? GB_I_FP : 0.0625 * GB_SQ3 * GB_I_SPSQ3;
   const double sh = neg ? -S0 : S0;
   const double s3n = S.quad ? 1.0 : 1.0 / 3.0;
-#pragma unroll
-  for (int q = 0; q < NDIR; q++) {
-    D.dF[q] = df_to(A.dF[q]) * sh;
-    if (!(fabs(D.dF[q]) <= GB_CBD_SDF - 0.05)) return false;
-  }
   const cplx eS = E0 * (S0 * s3n), eH = E0 * (sh * s3n), eDG = E0 * (-S0 * s3n);
 #pragma unroll
   for (int n = 0; n < 4; n++) {
-    D.G[n] = cmk(df_to(A.G[n].re), df_to(A.G[n].im)) * eS;
-    D.H[n] = cmk(df_to(A.H[n].re), df_to(A.H[n].im)) * eH;
+    D.G[n] = R.G[n] * eS;
+    D.H[n] = R.H[n] * eH;
 #pragma unroll
     for (int q = 0; q < NDIR; q++) {
-      D.dG[q][n] = cmk(df_to(A.dG[q][n].re), df_to(A.dG[q][n].im)) * eDG;
-      D.dH[q][n] = cmk(df_to(A.dH[q][n].re), df_to(A.dH[q][n].im)) * eH;
+      D.dG[q][n] = R.dG[q][n] * eDG;
+      D.dH[q][n] = R.dH[q][n] * eH;
     }
   }
-  D.F = df_to(A.F) * sh;
+  D.F = R.F * sh;
+#pragma unroll
+  for (int q = 0; q < NDIR; q++) D.dF[q] = R.dF[q] * sh;
+}
+
+// GLN x GLN integrals of source element S at the observation point rt (with
+// NDIR directions vt) in double-float, finished (scaled, sub-domain sign) into
+// D as reg_integrate<NDIR>(S, 2, ...) would; false if the pair must be
+// integrated in FP64 (a |dF| within 0.05 of CBD_SDF, or not finite).  why
+// (may be null) then tells which: 2 when every dF is finite and one exceeds
+// CBD_SDF + 0.05 (the pair certainly takes the GHN fallback rule), else 1.
+// adapt: the n x n rule of reg_order instead (n = GLN for near pairs).
+template <int NDIR>
+__device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double (*vt)[3], cplx k, bool neg,
+                                 RegAcc<NDIR>& D, bool adapt = false, int* why = nullptr) {
+  PairDN<NDIR> P;
+  const double a0 = pair_setup_dn<NDIR>(S, rt, vt, k, P);
+  const int nq = adapt ? reg_order(S, a0, k) : GB_GLN;
+  const int off = nq * (nq - 1) / 2;
+  const cplx E0 = cexpik(k, a0);
+  AccDN<NDIR> A;
+  acc_zero_dn<NDIR>(A);
+  // one loop over every point of the rule, so that the integrand is inlined
+  // at one site (the kernel is instruction-fetch bound otherwise)
+  reg_points_dn<NDIR, false>(S, P, nq, off, 0, 1, A);
+  RegAcc<NDIR> R;
+  acc_to_double<NDIR>(A, R);
+  finish_dn<NDIR>(R, S, neg, E0, D);
+  bool fin = true;
+  double mx = 0.0;
+#pragma unroll
+  for (int q = 0; q < NDIR; q++) {
+    if (!(fabs(D.dF[q]) <= 1e300)) fin = false;
+    else mx = fmax(mx, fabs(D.dF[q]));
+  }
+  if (!fin || mx > GB_CBD_SDF - 0.05) {
+    if (why) *why = (fin && mx > GB_CBD_SDF + 0.05) ? 2 : 1;
+    return false;
+  }
   return true;
+}
+
+// This thread's part (points lane, lane + nthr, ...) of the GHN x GHN rule
+// of the pair in double-float, as raw sums (acc_to_double) for a reduction
+// across the threads; E0 = e^{ik|R0|} for finish_dn.
+template <int NDIR>
+__device__ void reg_gh_part_dn(const Elem& S, const double rt[3], const double (*vt)[3], cplx k, int lane, int nthr,
+                               RegAcc<NDIR>& R, cplx& E0) {
+  PairDN<NDIR> P;
+  const double a0 = pair_setup_dn<NDIR>(S, rt, vt, k, P);
+  E0 = cexpik(k, a0);
+  AccDN<NDIR> A;
+  acc_zero_dn<NDIR>(A);
+  reg_points_dn<NDIR, true>(S, P, GB_GHN, 0, lane, nthr, A);
+  acc_to_double<NDIR>(A, R);
 }
