@@ -159,8 +159,11 @@ struct FieldArgs {
 
 // one warp per point; the point's domain (and therefore its source list and
 // wave number) is uniform across the warp
-template <bool DF>
+// MODE: FM_MEMP, FM_EH or FM_MEMP2, fixed at compile time so that each
+// variant holds only its own accumulators
+template <bool DF, int MODE>
 __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
+  constexpr int NACC = MODE == FM_MEMP ? 9 : (MODE == FM_EH ? 13 : 18);
   const int lane = threadIdx.x & 31;
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (p >= a.n) return;
@@ -178,8 +181,8 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
   const cplx* Hb = o.H[did];
   const cplx* dHb = o.dH[did];
   // accumulators (per lane), then reduced
-  double acc[34];
-  for (int i = 0; i < 34; i++) acc[i] = 0.0;
+  double acc[NACC];
+  for (int i = 0; i < NACC; i++) acc[i] = 0.0;
   int niter = (Ne + 31) / 32;
   for (int it = 0; it < niter; it++) {
     int s = 1 + it * 32 + lane;
@@ -188,12 +191,12 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
     Elem S;
     load_elem(S, o.cr, o.cw, o.etype, abs(sd));
     bool neg = sd < 0;
-    if (a.mode == FM_MEMP || a.mode == FM_EH) {
+    if (MODE == FM_MEMP || MODE == FM_EH) {
       if (!act) continue;
       RegAcc<0> A;
       reg_pair<DF, 0>(S, a.type, rt, nullptr, k, neg, A, o.prec == 3);
       acc[0] += A.F;
-      if (a.mode == FM_MEMP) {
+      if (MODE == FM_MEMP) {
         for (int n = 0; n < 4; n++)
           for (int l = 0; l < 4; l++) {
             cplx t = A.G[n] * dU[((size_t)s * 4 + n) * 4 + l] - A.H[n] * U[((size_t)s * 4 + n) * 4 + l];
@@ -212,7 +215,7 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
             acc[8 + 2 * l] += th.y;
           }
       }
-    } else if (a.mode == FM_MEMP2) {
+    } else if (MODE == FM_MEMP2) {
       double vt[1][3] = {{a.v[3 * p], a.v[3 * p + 1], a.v[3 * p + 2]}};
       RegAcc<1> A;
       bool fb = false;
@@ -236,16 +239,16 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
         }
     }
   }
-  warp_allreduce<34>(acc);
+  warp_allreduce<NACC>(acc);
   if (lane != 0) return;
   double F = acc[0];
   double den = (did == 0) ? 1.0 + F : F;
   cplx* out = a.out;
-  if (a.mode == FM_MEMP) {
+  if (MODE == FM_MEMP) {
     for (int l = 0; l < 4; l++) out[(size_t)p * 4 + l] = cdivr(cmk(acc[1 + 2 * l], acc[2 + 2 * l]), den);
-  } else if (a.mode == FM_EH) {
+  } else if (MODE == FM_EH) {
     for (int l = 0; l < 6; l++) out[(size_t)p * 6 + l] = cdivr(cmk(acc[1 + 2 * l], acc[2 + 2 * l]), den);
-  } else if (a.mode == FM_MEMP2) {
+  } else if (MODE == FM_MEMP2) {
     double dF = acc[1];
     for (int l = 0; l < 4; l++) {
       cplx u = cdivr(cmk(acc[2 + 2 * l], acc[3 + 2 * l]), den);
@@ -254,6 +257,30 @@ __global__ void __launch_bounds__(128) k_field(FieldArgs a) {
       out[(size_t)p * 8 + 4 + l] = du;
     }
   }
+}
+
+// Adds pair s's share to the FM_EH_MEMP accumulators: `take` bit d (d < 3)
+// selects the derivative terms of direction d, bit 3 the potential terms.
+__device__ __forceinline__ void eh_memp_add(double* acc, const RegAcc<3>& A, unsigned take, const cplx* U,
+                                            const cplx* dU, int s) {
+  if (take & 8u) acc[0] += A.F;
+  for (int d = 0; d < 3; d++)
+    if (take & (1u << d)) acc[1 + d] += A.dF[d];
+  for (int n = 0; n < 4; n++)
+    for (int l = 0; l < 4; l++) {
+      size_t q = ((size_t)s * 4 + n) * 4 + l;
+      if (take & 8u) {
+        cplx u = A.G[n] * dU[q] - A.H[n] * U[q];
+        acc[4 + 2 * l] += u.x;
+        acc[5 + 2 * l] += u.y;
+      }
+      for (int d = 0; d < 3; d++)
+        if (take & (1u << d)) {
+          cplx du = A.dG[d][n] * dU[q] - A.dH[d][n] * U[q];
+          acc[12 + d * 8 + 2 * l] += du.x;
+          acc[13 + d * 8 + 2 * l] += du.y;
+        }
+    }
 }
 
 // FM_EH_MEMP (reference EH_mEMP_s): U and the x,y,z derivatives of all four
@@ -284,37 +311,35 @@ __global__ void __launch_bounds__(128) k_field_eh_memp(FieldArgs a) {
     Elem S;
     load_elem(S, o.cr, o.cw, o.etype, abs(sd));
     bool neg = sd < 0;
-    RegAcc<3> A;
-    bool fb[3] = {false, false, false};
+    // fm: bit d = direction d needs the GHN rule, bit 3 = the potential
+    // terms do (they follow the z direction); the regular values of the
+    // other parts are added at once, so no copy of them is held while the
+    // warp integrates flagged pairs
+    unsigned fm = 0;
     if (act) {
+      RegAcc<3> A;
       reg_pair<DF, 3>(S, a.type, rt, vt, k, neg, A, o.prec == 3);
       if (a.type < 3)
-        for (int d = 0; d < 3; d++) fb[d] = fabs(A.dF[d]) > GB_CBD_SDF;
+        for (int d = 0; d < 3; d++)
+          if (fabs(A.dF[d]) > GB_CBD_SDF) fm |= 1u << d;
+      if (fm & 4u) fm |= 8u;
+      eh_memp_add(acc, A, ~fm & 15u, U, dU, s);
     }
-    bool any = fb[0] || fb[1] || fb[2];
-    RegAcc<3> B = A;
-    warp_fallback<3>(any, S, rt, vt, k, neg, B);
-    if (!act) continue;
-    if (fb[2]) { for (int n = 0; n < 4; n++) { A.G[n] = B.G[n]; A.H[n] = B.H[n]; } A.F = B.F; }
-    for (int d = 0; d < 3; d++)
-      if (fb[d]) {
-        for (int n = 0; n < 4; n++) { A.dG[d][n] = B.dG[d][n]; A.dH[d][n] = B.dH[d][n]; }
-        A.dF[d] = B.dF[d];
-      }
-    acc[0] += A.F;
-    for (int d = 0; d < 3; d++) acc[1 + d] += A.dF[d];
-    for (int n = 0; n < 4; n++)
-      for (int l = 0; l < 4; l++) {
-        size_t q = ((size_t)s * 4 + n) * 4 + l;
-        cplx u = A.G[n] * dU[q] - A.H[n] * U[q];
-        acc[4 + 2 * l] += u.x;
-        acc[5 + 2 * l] += u.y;
-        for (int d = 0; d < 3; d++) {
-          cplx du = A.dG[d][n] * dU[q] - A.dH[d][n] * U[q];
-          acc[12 + d * 8 + 2 * l] += du.x;
-          acc[13 + d * 8 + 2 * l] += du.y;
-        }
-      }
+    unsigned mask = __ballot_sync(0xffffffffu, fm != 0);
+    while (mask) {
+      int src = __ffs(mask) - 1;
+      mask &= mask - 1;
+      Elem Sb;
+      for (int i = 0; i < 12; i++) (&Sb.cr[0][0])[i] = __shfl_sync(0xffffffffu, (&S.cr[0][0])[i], src);
+      for (int i = 0; i < 9; i++) (&Sb.cw[0][0])[i] = __shfl_sync(0xffffffffu, (&S.cw[0][0])[i], src);
+      Sb.quad = __shfl_sync(0xffffffffu, S.quad, src);
+      bool negb = __shfl_sync(0xffffffffu, (int)neg, src) != 0;
+      RegAcc<3> B;
+      reg_integrate_gh_part<3>(Sb, lane, 32, rt, vt, k, B);
+      warp_allreduce<sizeof(RegAcc<3>) / sizeof(double)>((double*)&B);
+      reg_finish<3>(B, reg_scale_gh(Sb), negb);
+      if (lane == src) eh_memp_add(acc, B, fm, U, dU, s);
+    }
   }
   warp_allreduce<36>(acc);
   if (lane != 0) return;
@@ -758,8 +783,16 @@ extern "C" int gbi_field(const FieldObj* o, int mode, int type, int n, const dou
     if (dfp) k_field_eh_memp<true><<<nb, 128, 0, st>>>(a);
     else k_field_eh_memp<false><<<nb, 128, 0, st>>>(a);
   } else {
-    if (dfp) k_field<true><<<nb, 128, 0, st>>>(a);
-    else k_field<false><<<nb, 128, 0, st>>>(a);
+    if (a.mode == FM_MEMP) {
+      if (dfp) k_field<true, FM_MEMP><<<nb, 128, 0, st>>>(a);
+      else k_field<false, FM_MEMP><<<nb, 128, 0, st>>>(a);
+    } else if (a.mode == FM_EH) {
+      if (dfp) k_field<true, FM_EH><<<nb, 128, 0, st>>>(a);
+      else k_field<false, FM_EH><<<nb, 128, 0, st>>>(a);
+    } else {
+      if (dfp) k_field<true, FM_MEMP2><<<nb, 128, 0, st>>>(a);
+      else k_field<false, FM_MEMP2><<<nb, 128, 0, st>>>(a);
+    }
   }
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
