@@ -1733,8 +1733,15 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
   if (!rc) {
     const bool df = precision >= 2 && type == 2;
     if (df) {
+      void* kt = nullptr;
+      const int timed = gbi_kt_asm_start(st, &kt);
       k_asm_regular_df_list<<<breg[n], 128, 0, st>>>(dit, db, n);
       gbi_count_launch();
+      if (timed) {
+        double pairs = 0.0;
+        for (int i = 0; i < n; i++) pairs += (double)d[i].nrow * (double)d[i].m->sb_Ne[d[i].did];
+        gbi_kt_asm_stop(kt, st, pairs);
+      }
       unsigned ng = 0;
       if (cudaMemcpyAsync(&ng, ghn, sizeof(unsigned), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
           cudaStreamSynchronize(st) != cudaSuccess) {

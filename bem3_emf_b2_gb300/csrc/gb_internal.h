@@ -59,6 +59,8 @@ extern "C" {
 #endif
 void gbi_set_error(const char* fmt, ...);
 void gbi_count_launch(void);
+int gbi_kt_asm_start(cudaStream_t st, void** h);
+void gbi_kt_asm_stop(void* h, cudaStream_t st, double pairs);
 #ifdef __cplusplus
 }
 #endif

@@ -444,12 +444,65 @@ struct KtRec {
 std::mutex g_kt_mu;
 bool g_kt_on = false;
 std::vector<KtRec> g_kt;
+// launches of the double-float regular assembly (k_asm_regular_df_list):
+// events and the (collocation node, element) pairs each one covers
+struct KaRec {
+  cudaEvent_t a, b;
+  double pairs;
+};
+std::vector<KaRec> g_ka;
 }  // namespace
+
+// While timing is enabled: records an event on st before an assembly launch;
+// returns 1 if it did (the caller then calls gbi_kt_asm_stop after the launch)
+extern "C" int gbi_kt_asm_start(cudaStream_t st, void** h) {
+  std::lock_guard<std::mutex> lk(g_kt_mu);
+  if (!g_kt_on) return 0;
+  KaRec* r = new KaRec;
+  if (cudaEventCreate(&r->a) != cudaSuccess || cudaEventCreate(&r->b) != cudaSuccess ||
+      cudaEventRecord(r->a, st) != cudaSuccess) {
+    delete r;
+    return 0;
+  }
+  *h = r;
+  return 1;
+}
+
+extern "C" void gbi_kt_asm_stop(void* h, cudaStream_t st, double pairs) {
+  KaRec* r = (KaRec*)h;
+  r->pairs = pairs;
+  cudaEventRecord(r->b, st);
+  std::lock_guard<std::mutex> lk(g_kt_mu);
+  g_ka.push_back(*r);
+  delete r;
+}
+
+// recorded double-float assembly launches: total device ms, pairs, launches
+// (not cleared; gb_ktime_enable clears)
+extern "C" int gb_ktime_asm(double* ms, double* pairs, long* launches) {
+  std::lock_guard<std::mutex> lk(g_kt_mu);
+  double t = 0.0, p = 0.0;
+  for (auto& r : g_ka) {
+    float x = 0.f;
+    if (cudaEventSynchronize(r.b) != cudaSuccess || cudaEventElapsedTime(&x, r.a, r.b) != cudaSuccess) {
+      gbi_set_error("gb_ktime_asm: event query failed");
+      return -1;
+    }
+    t += x;
+    p += r.pairs;
+  }
+  *ms = t;
+  *pairs = p;
+  *launches = (long)g_ka.size();
+  return 0;
+}
 
 extern "C" void gb_ktime_enable(int on) {
   std::lock_guard<std::mutex> lk(g_kt_mu);
   for (auto& r : g_kt) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
   g_kt.clear();
+  for (auto& r : g_ka) { cudaEventDestroy(r.a); cudaEventDestroy(r.b); }
+  g_ka.clear();
   g_kt_on = on != 0;
 }
 

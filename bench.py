@@ -432,6 +432,9 @@ def run_gpu(args):
     t_instr = time.perf_counter() - t0
     kt = ktime_list()
     ktime_read()
+    asm_t = (ctypes.c_double(), ctypes.c_double(), ctypes.c_long())
+    if L.gb_ktime_asm(*[ctypes.byref(x) for x in asm_t]) != 0:
+        asm_t = None
     L.gb_ktime_enable(0)
     force_err = rel_vec(force_vec(F32, N32), force_vec(F64, N64))
     out = None
@@ -471,6 +474,9 @@ def run_gpu(args):
             out["iterations"] = {"count": iters[0], "cc": iters[1]}
         if roof:
             out["roofline"] = roof
+        roof_asm = roofline_assembly(asm_t, clk.summary()) if asm_t else None
+        if roof_asm:
+            out["roofline_assembly"] = roof_asm
         if cpu:
             out["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample", "estimated")}
     sc.close()
@@ -541,6 +547,41 @@ def roofline_live(klist, step_seconds, steps):
             out = inner
         else:
             out["inner_launches"] = inner
+    return out
+
+
+ASM_ISSUE_FILE = os.path.join(ROOT, "profiles", "asm_regular_df_issue.json")
+
+
+def roofline_assembly(rec, clocks):
+    """Issue-rate roofline of the double-float regular assembly
+    (k_asm_regular_df_list), the step's largest kernel: bound by the SM
+    sub-partitions' instruction issue (one warp instruction per clock each,
+    4 per SM) and within that by the FP32 pipe.  Live: device time and pairs
+    of its launches in the instrumented step (CUDA events on its stream).
+    Instructions per pair: an ncu count of the same launch on the same
+    workload (profiles/asm_regular_df_issue.json).  Peaks at the median SM
+    clock sampled during the timed steps."""
+    import torch
+    ms, pairs, n = rec[0].value, rec[1].value, rec[2].value
+    if n <= 0 or ms <= 0.0:
+        return None
+    rate = pairs / (ms / 1000.0)
+    out = {"kernel": "k_asm_regular_df_list (double-float regular pairs, all (object, domain) items)",
+           "bound": "fp32-issue", "launches_per_step": n, "kernel_ms_total": ms, "pairs_per_launch": pairs / n,
+           "pairs_per_s": rate}
+    iss = json.load(open(ASM_ISSUE_FILE)) if os.path.exists(ASM_ISSUE_FILE) else None
+    mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    if iss:
+        slots = nsm * 4 * float(mhz) * 1e6  # warp instructions per second, all sub-partitions
+        ach = iss["inst_per_pair"] * rate
+        fma = iss["fma_pipe_inst_per_pair"] * rate
+        out.update({"achieved": fma / 1e9, "peak": slots / 1e9, "unit": "G warp-inst/s (FP32 pipe)",
+                    "frac": fma / slots, "issue_achieved": ach / 1e9, "issue_frac": ach / slots,
+                    "peak_source": "%d SMs x 4 sub-partitions x 1 warp instruction per clock at %.0f MHz" % (nsm, mhz),
+                    "inst_counts": "ncu smsp__inst_executed.sum and smsp__inst_executed_pipe_fma.sum per pair, %s" %
+                                   iss.get("source", "")})
     return out
 
 

@@ -65,6 +65,9 @@ int gb_ktime_read(double *ms, long *launches, double *flops, double *bytes);
 /* the recorded launches one by one, without clearing: rec[4i..4i+3] = device
  * ms, M, N, K of launch i (i < cap); returns the number recorded, -1 on error */
 int gb_ktime_list(int cap, double *rec);
+/* the double-float regular assembly launches recorded while timing was on:
+ * total device ms, (collocation node, element) pairs they covered, launches */
+int gb_ktime_asm(double *ms, double *pairs, long *launches);
 
 int gb_obj_create(const gb_mesh_desc *m, gb_obj **out);
 void gb_obj_destroy(gb_obj *o);
