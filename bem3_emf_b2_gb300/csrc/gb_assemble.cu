@@ -338,10 +338,11 @@ __device__ __forceinline__ void asm_regular_df_body(const AsmArgs& a, uint8_t* r
   RegAcc<2> D;
   int why = 0;
   if (!reg_integrate_dn<2>(S, rt, vt, a.k, sd < 0, D, a.adapt != 0, &why)) {
-    redo[p] = 1;
     // certainly the GHN rule (the FP64 decision cannot differ): listed for
     // the double-float GHN kernel instead of the FP64 pass (the learned
-    // quadrature, when on, takes these pairs in the FP64 pass)
+    // quadrature, when on, takes these pairs in the FP64 pass, flagged 2 so
+    // that a reverted correction integrates them as this path does)
+    redo[p] = why == 2 ? 2 : 1;
     if (why == 2 && a.gh != nullptr && a.lq.p == nullptr) {
       const unsigned slot = atomicAdd(a.ghn, 1u);
       if (slot < a.ghcap) {
@@ -451,6 +452,7 @@ __device__ __forceinline__ void asm_regular_body(const AsmArgs& a, const uint8_t
         q.out[5] = (struct cplx*)(a.dH + (lr * 2 + 1) * N + col);
         q.f = a.Fs + (lr * a.Ne + sidx) * 3;
         q.neg = neg ? 1 : 0;
+        q.gh_df = (only != nullptr && only[p] == 2) ? 1 : 0;
         listed = 1;
       }
     }
@@ -1016,7 +1018,10 @@ __device__ __forceinline__ int find_item(const unsigned* __restrict__ blk0, int 
   }
   return lo;
 }
-__global__ void __launch_bounds__(128) k_asm_regular_df_list(const AsmArgs* __restrict__ items,
+#ifndef GB_ASM_MINB
+#define GB_ASM_MINB 1
+#endif
+__global__ void __launch_bounds__(128, GB_ASM_MINB) k_asm_regular_df_list(const AsmArgs* __restrict__ items,
                                                              const unsigned* __restrict__ blk0, int nitems) {
   const int i = find_item(blk0, nitems, blockIdx.x);
   asm_regular_df_body(items[i], items[i].redo, blockIdx.x - blk0[i]);
@@ -1233,7 +1238,20 @@ __global__ void __launch_bounds__(128) k_lq_exact(int n, const GbLqPair* __restr
   if (w >= n) return;
   const GbLqPair& q = P[w];
   RegAcc<2> GL, GH;
-  lq_rules(q, lane, q.neg != 0, false, GL, GH);
+  if (q.gh_df) {
+    // as k_asm_gh_df integrates the pair when the network is off
+    Elem S;
+    double h;
+    lq_elem(q, S, h);
+    const double vt[2][3] = {{q.vt[0], q.vt[1], q.vt[2]}, {q.vt[3], q.vt[4], q.vt[5]}};
+    RegAcc<2> R;
+    cplx E0;
+    reg_gh_part_dn<2>(S, q.rt, vt, cmk(q.k[0], q.k[1]), lane, 32, R, E0);
+    warp_allreduce<sizeof(RegAcc<2>) / sizeof(double)>((double*)&R);
+    finish_dn<2>(R, S, q.neg != 0, E0, GH);
+  } else {
+    lq_rules(q, lane, q.neg != 0, false, GL, GH);
+  }
   if (lane != 0) return;
   for (int nn = 0; nn < 4; nn++) {
     q.out[0][nn] = GH.G[nn];

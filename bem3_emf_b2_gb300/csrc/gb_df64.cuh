@@ -80,6 +80,21 @@ __device__ __forceinline__ df df_fma(df c, df a, df b) {
   const float e = __fadd_rn(__fsub_rn(c.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
   return quick_two_sum(s, __fadd_rn(e, __fadd_rn(c.lo, pe)));
 }
+// Accumulator step c + a b for sums that are only read through df_to: the
+// high parts are added exactly (two_sum) and every error term goes to the
+// low part, which is never renormalised (compensated summation).  The low
+// part stays within a few ulps of the high part over the short sums of a
+// quadrature rule, so hi + lo still holds the sum to the format's rounding
+// and converts to double exactly; three instructions fewer than df_fma.
+__device__ __forceinline__ df df_acc(df c, df a, df b) {
+  const float p = __fmul_rn(a.hi, b.hi);
+  float pe = fmaf(a.hi, b.hi, -p);
+  pe = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, pe));
+  const float s = __fadd_rn(c.hi, p);
+  const float bb = __fsub_rn(s, c.hi);
+  const float e = __fadd_rn(__fsub_rn(c.hi, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  return dfmk(s, __fadd_rn(c.lo, __fadd_rn(e, pe)));
+}
 __device__ __forceinline__ df df_sqr(df a) {
   df p = two_prod(a.hi, a.hi);
   p.lo = fmaf(2.0f * a.hi, a.lo, p.lo);

@@ -122,6 +122,16 @@ __global__ void __launch_bounds__(128) k_domain_id(FieldObj o, int n, const doub
   if (lane == 0) did[p] = res;
 }
 
+// Resident blocks of 128 threads per SM the point-sum kernels are compiled
+// for (register cap 65536 / (128 x blocks)): the double-float sums are
+// latency-bound chains, so more resident warps can outweigh spilled registers
+#ifndef GB_FIELD_MINB
+#define GB_FIELD_MINB 1
+#endif
+#ifndef GB_CROSS_MINB
+#define GB_CROSS_MINB 1
+#endif
+
 // ------------------------------------------------------------------ field sums
 enum { FM_MEMP = 0, FM_EH = 1, FM_EH_MEMP = 2, FM_MEMP2 = 3 };
 
@@ -162,7 +172,7 @@ struct FieldArgs {
 // MODE: FM_MEMP, FM_EH or FM_MEMP2, fixed at compile time so that each
 // variant holds only its own accumulators
 template <bool DF, int MODE>
-__global__ void __launch_bounds__(128) k_field(FieldArgs a) {
+__global__ void __launch_bounds__(128, GB_FIELD_MINB) k_field(FieldArgs a) {
   constexpr int NACC = MODE == FM_MEMP ? 9 : (MODE == FM_EH ? 13 : 18);
   const int lane = threadIdx.x & 31;
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -378,7 +388,7 @@ struct BdArgs {
 };
 
 template <bool DF>
-__global__ void __launch_bounds__(128) k_field_bd(BdArgs a) {
+__global__ void __launch_bounds__(128, GB_FIELD_MINB) k_field_bd(BdArgs a) {
   const int lane = threadIdx.x & 31;
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (p >= a.n) return;
@@ -546,7 +556,7 @@ __global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
 // double-float pass of the two-pass build: one thread per (point, source
 // element) pair, the GLN rule in double-float (reg_integrate_dn); pairs it
 // declines (near the CBD_SDF decision) are flagged for the FP64 pass
-__global__ void __launch_bounds__(128) k_cross_build_df(CrossArgs a, uint8_t* redo) {
+__global__ void __launch_bounds__(128, GB_CROSS_MINB) k_cross_build_df(CrossArgs a, uint8_t* redo) {
   const FieldObj& o = a.o;
   const int Ne = o.sb_Ne[0];
   const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -45,7 +45,8 @@ typedef struct GbLqPair {
   double k[2];
   struct cplx* out[6];
   double* f;
-  int neg, pad;
+  int neg;
+  int gh_df;  // the pair certainly takes the GHN rule: without the network it is integrated in double-float
 } GbLqPair;
 typedef struct GbLqList {
   GbLqPair* p;       // null: the assembly integrates every fallback pair by the 64 x 64 rule

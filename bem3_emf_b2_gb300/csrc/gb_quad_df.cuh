@@ -60,6 +60,9 @@ __device__ __forceinline__ df dot3d(const df a[3], const df b[3]) {
 __device__ __forceinline__ dfc dfc_fma_re(dfc acc, dfc v, df s) {  // acc + v s
   return dfcmk(df_fma(acc.re, v.re, s), df_fma(acc.im, v.im, s));
 }
+__device__ __forceinline__ dfc dfc_acc_re(dfc acc, dfc v, df s) {  // acc + v s (accumulators: df_acc)
+  return dfcmk(df_acc(acc.re, v.re, s), df_acc(acc.im, v.im, s));
+}
 
 #define GB_ND(n) ((n) > 0 ? (n) : 1)
 template <int NDIR>
@@ -104,11 +107,11 @@ __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[
 #pragma unroll
   for (int n = 0; n < 4; n++) {
     if (n < ns) {
-      A.G[n] = dfc_fma_re(A.G[n], g, N[n]);
-      A.H[n] = dfc_fma_re(A.H[n], h, N[n]);
+      A.G[n] = dfc_acc_re(A.G[n], g, N[n]);
+      A.H[n] = dfc_acc_re(A.H[n], h, N[n]);
     }
   }
-  A.F = df_fma(A.F, w, tD);
+  A.F = df_acc(A.F, w, tD);
   if (NDIR > 0) {
     const dfc t1 = dfc_add(dfc_mul(kR, kR), dfcmk(df_mul_f(cb.re, 3.0f), df_mul_f(cb.im, 3.0f)));
     const df iR3w = df_mul(df_mul(iR2, iR), w);
@@ -122,11 +125,11 @@ __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[
 #pragma unroll
       for (int n = 0; n < 4; n++) {
         if (n < ns) {
-          A.dG[q][n] = dfc_fma_re(A.dG[q][n], dg, N[n]);
-          A.dH[q][n] = dfc_fma_re(A.dH[q][n], dh, N[n]);
+          A.dG[q][n] = dfc_acc_re(A.dG[q][n], dg, N[n]);
+          A.dH[q][n] = dfc_acc_re(A.dH[q][n], dh, N[n]);
         }
       }
-      A.dF[q] = df_fma(A.dF[q], iR3w, df_sub(df_mul_f(df_mul(rdv, rdW), 3.0f), Wdv));
+      A.dF[q] = df_acc(A.dF[q], iR3w, df_sub(df_mul_f(df_mul(rdv, rdW), 3.0f), Wdv));
     }
   }
 }

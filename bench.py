@@ -439,7 +439,7 @@ def run_gpu(args):
     force_err = rel_vec(force_vec(F32, N32), force_vec(F64, N64))
     out = None
     if rank == 0:
-        roof = roofline_live(kt, t_instr, 1)
+        roof = roofline_live(kt, t_instr, 1, tf32_peak())
         cpu = cpu_baseline(args, wd, iters[0] if iters else 11) if (ws == 1 and not args.no_cpu and
                                                                     args.workload != "beams") else None
         cfg = {"workload": desc["workload"], "objects": desc["objects"],
@@ -488,19 +488,53 @@ def run_gpu(args):
 TRAFFIC_FILE = os.path.join(ROOT, "profiles", "tc_cgemm_traffic.json")
 
 
-def roofline_live(klist, step_seconds, steps):
+def gb_tc_passes():
+    """tensor-core passes of the library's FP32 factorisations"""
+    from bem3_emf_b2_gb300 import lib
+    return int(lib().gb_get_tc_passes())
+
+
+def tf32_peak(n=8192, reps=10):
+    """Dense TF32 GEMM rate of this GPU through cuBLAS (torch matmul of two
+    n x n FP32 matrices with TF32 allowed; CUDA events, after warm-up): the
+    ceiling of the single-pass TF32 tensor-core kernel, measured in the run
+    instead of taken from a data-sheet ratio.  TFLOP/s (2 n^3 per product)."""
+    import torch
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = True
+    try:
+        g = torch.Generator(device="cuda").manual_seed(5)
+        a = torch.randn(n, n, device="cuda", generator=g)
+        b = torch.randn(n, n, device="cuda", generator=g)
+        c = torch.empty(n, n, device="cuda")
+        for _ in range(3):
+            torch.matmul(a, b, out=c)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            torch.matmul(a, b, out=c)
+        e1.record()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1000.0 / reps
+        del a, b, c
+        return 2.0 * n ** 3 / t / 1e12
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+def roofline_live(klist, step_seconds, steps, tf32=None):
     """Roofline of the factorisation's tensor-core update kernel
-    k_tc_cgemm_sub (tcgen05, TF32 in three passes for FP32 accuracy) from
-    CUDA events around each of its launches on the library's streams in one
-    instrumented step.  Per launch M x N x K (complex): algorithmic flops
-    8 M N K (complex-equivalent), algorithmic HBM bytes 16 M N (C read and
-    written) + the split operands 2 x 4 (M + 2N) Kp.  Two classes: launches
-    with K >= 128 (outer-block updates and the block elimination's products:
-    >= 64 complex flop per byte, tensor-bound) and the inner-panel updates
-    (K <= 64, HBM-bound).  The tensor figures are against the measured dense
-    bf16 peak; tcgen05 kind::tf32 issues at 1.1/2.25 of the kind::f16 rate and
-    the FP32-accurate split needs three passes, so the ceiling this
-    arithmetic can reach is bf16 x (1.1 / 2.25) / 3, reported beside it."""
+    k_tc_cgemm_sub (tcgen05 kind::tf32; one pass by default, three split
+    passes for FP32-accurate products) from CUDA events around each of its
+    launches on the library's streams in one instrumented step.  Per launch
+    M x N x K (complex): algorithmic flops 8 M N K (complex-equivalent),
+    algorithmic HBM bytes 16 M N (C read and written) + the split operands
+    2 x 4 (M + 2N) Kp.  Two classes: launches with K >= 128 (outer-block
+    updates and the block elimination's products: >= 64 complex flop per
+    byte, tensor-bound) and the inner-panel updates (K <= 64, HBM-bound).
+    The tensor figures are against the measured dense bf16 peak and, beside
+    it, the TF32 rate cuBLAS reaches on the same GPU in the same run (tf32)."""
     if not klist:
         return None
     peaks = {}
@@ -526,12 +560,13 @@ def roofline_live(klist, step_seconds, steps):
         dt = o[1] / 1000.0
         ach = o[2] / dt / 1e12
         ratio = tr.get("outer", {}).get("dram_bytes_per_algorithmic_byte")
-        out = {"kernel": "k_tc_cgemm_sub (tcgen05 TF32 x3 complex update), launches with K >= 128",
+        out = {"kernel": "k_tc_cgemm_sub (tcgen05 TF32 complex update, passes %d), launches with K >= 128" % gb_tc_passes(),
                "bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16,
                "peak_source": src + " bf16_tflops",
                "traffic": ratio * o[3] / o[0] if ratio else None,
                "algorithmic_bytes_per_launch": o[3] / o[0], "algorithmic_flops_per_launch": o[2] / o[0],
                "tf32x3_ceiling_tflops": ceil3, "frac_of_tf32x3_ceiling": ach / ceil3,
+               "tf32_cublas_tflops_measured": tf32, "frac_of_tf32_measured": ach / tf32 if tf32 else None,
                "launches_per_step": o[0] / steps, "kernel_ms_total": o[1],
                "kernel_share_of_timed_steps": dt / step_seconds}
     i = cls["inner"]
