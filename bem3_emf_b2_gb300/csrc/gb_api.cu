@@ -452,7 +452,15 @@ static int check_asm_args(int type, int precision) {
   return 0;
 }
 
+// Newly assembled matrices: every factor, warm start and scattering operator
+// derived from the previous ones is dropped, so that a scene step after an
+// assembly repeats all of the scene's work (the scattering operators this
+// object holds are rebuilt by the next iteration that needs them)
 static void assembled(gb_obj* o, int precision) {
+  for (auto& e : o->xc) {
+    cudaFree(e.did); cudaFree(e.Gm); cudaFree(e.Hm); cudaFree(e.dGm); cudaFree(e.dHm); cudaFree(e.Fp);
+  }
+  o->xc.clear();
   o->have_invA = 0;
   o->have_lu32 = 0;
   o->have_blk64 = 0;

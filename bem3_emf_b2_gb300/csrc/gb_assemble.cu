@@ -1019,7 +1019,7 @@ __device__ __forceinline__ int find_item(const unsigned* __restrict__ blk0, int 
   return lo;
 }
 #ifndef GB_ASM_MINB
-#define GB_ASM_MINB 1
+#define GB_ASM_MINB 3
 #endif
 __global__ void __launch_bounds__(128, GB_ASM_MINB) k_asm_regular_df_list(const AsmArgs* __restrict__ items,
                                                              const unsigned* __restrict__ blk0, int nitems) {

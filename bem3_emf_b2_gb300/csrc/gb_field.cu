@@ -689,10 +689,11 @@ __global__ void k_bv_to_df(int C, const cplx* __restrict__ U, const cplx* __rest
 
 __device__ __forceinline__ dfc dfc_ld(const float4& f) { return dfcmk(dfmk(f.x, f.y), dfmk(f.z, f.w)); }
 // acc + a b (complex double-float)
+// acc + a b for accumulators read only through df_to (compensated steps)
 __device__ __forceinline__ dfc dfc_fma(dfc acc, dfc a, dfc b) {
   dfc r;
-  r.re = df_fma(df_fma(acc.re, a.re, b.re), df_neg(a.im), b.im);
-  r.im = df_fma(df_fma(acc.im, a.re, b.im), a.im, b.re);
+  r.re = df_acc(df_acc(acc.re, a.re, b.re), df_neg(a.im), b.im);
+  r.im = df_acc(df_acc(acc.im, a.re, b.im), a.im, b.re);
   return r;
 }
 

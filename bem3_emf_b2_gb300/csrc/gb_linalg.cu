@@ -319,11 +319,12 @@ extern "C" int gbi_to_df(size_t n, const cplx* src, void* dst, cudaStream_t st) 
 }
 
 __device__ __forceinline__ dfc dfc_ld4(const float4 f) { return dfcmk(dfmk(f.x, f.y), dfmk(f.z, f.w)); }
-// acc + a b, complex double-float
+// acc + a b, complex double-float, for accumulators read only through
+// df_to (compensated steps, df_acc)
 __device__ __forceinline__ dfc dfc_mac(dfc acc, dfc a, dfc b) {
   dfc r;
-  r.re = df_fma(df_fma(acc.re, a.re, b.re), df_neg(a.im), b.im);
-  r.im = df_fma(df_fma(acc.im, a.re, b.im), a.im, b.re);
+  r.re = df_acc(df_acc(acc.re, a.re, b.re), df_neg(a.im), b.im);
+  r.im = df_acc(df_acc(acc.im, a.re, b.im), a.im, b.re);
   return r;
 }
 
