@@ -688,8 +688,8 @@ __global__ void k_bv_to_df(int C, const cplx* __restrict__ U, const cplx* __rest
 }
 
 __device__ __forceinline__ dfc dfc_ld(const float4& f) { return dfcmk(dfmk(f.x, f.y), dfmk(f.z, f.w)); }
-// acc + a b (complex double-float)
-// acc + a b for accumulators read only through df_to (compensated steps)
+// acc + a b (complex double-float) for accumulators read only through df_to
+// (compensated steps)
 __device__ __forceinline__ dfc dfc_fma(dfc acc, dfc a, dfc b) {
   dfc r;
   r.re = df_acc(df_acc(acc.re, a.re, b.re), df_neg(a.im), b.im);
@@ -713,12 +713,30 @@ __global__ void __launch_bounds__(128) k_cross_apply_df(int n, int C, const floa
 #pragma unroll
   for (int l = 0; l < 4; l++) { u[l] = dfcmk(z, z); du[l] = dfcmk(z, z); }
   const size_t row = (size_t)p * C;
+  // software-pipelined: the next column's coefficients and boundary values
+  // are loaded before this column's products
+  const float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 mn[4] = {f0, f0, f0, f0}, an[4], bn[4];
+  if (lane < C) {
+    mn[0] = Gm[row + lane]; mn[1] = Hm[row + lane]; mn[2] = dGm[row + lane]; mn[3] = dHm[row + lane];
+#pragma unroll
+    for (int l = 0; l < 4; l++) { an[l] = dUd[(size_t)lane * 4 + l]; bn[l] = Ud[(size_t)lane * 4 + l]; }
+  }
   for (int c = lane; c < C; c += 32) {
-    const dfc g = dfc_ld(Gm[row + c]), h = dfc_ld(Hm[row + c]), dg = dfc_ld(dGm[row + c]), dh = dfc_ld(dHm[row + c]);
+    const dfc g = dfc_ld(mn[0]), h = dfc_ld(mn[1]), dg = dfc_ld(mn[2]), dh = dfc_ld(mn[3]);
+    float4 ac[4], bc[4];
+#pragma unroll
+    for (int l = 0; l < 4; l++) { ac[l] = an[l]; bc[l] = bn[l]; }
+    const int cn = c + 32;
+    if (cn < C) {
+      mn[0] = Gm[row + cn]; mn[1] = Hm[row + cn]; mn[2] = dGm[row + cn]; mn[3] = dHm[row + cn];
+#pragma unroll
+      for (int l = 0; l < 4; l++) { an[l] = dUd[(size_t)cn * 4 + l]; bn[l] = Ud[(size_t)cn * 4 + l]; }
+    }
     const dfc mh = dfcmk(df_neg(h.re), df_neg(h.im)), mdh = dfcmk(df_neg(dh.re), df_neg(dh.im));
 #pragma unroll
     for (int l = 0; l < 4; l++) {
-      const dfc a = dfc_ld(dUd[(size_t)c * 4 + l]), b = dfc_ld(Ud[(size_t)c * 4 + l]);
+      const dfc a = dfc_ld(ac[l]), b = dfc_ld(bc[l]);
       u[l] = dfc_fma(dfc_fma(u[l], g, a), mh, b);
       du[l] = dfc_fma(dfc_fma(du[l], dg, a), mdh, b);
     }

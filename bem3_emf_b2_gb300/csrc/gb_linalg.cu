@@ -345,13 +345,31 @@ __global__ void k_apply_rows_df(const float4* __restrict__ G, const float4* __re
   dfc acc[4];
 #pragma unroll
   for (int q = 0; q < 4; q++) acc[q] = dfcmk(z, z);
-  for (size_t c = lane; c < N; c += 32) {
-    const dfc gv = dfc_ld4(g[c]), hv = dfc_ld4(h[c]);
+  // software-pipelined: the next column's matrix entries and node vectors
+  // are loaded before this column's products (the loop was bound by the
+  // loads' latency)
+  const float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float4 gn = f0, hn = f0, vn[8];
+  if ((size_t)lane < N) {
+    gn = g[lane];
+    hn = h[lane];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      const dfc p = dfc_ld4(PQ[(size_t)q * N + c]), qq = dfc_ld4(PQ[(size_t)(4 + q) * N + c]);
-      acc[q] = dfc_mac(dfc_mac(acc[q], hv, p), gv, qq);
+    for (int q = 0; q < 8; q++) vn[q] = PQ[(size_t)q * N + lane];
+  }
+  for (size_t c = lane; c < N; c += 32) {
+    const dfc gv = dfc_ld4(gn), hv = dfc_ld4(hn);
+    float4 vc[8];
+#pragma unroll
+    for (int q = 0; q < 8; q++) vc[q] = vn[q];
+    const size_t cn = c + 32;
+    if (cn < N) {
+      gn = g[cn];
+      hn = h[cn];
+#pragma unroll
+      for (int q = 0; q < 8; q++) vn[q] = PQ[(size_t)q * N + cn];
     }
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc[q] = dfc_mac(dfc_mac(acc[q], hv, dfc_ld4(vc[q])), gv, dfc_ld4(vc[4 + q]));
   }
   double s[8];
 #pragma unroll
