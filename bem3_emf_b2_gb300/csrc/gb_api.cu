@@ -345,6 +345,8 @@ extern "C" int gb_obj_create(const gb_mesh_desc* md, gb_obj** out) {
   GbMeshDev& m = o->m;
   m.Ne = md->Ne; m.NN = md->NN; m.MN = md->MN;
   size_t ne1 = (size_t)md->Ne + 1;
+  m.ntri = m.nquad = 0;
+  for (int e = 1; e <= md->Ne; e++) (md->etype[e] ? m.nquad : m.ntri)++;
   int tot = 0;
   for (int d = 0; d <= md->MN; d++) { m.sb_Ne[d] = md->sb_Ne[d]; m.sb_off[d] = tot; tot += md->sb_Ne[d] + 1; }
   m.sb_off[md->MN + 1] = tot;
@@ -882,6 +884,8 @@ static FieldObj field_view(gb_obj* o) {
   f.MN = o->m.MN;
   f.lambda0 = o->lambda0;
   f.prec = o->field_prec;
+  f.ntri = o->m.ntri;
+  f.nquad = o->m.nquad;
   return f;
 }
 

@@ -317,6 +317,11 @@ __global__ void __launch_bounds__(128) k_asm_regular_f32(AsmArgs a, uint8_t* red
 // (reg_integrate_dn, gb_quad_df.cuh); pairs whose |Re dF/dt| is within 0.05
 // of the CBD_SDF decision (or not finite) are flagged and redone by the FP64
 // kernel, which decides GLN/GHN exactly as the reference.
+// TSEL: 0 every pair; 1 only pairs whose source element is a triangle
+// (compiled with three shape functions' sums: fewer registers), 2 only
+// quadrangle sources.  A launch of TSEL 1 or 2 writes nothing for the other
+// type's pairs, so the two launches together cover each pair once.
+template <int TSEL>
 __device__ __forceinline__ void asm_regular_df_body(const AsmArgs& a, uint8_t* redo, unsigned bx) {
   const size_t N = (size_t)a.Ne * 4;
   const size_t npair = (size_t)a.nrow * (size_t)a.Ne;
@@ -325,6 +330,7 @@ __device__ __forceinline__ void asm_regular_df_body(const AsmArgs& a, uint8_t* r
   const int row = a.row0 + (int)(p / a.Ne), sidx = (int)(p % a.Ne);
   const int t = row / 4 + 1, tn = row % 4;
   const int td = __ldg(a.sid + t), sd = __ldg(a.sid + sidx + 1);
+  if (TSEL != 0 && (__ldg(a.etype + abs(sd)) != 0) != (TSEL == 2)) return;
   const int atd = abs(td);
   Elem T;
   load_elem(T, a.cr, a.cw, a.etype, atd);
@@ -337,7 +343,7 @@ __device__ __forceinline__ void asm_regular_df_body(const AsmArgs& a, uint8_t* r
   node_tangents(T, tn, vt);
   RegAcc<2> D;
   int why = 0;
-  if (!reg_integrate_dn<2>(S, rt, vt, a.k, sd < 0, D, a.adapt != 0, &why)) {
+  if (!reg_integrate_dn<2, TSEL == 1 ? 3 : 4>(S, rt, vt, a.k, sd < 0, D, a.adapt != 0, &why)) {
     // certainly the GHN rule (the FP64 decision cannot differ): listed for
     // the double-float GHN kernel instead of the FP64 pass (the learned
     // quadrature, when on, takes these pairs in the FP64 pass, flagged 2 so
@@ -387,7 +393,7 @@ __global__ void __launch_bounds__(128) k_asm_gh_df(const AsmArgs* __restrict__ i
   store_pair(a, (size_t)a.Ne * 4, e.row, e.sidx, D);
 }
 __global__ void __launch_bounds__(128) k_asm_regular_df(AsmArgs a, uint8_t* redo) {
-  asm_regular_df_body(a, redo, blockIdx.x);
+  asm_regular_df_body<0>(a, redo, blockIdx.x);
 }
 
 // FP64 regular pairs (all, or those flagged in only); the whole warp
@@ -1018,13 +1024,19 @@ __device__ __forceinline__ int find_item(const unsigned* __restrict__ blk0, int 
   }
   return lo;
 }
+// resident blocks of 128 threads per SM the list kernel is compiled for
+// (quadrangle sources; GB_ASM_TRI_MINB for the triangle-only variant)
 #ifndef GB_ASM_MINB
 #define GB_ASM_MINB 3
 #endif
-__global__ void __launch_bounds__(128, GB_ASM_MINB) k_asm_regular_df_list(const AsmArgs* __restrict__ items,
+#ifndef GB_ASM_TRI_MINB
+#define GB_ASM_TRI_MINB 3
+#endif
+template <int TSEL>
+__global__ void __launch_bounds__(128, TSEL == 1 ? GB_ASM_TRI_MINB : GB_ASM_MINB) k_asm_regular_df_list(const AsmArgs* __restrict__ items,
                                                              const unsigned* __restrict__ blk0, int nitems) {
   const int i = find_item(blk0, nitems, blockIdx.x);
-  asm_regular_df_body(items[i], items[i].redo, blockIdx.x - blk0[i]);
+  asm_regular_df_body<TSEL>(items[i], items[i].redo, blockIdx.x - blk0[i]);
 }
 __global__ void __launch_bounds__(128) k_asm_regular_list(const AsmArgs* __restrict__ items,
                                                           const unsigned* __restrict__ blk0, int nitems, int flagged) {
@@ -1753,8 +1765,23 @@ extern "C" int gbi_assemble_list(const GbAsmItem* d, int n, int type, int precis
     if (df) {
       void* kt = nullptr;
       const int timed = gbi_kt_asm_start(st, &kt);
-      k_asm_regular_df_list<<<breg[n], 128, 0, st>>>(dit, db, n);
-      gbi_count_launch();
+      // triangle sources by the three-shape-function variant, quadrangles by
+      // the general one (one launch when the meshes hold one type)
+      bool tri = false, quad = false;
+      for (int i = 0; i < n; i++) {
+        tri = tri || d[i].m->ntri > 0;
+        quad = quad || d[i].m->nquad > 0;
+      }
+      if (!tri && !quad) quad = true;  // counts not known: the general variant
+      if (tri) {
+        k_asm_regular_df_list<1><<<breg[n], 128, 0, st>>>(dit, db, n);
+        gbi_count_launch();
+      }
+      if (quad) {
+        if (tri) k_asm_regular_df_list<2><<<breg[n], 128, 0, st>>>(dit, db, n);
+        else k_asm_regular_df_list<0><<<breg[n], 128, 0, st>>>(dit, db, n);
+        gbi_count_launch();
+      }
       if (timed) {
         double pairs = 0.0;
         for (int i = 0; i < n; i++) pairs += (double)d[i].nrow * (double)d[i].m->sb_Ne[d[i].did];

@@ -556,20 +556,24 @@ __global__ void __launch_bounds__(128) k_cross_build(CrossArgs a) {
 // double-float pass of the two-pass build: one thread per (point, source
 // element) pair, the GLN rule in double-float (reg_integrate_dn); pairs it
 // declines (near the CBD_SDF decision) are flagged for the FP64 pass
+// TSEL as for the assembly: 0 every pair, 1 triangle sources only (three
+// shape functions' sums), 2 quadrangle sources only
+template <int TSEL>
 __global__ void __launch_bounds__(128, GB_CROSS_MINB) k_cross_build_df(CrossArgs a, uint8_t* redo) {
   const FieldObj& o = a.o;
   const int Ne = o.sb_Ne[0];
   const size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= (size_t)a.n * Ne) return;
   const int p = (int)(q / Ne), s = 1 + (int)(q % Ne);
+  const int sd = o.sid[o.sb_off[0] + s];
+  if (TSEL != 0 && (o.etype[abs(sd)] != 0) != (TSEL == 2)) return;
   const double rt[3] = {a.rt[3 * p], a.rt[3 * p + 1], a.rt[3 * p + 2]};
   const double vt[1][3] = {{a.v[3 * p], a.v[3 * p + 1], a.v[3 * p + 2]}};
   const cplx k = cmk(o.kn[0], o.kn[1]);
-  const int sd = o.sid[o.sb_off[0] + s];
   Elem S;
   load_elem(S, o.cr, o.cw, o.etype, abs(sd));
   RegAcc<1> A;
-  if (!reg_integrate_dn<1>(S, rt, vt, k, sd < 0, A, o.prec == 3)) {
+  if (!reg_integrate_dn<1, TSEL == 1 ? 3 : 4>(S, rt, vt, k, sd < 0, A, o.prec == 3)) {
     redo[q] = 1;
     return;
   }
@@ -658,8 +662,16 @@ extern "C" int gbi_cross_build(const FieldObj* o, int type, int n, const double*
     GB_CUDA(cudaMallocAsync((void**)&redo, np, st));
     GB_CUDA(cudaMallocAsync((void**)&Fs, np * 2 * sizeof(double), st));
     a.Fs = Fs;
-    k_cross_build_df<<<(unsigned)((np + 127) / 128), 128, 0, st>>>(a, redo);
-    gbi_count_launch();
+    const unsigned nb = (unsigned)((np + 127) / 128);
+    if (o->ntri > 0) {
+      k_cross_build_df<1><<<nb, 128, 0, st>>>(a, redo);
+      gbi_count_launch();
+    }
+    if (o->nquad > 0 || o->ntri <= 0) {  // counts not known: the general variant
+      if (o->ntri > 0) k_cross_build_df<2><<<nb, 128, 0, st>>>(a, redo);
+      else k_cross_build_df<0><<<nb, 128, 0, st>>>(a, redo);
+      gbi_count_launch();
+    }
     a.only = redo;
     k_cross_build<false><<<nbw, 128, 0, st>>>(a);
     gbi_count_launch();

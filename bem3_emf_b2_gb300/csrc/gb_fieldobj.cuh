@@ -24,5 +24,6 @@ struct FieldObj {
   double lambda0;
   int prec;  // 2: regular GLN pairs in double-float (gb_quad_df.cuh); 3: the same with the
              // distance-adaptive order of reg_order; else FP64
+  int ntri, nquad;  // elements of each type
 };
 

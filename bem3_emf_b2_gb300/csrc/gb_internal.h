@@ -23,6 +23,7 @@ typedef struct GbMeshDev {
   int sb_Ne[GB_MAXDOM];
   int sb_off[GB_MAXDOM + 1];
   double kn[2 * GB_MAXDOM];
+  int ntri, nquad;  // elements of each type (host count)
 } GbMeshDev;
 
 // one item of a work-list assembly: rows row0 .. row0 + nrow - 1 of domain did

@@ -65,11 +65,13 @@ __device__ __forceinline__ dfc dfc_acc_re(dfc acc, dfc v, df s) {  // acc + v s 
 }
 
 #define GB_ND(n) ((n) > 0 ? (n) : 1)
-template <int NDIR>
+// sums of one pair; NS = the shape functions held: 4, or 3 where the
+// source element is known to be a triangle (its fourth shape function is zero)
+template <int NDIR, int NS = 4>
 struct AccDN {
-  dfc G[4], H[4];
+  dfc G[NS], H[NS];
   df F;
-  dfc dG[GB_ND(NDIR)][4], dH[GB_ND(NDIR)][4];
+  dfc dG[GB_ND(NDIR)][NS], dH[GB_ND(NDIR)][NS];
   df dF[GB_ND(NDIR)];
 };
 
@@ -80,16 +82,20 @@ struct PairDN {
   df w0[3], w1[3], w2[3];
   df vt[GB_ND(NDIR)][3];
   df kr, ki;
+  // a flat triangle's surface vector is w0 everywhere: |w0| and w0 . vt[q]
+  // once per pair instead of at every point
+  df aW, Wv[GB_ND(NDIR)];
 };
 
 // the integrand at one point (R = r - rt, W = the surface vector, shape
 // functions N, weight w) added to the sums
-template <int NDIR>
+template <int NDIR, int NS = 4>
 __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[3], const df W[3], const df N[4], df w,
-                                              AccDN<NDIR>& A, int ns = 4) {
+                                              AccDN<NDIR, NS>& A, int ns = NS) {
+  const bool tri = ns == 3;  // flat triangle: W = w0, |W| and W . vt[q] from the pair
   const df aR = df_sqrt(dot3d(R, R));
   const df iR = df_rcp(aR);
-  const df aW = df_sqrt(dot3d(W, W));
+  const df aW = tri ? P.aW : df_sqrt(dot3d(W, W));
   const df dl = df_sub(aR, P.a0);
   df sn, cs;
   df_sincos(df_mul(P.kr, dl), &sn, &cs);
@@ -105,7 +111,7 @@ __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[
   const dfc h = dfc_scale(cbe, df_mul(tD, w));
   // ns = 3 for a triangle, whose fourth shape function is zero: skipped
 #pragma unroll
-  for (int n = 0; n < 4; n++) {
+  for (int n = 0; n < NS; n++) {
     if (n < ns) {
       A.G[n] = dfc_acc_re(A.G[n], g, N[n]);
       A.H[n] = dfc_acc_re(A.H[n], h, N[n]);
@@ -118,12 +124,12 @@ __device__ __forceinline__ void reg_kernel_dn(const PairDN<NDIR>& P, const df R[
 #pragma unroll
     for (int q = 0; q < NDIR; q++) {
       const df rdv = df_mul(dot3d(R, P.vt[q]), iR);
-      const df Wdv = dot3d(W, P.vt[q]);
+      const df Wdv = tri ? P.Wv[q] : dot3d(W, P.vt[q]);
       const dfc dg = dfc_scale(cbe, df_mul(df_mul(iR2, rdv), df_mul(aW, w)));
       const dfc u = dfc_add(dfc_scale(t1, df_mul(rdv, rdW)), dfc_scale(cb, df_neg(Wdv)));
       const dfc dh = dfc_scale(dfc_mul(ph, u), iR3w);
 #pragma unroll
-      for (int n = 0; n < 4; n++) {
+      for (int n = 0; n < NS; n++) {
         if (n < ns) {
           A.dG[q][n] = dfc_acc_re(A.dG[q][n], dg, N[n]);
           A.dH[q][n] = dfc_acc_re(A.dH[q][n], dh, N[n]);
@@ -170,22 +176,23 @@ __device__ __forceinline__ int reg_order(const Elem& S, double a0, cplx k) {
 // element S -- the tensor rule on a quadrangle, the same on each of the
 // three sub-quadrangles of a triangle (the reference's maps) -- added to A.
 // GH: the GHN rule (n = GHN), else the rule of nq points (tables at off).
-template <int NDIR, bool GH>
+template <int NDIR, bool GH, int NS = 4>
 __device__ __forceinline__ void reg_points_dn(const Elem& S, const PairDN<NDIR>& P, int nq, int off, int q0, int qstep,
-                                              AccDN<NDIR>& A) {
-  const int npts = (S.quad ? 1 : 3) * nq * nq;
+                                              AccDN<NDIR, NS>& A) {
+  const bool quad = NS == 4 && S.quad;  // NS = 3: the source is a triangle
+  const int npts = (quad ? 1 : 3) * nq * nq;
   const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // sqrt(3)
 #pragma unroll 1
   for (int q = q0; q < npts; q += qstep) {
     int sub = 0, ij = q;
-    if (!S.quad) { sub = q % 3; ij = q / 3; }
+    if (!quad) { sub = q % 3; ij = q / 3; }
     const int i = ij / nq, j = ij - i * nq;
     const float2 xi = GH ? c_tabd.xh[i] : c_tabd.xn[off + i], wi = GH ? c_tabd.wh[i] : c_tabd.wn[off + i];
     const float2 xj = GH ? c_tabd.xh[j] : c_tabd.xn[off + j], wj = GH ? c_tabd.wh[j] : c_tabd.wn[off + j];
     const df x = dfmk(xi.x, xi.y), wx = dfmk(wi.x, wi.y);
     const df y = dfmk(xj.x, xj.y), wy = dfmk(wj.x, wj.y);
     df z, e, w, N[4];
-    if (S.quad) {
+    if (quad) {
       z = x;
       e = y;
       w = df_mul(wx, wy);
@@ -222,9 +229,9 @@ __device__ __forceinline__ void reg_points_dn(const Elem& S, const PairDN<NDIR>&
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       R[d] = df_add(P.R0[d], df_fma(df_fma(df_mul(P.c1[d], z), P.c2[d], e), P.c3[d], ze));
-      W[d] = df_fma(df_fma(P.w0[d], P.w1[d], z), P.w2[d], e);
+      W[d] = quad ? df_fma(df_fma(P.w0[d], P.w1[d], z), P.w2[d], e) : P.w0[d];
     }
-    reg_kernel_dn<NDIR>(P, R, W, N, w, A, S.quad ? 4 : 3);
+    reg_kernel_dn<NDIR, NS>(P, R, W, N, w, A, quad ? 4 : 3);
   }
 }
 
@@ -248,14 +255,19 @@ __device__ __forceinline__ double pair_setup_dn(const Elem& S, const double rt[3
   P.a0 = df_from(a0);
   P.kr = df_from(k.x);
   P.ki = df_from(k.y);
+  if (!S.quad) {
+    P.aW = df_sqrt(dot3d(P.w0, P.w0));
+#pragma unroll
+    for (int q = 0; q < NDIR; q++) P.Wv[q] = dot3d(P.w0, P.vt[q]);
+  }
   return a0;
 }
 
-template <int NDIR>
-__device__ __forceinline__ void acc_zero_dn(AccDN<NDIR>& A) {
+template <int NDIR, int NS = 4>
+__device__ __forceinline__ void acc_zero_dn(AccDN<NDIR, NS>& A) {
   const df zero = dfmk(0.0f, 0.0f);
 #pragma unroll
-  for (int n = 0; n < 4; n++) {
+  for (int n = 0; n < NS; n++) {
     A.G[n] = dfcmk(zero, zero);
     A.H[n] = dfcmk(zero, zero);
 #pragma unroll
@@ -267,10 +279,16 @@ __device__ __forceinline__ void acc_zero_dn(AccDN<NDIR>& A) {
 }
 
 // the sums of A as doubles (unscaled), for reductions across threads
-template <int NDIR>
-__device__ __forceinline__ void acc_to_double(const AccDN<NDIR>& A, RegAcc<NDIR>& R) {
+template <int NDIR, int NS = 4>
+__device__ __forceinline__ void acc_to_double(const AccDN<NDIR, NS>& A, RegAcc<NDIR>& R) {
 #pragma unroll
   for (int n = 0; n < 4; n++) {
+    if (n >= NS) {  // the triangle's zero fourth shape function
+      R.G[n] = R.H[n] = cmk(0.0, 0.0);
+#pragma unroll
+      for (int q = 0; q < NDIR; q++) R.dG[q][n] = R.dH[q][n] = cmk(0.0, 0.0);
+      continue;
+    }
     R.G[n] = cmk(df_to(A.G[n].re), df_to(A.G[n].im));
     R.H[n] = cmk(df_to(A.H[n].re), df_to(A.H[n].im));
 #pragma unroll
@@ -315,7 +333,7 @@ __device__ __forceinline__ void finish_dn(const RegAcc<NDIR>& R, const Elem& S, 
 // (may be null) then tells which: 2 when every dF is finite and one exceeds
 // CBD_SDF + 0.05 (the pair certainly takes the GHN fallback rule), else 1.
 // adapt: the n x n rule of reg_order instead (n = GLN for near pairs).
-template <int NDIR>
+template <int NDIR, int NS = 4>
 __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double (*vt)[3], cplx k, bool neg,
                                  RegAcc<NDIR>& D, bool adapt = false, int* why = nullptr) {
   PairDN<NDIR> P;
@@ -323,13 +341,13 @@ __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double
   const int nq = adapt ? reg_order(S, a0, k) : GB_GLN;
   const int off = nq * (nq - 1) / 2;
   const cplx E0 = cexpik(k, a0);
-  AccDN<NDIR> A;
-  acc_zero_dn<NDIR>(A);
+  AccDN<NDIR, NS> A;
+  acc_zero_dn<NDIR, NS>(A);
   // one loop over every point of the rule, so that the integrand is inlined
   // at one site (the kernel is instruction-fetch bound otherwise)
-  reg_points_dn<NDIR, false>(S, P, nq, off, 0, 1, A);
+  reg_points_dn<NDIR, false, NS>(S, P, nq, off, 0, 1, A);
   RegAcc<NDIR> R;
-  acc_to_double<NDIR>(A, R);
+  acc_to_double<NDIR, NS>(A, R);
   finish_dn<NDIR>(R, S, neg, E0, D);
   bool fin = true;
   double mx = 0.0;
