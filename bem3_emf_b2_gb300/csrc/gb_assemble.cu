@@ -1030,7 +1030,7 @@ __device__ __forceinline__ int find_item(const unsigned* __restrict__ blk0, int 
 #define GB_ASM_MINB 3
 #endif
 #ifndef GB_ASM_TRI_MINB
-#define GB_ASM_TRI_MINB 3
+#define GB_ASM_TRI_MINB 4
 #endif
 template <int TSEL>
 __global__ void __launch_bounds__(128, TSEL == 1 ? GB_ASM_TRI_MINB : GB_ASM_MINB) k_asm_regular_df_list(const AsmArgs* __restrict__ items,

@@ -26,10 +26,25 @@ extern "C" int gbi_upload_tables_field(const void* t) {
 // when DF and the rule is GLN (falling back to FP64 near the CBD_SDF
 // decision), else FP64 -- the same values to ~1e-14; adapt: the double-float
 // rule with the distance-adaptive order (reg_order)
-template <bool DF, int NDIR>
+// the FP64 rule as a called function: in the double-float kernels it serves
+// only the declined pairs, and its registers then do not count against the
+// double-float path's
+template <int NDIR>
+__device__ __noinline__ void reg_integrate_cold(const Elem& S, int type, const double* rt, const double (*vt)[3], cplx k,
+                                                bool neg, RegAcc<NDIR>& A) {
+  reg_integrate<NDIR>(S, type, rt, vt, k, neg, A);
+}
+
+// NS = 3: every source element is a triangle (the double-float sums then hold
+// three shape functions)
+template <bool DF, int NDIR, int NS = 4>
 __device__ __forceinline__ void reg_pair(const Elem& S, int type, const double rt[3], const double (*vt)[3], cplx k,
                                          bool neg, RegAcc<NDIR>& A, bool adapt) {
-  if (DF && type == 2 && reg_integrate_dn<NDIR>(S, rt, vt, k, neg, A, adapt)) return;
+  if (DF && type == 2) {
+    if (reg_integrate_dn<NDIR, NS>(S, rt, vt, k, neg, A, adapt)) return;
+    reg_integrate_cold<NDIR>(S, type, rt, vt, k, neg, A);
+    return;
+  }
   reg_integrate<NDIR>(S, type, rt, vt, k, neg, A);
 }
 
@@ -129,7 +144,7 @@ __global__ void __launch_bounds__(128) k_domain_id(FieldObj o, int n, const doub
 #define GB_FIELD_MINB 1
 #endif
 #ifndef GB_CROSS_MINB
-#define GB_CROSS_MINB 1
+#define GB_CROSS_MINB 3
 #endif
 
 // ------------------------------------------------------------------ field sums
@@ -171,7 +186,7 @@ struct FieldArgs {
 // wave number) is uniform across the warp
 // MODE: FM_MEMP, FM_EH or FM_MEMP2, fixed at compile time so that each
 // variant holds only its own accumulators
-template <bool DF, int MODE>
+template <bool DF, int MODE, int NS = 4>
 __global__ void __launch_bounds__(128, GB_FIELD_MINB) k_field(FieldArgs a) {
   constexpr int NACC = MODE == FM_MEMP ? 9 : (MODE == FM_EH ? 13 : 18);
   const int lane = threadIdx.x & 31;
@@ -204,7 +219,7 @@ __global__ void __launch_bounds__(128, GB_FIELD_MINB) k_field(FieldArgs a) {
     if (MODE == FM_MEMP || MODE == FM_EH) {
       if (!act) continue;
       RegAcc<0> A;
-      reg_pair<DF, 0>(S, a.type, rt, nullptr, k, neg, A, o.prec == 3);
+      reg_pair<DF, 0, NS>(S, a.type, rt, nullptr, k, neg, A, o.prec == 3);
       acc[0] += A.F;
       if (MODE == FM_MEMP) {
         for (int n = 0; n < 4; n++)
@@ -230,7 +245,7 @@ __global__ void __launch_bounds__(128, GB_FIELD_MINB) k_field(FieldArgs a) {
       RegAcc<1> A;
       bool fb = false;
       if (act) {
-        reg_pair<DF, 1>(S, a.type, rt, vt, k, neg, A, o.prec == 3);
+        reg_pair<DF, 1, NS>(S, a.type, rt, vt, k, neg, A, o.prec == 3);
         fb = a.type < 3 && fabs(A.dF[0]) > GB_CBD_SDF;
       }
       warp_fallback<1>(fb, S, rt, vt, k, neg, A);
@@ -387,7 +402,7 @@ struct BdArgs {
   cplx* out;         // [n][6]: E, H
 };
 
-template <bool DF>
+template <bool DF, int NS = 4>
 __global__ void __launch_bounds__(128, GB_FIELD_MINB) k_field_bd(BdArgs a) {
   const int lane = threadIdx.x & 31;
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -419,7 +434,7 @@ __global__ void __launch_bounds__(128, GB_FIELD_MINB) k_field_bd(BdArgs a) {
     Elem S;
     load_elem(S, o.cr, o.cw, o.etype, abs(sd));
     RegAcc<0> A;
-    reg_pair<DF, 0>(S, a.type, rt, nullptr, k, sd < 0, A, o.prec == 3);
+    reg_pair<DF, 0, NS>(S, a.type, rt, nullptr, k, sd < 0, A, o.prec == 3);
     acc[0] += A.F;
     for (int n = 0; n < 4; n++)
       for (int l = 0; l < 3; l++) {
@@ -820,18 +835,22 @@ extern "C" int gbi_field(const FieldObj* o, int mode, int type, int n, const dou
   a.flag = flag;
   unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
   const bool dfp = o->prec >= 2;
+  const bool tri = dfp && o->ntri > 0 && o->nquad == 0;  // only triangles: three shape functions' sums
   if (mode == FM_EH_MEMP) {
     if (dfp) k_field_eh_memp<true><<<nb, 128, 0, st>>>(a);
     else k_field_eh_memp<false><<<nb, 128, 0, st>>>(a);
   } else {
     if (a.mode == FM_MEMP) {
-      if (dfp) k_field<true, FM_MEMP><<<nb, 128, 0, st>>>(a);
+      if (tri) k_field<true, FM_MEMP, 3><<<nb, 128, 0, st>>>(a);
+      else if (dfp) k_field<true, FM_MEMP><<<nb, 128, 0, st>>>(a);
       else k_field<false, FM_MEMP><<<nb, 128, 0, st>>>(a);
     } else if (a.mode == FM_EH) {
-      if (dfp) k_field<true, FM_EH><<<nb, 128, 0, st>>>(a);
+      if (tri) k_field<true, FM_EH, 3><<<nb, 128, 0, st>>>(a);
+      else if (dfp) k_field<true, FM_EH><<<nb, 128, 0, st>>>(a);
       else k_field<false, FM_EH><<<nb, 128, 0, st>>>(a);
     } else {
-      if (dfp) k_field<true, FM_MEMP2><<<nb, 128, 0, st>>>(a);
+      if (tri) k_field<true, FM_MEMP2, 3><<<nb, 128, 0, st>>>(a);
+      else if (dfp) k_field<true, FM_MEMP2><<<nb, 128, 0, st>>>(a);
       else k_field<false, FM_MEMP2><<<nb, 128, 0, st>>>(a);
     }
   }
@@ -852,7 +871,8 @@ extern "C" int gbi_field_bd(const FieldObj* o, int type, int n, const int* did, 
   a.zt = zt;
   a.out = out;
   unsigned nb = (unsigned)(((size_t)n * 32 + 127) / 128);
-  if (o->prec >= 2) k_field_bd<true><<<nb, 128, 0, st>>>(a);
+  if (o->prec >= 2 && o->ntri > 0 && o->nquad == 0) k_field_bd<true, 3><<<nb, 128, 0, st>>>(a);
+  else if (o->prec >= 2) k_field_bd<true><<<nb, 128, 0, st>>>(a);
   else k_field_bd<false><<<nb, 128, 0, st>>>(a);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
