@@ -23,12 +23,64 @@
 #include "gb_df64.cuh"
 #include "gb_internal.h"
 
+// Conical product rules over a triangle for n = 5..8 points per direction
+// (n^2 points, rule n at gb_con_off(n)): the element's reference triangle,
+// vertices (1, 0), (-1/2, +-sqrt(3)/2) in (z, e), as the image of the unit
+// square under (s, t) -> V0 + s (V1 - V0) + s t (V2 - V1) with Jacobian
+// proportional to s; Gauss-Jacobi nodes for the weight s in s, Gauss-Legendre
+// in t (Stroud's conical product; exact for polynomials of degree 2n - 1 in
+// z, e).  Weights scaled to the sub-quadrangle rule's total (12).
+#define GB_NCON (25 + 36 + 49 + 64)
+__host__ __device__ __forceinline__ int gb_con_off(int n) { return n == 5 ? 0 : (n == 6 ? 25 : (n == 7 ? 61 : 110)); }
+
 struct GbTablesD {  // GL nodes and weights in double-float (hi, lo)
   float2 x[GB_GLN], w[GB_GLN];
   float2 xh[GB_GHN], wh[GB_GHN];
   float2 xn[GB_NTAB], wn[GB_NTAB];  // the rules of 1..GLN points, rule n at n (n - 1) / 2
+  float2 cz[GB_NCON], ce[GB_NCON], cwt[GB_NCON];  // conical rules: z, e, weight per point
 };
 static __constant__ GbTablesD c_tabd;
+
+// Gauss-Jacobi nodes and weights on [-1, 1] for the weight (1 + x) (Jacobi
+// alpha = 0, beta = 1): Newton on P_n from its three-term recurrence, with the
+// roots already found divided out; w_i = 4 / ((1 - x_i^2) P_n'(x_i)^2)
+static void gb_gauss_jacobi01(int n, double* xo, double* wo) {
+  auto jac = [n](long double x, long double* dp) {
+    const long double a = 0.0L, b = 1.0L;
+    long double pm = 1.0L, p = ((a + b + 2.0L) * x + (a - b)) / 2.0L;
+    for (int m = 2; m <= n; m++) {
+      const long double c1 = 2.0L * m * (m + a + b) * (2.0L * m + a + b - 2.0L);
+      const long double c2 = (2.0L * m + a + b - 1.0L) * (a * a - b * b);
+      const long double c3 = (2.0L * m + a + b - 2.0L) * (2.0L * m + a + b - 1.0L) * (2.0L * m + a + b);
+      const long double c4 = 2.0L * (m + a - 1.0L) * (m + b - 1.0L) * (2.0L * m + a + b);
+      const long double pn = ((c2 + c3 * x) * p - c4 * pm) / c1;
+      pm = p;
+      p = pn;
+    }
+    *dp = (n * ((a - b) - (2.0L * n + a + b) * x) * p + 2.0L * (n + a) * (n + b) * pm) / ((2.0L * n + a + b) * (1.0L - x * x));
+    return p;
+  };
+  long double r[16];
+  for (int k = 0; k < n; k++) {
+    long double x = cosl(3.14159265358979323846264338327950288L * (k + 0.75L) / (n + 0.5L));
+    for (int it = 0; it < 100; it++) {
+      long double dp = 0.0L;
+      const long double p = jac(x, &dp);
+      long double sdef = 0.0L;
+      for (int j = 0; j < k; j++) sdef += 1.0L / (x - r[j]);
+      const long double dx = p / (dp - p * sdef);
+      x -= dx;
+      if (fabsl(dx) < 1e-19L) break;
+    }
+    r[k] = x;
+  }
+  for (int k = 0; k < n; k++) {
+    long double dp = 0.0L;
+    jac(r[k], &dp);
+    xo[k] = (double)r[k];
+    wo[k] = (double)(4.0L / ((1.0L - r[k] * r[k]) * dp * dp));
+  }
+}
 
 static int gbi_upload_tabd(const GbTables* d) {
   GbTablesD g;
@@ -49,6 +101,25 @@ static int gbi_upload_tabd(const GbTables* d) {
     g.xh[i].y = (float)(d->xhi[i] - (double)g.xh[i].x);
     g.wh[i].x = (float)d->whi[i];
     g.wh[i].y = (float)(d->whi[i] - (double)g.wh[i].x);
+  }
+  // conical rules: s = (1 + x) / 2 with int_0^1 f(s) s ds = sum w_i / 4 f(s_i),
+  // t from the n-point Gauss-Legendre rule on [0, 1]; z = 1 - 3 s / 2,
+  // e = sqrt(3) s (1/2 - t); weight 24 (w_i / 4) (wl_j / 2)
+  auto split = [](double v, float2& f) {
+    f.x = (float)v;
+    f.y = (float)(v - (double)f.x);
+  };
+  for (int n = 5; n <= 8; n++) {
+    double xj[16], wj[16];
+    gb_gauss_jacobi01(n, xj, wj);
+    const int o = gb_con_off(n), ol = n * (n - 1) / 2;
+    for (int i = 0; i < n; i++)
+      for (int j = 0; j < n; j++) {
+        const double sv = 0.5 * (1.0 + xj[i]), tv = 0.5 * (1.0 + d->xn[ol + j]);
+        split(1.0 - 1.5 * sv, g.cz[o + i * n + j]);
+        split(sqrt(3.0) * sv * (0.5 - tv), g.ce[o + i * n + j]);
+        split(24.0 * (0.25 * wj[i]) * (0.5 * d->wn[ol + j]), g.cwt[o + i * n + j]);
+      }
   }
   GB_CUDA(cudaMemcpyToSymbol(c_tabd, &g, sizeof(GbTablesD)));
   return 0;
@@ -168,6 +239,13 @@ __device__ __forceinline__ int reg_order(const Elem& S, double a0, cplx k) {
   const int nD = D < 2.0 ? GB_GLN : (D < 3.0 ? 9 : (D < 5.0 ? 6 : 5));
   const int nk = S.quad ? (ka <= 0.75 ? 5 : (ka <= 2.4 ? 7 : (ka <= 4.5 ? 8 : GB_GLN)))
                         : (ka <= 1.2 ? 5 : (ka <= 2.4 ? 6 : (ka <= 4.5 ? 8 : GB_GLN)));
+  // a triangle at D >= 3 with ka <= 3.6: the conical product rule over the
+  // whole triangle, returned as -n (n^2 points instead of 3 n^2; largest
+  // error over random triangles against a 40-point sub-quadrangle rule:
+  // 7e-13 of the natural scale for n = 5, ka <= 0.6, D >= 8; 1e-13 for n = 6,
+  // ka <= 1.2, D >= 5; 2e-13 for n = 7, ka <= 2.4; 1e-13 for n = 8, ka <= 3.6)
+  if (!S.quad && D >= 3.0 && ka <= 3.6)
+    return (ka <= 0.6 && D >= 8.0) ? -5 : ((ka <= 1.2 && D >= 5.0) ? -6 : (ka <= 2.4 ? -7 : -8));
   const int n = nD > nk ? nD : nk;
   return n < GB_GLN ? n : GB_GLN;
 }
@@ -176,14 +254,29 @@ __device__ __forceinline__ int reg_order(const Elem& S, double a0, cplx k) {
 // element S -- the tensor rule on a quadrangle, the same on each of the
 // three sub-quadrangles of a triangle (the reference's maps) -- added to A.
 // GH: the GHN rule (n = GHN), else the rule of nq points (tables at off).
+// con > 0 (a triangle): the conical rule of con^2 points instead (tables at
+// gb_con_off(con)).
 template <int NDIR, bool GH, int NS = 4>
 __device__ __forceinline__ void reg_points_dn(const Elem& S, const PairDN<NDIR>& P, int nq, int off, int q0, int qstep,
-                                              AccDN<NDIR, NS>& A) {
+                                              AccDN<NDIR, NS>& A, int con = 0) {
   const bool quad = NS == 4 && S.quad;  // NS = 3: the source is a triangle
-  const int npts = (quad ? 1 : 3) * nq * nq;
+  const int npts = con ? con * con : (quad ? 1 : 3) * nq * nq;
+  const int coff = con ? gb_con_off(con) : 0;
   const df s3 = dfmk(1.7320507764816284f, 3.1087250107475484e-08f);  // sqrt(3)
 #pragma unroll 1
   for (int q = q0; q < npts; q += qstep) {
+    df z, e, w, N[4];
+    if (!GH && con) {
+      const float2 cz = c_tabd.cz[coff + q], ce = c_tabd.ce[coff + q], cw = c_tabd.cwt[coff + q];
+      z = dfmk(cz.x, cz.y);
+      e = dfmk(ce.x, ce.y);
+      w = dfmk(cw.x, cw.y);
+      const df se = df_mul(s3, e);  // 3 x the shape functions, as below
+      N[0] = df_add_f(df_mul_f(df_add(z, se), -2.5f), 1.0f);
+      N[1] = df_add_f(df_mul_f(z, 5.0f), 1.0f);
+      N[2] = df_add_f(df_mul_f(df_sub(z, se), -2.5f), 1.0f);
+      N[3] = dfmk(0.0f, 0.0f);
+    } else {
     int sub = 0, ij = q;
     if (!quad) { sub = q % 3; ij = q / 3; }
     const int i = ij / nq, j = ij - i * nq;
@@ -191,7 +284,6 @@ __device__ __forceinline__ void reg_points_dn(const Elem& S, const PairDN<NDIR>&
     const float2 xj = GH ? c_tabd.xh[j] : c_tabd.xn[off + j], wj = GH ? c_tabd.wh[j] : c_tabd.wn[off + j];
     const df x = dfmk(xi.x, xi.y), wx = dfmk(wi.x, wi.y);
     const df y = dfmk(xj.x, xj.y), wy = dfmk(wj.x, wj.y);
-    df z, e, w, N[4];
     if (quad) {
       z = x;
       e = y;
@@ -223,6 +315,7 @@ __device__ __forceinline__ void reg_points_dn(const Elem& S, const PairDN<NDIR>&
       N[1] = df_add_f(df_mul_f(z, 5.0f), 1.0f);
       N[2] = df_add_f(df_mul_f(df_sub(z, se), -2.5f), 1.0f);
       N[3] = dfmk(0.0f, 0.0f);
+    }
     }
     df R[3], W[3];
     const df ze = df_mul(z, e);
@@ -338,14 +431,16 @@ __device__ bool reg_integrate_dn(const Elem& S, const double rt[3], const double
                                  RegAcc<NDIR>& D, bool adapt = false, int* why = nullptr) {
   PairDN<NDIR> P;
   const double a0 = pair_setup_dn<NDIR>(S, rt, vt, k, P);
-  const int nq = adapt ? reg_order(S, a0, k) : GB_GLN;
+  int nq = adapt ? reg_order(S, a0, k) : GB_GLN;
+  const int con = nq < 0 ? -nq : 0;  // a triangle's conical rule
+  if (con) nq = 1;
   const int off = nq * (nq - 1) / 2;
   const cplx E0 = cexpik(k, a0);
   AccDN<NDIR, NS> A;
   acc_zero_dn<NDIR, NS>(A);
   // one loop over every point of the rule, so that the integrand is inlined
   // at one site (the kernel is instruction-fetch bound otherwise)
-  reg_points_dn<NDIR, false, NS>(S, P, nq, off, 0, 1, A);
+  reg_points_dn<NDIR, false, NS>(S, P, nq, off, 0, 1, A, con);
   RegAcc<NDIR> R;
   acc_to_double<NDIR, NS>(A, R);
   finish_dn<NDIR>(R, S, neg, E0, D);
