@@ -206,10 +206,13 @@ typedef struct { MOBJ *mo; int phase,dev; int *next; pthread_mutex_t *mu; } gb_p
 static void gb_phase_object(MOBJ *mo,int m,int phase)
 {
   if(phase==0){
+    /* object m alone is written: its incident field is reset and receives
+     * the other objects' scattered potentials in object order (their
+     * boundary values are not written in this phase) */
     if(gb_reset_incident(gb_dev(&mo->md[m]))) gb_die("mo_solve.c, reset_incident_bd()");
     for(int d=0;d<mo->N;d++){
       if(d==m) continue;
-      if(gb_add_scattered(gb_dev(&mo->md[d]),gb_dev(&mo->md[m]),PREC_DEF)) gb_die("mo_solve.c, add_scattered_mEMP()");
+      if(gb_add_scattered(gb_dev(&mo->md[m]),gb_dev(&mo->md[d]),PREC_DEF)) gb_die("mo_solve.c, add_scattered_mEMP()");
     }
   }
   else if(phase==1){ if(gb_solve_mEMP(gb_dev(&mo->md[m]))) gb_die("mo_solve.c, solve_coefficient_mEMP()"); }
@@ -285,7 +288,7 @@ void mo_solve_bv(MOBJ *mo)
       time(&ms);
       for(int d=0;d<mo->N;d++){
         if(d==m) continue;
-        if(gb_add_scattered(gb_dev(&mo->md[d]),gb_dev(&mo->md[m]),PREC_DEF)) gb_die("mo_solve.c, add_scattered_mEMP()");
+        if(gb_add_scattered(gb_dev(&mo->md[m]),gb_dev(&mo->md[d]),PREC_DEF)) gb_die("mo_solve.c, add_scattered_mEMP()");
       }
       time(&me);
       MSG("finished. Elapsed time : %5g (sec)\n",difftime(me,ms));
