@@ -198,41 +198,6 @@ __device__ __forceinline__ void schur_row(const SchurMv<T>& a, int i, int lane, 
   }
 }
 
-// complex FP32 rows of even length: two entries per 16-byte load, two
-// coalesced loads per lane and step, the next step's loads issued before
-// this step's products (the scalar loop kept too few bytes in flight)
-template <int NC>
-__device__ __forceinline__ void schur_row_v(const SchurMv<cplxf>& a, int i, int lane, float* sr, float* si) {
-  const float4* m4 = reinterpret_cast<const float4*>(a.Mat + (size_t)i * a.n);
-  const int nf = a.n >> 1;  // float4 per row: entries 2k, 2k + 1
-  const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float4 n0 = lane < nf ? m4[lane] : z4, n1 = lane + 32 < nf ? m4[lane + 32] : z4;
-  for (int k0 = 0; k0 < nf; k0 += 64) {
-    const float4 c0 = n0, c1 = n1;
-    if (k0 + 64 < nf) {
-      n0 = k0 + 64 + lane < nf ? m4[k0 + 64 + lane] : z4;
-      n1 = k0 + 96 + lane < nf ? m4[k0 + 96 + lane] : z4;
-    }
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-      const int k = k0 + 32 * h + lane;
-      if (k >= nf) break;
-      const float4 mv = h ? c1 : c0;
-      const float mr[2] = {mv.x, mv.z}, mi[2] = {mv.y, mv.w};
-#pragma unroll
-      for (int q = 0; q < 2; q++) {
-        const cplxf* xv = a.X + (size_t)(2 * k + q) * SC_W + a.xoff;
-#pragma unroll
-        for (int c = 0; c < NC; c++) {
-          const cplxf v = xv[c];
-          sr[c] = fmaf(mr[q], v.x, fmaf(-mi[q], v.y, sr[c]));
-          si[c] = fmaf(mr[q], v.y, fmaf(mi[q], v.x, si[c]));
-        }
-      }
-    }
-  }
-}
-
 template <class T, int NC>
 __global__ void __launch_bounds__(256) k_schur_mv(SchurMv<T> a, int mode) {
   typedef typename SchurTy<T>::R R;
@@ -242,12 +207,7 @@ __global__ void __launch_bounds__(256) k_schur_mv(SchurMv<T> a, int mode) {
   R sr[NC], si[NC];
 #pragma unroll
   for (int c = 0; c < NC; c++) { sr[c] = (R)0; si[c] = (R)0; }
-  if constexpr (sizeof(T) == 8) {
-    if ((a.n & 1) == 0) schur_row_v<NC>(a, i, lane, sr, si);
-    else schur_row<T, NC>(a, i, lane, sr, si);
-  } else {
-    schur_row<T, NC>(a, i, lane, sr, si);
-  }
+  schur_row<T, NC>(a, i, lane, sr, si);
 #pragma unroll
   for (int c = 0; c < NC; c++)
     for (int o = 16; o > 0; o >>= 1) {
