@@ -402,7 +402,9 @@ __device__ __forceinline__ void asm_regular_body(const AsmArgs& a, const uint8_t
   const size_t N = (size_t)a.Ne * 4;
   const size_t npair = (size_t)a.nrow * (size_t)a.Ne;
   size_t p = (size_t)bx * blockDim.x + threadIdx.x;
-  bool active = p < npair;
+  // a pair the flags leave out reads nothing else (the pass over the pairs a
+  // double-float pass declined touches a few of them)
+  bool active = p < npair && (only == nullptr || only[p] != 0);
   int row = 0, sidx = 0;
   bool work = false, fb = false;
   Elem S;
@@ -420,7 +422,7 @@ __device__ __forceinline__ void asm_regular_body(const AsmArgs& a, const uint8_t
     Elem T;
     load_elem(T, a.cr, a.cw, a.etype, atd);
     bool rowok = T.quad || tn < 3;
-    if (rowok && sd != td && (only == nullptr || only[p] != 0)) {
+    if (rowok && sd != td) {
       work = true;
       for (int d = 0; d < 3; d++) rt[d] = __ldg(a.ren + (size_t)atd * 12 + tn * 3 + d);
       node_tangents(T, tn, vt);

@@ -105,11 +105,83 @@ __device__ double elem_solid_angle(int quad, double r[4][3], int* onb) {
 // returns d at its first hit), and the region tests after domain d read the
 // warp-reduced sums Og (their summation order differs from the sequential
 // loop only by rounding).
+// FP32 screen of the same decision: unit vectors, spherical angles and sums
+// in FP32; a point is decided here only when no element's plane passes within
+// a relative 1e-4 of it, no corner coincides with it and every decision sum
+// is farther than 0.01 from 2 pi (FP32 sums of up to ~1e5 solid angles err
+// by far less); otherwise (and for a boundary hit) the FP64 path below
+// decides, so the result is the FP64 path's.
+__device__ __forceinline__ void cross3f(const float a[3], const float b[3], float r[3]) {
+  r[0] = a[1] * b[2] - a[2] * b[1];
+  r[1] = a[2] * b[0] - a[0] * b[2];
+  r[2] = a[0] * b[1] - a[1] * b[0];
+}
+__device__ __forceinline__ float dot3f(const float a[3], const float b[3]) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+__device__ __forceinline__ float norm3f(const float a[3]) { return sqrtf(dot3f(a, a)); }
+// solid angle of the triangle of unit vectors (r0, r1, r2); *unsure when the
+// point lies within a relative 1e-4 of the triangle's plane
+__device__ __forceinline__ float tri_solid_f(const float r0[3], const float r1[3], const float r2[3], bool* unsure) {
+  float n01[3], n12[3], n20[3], nt[3];
+  cross3f(r0, r1, n01);
+  cross3f(r1, r2, n12);
+  cross3f(r2, r0, n20);
+  cross3f(n01, n20, nt);
+  const float a0 = atan2f(norm3f(nt), -dot3f(n01, n20));
+  cross3f(n12, n01, nt);
+  const float a1 = atan2f(norm3f(nt), -dot3f(n12, n01));
+  cross3f(n20, n12, nt);
+  const float a2 = atan2f(norm3f(nt), -dot3f(n20, n12));
+  const float D = dot3f(r0, n12);
+  if (!(fabsf(D) > 1e-4f * norm3f(n12))) { *unsure = true; return 0.0f; }
+  return D > 0.0f ? a0 + a1 + a2 - (float)GB_PI : -(a0 + a1 + a2 - (float)GB_PI);
+}
+// the FP32 decision of k_domain_id for the warp's point: the domain id, or -2
+// when the FP64 path must decide
+__device__ int domain_id_f32(const FieldObj& o, const double r0[3], int lane) {
+  float Og[GB_MAXDOM];
+  for (int d = 0; d <= o.MN; d++) Og[d] = 0.0f;
+  for (int d = 0; d <= o.MN; d++) {
+    const int* sid = o.sid + o.sb_off[d];
+    bool unsure = false;
+    for (int i = 1 + lane; i <= o.sb_Ne[d]; i += 32) {
+      const int s = sid[i];
+      if (s <= 0) continue;
+      float r[4][3];
+      const int nv = o.etype[s] ? 4 : 3;
+      for (int j = 0; j < nv; j++) {
+        for (int k = 0; k < 3; k++) r[j][k] = (float)(o.corner[(size_t)s * 12 + j * 3 + k] - r0[k]);
+        const float nr = norm3f(r[j]);
+        if (!(nr > 0.0f)) { unsure = true; break; }
+        for (int k = 0; k < 3; k++) r[j][k] /= nr;
+      }
+      if (unsure) break;
+      float om = tri_solid_f(r[0], r[1], r[2], &unsure);
+      if (nv == 4 && !unsure) om += tri_solid_f(r[0], r[2], r[3], &unsure);
+      if (unsure) break;
+      Og[d] += om;
+      Og[o.sd[s]] -= om;
+    }
+    if (__any_sync(0xffffffffu, unsure)) return -2;
+    float od = Og[d];
+    for (int off = 16; off > 0; off >>= 1) od += __shfl_xor_sync(0xffffffffu, od, off);
+    const float tp = 2.0f * (float)GB_PI;
+    if (fabsf(fabsf(od) - tp) < 0.01f || fabsf(od - tp) < 0.01f) return -2;
+    if (d == 0 && fabsf(od) < tp) return 0;
+    if (od > tp) return d;
+  }
+  return -1;
+}
+
 __global__ void __launch_bounds__(128) k_domain_id(FieldObj o, int n, const double* rt, int* did) {
   const int lane = threadIdx.x & 31;
   const int p = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (p >= n) return;
   const double r0[3] = {rt[3 * p], rt[3 * p + 1], rt[3 * p + 2]};
+  const int fast = domain_id_f32(o, r0, lane);
+  if (fast != -2) {
+    if (lane == 0) did[p] = fast;
+    return;
+  }
   double Og[GB_MAXDOM];
   for (int d = 0; d <= o.MN; d++) Og[d] = 0.0;
   int res = -1;
