@@ -22,6 +22,7 @@
 #include "gb_quad.cuh"
 #include "gb_df64.cuh"
 #include "gb_internal.h"
+#include "gb_rules.h"
 
 // Conical product rules over a triangle for n = 5..8 points per direction
 // (n^2 points, rule n at gb_con_off(n)): the element's reference triangle,
@@ -40,47 +41,6 @@ struct GbTablesD {  // GL nodes and weights in double-float (hi, lo)
   float2 cz[GB_NCON], ce[GB_NCON], cwt[GB_NCON];  // conical rules: z, e, weight per point
 };
 static __constant__ GbTablesD c_tabd;
-
-// Gauss-Jacobi nodes and weights on [-1, 1] for the weight (1 + x) (Jacobi
-// alpha = 0, beta = 1): Newton on P_n from its three-term recurrence, with the
-// roots already found divided out; w_i = 4 / ((1 - x_i^2) P_n'(x_i)^2)
-static void gb_gauss_jacobi01(int n, double* xo, double* wo) {
-  auto jac = [n](long double x, long double* dp) {
-    const long double a = 0.0L, b = 1.0L;
-    long double pm = 1.0L, p = ((a + b + 2.0L) * x + (a - b)) / 2.0L;
-    for (int m = 2; m <= n; m++) {
-      const long double c1 = 2.0L * m * (m + a + b) * (2.0L * m + a + b - 2.0L);
-      const long double c2 = (2.0L * m + a + b - 1.0L) * (a * a - b * b);
-      const long double c3 = (2.0L * m + a + b - 2.0L) * (2.0L * m + a + b - 1.0L) * (2.0L * m + a + b);
-      const long double c4 = 2.0L * (m + a - 1.0L) * (m + b - 1.0L) * (2.0L * m + a + b);
-      const long double pn = ((c2 + c3 * x) * p - c4 * pm) / c1;
-      pm = p;
-      p = pn;
-    }
-    *dp = (n * ((a - b) - (2.0L * n + a + b) * x) * p + 2.0L * (n + a) * (n + b) * pm) / ((2.0L * n + a + b) * (1.0L - x * x));
-    return p;
-  };
-  long double r[16];
-  for (int k = 0; k < n; k++) {
-    long double x = cosl(3.14159265358979323846264338327950288L * (k + 0.75L) / (n + 0.5L));
-    for (int it = 0; it < 100; it++) {
-      long double dp = 0.0L;
-      const long double p = jac(x, &dp);
-      long double sdef = 0.0L;
-      for (int j = 0; j < k; j++) sdef += 1.0L / (x - r[j]);
-      const long double dx = p / (dp - p * sdef);
-      x -= dx;
-      if (fabsl(dx) < 1e-19L) break;
-    }
-    r[k] = x;
-  }
-  for (int k = 0; k < n; k++) {
-    long double dp = 0.0L;
-    jac(r[k], &dp);
-    xo[k] = (double)r[k];
-    wo[k] = (double)(4.0L / ((1.0L - r[k] * r[k]) * dp * dp));
-  }
-}
 
 static int gbi_upload_tabd(const GbTables* d) {
   GbTablesD g;
@@ -102,24 +62,19 @@ static int gbi_upload_tabd(const GbTables* d) {
     g.wh[i].x = (float)d->whi[i];
     g.wh[i].y = (float)(d->whi[i] - (double)g.wh[i].x);
   }
-  // conical rules: s = (1 + x) / 2 with int_0^1 f(s) s ds = sum w_i / 4 f(s_i),
-  // t from the n-point Gauss-Legendre rule on [0, 1]; z = 1 - 3 s / 2,
-  // e = sqrt(3) s (1/2 - t); weight 24 (w_i / 4) (wl_j / 2)
   auto split = [](double v, float2& f) {
     f.x = (float)v;
     f.y = (float)(v - (double)f.x);
   };
   for (int n = 5; n <= 8; n++) {
-    double xj[16], wj[16];
-    gb_gauss_jacobi01(n, xj, wj);
+    double z[64], e[64], w[64];
     const int o = gb_con_off(n), ol = n * (n - 1) / 2;
-    for (int i = 0; i < n; i++)
-      for (int j = 0; j < n; j++) {
-        const double sv = 0.5 * (1.0 + xj[i]), tv = 0.5 * (1.0 + d->xn[ol + j]);
-        split(1.0 - 1.5 * sv, g.cz[o + i * n + j]);
-        split(sqrt(3.0) * sv * (0.5 - tv), g.ce[o + i * n + j]);
-        split(24.0 * (0.25 * wj[i]) * (0.5 * d->wn[ol + j]), g.cwt[o + i * n + j]);
-      }
+    gb_conical_rule(n, d->xn + ol, d->wn + ol, z, e, w);
+    for (int q = 0; q < n * n; q++) {
+      split(z[q], g.cz[o + q]);
+      split(e[q], g.ce[o + q]);
+      split(w[q], g.cwt[o + q]);
+    }
   }
   GB_CUDA(cudaMemcpyToSymbol(c_tabd, &g, sizeof(GbTablesD)));
   return 0;
