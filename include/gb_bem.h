@@ -156,7 +156,9 @@ int gb_reset_incident(gb_obj *o);
  * The first call for a (src, type) pair fixes the nodes' domains and, when
  * they fit in a quarter of the free device memory, integrates the
  * coefficients of src's potential at dst's nodes once; later calls are a
- * product with src's current boundary values. */
+ * product with src's current boundary values, until dst is assembled again
+ * (an assembly drops the operators dst holds).  Concurrent calls must not
+ * share dst. */
 int gb_add_scattered(gb_obj *dst, gb_obj *src, int type);
 /* sums of the convergence measure over the exterior nodes (ccd_f, mo_solve.c:413-455):
  * out[0] sum of potential changes, out[1] sum of phi changes, out[2] node count */
