@@ -530,9 +530,13 @@ def roofline_live(klist, step_seconds, steps, tf32=None):
     launches on the library's streams in one instrumented step.  Per launch
     M x N x K (complex): algorithmic flops 8 M N K (complex-equivalent),
     algorithmic HBM bytes 16 M N (C read and written) + the split operands
-    2 x 4 (M + 2N) Kp.  Two classes: launches with K >= 128 (outer-block
-    updates and the block elimination's products: >= 64 complex flop per
-    byte, tensor-bound) and the inner-panel updates (K <= 64, HBM-bound).
+    4 (M + 2N) Kp per plane (two planes for three passes, one for one).
+    Two classes: launches with K >= 128 (outer-block updates and the block
+    elimination's products: >= 64 complex flop per byte, tensor-bound) and
+    the inner-panel updates (K <= 64, HBM-bound).  `traffic` scales the
+    measured DRAM bytes per algorithmic byte of one ncu capture
+    (profiles/tc_cgemm_traffic.json, taken on the three-pass kernel) to
+    these launches.
     The tensor figures are against the measured dense bf16 peak and, beside
     it, the TF32 rate cuBLAS reaches on the same GPU in the same run (tf32)."""
     if not klist:
@@ -547,13 +551,14 @@ def roofline_live(klist, step_seconds, steps, tf32=None):
     ceil3 = bf16 * 1.1 / 2.25 / 3.0
     tr = json.load(open(TRAFFIC_FILE)) if os.path.exists(TRAFFIC_FILE) else {}
     cls = {"outer": [0, 0.0, 0.0, 0.0], "inner": [0, 0.0, 0.0, 0.0]}
+    planes = 2.0 if gb_tc_passes() == 3 else 1.0  # split operand planes read (hi, lo) or (hi)
     for ms, M, N, K in klist:
         Kp = ((2 * int(K) + 31) // 32) * 32
         c = cls["outer" if K >= 128 else "inner"]
         c[0] += 1
         c[1] += ms
         c[2] += 8.0 * M * N * K
-        c[3] += 16.0 * M * N + 8.0 * (M + 2.0 * N) * Kp
+        c[3] += 16.0 * M * N + planes * 4.0 * (M + 2.0 * N) * Kp
     out = None
     o = cls["outer"]
     if o[0]:
