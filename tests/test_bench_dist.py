@@ -56,6 +56,7 @@ def test_roofline_classes_and_arithmetic():
     inner = r["inner_launches"]
     assert inner["bound"] == "hbm" and inner["unit"] == "GB/s" and inner["launches_per_step"] == 2
     Kp = 128
-    nbytes = (16.0 * M * 128 + 8.0 * (M + 256) * Kp) + (16.0 * 200 * N + 8.0 * (200 + 2 * N) * Kp)
+    sp = 8.0 if bench.gb_tc_passes() == 3 else 4.0  # bytes per operand element: two split planes or one
+    nbytes = (16.0 * M * 128 + sp * (M + 256) * Kp) + (16.0 * 200 * N + sp * (200 + 2 * N) * Kp)
     assert abs(inner["achieved"] - nbytes / 1.0e-3 / 1e9) < 1e-9 * inner["achieved"]
     assert bench.roofline_live([], 0.1, 1) is None
