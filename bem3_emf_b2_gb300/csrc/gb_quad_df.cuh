@@ -273,10 +273,12 @@ __device__ __forceinline__ void reg_points_dn(const Elem& S, const PairDN<NDIR>&
     }
     }
     df R[3], W[3];
-    const df ze = df_mul(z, e);
+    // a triangle's map has no z e term (c3 = 0) and a constant surface vector
+    const df ze = quad ? df_mul(z, e) : dfmk(0.0f, 0.0f);
 #pragma unroll
     for (int d = 0; d < 3; d++) {
-      R[d] = df_add(P.R0[d], df_fma(df_fma(df_mul(P.c1[d], z), P.c2[d], e), P.c3[d], ze));
+      const df lin = df_fma(df_mul(P.c1[d], z), P.c2[d], e);
+      R[d] = df_add(P.R0[d], quad ? df_fma(lin, P.c3[d], ze) : lin);
       W[d] = quad ? df_fma(df_fma(P.w0[d], P.w1[d], z), P.w2[d], e) : P.w0[d];
     }
     reg_kernel_dn<NDIR, NS>(P, R, W, N, w, A, quad ? 4 : 3);
