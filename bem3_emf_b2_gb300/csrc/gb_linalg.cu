@@ -330,54 +330,61 @@ __device__ __forceinline__ dfc dfc_mac(dfc acc, dfc a, dfc b) {
 
 // k_apply_rows with the matrices and node vectors in double-float: the
 // products of the GMRES iterations on the FP32 pipes (the FP64 version is
-// bound by the DFMA rate); sums finished in FP64
-__global__ void k_apply_rows_df(const float4* __restrict__ G, const float4* __restrict__ H, const int* rowk, int Ne,
-                                int nrows, size_t base, const float4* __restrict__ PQ, cplx* y) {
+// bound by the DFMA rate); sums finished in FP64.  Two rows per warp: each
+// node-vector load serves both rows (half the L1 traffic per product) and
+// the two rows' sums are independent chains; the next column's matrix
+// entries are loaded before this column's products (the loop was bound by
+// load latency).  Each lane sums its columns in order and the warp reduces
+// the lanes in a fixed pattern.
+__global__ void __launch_bounds__(128) k_apply_rows_df2(const float4* __restrict__ G, const float4* __restrict__ H,
+                                                        const int* rowk, int Ne, int nrows, size_t base,
+                                                        const float4* __restrict__ PQ, cplx* y) {
   const int lane = threadIdx.x & 31;
   const size_t N = (size_t)Ne * 4;
-  size_t row = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (row >= N) return;
-  int k = rowk[row];
-  if (k < 0) return;
-  const float4* g = G + row * N;
-  const float4* h = H + row * N;
+  const size_t r0 = (((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2;
+  if (r0 >= N) return;
+  const bool two = r0 + 1 < N;
+  const int k0 = rowk[r0], k1 = two ? rowk[r0 + 1] : -1;
+  if (k0 < 0 && k1 < 0) return;
+  const size_t r1 = two ? r0 + 1 : r0;
+  const float4* g0 = G + r0 * N;
+  const float4* h0 = H + r0 * N;
+  const float4* g1 = G + r1 * N;
+  const float4* h1 = H + r1 * N;
   const df z = dfmk(0.0f, 0.0f);
-  dfc acc[4];
+  dfc a0[4], a1[4];
 #pragma unroll
-  for (int q = 0; q < 4; q++) acc[q] = dfcmk(z, z);
-  // software-pipelined: the next column's matrix entries and node vectors
-  // are loaded before this column's products (the loop was bound by the
-  // loads' latency)
+  for (int q = 0; q < 4; q++) { a0[q] = dfcmk(z, z); a1[q] = dfcmk(z, z); }
   const float4 f0 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float4 gn = f0, hn = f0, vn[8];
-  if ((size_t)lane < N) {
-    gn = g[lane];
-    hn = h[lane];
-#pragma unroll
-    for (int q = 0; q < 8; q++) vn[q] = PQ[(size_t)q * N + lane];
-  }
+  float4 gn0 = f0, hn0 = f0, gn1 = f0, hn1 = f0;
+  if ((size_t)lane < N) { gn0 = g0[lane]; hn0 = h0[lane]; gn1 = g1[lane]; hn1 = h1[lane]; }
   for (size_t c = lane; c < N; c += 32) {
-    const dfc gv = dfc_ld4(gn), hv = dfc_ld4(hn);
-    float4 vc[8];
+    const dfc gv0 = dfc_ld4(gn0), hv0 = dfc_ld4(hn0), gv1 = dfc_ld4(gn1), hv1 = dfc_ld4(hn1);
+    float4 v[8];
 #pragma unroll
-    for (int q = 0; q < 8; q++) vc[q] = vn[q];
+    for (int q = 0; q < 8; q++) v[q] = PQ[(size_t)q * N + c];
     const size_t cn = c + 32;
-    if (cn < N) {
-      gn = g[cn];
-      hn = h[cn];
+    if (cn < N) { gn0 = g0[cn]; hn0 = h0[cn]; gn1 = g1[cn]; hn1 = h1[cn]; }
 #pragma unroll
-      for (int q = 0; q < 8; q++) vn[q] = PQ[(size_t)q * N + cn];
+    for (int q = 0; q < 4; q++) {
+      const dfc p = dfc_ld4(v[q]), qq = dfc_ld4(v[4 + q]);
+      a0[q] = dfc_mac(dfc_mac(a0[q], hv0, p), gv0, qq);
+      a1[q] = dfc_mac(dfc_mac(a1[q], hv1, p), gv1, qq);
     }
-#pragma unroll
-    for (int q = 0; q < 4; q++) acc[q] = dfc_mac(dfc_mac(acc[q], hv, dfc_ld4(vc[q])), gv, dfc_ld4(vc[4 + q]));
   }
-  double s[8];
+  double s[16];
 #pragma unroll
-  for (int q = 0; q < 4; q++) { s[2 * q] = df_to(acc[q].re); s[2 * q + 1] = df_to(acc[q].im); }
-  for (int i = 0; i < 8; i++)
+  for (int q = 0; q < 4; q++) {
+    s[2 * q] = df_to(a0[q].re); s[2 * q + 1] = df_to(a0[q].im);
+    s[8 + 2 * q] = df_to(a1[q].re); s[9 + 2 * q] = df_to(a1[q].im);
+  }
+  for (int i = 0; i < 16; i++)
     for (int o = 16; o > 0; o >>= 1) s[i] += __shfl_down_sync(0xffffffffu, s[i], o);
-  if (lane == 0)
-    for (int q = 0; q < 4; q++) y[base + (size_t)q * nrows + k] = cmk(s[2 * q], s[2 * q + 1]);
+  if (lane != 0) return;
+  if (k0 >= 0)
+    for (int q = 0; q < 4; q++) y[base + (size_t)q * nrows + k0] = cmk(s[2 * q], s[2 * q + 1]);
+  if (k1 >= 0)
+    for (int q = 0; q < 4; q++) y[base + (size_t)q * nrows + k1] = cmk(s[8 + 2 * q], s[9 + 2 * q]);
 }
 
 extern "C" int gbi_apply_A_domain_df(const void* Gd, const void* Hd, const int* sid, const int* rowk,
@@ -393,8 +400,8 @@ extern "C" int gbi_apply_A_domain_df(const void* Gd, const void* Hd, const int* 
   gbi_count_launch();
   k_to_df<<<(unsigned)((8 * N + 255) / 256), 256, 0, st>>>(8 * N, PQ, (float4*)PQd);
   gbi_count_launch();
-  k_apply_rows_df<<<(unsigned)((N * 32 + 255) / 256), 256, 0, st>>>((const float4*)Gd, (const float4*)Hd, rowk, Ne,
-                                                                     nrows, base, (const float4*)PQd, y);
+  k_apply_rows_df2<<<(unsigned)(((N + 1) / 2 * 32 + 127) / 128), 128, 0, st>>>((const float4*)Gd, (const float4*)Hd, rowk,
+                                                                                Ne, nrows, base, (const float4*)PQd, y);
   gbi_count_launch();
   GB_CUDA(cudaGetLastError());
   return 0;
@@ -409,8 +416,9 @@ extern "C" int gbi_rows_apply(const cplx* G, const cplx* H, const void* Gd, cons
   if (Gd && Hd) {
     k_to_df<<<(unsigned)((8 * N + 255) / 256), 256, 0, st>>>(8 * N, PQ, (float4*)PQd);
     gbi_count_launch();
-    k_apply_rows_df<<<(unsigned)((N * 32 + 255) / 256), 256, 0, st>>>((const float4*)Gd, (const float4*)Hd, rowk, Ne,
-                                                                       nrows, base, (const float4*)PQd, y);
+    k_apply_rows_df2<<<(unsigned)(((N + 1) / 2 * 32 + 127) / 128), 128, 0, st>>>((const float4*)Gd, (const float4*)Hd,
+                                                                                  rowk, Ne, nrows, base,
+                                                                                  (const float4*)PQd, y);
   } else {
     k_apply_rows<<<(unsigned)((N * 32 + 255) / 256), 256, 0, st>>>(G, H, rowk, Ne, nrows, base, PQ, y);
   }
