@@ -61,7 +61,7 @@ CONES = dict(name="two cones (base radius 0.5, height 1, n = 1.59 in 1.33, lambd
                   "seed 7); cone 2 rotated pi about x and shifted 1.5 along x; right-circularly polarised plane "
                   "wave along +z; multiple-scattering iteration to the reference's convergence rule",
              m=16, radius=0.5, height=1.0, n_obj=1.59, n_host=1.33, lambda0=1.0, seed=7)
-VS_BASELINE_NOTE = "no published number for this metric (BASELINE.md: the reference publishes no benchmark)"
+VS_BASELINE_NOTE = "no published number for this metric: the reference publishes no benchmark"
 
 
 def write_sphere(wd, n_face=8):
