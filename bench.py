@@ -612,7 +612,7 @@ def roofline_assembly(rec, clocks):
            "pairs_per_s": rate}
     iss = json.load(open(ASM_ISSUE_FILE)) if os.path.exists(ASM_ISSUE_FILE) else None
     mhz = (clocks or {}).get("sm_mhz") or (clocks or {}).get("sm_max_mhz") or 2070.0
-    nsm = torch.cuda.get_device_properties(0).multi_processor_count
+    nsm = torch.cuda.get_device_properties(0).multi_processor_count if torch.cuda.is_available() else 152
     if iss:
         slots = nsm * 4 * float(mhz) * 1e6  # warp instructions per second, all sub-partitions
         ach = iss["inst_per_pair"] * rate

@@ -60,3 +60,23 @@ def test_roofline_classes_and_arithmetic():
     nbytes = (16.0 * M * 128 + sp * (M + 256) * Kp) + (16.0 * 200 * N + sp * (200 + 2 * N) * Kp)
     assert abs(inner["achieved"] - nbytes / 1.0e-3 / 1e9) < 1e-9 * inner["achieved"]
     assert bench.roofline_live([], 0.1, 1) is None
+
+
+def test_roofline_assembly_arithmetic():
+    """bench.roofline_assembly on synthetic timings: pairs per second from the
+    recorded launches, issue and FP32-pipe fractions from the committed
+    per-pair instruction counts at the sampled SM clock."""
+    import ctypes
+    import json
+    sys.path.insert(0, ROOT)
+    import bench
+    rec = (ctypes.c_double(500.0), ctypes.c_double(1.0e8), ctypes.c_long(1))
+    r = bench.roofline_assembly(rec, {"sm_mhz": 2000.0, "sm_max_mhz": 2070.0})
+    assert r["bound"] == "fp32-issue" and r["launches_per_step"] == 1
+    assert abs(r["pairs_per_s"] - 2.0e8) < 1e-6
+    iss = json.load(open(bench.ASM_ISSUE_FILE))
+    slots = 152 * 4 * 2000.0e6
+    assert abs(r["issue_frac"] - iss["inst_per_pair"] * 2.0e8 / slots) < 1e-12
+    assert abs(r["frac"] - iss["fma_pipe_inst_per_pair"] * 2.0e8 / slots) < 1e-12
+    assert 0.0 < r["frac"] < r["issue_frac"] < 1.0
+    assert bench.roofline_assembly((ctypes.c_double(0.0), ctypes.c_double(0.0), ctypes.c_long(0)), {}) is None
