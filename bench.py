@@ -28,7 +28,12 @@ GPU.  --workload sphere: the 384-element dielectric sphere (single object).
                timed the same way, and the relative force/torque difference
   roofline     the tensor-core update kernel of the factorisation, timed per
                launch in a separate instrumented step (not inside the timed
-               steps)
+               steps), against the measured bf16 peak and the TF32 rate
+               cuBLAS reaches in the same run
+  roofline_assembly
+               the double-float assembly kernel (the step's largest): pairs
+               per second from the same instrumented step, issue and FP32-pipe
+               fractions from its committed per-pair instruction counts
   cpu_baseline the CPU oracle (oracle/port: C restatement of the quadrature,
                LAPACK for the dense LU/inverse) on this host's cores: a
                bounded sample scaled to one scene ("estimated": true)
