@@ -14,6 +14,7 @@ pivoted LUs or butterfly-randomised LUs without interchanges (Parker 1995),
 for refinement experiments:
 
     python -m oracle.block_model [quadrangles per cube face]
+    python -m oracle.block_model 8 bf16   # GMRES with bf16-stored factors
 """
 import os
 import sys
@@ -156,7 +157,51 @@ def refine(o, GH, inv, b, tol=1e-13, itmax=30):
     return hist
 
 
+def bf16_round(x):
+    """each real component of a complex array rounded to bfloat16 (8
+    significant bits, round to nearest even on the FP32 bits), returned as
+    complex64: the 16-bit storage of the factors modelled on the CPU"""
+    f = np.ascontiguousarray(x.astype(np.complex64)).view(np.float32)
+    u = f.view(np.uint32).astype(np.uint64)
+    u = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return u.astype(np.uint32).view(np.float32).view(np.complex64)
+
+
+def gmres_with_factors(o, GH, b, store=None, restart=30, tol=1e-13):
+    """GMRES(restart) from zero on the coupled matrix A (complex128),
+    preconditioned by the block elimination's complex64 factors (pivoted
+    LUs), their five matrices optionally passed through `store` (e.g.
+    bf16_round); returns (iterations, true relative residual)"""
+    import scipy.sparse.linalg as spla
+    P = list(_factors(o, GH, inverse_pivoted32, np.complex64))
+    if store is not None:
+        P[:5] = [store(m) for m in P[:5]]
+    A = o.build_A(GH)
+    M = spla.LinearOperator(A.shape, matvec=lambda r: _apply(o.NN, P, r, np.complex64), dtype=complex)
+    res = []
+    x, _ = spla.gmres(A, b, rtol=tol, restart=restart, maxiter=20, M=M, callback=lambda r: res.append(r),
+                      callback_type="pr_norm")
+    return len(res), float(np.linalg.norm(b - A @ x) / np.linalg.norm(b))
+
+
 if __name__ == "__main__":
+    if len(sys.argv) > 2 and sys.argv[2] == "bf16":
+        # the 24,576-element sphere's geometry (radius 3, n = 1.5 + 0.01i in
+        # 1.33) at a coarser resolution: GMRES with FP32 and bf16-stored factors
+        from bem3_emf_b2_gb300 import meshgen
+        from oracle import port
+        nface = int(sys.argv[1])
+        wd = tempfile.mkdtemp()
+        nodes, elems = meshgen.cubed_sphere(nface, 3.0)
+        meshgen.write_mesh(os.path.join(wd, "mesh.msh"), nodes, elems)
+        o = port.Obj(os.path.join(wd, "mesh.msh"), [complex(1.5, 0.01)], 1.0, 1.33)
+        GH = {d: o.rows(d)[:2] for d in range(2)}
+        b = np.random.default_rng(1).standard_normal(8 * o.NN) * (1 + 1j)
+        for name, store in (("complex FP32 factors", None), ("bf16-stored factors", bf16_round)):
+            it, rr = gmres_with_factors(o, GH, b, store)
+            print("%d per face (NN = %d), %s: %d GMRES(30) iterations, true relative residual %.1e"
+                  % (nface, o.NN, name, it, rr))
+        sys.exit(0)
     from bem3_emf_b2_gb300 import meshgen
     from oracle import port
     nface = int(sys.argv[1]) if len(sys.argv) > 1 else 8
